@@ -1,0 +1,849 @@
+// dsmc_api.cu -- the C ABI of include/hystrath_gb300.h: handle life cycle,
+// device memory, the captured step graph and host<->device transfers.
+//
+// The handle plays the role of dsmcCloud (src/lagrangian/dsmc/clouds/
+// dsmcCloud.C): construction resolves the runtime-selected models
+// (BinaryCollisionModel::New, collisionPartnerSelection::New,
+// dsmcPatchBoundary::New), dsmc_initialise is dsmcMeshFill, dsmc_evolve is
+// dsmcCloud::evolve.  One step is captured once per buffer parity as a CUDA
+// graph and replayed; nothing in a step waits on the host.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "dsmc_kernels.h"
+
+using namespace dsmc;
+
+struct dsmc_handle {
+    dsmc_case_spec spec{};
+    std::vector<std::vector<int>> facePatch;
+    CaseDev cs{};
+    InflowDev inflow{};
+    StepBuffers B{};
+    Soa buf[2]{};
+    int cur = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    unsigned char* solid = nullptr;
+    double* info6 = nullptr;
+    double* fieldTmp = nullptr;
+    Counters* ctrHost = nullptr;   // pinned mirror
+    std::vector<void*> allocs;
+    std::string err;
+    double phaseMs[5] = {0, 0, 0, 0, 0};
+    bool hasInflow = false;
+    long long expectedN = 0;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(dsmc_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    g_err = msg;
+    return code;
+}
+
+#define CUDA_TRY(h, call)                                                                   \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(h, DSMC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dalloc(dsmc_handle* h, T** p, long long count) {
+    void* q = nullptr;
+    const size_t bytes = (size_t)(count > 0 ? count : 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess)
+        return fail(h, e == cudaErrorMemoryAllocation ? DSMC_ERR_CAPACITY : DSMC_ERR_CUDA,
+                    std::string("cudaMalloc of ") + std::to_string(bytes) + " bytes: " + cudaGetErrorString(e));
+    cudaMemset(q, 0, bytes);
+    h->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return DSMC_OK;
+}
+
+int alloc_soa(dsmc_handle* h, Soa* s, long long cap) {
+    int rc;
+    if ((rc = dalloc(h, &s->x, cap))) return rc;
+    if ((rc = dalloc(h, &s->y, cap))) return rc;
+    if ((rc = dalloc(h, &s->z, cap))) return rc;
+    if ((rc = dalloc(h, &s->ux, cap))) return rc;
+    if ((rc = dalloc(h, &s->uy, cap))) return rc;
+    if ((rc = dalloc(h, &s->uz, cap))) return rc;
+    if ((rc = dalloc(h, &s->erot, cap))) return rc;
+    if ((rc = dalloc(h, &s->vib, cap))) return rc;
+    if ((rc = dalloc(h, &s->cellw, cap))) return rc;
+    if ((rc = dalloc(h, &s->spc, cap))) return rc;
+    if ((rc = dalloc(h, &s->id, cap))) return rc;
+    return DSMC_OK;
+}
+
+const char* patch_type_names[] = {"wall", "patch", "symmetry", "cyclic"};
+
+int validate(dsmc_handle* h, const dsmc_case_spec& s) {
+    for (int a = 0; a < 3; ++a) {
+        if (s.n_cells[a] <= 0) return fail(h, DSMC_ERR_INVALID, "n_cells must be positive");
+        if (!(s.cell_size[a] > 0)) return fail(h, DSMC_ERR_INVALID, "cell_size must be positive");
+    }
+    const long long C = (long long)s.n_cells[0] * s.n_cells[1] * s.n_cells[2];
+    if (C > (1LL << 28)) return fail(h, DSMC_ERR_INVALID, "more than 2^28 cells");
+    if (s.n_species < 1 || s.n_species > DSMC_MAX_SPECIES)
+        return fail(h, DSMC_ERR_INVALID, "n_species must be 1.." + std::to_string(DSMC_MAX_SPECIES));
+    for (int i = 0; i < s.n_species; ++i) {
+        const dsmc_species& q = s.species[i];
+        if (!(q.mass > 0) || !(q.diameter > 0))
+            return fail(h, DSMC_ERR_INVALID, std::string("species ") + q.name + ": mass and diameter must be positive");
+        if (q.n_vib_modes < 0 || q.n_vib_modes > 1)
+            return fail(h, DSMC_ERR_INVALID, std::string("species ") + q.name +
+                                                 ": nVibrationalModes > 1 is not supported on this path");
+    }
+    if (s.binary_collision_model != DSMC_COLL_VHS && s.binary_collision_model != DSMC_COLL_LB_VHS)
+        return fail(h, DSMC_ERR_UNKNOWN_MODEL,
+                    "Unknown BinaryCollisionModel type. Valid BinaryCollisionModel types are: "
+                    "2(VariableHardSphere LarsenBorgnakkeVariableHardSphere)");
+    if (s.partner_selection_model != DSMC_SEL_NTC)
+        return fail(h, DSMC_ERR_UNKNOWN_MODEL,
+                    "Unknown collisionPartnerSelectionModel type. Valid types are: 1(noTimeCounter)");
+    if (s.n_patches < 1 || s.n_patches > DSMC_MAX_PATCHES)
+        return fail(h, DSMC_ERR_INVALID, "n_patches must be 1.." + std::to_string(DSMC_MAX_PATCHES));
+    for (int p = 0; p < s.n_patches; ++p) {
+        const dsmc_patch& pt = s.patches[p];
+        if (pt.type < 0 || pt.type > 3) return fail(h, DSMC_ERR_INVALID, std::string("patch ") + pt.name + ": bad type");
+        if ((pt.type == DSMC_PATCH_WALL || pt.type == DSMC_PATCH_PATCH) &&
+            (pt.model < DSMC_BC_SPECULAR || pt.model > DSMC_BC_DELETION))
+            return fail(h, DSMC_ERR_UNKNOWN_MODEL,
+                        std::string("patch ") + pt.name + " (" + patch_type_names[pt.type] +
+                            ") has no dsmcPatchBoundary model. Valid models are: "
+                            "3(dsmcSpecularWallPatch dsmcDiffuseWallPatch dsmcDeletionPatch)");
+    }
+    for (int q = 0; q < 6; ++q) {
+        if (s.side_patch[q] < 0 || s.side_patch[q] >= s.n_patches)
+            return fail(h, DSMC_ERR_INVALID, "side_patch out of range");
+        if (s.patches[s.side_patch[q]].type == DSMC_PATCH_CYCLIC) {
+            const int o = q ^ 1;
+            if (s.patches[s.side_patch[o]].type != DSMC_PATCH_CYCLIC)
+                return fail(h, DSMC_ERR_INVALID, "a cyclic side needs a cyclic opposite side");
+        }
+    }
+    if (s.n_obstacles < 0 || s.n_obstacles > DSMC_MAX_OBSTACLES)
+        return fail(h, DSMC_ERR_INVALID, "too many obstacles");
+    for (int o = 0; o < s.n_obstacles; ++o) {
+        const dsmc_obstacle& ob = s.obstacles[o];
+        for (int a = 0; a < 3; ++a)
+            if (ob.lo[a] < 0 || ob.hi[a] > s.n_cells[a] || ob.lo[a] >= ob.hi[a])
+                return fail(h, DSMC_ERR_INVALID, "obstacle outside the mesh");
+        for (int q = 0; q < 6; ++q)
+            if (ob.patch[q] < 0 || ob.patch[q] >= s.n_patches)
+                return fail(h, DSMC_ERR_INVALID, "obstacle patch out of range");
+    }
+    if (!(s.n_equivalent_particles > 0)) return fail(h, DSMC_ERR_INVALID, "nEquivalentParticles must be positive");
+    if (!(s.delta_t > 0)) return fail(h, DSMC_ERR_INVALID, "deltaT must be positive");
+    return DSMC_OK;
+}
+
+// Boundary-face patch map: 6 domain sides then obstacle sides.
+void build_faces(dsmc_handle* h, std::vector<int>& bfPatch, std::vector<long long>& inflowFace,
+                 std::vector<int>& inflowSide, std::vector<int>& inflowCell) {
+    const dsmc_case_spec& s = h->spec;
+    CaseDev& cs = h->cs;
+    long long off = 0;
+    for (int q = 0; q < 6; ++q) {
+        const int a = q / 2;
+        const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+        cs.sideOff[q] = off;
+        const long long nf = (long long)s.n_cells[b] * s.n_cells[c];
+        for (long long f = 0; f < nf; ++f) {
+            const int p = s.face_patch[q] ? s.face_patch[q][f] : s.side_patch[q];
+            bfPatch.push_back(p);
+            if (p >= 0 && p < s.n_patches && s.patches[p].inflow) {
+                inflowFace.push_back(off + f);
+                inflowSide.push_back(q);
+                long long cc[3];
+                cc[a] = (q & 1) ? s.n_cells[a] - 1 : 0;
+                cc[b] = f % s.n_cells[b];
+                cc[c] = f / s.n_cells[b];
+                inflowCell.push_back((int)(cc[0] + (long long)s.n_cells[0] * (cc[1] + (long long)s.n_cells[1] * cc[2])));
+            }
+        }
+        off += nf;
+    }
+    cs.sideOff[6] = off;
+    for (int o = 0; o < s.n_obstacles; ++o) {
+        const dsmc_obstacle& ob = s.obstacles[o];
+        for (int q = 0; q < 6; ++q) {
+            const int a = q / 2;
+            const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+            cs.obstOff[o][q] = off;
+            const long long nf = (long long)(ob.hi[b] - ob.lo[b]) * (ob.hi[c] - ob.lo[c]);
+            for (long long f = 0; f < nf; ++f) bfPatch.push_back(ob.patch[q]);
+            off += nf;
+        }
+    }
+    cs.nBFaces = off;
+}
+
+void fill_case_dev(dsmc_handle* h) {
+    const dsmc_case_spec& s = h->spec;
+    CaseDev& cs = h->cs;
+    for (int a = 0; a < 3; ++a) {
+        cs.n[a] = s.n_cells[a];
+        cs.dx[a] = s.cell_size[a];
+        cs.inv[a] = 1.0 / s.cell_size[a];
+        cs.negOinv[a] = -(s.origin[a] * cs.inv[a]);
+        cs.lo[a] = s.origin[a];
+        cs.hi[a] = s.origin[a] + s.n_cells[a] * s.cell_size[a];
+    }
+    cs.C = (long long)cs.n[0] * cs.n[1] * cs.n[2];
+    cs.V = cs.dx[0] * cs.dx[1] * cs.dx[2];
+    cs.FN = s.n_equivalent_particles;
+    cs.dt = s.delta_t;
+    cs.seedLo = (uint32_t)s.seed;
+    cs.seedHi = (uint32_t)(s.seed >> 32);
+    cs.nSpecies = s.n_species;
+    cs.collModel = s.binary_collision_model;
+    cs.zrot = s.zrot;
+    cs.fixedZv = s.fixed_zv;
+    cs.invZvForm = s.inv_zv_formulation;
+    cs.nPatches = s.n_patches;
+    for (int i = 0; i < s.n_species; ++i) {
+        const dsmc_species& q = s.species[i];
+        SpeciesDev& d = cs.sp[i];
+        d.m = q.mass; d.d = q.diameter; d.omega = q.omega; d.rotDof = q.rotational_dof;
+        d.thetaV = q.theta_v; d.thetaD = q.theta_d; d.zref = q.zref; d.trefZv = q.tref_zv;
+        d.nVib = q.n_vib_modes;
+        d.kThetaV = kB * q.theta_v;
+        d.sqrtKoverM = std::sqrt(kB / q.mass);
+    }
+    for (int i = 0; i < s.n_species; ++i) {
+        for (int j = 0; j < s.n_species; ++j) {
+            const dsmc_species& a = s.species[i];
+            const dsmc_species& b = s.species[j];
+            PairDev& p = cs.pair[i * DSMC_MAX_SPECIES + j];
+            const double dPQ = 0.5 * (a.diameter + b.diameter);
+            const double om = 0.5 * (a.omega + b.omega);
+            const double mR = a.mass * b.mass / (a.mass + b.mass);
+            p.omegaPQ = om;
+            p.mR = mR;
+            p.expo = 1.0 - om;
+            p.sigmaPrefactor = PI * dPQ * dPQ * std::pow(2.0 * kB * s.tref / mR, om - 0.5) /
+                               std::exp(std::lgamma(2.5 - om));
+            p.mPfrac = a.mass / (a.mass + b.mass);
+            p.mQfrac = b.mass / (a.mass + b.mass);
+        }
+    }
+    for (int p = 0; p < s.n_patches; ++p) {
+        const dsmc_patch& pt = s.patches[p];
+        cs.patch[p].type = pt.type;
+        cs.patch[p].model = pt.model;
+        cs.patch[p].Twall = pt.wall_temperature;
+        for (int a = 0; a < 3; ++a) cs.patch[p].Uwall[a] = pt.wall_velocity[a];
+        InflowPatchDev& ip = h->inflow.p[p];
+        for (int m = 0; m < DSMC_MAX_SPECIES; ++m) ip.nd[m] = pt.inflow ? pt.inflow_number_density[m] : 0.0;
+        ip.Ttra = pt.inflow_t_tra;
+        ip.Trot = pt.inflow_t_rot;
+        ip.Tvib = pt.inflow_t_vib;
+        for (int a = 0; a < 3; ++a) ip.U[a] = pt.inflow_velocity[a];
+        if (pt.inflow) h->hasInflow = true;
+        cs.hasWallMeasure = 1;
+    }
+    h->inflow.nPatches = s.n_patches;
+    cs.nObst = s.n_obstacles;
+    for (int o = 0; o < s.n_obstacles; ++o) {
+        for (int a = 0; a < 3; ++a) {
+            cs.obLoI[o][a] = s.obstacles[o].lo[a];
+            cs.obHiI[o][a] = s.obstacles[o].hi[a];
+            cs.obLo[o][a] = s.origin[a] + s.obstacles[o].lo[a] * s.cell_size[a];
+            cs.obHi[o][a] = s.origin[a] + s.obstacles[o].hi[a] * s.cell_size[a];
+        }
+    }
+    cs.nAcc = s.n_species * SACC + CACC;
+}
+
+Soa& cur_soa(dsmc_handle* h) { return h->buf[h->cur]; }
+
+int check_device_error(dsmc_handle* h) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    const unsigned e = h->ctrHost->err;
+    if (e) {
+        std::string m = "device error bits 0x" + std::to_string(e) + ":";
+        if (e & ERRB_CROSSINGS) m += " face-crossing cap reached;";
+        if (e & ERRB_REJECTION) m += " acceptance-rejection cap reached;";
+        if (e & ERRB_CAPACITY) m += " particle capacity exceeded;";
+        if (e & ERRB_BOUNDS) m += " index out of bounds;";
+        if (e & ERRB_PATCH) m += " boundary face without a patch;";
+        return fail(h, e & ERRB_CAPACITY ? DSMC_ERR_CAPACITY : DSMC_ERR_DEVICE, m);
+    }
+    return DSMC_OK;
+}
+
+// Enqueue one step on the handle's stream (graph capture or direct launch).
+void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) {
+    const CaseDev& cs = h->cs;
+    StepBuffers& B = h->B;
+    cudaStream_t st = h->stream;
+    Soa& a = h->buf[parity];
+    Soa& b = h->buf[parity ^ 1];
+    if (ev) cudaEventRecord(ev[0], st);
+    launch_zero_step(B, st);
+    if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
+    if (ev) cudaEventRecord(ev[1], st);
+    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st);
+    if (ev) cudaEventRecord(ev[2], st);
+    if (phases & DSMC_PHASE_SORT) {
+        if (!(phases & DSMC_PHASE_MOVE)) launch_count(cs, B, a, st);
+        launch_scan(cs, B, st);
+        launch_scatter(cs, B, a, b, st);
+        launch_finish_sort(B, st);
+    } else if (phases & DSMC_PHASE_MOVE) {
+        cudaMemsetAsync(B.count, 0, sizeof(int) * cs.C, st);
+    }
+    if (ev) cudaEventRecord(ev[3], st);
+    const int doColl = (phases & DSMC_PHASE_COLLIDE) ? 1 : 0;
+    const int doSamp = (phases & DSMC_PHASE_SAMPLE) ? 1 : 0;
+    if (doColl || doSamp) launch_collide_sample(cs, B, (phases & DSMC_PHASE_SORT) ? b : a, doColl, doSamp, st);
+    if (ev) cudaEventRecord(ev[4], st);
+    launch_end_step(B, doSamp, st);
+    if (ev) cudaEventRecord(ev[5], st);
+}
+
+int build_graphs(dsmc_handle* h) {
+    for (int p = 0; p < 2; ++p) {
+        if (h->graph[p]) continue;
+        cudaGraph_t g;
+        CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step(h, p, DSMC_PHASE_ALL, nullptr);
+        CUDA_TRY(h, cudaStreamEndCapture(h->stream, &g));
+        CUDA_TRY(h, cudaGraphInstantiate(&h->graph[p], g, 0));
+        cudaGraphDestroy(g);
+    }
+    return DSMC_OK;
+}
+
+int sort_current(dsmc_handle* h, long long n) {
+    // particles [0,n) of the current buffer: recompute cells, count, scan, scatter
+    const CaseDev& cs = h->cs;
+    StepBuffers& B = h->B;
+    cudaStream_t st = h->stream;
+    Counters c{};
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    c = *h->ctrHost;
+    c.n = n;
+    c.nMoved = n;
+    *h->ctrHost = c;
+    CUDA_TRY(h, cudaMemcpy(B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
+    launch_cellw(cs, cur_soa(h), n, st);
+    CUDA_TRY(h, cudaMemsetAsync(B.count, 0, sizeof(int) * cs.C, st));
+    launch_count_n(cur_soa(h), n, B.count, st);
+    launch_scan(cs, B, st);
+    launch_scatter(cs, B, h->buf[h->cur], h->buf[h->cur ^ 1], st);
+    launch_finish_sort(B, st);
+    h->cur ^= 1;
+    CUDA_TRY(h, cudaGetLastError());
+    return check_device_error(h);
+}
+
+}  // namespace
+
+extern "C" {
+
+void dsmc_spec_defaults(dsmc_case_spec* s) {
+    std::memset(s, 0, sizeof(*s));
+    s->tref = 273.0;
+    s->zrot = 5.0;
+    s->fixed_zv = 0.0;
+    s->inv_zv_formulation = 2;
+    s->mfp_tref = 273.0;
+    s->measure_mean_free_path = 1;
+    s->binary_collision_model = DSMC_COLL_VHS;
+    s->partner_selection_model = DSMC_SEL_NTC;
+}
+
+const char* dsmc_last_global_error(void) { return g_err.c_str(); }
+const char* dsmc_last_error(const dsmc_handle* h) { return h ? h->err.c_str() : g_err.c_str(); }
+
+int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
+    *out = nullptr;
+    std::unique_ptr<dsmc_handle> hp(new dsmc_handle());
+    dsmc_handle* h = hp.get();
+    int rc = validate(h, *spec);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(h, DSMC_ERR_NO_DEVICE, "no CUDA device: this library has no CPU path");
+    CUDA_TRY(h, cudaGetDevice(&h->device));
+    h->spec = *spec;
+    for (int q = 0; q < 6; ++q) {
+        if (spec->face_patch[q]) {
+            const int a = q / 2;
+            const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+            h->facePatch.emplace_back(spec->face_patch[q],
+                                      spec->face_patch[q] + (long long)spec->n_cells[b] * spec->n_cells[c]);
+            h->spec.face_patch[q] = h->facePatch.back().data();
+        }
+    }
+    fill_case_dev(h);
+    CaseDev& cs = h->cs;
+    std::vector<int> bfPatch;
+    std::vector<long long> inflowFace;
+    std::vector<int> inflowSide, inflowCell;
+    build_faces(h, bfPatch, inflowFace, inflowSide, inflowCell);
+    for (size_t f = 0; f < bfPatch.size(); ++f)
+        if (bfPatch[f] < 0 || bfPatch[f] >= spec->n_patches)
+            return fail(h, DSMC_ERR_INVALID, "boundary face " + std::to_string(f) + " has no patch");
+
+    // capacity
+    std::vector<unsigned char> solid(cs.C, 0);
+    long long fluid = cs.C;
+    for (int o = 0; o < spec->n_obstacles; ++o) {
+        const dsmc_obstacle& ob = spec->obstacles[o];
+        for (int k = ob.lo[2]; k < ob.hi[2]; ++k)
+            for (int j = ob.lo[1]; j < ob.hi[1]; ++j)
+                for (int i = ob.lo[0]; i < ob.hi[0]; ++i) {
+                    unsigned char& sv = solid[i + (long long)cs.n[0] * (j + (long long)cs.n[1] * k)];
+                    if (!sv) { sv = 1; --fluid; }
+                }
+    }
+    double perCell = 0;
+    for (int m = 0; m < spec->n_species; ++m) perCell += spec->init_number_density[m] * cs.V / cs.FN;
+    h->expectedN = (long long)(perCell * fluid);
+    long long cap = spec->max_particles;
+    if (cap <= 0) cap = (long long)((h->hasInflow ? 2.0 : 1.3) * h->expectedN) + 65536;
+    h->B.capacity = cap;
+
+    CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    StepBuffers& B = h->B;
+    if ((rc = alloc_soa(h, &h->buf[0], cap))) return rc;
+    if ((rc = alloc_soa(h, &h->buf[1], cap))) return rc;
+    // big-cell staging: id, ux, uy, uz, erot, vib, cellw (as bytes) only
+    if ((rc = dalloc(h, &B.stage.id, cap))) return rc;
+    if ((rc = dalloc(h, &B.stage.ux, cap))) return rc;
+    if ((rc = dalloc(h, &B.stage.uy, cap))) return rc;
+    if ((rc = dalloc(h, &B.stage.uz, cap))) return rc;
+    if ((rc = dalloc(h, &B.stage.erot, cap))) return rc;
+    if ((rc = dalloc(h, &B.stage.vib, cap))) return rc;
+    if ((rc = dalloc(h, &B.stage.cellw, cap))) return rc;
+    if ((rc = dalloc(h, &B.perm, cap))) return rc;
+    if ((rc = dalloc(h, &B.scl, cap))) return rc;
+    if ((rc = dalloc(h, &B.dirty, cap))) return rc;
+    if ((rc = dalloc(h, &B.count, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.start, cs.C + 1))) return rc;
+    if ((rc = dalloc(h, &B.blockSums, scan_scratch_ints(cs.C) + 1))) return rc;
+    if ((rc = dalloc(h, &B.smax, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.rem, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.acc, cs.C * cs.nAcc))) return rc;
+    if ((rc = dalloc(h, &B.wall, cs.nBFaces * W_N))) return rc;
+    if ((rc = dalloc(h, &B.bfPatch, cs.nBFaces))) return rc;
+    if ((rc = dalloc(h, &B.bigList, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.ctr, 1))) return rc;
+    if ((rc = dalloc(h, &h->solid, cs.C))) return rc;
+    if ((rc = dalloc(h, &h->info6, 8))) return rc;
+    if ((rc = dalloc(h, &h->fieldTmp, cs.C))) return rc;
+    B.nInflowFaces = (int)inflowFace.size();
+    const long long ni = (long long)B.nInflowFaces * spec->n_species;
+    if ((rc = dalloc(h, &B.inflowFace, B.nInflowFaces))) return rc;
+    if ((rc = dalloc(h, &B.inflowSide, B.nInflowFaces))) return rc;
+    if ((rc = dalloc(h, &B.inflowCell, B.nInflowFaces))) return rc;
+    if ((rc = dalloc(h, &B.inflowAcc, ni))) return rc;
+    if ((rc = dalloc(h, &B.inflowCount, ni))) return rc;
+    if ((rc = dalloc(h, &B.inflowOff, ni + 1))) return rc;
+    CUDA_TRY(h, cudaMemcpy(B.bfPatch, bfPatch.data(), sizeof(int) * bfPatch.size(), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(h->solid, solid.data(), cs.C, cudaMemcpyHostToDevice));
+    if (B.nInflowFaces) {
+        CUDA_TRY(h, cudaMemcpy(B.inflowFace, inflowFace.data(), sizeof(long long) * inflowFace.size(),
+                               cudaMemcpyHostToDevice));
+        CUDA_TRY(h, cudaMemcpy(B.inflowSide, inflowSide.data(), sizeof(int) * inflowSide.size(),
+                               cudaMemcpyHostToDevice));
+        CUDA_TRY(h, cudaMemcpy(B.inflowCell, inflowCell.data(), sizeof(int) * inflowCell.size(),
+                               cudaMemcpyHostToDevice));
+    }
+    void* pinned = nullptr;
+    CUDA_TRY(h, cudaMallocHost(&pinned, sizeof(Counters)));
+    h->ctrHost = static_cast<Counters*>(pinned);
+    std::memset(h->ctrHost, 0, sizeof(Counters));
+    launch_remainder_init(cs, B.rem, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    *out = hp.release();
+    return DSMC_OK;
+}
+
+void dsmc_destroy(dsmc_handle* h) {
+    if (!h) return;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    for (int p = 0; p < 2; ++p)
+        if (h->graph[p]) cudaGraphExecDestroy(h->graph[p]);
+    for (void* q : h->allocs) cudaFree(q);
+    if (h->ctrHost) cudaFreeHost(h->ctrHost);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+int dsmc_initialise(dsmc_handle* h) {
+    const CaseDev& cs = h->cs;
+    StepBuffers& B = h->B;
+    cudaStream_t st = h->stream;
+    const dsmc_case_spec& s = h->spec;
+    // device copy of the number densities in the info scratch
+    double nd[DSMC_MAX_SPECIES] = {0};
+    for (int m = 0; m < s.n_species; ++m) nd[m] = s.init_number_density[m];
+    double* dnd = nullptr;
+    CUDA_TRY(h, cudaMalloc(&dnd, sizeof(nd)));
+    CUDA_TRY(h, cudaMemcpy(dnd, nd, sizeof(nd), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemsetAsync(B.count, 0, sizeof(int) * cs.C, st));
+    launch_init_count(cs, dnd, h->solid, B.count, st);
+    launch_scan(cs, B, st);
+    CUDA_TRY(h, cudaStreamSynchronize(st));
+    int total = 0;
+    CUDA_TRY(h, cudaMemcpy(&total, B.start + cs.C, sizeof(int), cudaMemcpyDeviceToHost));
+    if (total > B.capacity) {
+        cudaFree(dnd);
+        return fail(h, DSMC_ERR_CAPACITY, "initial fill of " + std::to_string(total) +
+                                              " parcels exceeds capacity " + std::to_string(B.capacity));
+    }
+    const double Txyz[3] = {s.init_t_tra_xyz[0], s.init_t_tra_xyz[1], s.init_t_tra_xyz[2]};
+    const double U[3] = {s.init_velocity[0], s.init_velocity[1], s.init_velocity[2]};
+    launch_init_fill(cs, B, cur_soa(h), dnd, h->solid, B.start, s.init_t_tra, Txyz, s.init_t_rot, s.init_t_vib,
+                     U, st);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaStreamSynchronize(st));
+    cudaFree(dnd);
+    // sigmaTcRMax = sigmaT * most probable speed of the most abundant species
+    int most = 0;
+    for (int m = 1; m < s.n_species; ++m)
+        if (s.init_number_density[m] > s.init_number_density[most]) most = m;
+    const dsmc_species& sp = s.species[most];
+    const double smax = PI * sp.diameter * sp.diameter * std::sqrt(2.0 * kB * s.init_t_tra / sp.mass);
+    std::vector<double> sm(cs.C, smax);
+    CUDA_TRY(h, cudaMemcpy(B.smax, sm.data(), sizeof(double) * cs.C, cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    h->ctrHost->nextId = total;
+    CUDA_TRY(h, cudaMemcpy(B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
+    return sort_current(h, total);
+}
+
+int dsmc_evolve(dsmc_handle* h, long long n) {
+    int rc = build_graphs(h);
+    if (rc) return rc;
+    for (long long i = 0; i < n; ++i) {
+        CUDA_TRY(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
+        h->cur ^= 1;
+    }
+    return check_device_error(h);
+}
+
+int dsmc_run_phases(dsmc_handle* h, unsigned phases) {
+    cudaEvent_t ev[6];
+    for (int k = 0; k < 6; ++k) cudaEventCreate(&ev[k]);
+    enqueue_step(h, h->cur, phases, ev);
+    CUDA_TRY(h, cudaGetLastError());
+    if (phases & DSMC_PHASE_SORT) h->cur ^= 1;
+    int rc = check_device_error(h);
+    float ms;
+    for (int k = 0; k < 5; ++k) {
+        cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+        h->phaseMs[k] = ms;
+    }
+    for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
+    return rc;
+}
+
+int dsmc_phase_times(dsmc_handle* h, double* a, double* b, double* c, double* d, double* e) {
+    // times of the last dsmc_run_phases call: inflow, move, sort, collide+sample, end
+    if (a) *a = h->phaseMs[0];
+    if (b) *b = h->phaseMs[1];
+    if (c) *c = h->phaseMs[2];
+    if (d) *d = h->phaseMs[3];
+    if (e) *e = h->phaseMs[4];
+    return DSMC_OK;
+}
+
+int dsmc_set_particles(dsmc_handle* h, long long n, const double* pos, const double* U, const double* erot,
+                       const int* vib, const int* species, const unsigned* id) {
+    if (n < 0 || n > h->B.capacity) return fail(h, DSMC_ERR_CAPACITY, "particle count exceeds capacity");
+    Soa& s = cur_soa(h);
+    std::vector<double> tmp(n);
+    auto put = [&](double* dst, const double* src, int stride, int k) -> int {
+        for (long long i = 0; i < n; ++i) tmp[i] = src ? src[stride * i + k] : 0.0;
+        CUDA_TRY(h, cudaMemcpy(dst, tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+        return DSMC_OK;
+    };
+    int rc;
+    if ((rc = put(s.x, pos, 3, 0)) || (rc = put(s.y, pos, 3, 1)) || (rc = put(s.z, pos, 3, 2))) return rc;
+    if ((rc = put(s.ux, U, 3, 0)) || (rc = put(s.uy, U, 3, 1)) || (rc = put(s.uz, U, 3, 2))) return rc;
+    if ((rc = put(s.erot, erot, 1, 0))) return rc;
+    std::vector<int> iv(n, 0);
+    std::vector<uint32_t> uv(n, 0);
+    uint32_t maxId = 0;
+    for (long long i = 0; i < n; ++i) {
+        iv[i] = vib ? vib[i] : 0;
+        if (species && (species[i] < 0 || species[i] >= h->spec.n_species))
+            return fail(h, DSMC_ERR_INVALID, "species index out of range");
+    }
+    CUDA_TRY(h, cudaMemcpy(s.vib, iv.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+    for (long long i = 0; i < n; ++i) uv[i] = species ? (uint32_t)species[i] : 0u;
+    CUDA_TRY(h, cudaMemcpy(s.spc, uv.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    for (long long i = 0; i < n; ++i) {
+        uv[i] = id ? id[i] : (uint32_t)i;
+        if (uv[i] + 1 > maxId) maxId = uv[i] + 1;
+    }
+    CUDA_TRY(h, cudaMemcpy(s.id, uv.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemset(s.cellw, 0, sizeof(uint32_t) * n));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    h->ctrHost->nextId = maxId;
+    CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
+    return sort_current(h, n);
+}
+
+int dsmc_get_particles(dsmc_handle* h, long long capacity, long long* n_out, double* pos, double* U, double* erot,
+                       int* vib, int* species, unsigned* id, int* cell) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    const long long n = h->ctrHost->n;
+    if (n_out) *n_out = n;
+    if (capacity < n) return fail(h, DSMC_ERR_CAPACITY, "output capacity smaller than the particle count");
+    Soa& s = cur_soa(h);
+    std::vector<double> tmp(n);
+    auto get = [&](double* dst, const double* src, int stride, int k) -> int {
+        if (!dst) return DSMC_OK;
+        CUDA_TRY(h, cudaMemcpy(tmp.data(), src, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < n; ++i) dst[stride * i + k] = tmp[i];
+        return DSMC_OK;
+    };
+    int rc;
+    if ((rc = get(pos, s.x, 3, 0)) || (rc = get(pos, s.y, 3, 1)) || (rc = get(pos, s.z, 3, 2))) return rc;
+    if ((rc = get(U, s.ux, 3, 0)) || (rc = get(U, s.uy, 3, 1)) || (rc = get(U, s.uz, 3, 2))) return rc;
+    if ((rc = get(erot, s.erot, 1, 0))) return rc;
+    if (vib) CUDA_TRY(h, cudaMemcpy(vib, s.vib, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> uv(n);
+    if (species) {
+        CUDA_TRY(h, cudaMemcpy(uv.data(), s.spc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < n; ++i) species[i] = (int)uv[i];
+    }
+    if (id) CUDA_TRY(h, cudaMemcpy(id, s.id, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    if (cell) {
+        CUDA_TRY(h, cudaMemcpy(uv.data(), s.cellw, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < n; ++i) cell[i] = uv[i] == CELLW_DELETED ? -1 : (int)cellw_cell(uv[i]);
+    }
+    return DSMC_OK;
+}
+
+int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n) {
+    const std::string nm(name);
+    const long long C = h->cs.C;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (nm == "count" || nm == "start") {
+        if (n != C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
+        std::vector<int> st(C + 1);
+        CUDA_TRY(h, cudaMemcpy(st.data(), h->B.start, sizeof(int) * (C + 1), cudaMemcpyDeviceToHost));
+        int* o = static_cast<int*>(out);
+        for (long long c = 0; c < C; ++c) o[c] = (nm == "start") ? st[c] : st[c + 1] - st[c];
+        return DSMC_OK;
+    }
+    if (nm == "sigmaTcRMax" || nm == "collisionSelectionRemainder") {
+        if (n != C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
+        CUDA_TRY(h, cudaMemcpy(out, nm == "sigmaTcRMax" ? h->B.smax : h->B.rem, sizeof(double) * C,
+                               cudaMemcpyDeviceToHost));
+        return DSMC_OK;
+    }
+    if (nm == "accumulators") {
+        if (n != C * h->cs.nAcc) return fail(h, DSMC_ERR_INVALID, "n must equal cells x accumulators");
+        CUDA_TRY(h, cudaMemcpy(out, h->B.acc, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        return DSMC_OK;
+    }
+    return fail(h, DSMC_ERR_INVALID, "unknown cell array " + nm +
+                                         "; valid: count start sigmaTcRMax collisionSelectionRemainder accumulators");
+}
+
+int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long long n) {
+    const std::string nm(name);
+    const long long C = h->cs.C;
+    if (n != C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (nm == "sigmaTcRMax" || nm == "collisionSelectionRemainder") {
+        CUDA_TRY(h, cudaMemcpy(nm == "sigmaTcRMax" ? h->B.smax : h->B.rem, in, sizeof(double) * C,
+                               cudaMemcpyHostToDevice));
+        return DSMC_OK;
+    }
+    return fail(h, DSMC_ERR_INVALID, "unknown settable cell array " + nm);
+}
+
+int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n) {
+    static const char* names[F_COUNT_FIELDS] = {"rhoN", "rhoM", "Ux", "Uy", "Uz", "Ttra", "p", "Trot", "Tvib",
+                                                "Tov", "dsmcNMean", "nColls", "measuredCollisionRate",
+                                                "meanCollisionRate", "mfp"};
+    int which = -1;
+    for (int k = 0; k < F_COUNT_FIELDS; ++k)
+        if (!std::strcmp(name, names[k])) which = k;
+    if (which < 0) {
+        std::string valid;
+        for (int k = 0; k < F_COUNT_FIELDS; ++k) valid += std::string(" ") + names[k];
+        return fail(h, DSMC_ERR_INVALID, std::string("unknown field ") + name + "; valid:" + valid);
+    }
+    if (n != h->cs.C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
+    launch_field(h->cs, h->B, which, h->fieldTmp, h->spec.measure_mean_free_path, h->spec.mfp_tref, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemcpyAsync(out, h->fieldTmp, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return DSMC_OK;
+}
+
+long long dsmc_n_boundary_faces(const dsmc_handle* h) { return h->cs.nBFaces; }
+
+int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long n) {
+    const long long nf = h->cs.nBFaces;
+    const std::string nm(name);
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (nm == "wallAccumulators") {
+        if (n != nf * W_N) return fail(h, DSMC_ERR_INVALID, "n must equal faces x 14");
+        CUDA_TRY(h, cudaMemcpy(out, h->B.wall, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        return DSMC_OK;
+    }
+    if (n != nf) return fail(h, DSMC_ERR_INVALID, "n must equal the number of boundary faces");
+    std::vector<double> w(nf * W_N);
+    CUDA_TRY(h, cudaMemcpy(w.data(), h->B.wall, sizeof(double) * nf * W_N, cudaMemcpyDeviceToHost));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    const double nT = h->ctrHost->step > 0 ? (double)h->ctrHost->step : 1.0;
+    for (long long f = 0; f < nf; ++f) {
+        const double* W = &w[f * W_N];
+        double v;
+        if (nm == "wallHeatFlux") v = W[W_Q] / nT;
+        else if (nm == "wallShearStress_x") v = W[W_FDX] / nT;
+        else if (nm == "wallShearStress_y") v = W[W_FDY] / nT;
+        else if (nm == "wallShearStress_z") v = W[W_FDZ] / nT;
+        else if (nm == "rhoN_wall") v = W[W_RHON] * h->cs.FN / nT;
+        else return fail(h, DSMC_ERR_INVALID, "unknown wall field " + nm);
+        out[f] = v;
+    }
+    return DSMC_OK;
+}
+
+int dsmc_reset_sampling(dsmc_handle* h) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaMemset(h->B.acc, 0, sizeof(double) * h->cs.C * h->cs.nAcc));
+    CUDA_TRY(h, cudaMemset(h->B.wall, 0, sizeof(double) * h->cs.nBFaces * W_N));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    h->ctrHost->sampleSteps = 0;
+    CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
+    return DSMC_OK;
+}
+
+int dsmc_info(dsmc_handle* h, dsmc_info_t* o) {
+    std::memset(o, 0, sizeof(*o));
+    launch_info(h->cs, cur_soa(h), h->B.ctr, h->info6, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    double v[6];
+    CUDA_TRY(h, cudaMemcpyAsync(v, h->info6, sizeof(v), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    const Counters& c = *h->ctrHost;
+    const double FN = h->cs.FN;
+    o->n_particles = c.n;
+    o->step = c.step;
+    o->linear_ke = v[0] * FN;
+    o->rotational_e = v[1] * FN;
+    o->vibrational_e = v[2] * FN;
+    for (int a = 0; a < 3; ++a) o->momentum[a] = v[3 + a] * FN;
+    o->collisions_last_step = (long long)c.coll;
+    o->candidates_last_step = (long long)c.cand;
+    o->collisions_total = (long long)c.collTot;
+    o->candidates_total = (long long)c.candTot;
+    o->wall_hits_last_step = (long long)c.wallHits;
+    o->inserted_last_step = (long long)c.inserted;
+    o->deleted_last_step = (long long)c.deleted;
+    o->sample_steps = c.sampleSteps;
+    return DSMC_OK;
+}
+
+// Checkpoint layout: magic, version, C, nAcc, nBFaces, nInflow, counters,
+// particles (SoA arrays of n), smax, rem, acc, wall, inflow accumulators.
+int dsmc_checkpoint(dsmc_handle* h, const char* path) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    const Counters c = *h->ctrHost;
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return fail(h, DSMC_ERR_IO, std::string("cannot write ") + path);
+    const long long hdr[6] = {0x44534D4347423330LL, 1, h->cs.C, h->cs.nAcc, h->cs.nBFaces,
+                              (long long)h->B.nInflowFaces * h->spec.n_species};
+    f.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
+    f.write(reinterpret_cast<const char*>(&c), sizeof(c));
+    const long long n = c.n;
+    Soa& s = cur_soa(h);
+    std::vector<char> buf;
+    auto dump = [&](const void* dptr, size_t bytes) -> int {
+        buf.resize(bytes);
+        if (bytes) CUDA_TRY(h, cudaMemcpy(buf.data(), dptr, bytes, cudaMemcpyDeviceToHost));
+        f.write(buf.data(), (std::streamsize)bytes);
+        return DSMC_OK;
+    };
+    int rc;
+    const double* d8[7] = {s.x, s.y, s.z, s.ux, s.uy, s.uz, s.erot};
+    for (int k = 0; k < 7; ++k)
+        if ((rc = dump(d8[k], sizeof(double) * n))) return rc;
+    const void* d4[4] = {s.vib, s.cellw, s.spc, s.id};
+    for (int k = 0; k < 4; ++k)
+        if ((rc = dump(d4[k], 4 * n))) return rc;
+    if ((rc = dump(h->B.start, sizeof(int) * (h->cs.C + 1)))) return rc;
+    if ((rc = dump(h->B.smax, sizeof(double) * h->cs.C))) return rc;
+    if ((rc = dump(h->B.rem, sizeof(double) * h->cs.C))) return rc;
+    if ((rc = dump(h->B.acc, sizeof(double) * h->cs.C * h->cs.nAcc))) return rc;
+    if ((rc = dump(h->B.wall, sizeof(double) * h->cs.nBFaces * W_N))) return rc;
+    if ((rc = dump(h->B.inflowAcc, sizeof(double) * hdr[5]))) return rc;
+    if (!f) return fail(h, DSMC_ERR_IO, std::string("write failed: ") + path);
+    return DSMC_OK;
+}
+
+int dsmc_restore(dsmc_handle* h, const char* path) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(h, DSMC_ERR_IO, std::string("cannot read ") + path);
+    long long hdr[6];
+    f.read(reinterpret_cast<char*>(hdr), sizeof(hdr));
+    if (!f || hdr[0] != 0x44534D4347423330LL || hdr[1] != 1 || hdr[2] != h->cs.C || hdr[3] != h->cs.nAcc ||
+        hdr[4] != h->cs.nBFaces || hdr[5] != (long long)h->B.nInflowFaces * h->spec.n_species)
+        return fail(h, DSMC_ERR_INVALID, "checkpoint does not match this case");
+    Counters c;
+    f.read(reinterpret_cast<char*>(&c), sizeof(c));
+    const long long n = c.n;
+    if (n > h->B.capacity) return fail(h, DSMC_ERR_CAPACITY, "checkpoint holds more parcels than the capacity");
+    Soa& s = cur_soa(h);
+    std::vector<char> buf;
+    auto load = [&](void* dptr, size_t bytes) -> int {
+        buf.resize(bytes);
+        f.read(buf.data(), (std::streamsize)bytes);
+        if (!f) return fail(h, DSMC_ERR_IO, "truncated checkpoint");
+        if (bytes) CUDA_TRY(h, cudaMemcpy(dptr, buf.data(), bytes, cudaMemcpyHostToDevice));
+        return DSMC_OK;
+    };
+    int rc;
+    double* d8[7] = {s.x, s.y, s.z, s.ux, s.uy, s.uz, s.erot};
+    for (int k = 0; k < 7; ++k)
+        if ((rc = load(d8[k], sizeof(double) * n))) return rc;
+    void* d4[4] = {s.vib, s.cellw, s.spc, s.id};
+    for (int k = 0; k < 4; ++k)
+        if ((rc = load(d4[k], 4 * n))) return rc;
+    if ((rc = load(h->B.start, sizeof(int) * (h->cs.C + 1)))) return rc;
+    if ((rc = load(h->B.smax, sizeof(double) * h->cs.C))) return rc;
+    if ((rc = load(h->B.rem, sizeof(double) * h->cs.C))) return rc;
+    if ((rc = load(h->B.acc, sizeof(double) * h->cs.C * h->cs.nAcc))) return rc;
+    if ((rc = load(h->B.wall, sizeof(double) * h->cs.nBFaces * W_N))) return rc;
+    if ((rc = load(h->B.inflowAcc, sizeof(double) * hdr[5]))) return rc;
+    c.err = 0;
+    *h->ctrHost = c;
+    CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemset(h->B.count, 0, sizeof(int) * h->cs.C));
+    return DSMC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,205 @@
+// dsmc_device.cuh -- device-side constants, case description, Philox stream,
+// integer-pipe floor and warp helpers shared by the dsmcFoam+ kernels.
+//
+// GB300 runs FP64 at roughly 1/57 of its FP32 rate (about 0.6 T DFMA/s
+// against 34 T FFMA/s, measured), so the per-particle kernels keep FP64
+// instructions to the state updates and do index arithmetic, comparisons and
+// random-number work on the integer pipe.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "hystrath_gb300.h"
+
+namespace dsmc {
+
+// OpenFOAM v1706 constants (physicoChemicalConstants, doubleScalar.H)
+constexpr double kB = 1.3806504e-23;
+constexpr double PI = 3.14159265358979323846;
+constexpr double SMALL = 1.0e-15;
+constexpr double VSMALL = 1.0e-300;
+constexpr double ROOTVSMALL = 1.0e-150;
+constexpr double GREAT = 1.0e15;
+
+// Bounds on the loops that the reference runs without limit.  Hitting one
+// sets an error bit that the host turns into DSMC_ERR_DEVICE.
+constexpr int MAX_CROSSINGS = 64;
+constexpr int MAX_REJECTION = 100000;
+
+// Error bits of the device error word.
+enum : unsigned {
+    ERRB_CROSSINGS = 1u, ERRB_REJECTION = 2u, ERRB_CAPACITY = 4u, ERRB_BOUNDS = 8u,
+    ERRB_PATCH = 16u
+};
+
+// Random-stream tags (counter word 3) shared with the CPU replay.
+enum : uint32_t {
+    TAG_MOVE = 1, TAG_COLLIDE = 2, TAG_INFLOW = 3, TAG_INIT_CELL = 4,
+    TAG_INIT_PARTICLE = 5, TAG_REMAINDER = 6
+};
+
+// Cell word layout: bits 0-2 sub-cell (x | y<<1 | z<<2), bits 3-30 cell,
+// bit 31 "fresh" (inserted this step: random step fraction on first move).
+constexpr uint32_t CELLW_DELETED = 0xFFFFFFFFu;
+constexpr uint32_t CELLW_FRESH = 0x80000000u;
+__host__ __device__ inline uint32_t cellw_cell(uint32_t w) { return (w & 0x7FFFFFFFu) >> 3; }
+__host__ __device__ inline uint32_t cellw_sub(uint32_t w) { return w & 7u; }
+
+struct SpeciesDev {
+    double m, d, omega, rotDof, thetaV, thetaD, zref, trefZv;
+    double kThetaV;     // kB * thetaV
+    double sqrtKoverM;  // sqrt(kB / m)
+    int nVib;
+    int pad;
+};
+
+struct PairDev {
+    double sigmaPrefactor;  // pi dPQ^2 (2 kB Tref / mR)^(omegaPQ - 1/2) / Gamma(5/2 - omegaPQ)
+    double expo;            // 1 - omegaPQ: sigma_T cR = prefactor * (cR^2)^expo
+    double omegaPQ;
+    double mR;
+    double mPfrac;          // mP / (mP + mQ)
+    double mQfrac;          // mQ / (mP + mQ)
+};
+
+struct PatchDev {
+    int type;
+    int model;
+    double Twall;
+    double Uwall[3];
+};
+
+// Everything a kernel needs about the case, passed by value (constant bank).
+struct CaseDev {
+    int n[3];
+    int nObst;
+    long long C;
+    double lo[3], hi[3], dx[3], inv[3], negOinv[3];
+    double V;
+    double FN, dt;
+    uint32_t seedLo, seedHi;
+    int nSpecies;
+    int collModel;
+    double zrot, fixedZv;
+    int invZvForm;
+    int nPatches;
+    SpeciesDev sp[DSMC_MAX_SPECIES];
+    PairDev pair[DSMC_MAX_SPECIES * DSMC_MAX_SPECIES];
+    PatchDev patch[DSMC_MAX_PATCHES];
+    int obLoI[DSMC_MAX_OBSTACLES][3], obHiI[DSMC_MAX_OBSTACLES][3];
+    double obLo[DSMC_MAX_OBSTACLES][3], obHi[DSMC_MAX_OBSTACLES][3];
+    long long sideOff[7];
+    long long obstOff[DSMC_MAX_OBSTACLES][6];
+    long long nBFaces;
+    int nAcc;           // doubles per cell of sampling accumulators
+    int hasWallMeasure;
+};
+
+// Sampling accumulators: per cell, per species s at s*SACC + k.
+enum { SACC_N = 0, SACC_UX, SACC_UY, SACC_UZ, SACC_UU, SACC_EROT, SACC_VIB, SACC };
+// per-cell collision counters after the species blocks
+enum { CACC_NCOLLS = 0, CACC_COLLSEP, CACC };
+// wall accumulators per boundary face
+enum { W_RHON = 0, W_RHOM, W_LINKE, W_MCC, W_MOMX, W_MOMY, W_MOMZ, W_EROT, W_ZETAROT, W_EVIB,
+       W_Q, W_FDX, W_FDY, W_FDZ, W_N };
+
+// Structure-of-arrays particle state.
+struct Soa {
+    double *x, *y, *z, *ux, *uy, *uz, *erot;
+    int* vib;
+    uint32_t* cellw;
+    uint32_t* spc;   // species index
+    uint32_t* id;
+};
+
+// ------------------------------------------------------------------ Philox
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): two 32x32->64
+// multiplies per round with the published multipliers and Weyl key steps.
+__device__ __forceinline__ void philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                              uint32_t k0, uint32_t k1, uint32_t out[4]) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t lo0 = 0xD2511F53u * c0;
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+        const uint32_t lo1 = 0xCD9E8D57u * c2;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+        const uint32_t n0 = hi1 ^ c1 ^ k0;
+        const uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+// (2k+1) 2^-53 for the top 52 bits k of (hi:lo); one FP64 add.
+__device__ __forceinline__ double u01_from(uint32_t lo, uint32_t hi) {
+    const unsigned long long k = ((((unsigned long long)hi) << 32) | lo) >> 12;
+    const double d = __longlong_as_double((long long)(0x3FF0000000000000ull | k));
+    return __dsub_rn(d, 1.0 - 0x1p-53);
+}
+
+struct Rng {
+    uint32_t c0, c1, blk, tag, k0, k1;
+    uint32_t b2, b3;
+    int have;
+    __device__ __forceinline__ Rng(const CaseDev& cs, uint32_t obj, uint32_t step, uint32_t t)
+        : c0(obj), c1(step), blk(0), tag(t), k0(cs.seedLo), k1(cs.seedHi), b2(0), b3(0), have(0) {}
+    __device__ __forceinline__ double u01() {
+        if (have == 0) {
+            uint32_t o[4];
+            philox4x32_10(c0, c1, blk, tag, k0, k1, o);
+            ++blk;
+            b2 = o[2]; b3 = o[3];
+            have = 1;
+            return u01_from(o[0], o[1]);
+        }
+        have = 0;
+        return u01_from(b2, b3);
+    }
+    // dsmcCloud::randomLabel (dsmcCloud.C:1015-1040), bounded redraw
+    __device__ __forceinline__ int label(int a, int b, unsigned* err) {
+        if (a == b) return a;
+        const int s = a < b ? a : b, e = a < b ? b : a;
+        for (int it = 0; it < MAX_REJECTION; ++it) {
+            const int v = s + (int)(u01() * (double)(e - s + 1));
+            if (v != e + 1) return v;
+        }
+        *err |= ERRB_REJECTION;
+        return s;
+    }
+    __device__ __forceinline__ void gauss2(double* g1, double* g2) {
+        const double u1 = u01();
+        const double u2 = u01();
+        const double r = sqrt(-2.0 * log(u1));
+        double s, c;
+        sincos(2.0 * PI * u2, &s, &c);
+        *g1 = r * c;
+        *g2 = r * s;
+    }
+};
+
+// floor(2 t) computed from the bits of t on the integer pipe.  Exact for
+// |2t| < 2^30; larger magnitudes saturate to +-2^30 (treated as outside).
+__device__ __forceinline__ int floor2_bits(double t) {
+    const long long b = __double_as_longlong(t);
+    const int e = (int)((b >> 52) & 0x7FF) - 1022;   // exponent of 2t
+    if (e < 0) return (b < 0 && (b << 1) != 0) ? -1 : 0;
+    if (e > 29) return b < 0 ? -(1 << 30) : (1 << 30);
+    const unsigned long long m = ((unsigned long long)b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+    const int sh = 52 - e;
+    const int ip = (int)(m >> sh);
+    const int frac = (m << (64 - sh)) != 0ull;
+    return b < 0 ? -(ip + frac) : ip;
+}
+
+__device__ __forceinline__ int floor2_coord(const CaseDev& cs, double x, int a) {
+    return floor2_bits(fma(x, cs.inv[a], cs.negOinv[a]));
+}
+
+__device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+}  // namespace dsmc

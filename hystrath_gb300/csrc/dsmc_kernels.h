@@ -1,0 +1,99 @@
+// dsmc_kernels.h -- host-side launchers of the dsmcFoam+ step kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "dsmc_device.cuh"
+
+namespace dsmc {
+
+// Device-resident counters of one cloud (one cache line each).
+struct Counters {
+    long long n;            // parcels in the current sorted buffer
+    long long nMoved;       // parcels in [0, nMoved) taken by move/scatter (n + inserted)
+    long long nKept;        // parcels after the last sort
+    long long step;
+    unsigned long long coll, cand;          // last step
+    unsigned long long collTot, candTot;
+    unsigned long long wallHits, inserted, deleted;
+    long long nextId;
+    long long sampleSteps;
+    unsigned err;
+    int bigCells;
+    long long inflowTotal;
+};
+
+struct StepBuffers {
+    Soa a, b;                 // current / other particle buffers
+    Soa stage;                // slot-indexed staging for cells too big for shared memory
+    int* perm;                // slot-indexed scratch for big cells
+    int* scl;
+    unsigned char* dirty;
+    int* count;               // [C]
+    int* start;               // [C+1]
+    int* blockSums;           // scan scratch
+    double* smax;             // sigmaTcRMax [C]
+    double* rem;              // collisionSelectionRemainder [C]
+    double* acc;              // sampling accumulators [C][nAcc]
+    double* wall;             // [nBFaces][W_N]
+    int* bfPatch;             // [nBFaces]
+    int* bigList;             // [C]
+    // inflow
+    int nInflowFaces;
+    long long* inflowFace;    // boundary face ids with inflow [nInflowFaces]
+    int* inflowSide;          // side of each inflow face
+    int* inflowCell;          // owner cell
+    double* inflowAcc;        // [nInflowFaces * nSpecies]
+    int* inflowCount;         // [nInflowFaces * nSpecies]
+    int* inflowOff;           // [nInflowFaces * nSpecies + 1]
+    double inflowND[DSMC_MAX_PATCHES][DSMC_MAX_SPECIES];
+    long long capacity;
+    Counters* ctr;
+};
+
+struct InflowPatchDev {
+    double nd[DSMC_MAX_SPECIES];
+    double Ttra, Trot, Tvib;
+    double U[3];
+};
+
+struct InflowDev {
+    int nPatches;
+    int pad;
+    InflowPatchDev p[DSMC_MAX_PATCHES];
+};
+
+int scan_scratch_ints(long long C);
+
+void launch_count(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st);
+void launch_move(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st);
+void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
+void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Soa& src, const Soa& dst,
+                    cudaStream_t st);
+void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
+void launch_collide_sample(const CaseDev& cs, const StepBuffers& B, const Soa& s, int doCollide,
+                           int doSample, cudaStream_t st);
+void launch_end_step(const StepBuffers& B, int sampled, cudaStream_t st);
+void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Soa& s,
+                   cudaStream_t st);
+void launch_init_count(const CaseDev& cs, const double* dnd, const unsigned char* solid, int* cellCounts,
+                       cudaStream_t st);
+void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Soa& s, const double* dnd,
+                      const unsigned char* solid, const int* cellOff, double Ttra, const double* Txyz,
+                      double Trot, double Tvib, const double* U, cudaStream_t st);
+void launch_count_n(const Soa& s, long long n, int* count, cudaStream_t st);
+void launch_zero_step(const StepBuffers& B, cudaStream_t st);
+void launch_cellw(const CaseDev& cs, const Soa& s, long long n, cudaStream_t st);
+void launch_remainder_init(const CaseDev& cs, double* rem, cudaStream_t st);
+void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* out,
+                  int measureMfp, double mfpTref, cudaStream_t st);
+void launch_info(const CaseDev& cs, const Soa& s, const Counters* ctr, double* out7,
+                 cudaStream_t st);
+
+// field selectors of launch_field
+enum {
+    F_RHON = 0, F_RHOM, F_UX, F_UY, F_UZ, F_TTRA, F_P, F_TROT, F_TVIB, F_TOV, F_NMEAN, F_NCOLLS,
+    F_MEASCR, F_MEANCR, F_MFP, F_COUNT_FIELDS
+};
+
+}  // namespace dsmc

@@ -1,0 +1,867 @@
+// dsmc_move.cu -- move, occupancy sort, inflow and mesh-fill kernels.
+//
+// move       dsmcParcel::move (src/lagrangian/dsmc/parcels/dsmcParcel.C:38-148)
+//            with the patch models it dispatches to (dsmcParcel.C:174-204):
+//            dsmcSpecularWallPatch.C:47-62, dsmcDiffuseWallPatch.C:67-138,
+//            dsmcDeletionPatch.C:140-172, particleTemplates.C:1511-1570 and the
+//            wall measurements of dsmcPatchBoundary.C:263-482.
+// sort       dsmcCloud::buildCellOccupancy (dsmcCloud.C:63-74) as a counting
+//            sort: the per-cell histogram is fused into the move (warp-
+//            aggregated atomics), an exclusive scan gives the cell starts and
+//            a scatter moves the structure-of-arrays state into cell order.
+// inflow     dsmcFreeStreamInflowPatch::controlParcelsBeforeMove
+//            (dsmcFreeStreamInflowPatch.C:91-364).
+// mesh fill  dsmcMeshFill::setInitialConfiguration (dsmcMeshFill.C:68-238).
+//
+// Compiled with -fmad=false: every FP64 operation is written out as the CPU
+// replay performs it, so positions, cells and crossings agree bit for bit.
+
+#include "dsmc_kernels.h"
+
+namespace dsmc {
+
+namespace {
+
+constexpr int MOVE_THREADS = 256;
+
+__device__ __forceinline__ double eq_rot(Rng& r, double T, double dof, unsigned* err) {
+    if (dof < SMALL) return 0.0;
+    if (dof < 2.0 + SMALL && dof > 2.0 - SMALL) return -log(r.u01()) * kB * T;
+    const double a = 0.5 * dof - 1;
+    for (int it = 0; it < MAX_REJECTION; ++it) {
+        const double ratio = 10 * r.u01();
+        const double Pr = pow(ratio / a, a) * exp(a - ratio);
+        if (!(Pr < r.u01())) return ratio * kB * T;
+    }
+    *err |= ERRB_REJECTION;
+    return 0.0;
+}
+
+__device__ __forceinline__ int eq_vib(Rng& r, double T, const SpeciesDev& s) {
+    if (s.nVib == 0) return 0;
+    return (int)(-log(r.u01()) * T / s.thetaV);
+}
+
+__device__ void wall_measure(const CaseDev& cs, double* wall, long long bf, int axis, double sgn,
+                             const double U[3], double erot, int vib, const SpeciesDev& s,
+                             bool after, double* preE, double preMom[3]) {
+    const int ax1 = (axis == 0) ? 1 : 0;
+    const int ax2 = (axis == 2) ? 1 : 2;
+    const double fA = cs.dx[ax1] * cs.dx[ax2];
+    const double Un = U[axis] * sgn;
+    double Ut[3] = {U[0], U[1], U[2]};
+    Ut[axis] = U[axis] - Un * sgn;
+    double w = fabs(Un) * fA * cs.dt;
+    w = 1.0 / (w < SMALL ? SMALL : w);
+    const double UU = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
+    const double evib = s.nVib ? vib * s.kThetaV : 0.0;
+    double* W = wall + bf * W_N;
+    atomicAdd(W + W_RHON, w);
+    atomicAdd(W + W_RHOM, s.m * w);
+    atomicAdd(W + W_LINKE, 0.5 * s.m * UU * w);
+    atomicAdd(W + W_MCC, s.m * UU * w);
+    atomicAdd(W + W_MOMX, s.m * Ut[0] * w);
+    atomicAdd(W + W_MOMY, s.m * Ut[1] * w);
+    atomicAdd(W + W_MOMZ, s.m * Ut[2] * w);
+    atomicAdd(W + W_EROT, erot * w);
+    atomicAdd(W + W_ZETAROT, s.rotDof * w);
+    atomicAdd(W + W_EVIB, evib * w);
+    const double E = 0.5 * s.m * UU + erot + evib;
+    if (!after) {
+        *preE = E;
+        for (int a = 0; a < 3; ++a) preMom[a] = s.m * U[a];
+    } else {
+        atomicAdd(W + W_Q, cs.FN * (*preE - E) / (cs.dt * fA));
+        atomicAdd(W + W_FDX, cs.FN * (preMom[0] - s.m * U[0]) / (cs.dt * fA));
+        atomicAdd(W + W_FDY, cs.FN * (preMom[1] - s.m * U[1]) / (cs.dt * fA));
+        atomicAdd(W + W_FDZ, cs.FN * (preMom[2] - s.m * U[2]) / (cs.dt * fA));
+    }
+}
+
+// dsmcDiffuseWallPatch::performDiffuseReflection for a face of outward normal
+// sgn * e_axis, with dsmcPatchBoundary::calculateWallUnitVectors.
+__device__ void diffuse_reflect(const CaseDev& cs, Rng& r, int axis, double sgn, const PatchDev& pt,
+                                const SpeciesDev& s, double U[3], double* erot, int* vib,
+                                unsigned* err) {
+    double nw[3] = {0.0, 0.0, 0.0};
+    nw[axis] = sgn;
+    double Un = U[0] * nw[0] + U[1] * nw[1] + U[2] * nw[2];
+    double Ut[3];
+    for (int a = 0; a < 3; ++a) Ut[a] = U[a] - Un * nw[a];
+    double magUt = sqrt(Ut[0] * Ut[0] + Ut[1] * Ut[1] + Ut[2] * Ut[2]);
+    int it = 0;
+    while (magUt < SMALL) {
+        if (++it > MAX_REJECTION) {
+            *err |= ERRB_REJECTION;
+            Ut[0] = Ut[1] = Ut[2] = 0.0;
+            Ut[(axis + 1) % 3] = 1.0;
+            magUt = 1.0;
+            break;
+        }
+        for (int a = 0; a < 3; ++a) U[a] = U[a] * (0.8 + 0.2 * r.u01());
+        Un = U[0] * nw[0] + U[1] * nw[1] + U[2] * nw[2];
+        for (int a = 0; a < 3; ++a) Ut[a] = U[a] - Un * nw[a];
+        magUt = sqrt(Ut[0] * Ut[0] + Ut[1] * Ut[1] + Ut[2] * Ut[2]);
+    }
+    double t1[3], t2[3];
+    for (int a = 0; a < 3; ++a) t1[a] = Ut[a] / magUt;
+    t2[0] = nw[1] * t1[2] - nw[2] * t1[1];
+    t2[1] = nw[2] * t1[0] - nw[0] * t1[2];
+    t2[2] = nw[0] * t1[1] - nw[1] * t1[0];
+    const double T = pt.Twall;
+    double g1, g2;
+    r.gauss2(&g1, &g2);
+    double om = 1 - r.u01();
+    om = om < VSMALL ? VSMALL : om;
+    const double un = sqrt(-2.0 * log(om));
+    const double sc = sqrt(kB * T / s.m);
+    for (int a = 0; a < 3; ++a) U[a] = sc * (g1 * t1[a] + g2 * t2[a] - un * nw[a]);
+    *erot = eq_rot(r, T, s.rotDof, err);
+    *vib = eq_vib(r, T, s);
+    for (int a = 0; a < 3; ++a) U[a] += pt.Uwall[a];
+}
+
+// Full Cartesian tracking of one parcel: the same steps as the CPU replay.
+// Returns the new cell word (CELLW_DELETED when removed).
+__device__ uint32_t move_slow(const CaseDev& cs, const Soa& s, long long i, uint32_t step,
+                              uint32_t w, const int* bfPatch, double* wall, unsigned* err,
+                              unsigned long long* hits) {
+    double x[3] = {s.x[i], s.y[i], s.z[i]};
+    double U[3] = {s.ux[i], s.uy[i], s.uz[i]};
+    const uint32_t pid = s.id[i];
+    const int type = (int)s.spc[i];
+    const SpeciesDev& sp = cs.sp[type];
+    double erot = 0.0;
+    int vib = 0;
+    bool internalLoaded = false;
+    bool internalChanged = false;
+    Rng r(cs, pid, step, TAG_MOVE);
+    double tr = cs.dt;
+    if (w & CELLW_FRESH) {
+        const double sf = r.u01();
+        tr = (1.0 - sf) * cs.dt;
+    }
+    int sc[3];
+    {
+        const uint32_t c = cellw_cell(w);
+        sc[0] = (int)(c % (uint32_t)cs.n[0]);
+        sc[1] = (int)((c / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]);
+        sc[2] = (int)(c / ((uint32_t)cs.n[0] * (uint32_t)cs.n[1]));
+    }
+    uint32_t result = 0;
+    bool done = false;
+    for (int it = 0; !done; ++it) {
+        if (!(tr > ROOTVSMALL)) break;
+        if (it >= MAX_CROSSINGS) { *err |= ERRB_CROSSINGS; break; }
+        double ex[3];
+        int c2[3], ci[3];
+        bool out = false;
+        for (int a = 0; a < 3; ++a) {
+            ex[a] = fma(U[a], tr, x[a]);
+            c2[a] = floor2_coord(cs, ex[a], a);
+            ci[a] = c2[a] >> 1;
+            if (ci[a] < 0 || ci[a] >= cs.n[a]) out = true;
+        }
+        bool obst = false;
+        for (int o = 0; o < cs.nObst && !obst; ++o) {
+            bool ov = true;
+            for (int a = 0; a < 3; ++a) {
+                const int mn = min(sc[a], ci[a]) - 1;
+                const int mx = max(sc[a], ci[a]) + 1;
+                if (mx < cs.obLoI[o][a] || mn > cs.obHiI[o][a] - 1) ov = false;
+            }
+            obst = ov;
+        }
+        if (!out && !obst) {
+            x[0] = ex[0]; x[1] = ex[1]; x[2] = ex[2];
+            result = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) |
+                     (uint32_t)((c2[0] & 1) | ((c2[1] & 1) << 1) | ((c2[2] & 1) << 2));
+            done = true;
+            break;
+        }
+        double tHit = GREAT * GREAT;
+        int hitKind = -1, hitSide = -1;
+        for (int a = 0; a < 3; ++a) {
+            if (ci[a] < 0) {
+                double t = (cs.lo[a] - x[a]) / U[a];
+                if (!(t >= 0.0)) t = 0.0;
+                if (t > tr) t = tr;
+                if (t < tHit) { tHit = t; hitKind = 0; hitSide = 2 * a; }
+            } else if (ci[a] >= cs.n[a]) {
+                double t = (cs.hi[a] - x[a]) / U[a];
+                if (!(t >= 0.0)) t = 0.0;
+                if (t > tr) t = tr;
+                if (t < tHit) { tHit = t; hitKind = 0; hitSide = 2 * a + 1; }
+            }
+        }
+        for (int o = 0; o < cs.nObst; ++o) {
+            double tin = -GREAT * GREAT, tout = GREAT * GREAT;
+            int ax = -1;
+            bool miss = false;
+            for (int a = 0; a < 3; ++a) {
+                if (U[a] != 0.0) {
+                    const double t1 = (cs.obLo[o][a] - x[a]) / U[a];
+                    const double t2 = (cs.obHi[o][a] - x[a]) / U[a];
+                    const double ta = dmin(t1, t2), tb = dmax(t1, t2);
+                    if (ta > tin) { tin = ta; ax = a; }
+                    if (tb < tout) tout = tb;
+                } else if (x[a] < cs.obLo[o][a] || x[a] > cs.obHi[o][a]) {
+                    miss = true;
+                }
+            }
+            if (!miss && ax >= 0 && tin >= 0.0 && tin < tout && tin <= tr && tin < tHit) {
+                tHit = tin;
+                hitKind = 1 + o;
+                hitSide = 2 * ax + (U[ax] > 0.0 ? 0 : 1);
+            }
+        }
+        if (hitKind < 0) {
+            x[0] = ex[0]; x[1] = ex[1]; x[2] = ex[2];
+            result = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) |
+                     (uint32_t)((c2[0] & 1) | ((c2[1] & 1) << 1) | ((c2[2] & 1) << 2));
+            done = true;
+            break;
+        }
+        const int axis = hitSide / 2;
+        double plane;
+        if (hitKind == 0) plane = (hitSide & 1) ? cs.hi[axis] : cs.lo[axis];
+        else plane = (hitSide & 1) ? cs.obHi[hitKind - 1][axis] : cs.obLo[hitKind - 1][axis];
+        for (int a = 0; a < 3; ++a) x[a] = (a == axis) ? plane : fma(U[a], tHit, x[a]);
+        tr = tr - tHit;
+        const int b = (axis == 0) ? 1 : 0;
+        const int c = (axis == 2) ? 1 : 2;
+        long long bf;
+        double sgn;
+        if (hitKind == 0) {
+            int ib = floor2_coord(cs, x[b], b) >> 1;
+            int ic = floor2_coord(cs, x[c], c) >> 1;
+            ib = min(max(ib, 0), cs.n[b] - 1);
+            ic = min(max(ic, 0), cs.n[c] - 1);
+            bf = cs.sideOff[hitSide] + ib + (long long)cs.n[b] * ic;
+            sgn = (hitSide & 1) ? 1.0 : -1.0;
+        } else {
+            const int o = hitKind - 1;
+            const int nb = cs.obHiI[o][b] - cs.obLoI[o][b];
+            const int nc = cs.obHiI[o][c] - cs.obLoI[o][c];
+            int ib = (floor2_coord(cs, x[b], b) >> 1) - cs.obLoI[o][b];
+            int ic = (floor2_coord(cs, x[c], c) >> 1) - cs.obLoI[o][c];
+            ib = min(max(ib, 0), nb - 1);
+            ic = min(max(ic, 0), nc - 1);
+            bf = cs.obstOff[o][hitSide] + ib + (long long)nb * ic;
+            sgn = (hitSide & 1) ? -1.0 : 1.0;
+        }
+        const int patch = bfPatch[bf];
+        if (patch < 0 || patch >= cs.nPatches) { *err |= ERRB_PATCH; result = CELLW_DELETED; done = true; break; }
+        const PatchDev& pt = cs.patch[patch];
+        if (pt.type == DSMC_PATCH_SYMMETRY) {
+            U[axis] = -U[axis];
+        } else if (pt.type == DSMC_PATCH_CYCLIC) {
+            if (hitKind == 0) x[axis] = (hitSide & 1) ? cs.lo[axis] : cs.hi[axis];
+        } else if (pt.model == DSMC_BC_SPECULAR || pt.model == DSMC_BC_DIFFUSE) {
+            if (!internalLoaded) {
+                erot = s.erot[i];
+                vib = s.vib[i];
+                internalLoaded = true;
+            }
+            double preE, preM[3];
+            if (cs.hasWallMeasure)
+                wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, false, &preE, preM);
+            if (pt.model == DSMC_BC_SPECULAR) {
+                if (U[axis] * sgn > 0.0) U[axis] = -U[axis];
+            } else {
+                diffuse_reflect(cs, r, axis, sgn, pt, sp, U, &erot, &vib, err);
+                internalChanged = true;
+            }
+            if (cs.hasWallMeasure)
+                wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, true, &preE, preM);
+            atomicAdd(hits, 1ull);
+        } else {
+            // deletion (and any patch without a model) removes the parcel
+            result = CELLW_DELETED;
+            done = true;
+            break;
+        }
+        for (int a = 0; a < 3; ++a) {
+            int cc = floor2_coord(cs, x[a], a) >> 1;
+            sc[a] = min(max(cc, 0), cs.n[a] - 1);
+        }
+    }
+    if (!done) {
+        int ci[3], sb = 0;
+        for (int a = 0; a < 3; ++a) {
+            int c2 = floor2_coord(cs, x[a], a);
+            c2 = min(max(c2, 0), 2 * cs.n[a] - 1);
+            ci[a] = c2 >> 1;
+            sb |= (c2 & 1) << a;
+        }
+        result = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) | (uint32_t)sb;
+    }
+    s.x[i] = x[0]; s.y[i] = x[1]; s.z[i] = x[2];
+    s.ux[i] = U[0]; s.uy[i] = U[1]; s.uz[i] = U[2];
+    if (internalChanged) {
+        s.erot[i] = erot;
+        s.vib[i] = vib;
+    }
+    return result;
+}
+
+// Warp-aggregated histogram increment for a key (or -1 for none).
+__device__ __forceinline__ void agg_count(int* count, int key) {
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+    const int leader = __ffs(peers) - 1;
+    if (key >= 0 && (int)lane_id() == leader) atomicAdd(&count[key], __popc(peers));
+}
+
+__global__ void __launch_bounds__(MOVE_THREADS)
+k_move(CaseDev cs, Soa s, Counters* ctr, const int* __restrict__ bfPatch, double* wall, int* count) {
+    const long long n = ctr->nMoved;
+    const uint32_t step = (uint32_t)ctr->step;
+    unsigned err = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const long long i = base + threadIdx.x;
+        int key = -1;
+        if (i < n) {
+            const uint32_t w = s.cellw[i];
+            bool fast = false;
+            if (!(w & CELLW_FRESH)) {
+                const double x = s.x[i], y = s.y[i], z = s.z[i];
+                const double ux = s.ux[i], uy = s.uy[i], uz = s.uz[i];
+                const double ex = fma(ux, cs.dt, x);
+                const double ey = fma(uy, cs.dt, y);
+                const double ez = fma(uz, cs.dt, z);
+                const int c2x = floor2_coord(cs, ex, 0);
+                const int c2y = floor2_coord(cs, ey, 1);
+                const int c2z = floor2_coord(cs, ez, 2);
+                const int cx = c2x >> 1, cy = c2y >> 1, cz = c2z >> 1;
+                bool inside = (unsigned)cx < (unsigned)cs.n[0] && (unsigned)cy < (unsigned)cs.n[1] &&
+                              (unsigned)cz < (unsigned)cs.n[2];
+                if (inside && cs.nObst) {
+                    const uint32_t c = cellw_cell(w);
+                    const int sx = (int)(c % (uint32_t)cs.n[0]);
+                    const int sy = (int)((c / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]);
+                    const int sz = (int)(c / ((uint32_t)cs.n[0] * (uint32_t)cs.n[1]));
+                    for (int o = 0; o < cs.nObst; ++o) {
+                        if (max(sx, cx) + 1 >= cs.obLoI[o][0] && min(sx, cx) - 1 <= cs.obHiI[o][0] - 1 &&
+                            max(sy, cy) + 1 >= cs.obLoI[o][1] && min(sy, cy) - 1 <= cs.obHiI[o][1] - 1 &&
+                            max(sz, cz) + 1 >= cs.obLoI[o][2] && min(sz, cz) - 1 <= cs.obHiI[o][2] - 1)
+                            inside = false;
+                    }
+                }
+                if (inside) {
+                    s.x[i] = ex; s.y[i] = ey; s.z[i] = ez;
+                    const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
+                                        (uint32_t)((c2x & 1) | ((c2y & 1) << 1) | ((c2z & 1) << 2));
+                    s.cellw[i] = nw;
+                    key = (int)(nw >> 3);
+                    fast = true;
+                }
+            }
+            if (!fast) {
+                const uint32_t nw = move_slow(cs, s, i, step, w, bfPatch, wall, &err, &ctr->wallHits);
+                s.cellw[i] = nw;
+                key = (nw == CELLW_DELETED) ? -1 : (int)(nw >> 3);
+            }
+        }
+        agg_count(count, key);
+    }
+    if (err) atomicOr(&ctr->err, err);
+}
+
+__global__ void k_count(Soa s, long long n, int* count) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const long long i = base + threadIdx.x;
+        int key = -1;
+        if (i < n) {
+            const uint32_t w = s.cellw[i];
+            key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
+        }
+        agg_count(count, key);
+    }
+}
+
+__global__ void k_count_dev(Soa s, const Counters* ctr, int* count) {
+    const long long n = ctr->nMoved;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const long long i = base + threadIdx.x;
+        int key = -1;
+        if (i < n) {
+            const uint32_t w = s.cellw[i];
+            key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
+        }
+        agg_count(count, key);
+    }
+}
+
+// ---------------------------------------------------------------- scan
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* total) {
+    __shared__ int warpSums[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warpSums[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int ws = (lane < (int)(blockDim.x >> 5)) ? warpSums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, ws, o);
+            if (lane >= o) ws += y;
+        }
+        warpSums[lane] = ws;
+    }
+    __syncthreads();
+    const int warpOff = wid ? warpSums[wid - 1] : 0;
+    *total = warpSums[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return warpOff + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_reduce(const int* __restrict__ count, long long C, int* blockSums) {
+    const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k)
+        if (base + k < C) s += count[base + k];
+    int total;
+    block_exclusive_scan(s, &total);
+    if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_top(int* blockSums, int nb, int* start, long long C,
+                                                           Counters* ctr) {
+    int carry = 0;
+    for (int b0 = 0; b0 < nb; b0 += SCAN_THREADS) {
+        const int b = b0 + threadIdx.x;
+        const int v = (b < nb) ? blockSums[b] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, &total);
+        if (b < nb) blockSums[b] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        start[C] = carry;
+        ctr->nKept = carry;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restrict__ count, long long C,
+                                                            const int* __restrict__ blockSums, int* start) {
+    const long long base = (long long)blockIdx.x * SCAN_TILE + (long long)threadIdx.x * SCAN_ITEMS;
+    int v[SCAN_ITEMS];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        v[k] = (base + k < C) ? count[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int ex = block_exclusive_scan(s, &total) + blockSums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        if (base + k < C) start[base + k] = ex;
+        ex += v[k];
+    }
+}
+
+// ---------------------------------------------------------------- scatter
+__global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, const Counters* ctr,
+                                                 const int* __restrict__ start, int* count) {
+    const long long n = ctr->nMoved;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    const unsigned lane = lane_id();
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const long long i = base + threadIdx.x;
+        int key = -1;
+        uint32_t w = CELLW_DELETED;
+        if (i < n) {
+            w = src.cellw[i];
+            key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
+        }
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+        const int leader = __ffs(peers) - 1;
+        int old = 0;
+        if (key >= 0 && (int)lane == leader) old = atomicSub(&count[key], __popc(peers));
+        old = __shfl_sync(0xFFFFFFFFu, old, leader);
+        if (key >= 0) {
+            const int rank = __popc(peers & ((1u << lane) - 1u));
+            const long long slot = (long long)start[key] + old - 1 - rank;
+            dst.x[slot] = src.x[i];
+            dst.y[slot] = src.y[i];
+            dst.z[slot] = src.z[i];
+            dst.ux[slot] = src.ux[i];
+            dst.uy[slot] = src.uy[i];
+            dst.uz[slot] = src.uz[i];
+            dst.erot[slot] = src.erot[i];
+            dst.vib[slot] = src.vib[i];
+            dst.cellw[slot] = w;
+            dst.spc[slot] = src.spc[i];
+            dst.id[slot] = src.id[i];
+        }
+    }
+}
+
+__global__ void k_finish_sort(Counters* ctr) {
+    ctr->deleted += (unsigned long long)(ctr->nMoved - ctr->nKept);
+    ctr->n = ctr->nKept;
+    ctr->nMoved = ctr->nKept;
+}
+
+__global__ void k_end_step(Counters* ctr, int sampled) {
+    ctr->collTot += ctr->coll;
+    ctr->candTot += ctr->cand;
+    ctr->bigCells = 0;
+    ctr->step += 1;
+    if (sampled) ctr->sampleSteps += 1;
+}
+
+// ---------------------------------------------------------------- inflow
+// One thread per (inflow face, species): Bird eq. 4.22 flux accumulation and
+// the integer-plus-remainder count (dsmcFreeStreamInflowPatch.C:96-141,226-236).
+__global__ void k_inflow_count(CaseDev cs, InflowDev in, int nFaces, const long long* __restrict__ face,
+                               const int* __restrict__ side, const int* __restrict__ bfPatch,
+                               double* accum, int* cnt, const Counters* ctr) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ns = cs.nSpecies;
+    if (t >= nFaces * ns) return;
+    const int f = t / ns, m = t % ns;
+    const long long bf = face[f];
+    const int sd = side[f];
+    const int a = sd / 2;
+    const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+    const double sgnOut = (sd & 1) ? 1.0 : -1.0;
+    const InflowPatchDev& pt = in.p[bfPatch[bf]];
+    const double nd = pt.nd[m];
+    int nI = 0;
+    if (nd > 0) {
+        const SpeciesDev& s = cs.sp[m];
+        const double fA = cs.dx[b] * cs.dx[c];
+        const double cmp = sqrt(2.0 * kB * pt.Ttra / s.m);
+        const double sCos = (pt.U[a] * (-sgnOut)) / cmp;
+        const double sqrtPi = sqrt(PI);
+        double A = accum[t];
+        A += (fA * nd * cs.dt * cmp * (exp(-sCos * sCos) + sqrtPi * sCos * (1 + erf(sCos)))) /
+             (2.0 * sqrtPi * cs.FN);
+        Rng r(cs, (uint32_t)bf, (uint32_t)ctr->step, TAG_INFLOW | ((uint32_t)m << 8));
+        nI = (int)A;
+        if (nI < 0) nI = 0;
+        if ((A - nI) > r.u01()) nI++;
+        A -= nI;
+        accum[t] = A;
+    }
+    cnt[t] = nI;
+}
+
+__global__ void k_inflow_scan(const int* cnt, int n, int* off, Counters* ctr, long long capacity) {
+    // single block
+    int carry = 0;
+    for (int b0 = 0; b0 < n; b0 += blockDim.x) {
+        const int b = b0 + threadIdx.x;
+        const int v = (b < n) ? cnt[b] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, &total);
+        if (b < n) off[b] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) {
+        off[n] = carry;
+        if (ctr->n + carry > capacity) {
+            atomicOr(&ctr->err, ERRB_CAPACITY);
+            off[n] = -1;
+            ctr->inflowTotal = 0;
+        } else {
+            ctr->inflowTotal = carry;
+        }
+    }
+}
+
+__global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long long* __restrict__ face,
+                              const int* __restrict__ side, const int* __restrict__ cellOf,
+                              const int* __restrict__ bfPatch, const int* __restrict__ cnt,
+                              const int* __restrict__ off, Soa s, Counters* ctr) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ns = cs.nSpecies;
+    if (off[nFaces * ns] < 0) return;     // capacity exceeded: nothing inserted
+    if (t < nFaces * ns) {
+        const int nI = cnt[t];
+        if (nI > 0) {
+            unsigned err = 0;
+            const int f = t / ns, m = t % ns;
+            const long long bf = face[f];
+            const int sd = side[f];
+            const int a = sd / 2;
+            const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+            const double sgnOut = (sd & 1) ? 1.0 : -1.0;
+            const InflowPatchDev& pt = in.p[bfPatch[bf]];
+            const SpeciesDev& sp = cs.sp[m];
+            const double cmp = sqrt(2.0 * kB * pt.Ttra / sp.m);
+            const double sCos = (pt.U[a] * (-sgnOut)) / cmp;
+            const double coeffA = sCos + sqrt(sCos * sCos + 2.0);
+            const double coeffB = 0.5 * (1.0 + sCos * (sCos - sqrt(sCos * sCos + 2.0)));
+            double scaling = 3.0;
+            if (sCos < -3) scaling = fabs(sCos) + 1;
+            const long long fl = bf - cs.sideOff[sd];
+            const long long ib = fl % cs.n[b], ic = fl / cs.n[b];
+            const double lob = cs.lo[b] + (double)ib * cs.dx[b];
+            const double loc = cs.lo[c] + (double)ic * cs.dx[c];
+            const int cell = cellOf[f];
+            const double scT = sqrt(kB * pt.Ttra / sp.m);
+            Rng r(cs, (uint32_t)bf, (uint32_t)ctr->step, TAG_INFLOW | ((uint32_t)m << 8));
+            (void)r.u01();   // the remainder draw of k_inflow_count
+            const long long base = ctr->n + off[t];
+            const long long id0 = ctr->nextId + off[t];
+            for (int q = 0; q < nI; ++q) {
+                double x[3], U[3];
+                x[a] = (sd & 1) ? cs.hi[a] : cs.lo[a];
+                x[b] = fma(r.u01(), cs.dx[b], lob);
+                x[c] = fma(r.u01(), cs.dx[c], loc);
+                double uNormal = 0;
+                if (fabs(pt.U[a]) > VSMALL) {
+                    int it = 0;
+                    for (;;) {
+                        const double uth = scaling * (2.0 * r.u01() - 1);
+                        uNormal = uth + sCos;
+                        double Pr;
+                        if (uNormal < 0.0) Pr = -1;
+                        else Pr = 2.0 * uNormal / coeffA * exp(coeffB - uth * uth);
+                        if (!(Pr < r.u01())) break;
+                        if (++it >= MAX_REJECTION) { err |= ERRB_REJECTION; break; }
+                    }
+                } else {
+                    uNormal = sqrt(-log(r.u01()));
+                }
+                double g1, g2;
+                r.gauss2(&g1, &g2);
+                U[a] = cmp * uNormal * (-sgnOut);
+                U[b] = scT * g1 + pt.U[b];
+                U[c] = scT * g2 + pt.U[c];
+                const double erot = eq_rot(r, pt.Trot, sp.rotDof, &err);
+                const int vib = eq_vib(r, pt.Tvib, sp);
+                const long long slot = base + q;
+                s.x[slot] = x[0]; s.y[slot] = x[1]; s.z[slot] = x[2];
+                s.ux[slot] = U[0]; s.uy[slot] = U[1]; s.uz[slot] = U[2];
+                s.erot[slot] = erot;
+                s.vib[slot] = vib;
+                s.cellw[slot] = ((uint32_t)cell << 3) | CELLW_FRESH;
+                s.spc[slot] = (uint32_t)m;
+                s.id[slot] = (uint32_t)(id0 + q);
+            }
+            if (err) atomicOr(&ctr->err, err);
+        }
+    }
+}
+
+__global__ void k_inflow_commit(Counters* ctr) {
+    const long long add = ctr->inflowTotal;
+    ctr->inserted = (unsigned long long)add;
+    ctr->nextId += add;
+    ctr->nMoved = ctr->n + add;
+}
+
+// ---------------------------------------------------------------- mesh fill
+// Per cell: 12 equal sub-volumes (the tets of a hex) each get
+// floor(n V/12 / FN) parcels plus one with the remainder probability.
+__global__ void k_init_count(CaseDev cs, const double* __restrict__ nd, const unsigned char* __restrict__ solid,
+                             int* cellCounts) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cs.C) return;
+    int total = 0;
+    if (!solid[c]) {
+        Rng r(cs, (uint32_t)c, 0, TAG_INIT_CELL);
+        for (int tet = 0; tet < 12; ++tet) {
+            for (int m = 0; m < cs.nSpecies; ++m) {
+                if (!(nd[m] > 0)) continue;
+                const double req = nd[m] * (cs.V / 12.0) / cs.FN;
+                int k = (int)req;
+                if ((req - k) > r.u01()) k++;
+                total += k;
+            }
+        }
+    }
+    cellCounts[c] = total;
+}
+
+// Per-species counts again (same draws) so that parcels come out grouped by
+// species inside a cell, in the replay's order.
+__global__ void k_init_fill(CaseDev cs, const double* __restrict__ nd, const unsigned char* __restrict__ solid,
+                            const int* __restrict__ cellOff, Soa s, double Ttra, double Tx, double Ty, double Tz,
+                            double Trot, double Tvib, double U0, double U1, double U2, Counters* ctr) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cs.C || solid[c]) return;
+    int per[DSMC_MAX_SPECIES];
+    for (int m = 0; m < DSMC_MAX_SPECIES; ++m) per[m] = 0;
+    {
+        Rng r(cs, (uint32_t)c, 0, TAG_INIT_CELL);
+        for (int tet = 0; tet < 12; ++tet) {
+            for (int m = 0; m < cs.nSpecies; ++m) {
+                if (!(nd[m] > 0)) continue;
+                const double req = nd[m] * (cs.V / 12.0) / cs.FN;
+                int k = (int)req;
+                if ((req - k) > r.u01()) k++;
+                per[m] += k;
+            }
+        }
+    }
+    const int i0 = (int)(c % cs.n[0]);
+    const int j0 = (int)((c / cs.n[0]) % cs.n[1]);
+    const int k0 = (int)(c / ((long long)cs.n[0] * cs.n[1]));
+    const double cl[3] = {cs.lo[0] + i0 * cs.dx[0], cs.lo[1] + j0 * cs.dx[1], cs.lo[2] + k0 * cs.dx[2]};
+    const double Ta[3] = {Tx > 0 ? Tx : Ttra, Ty > 0 ? Ty : Ttra, Tz > 0 ? Tz : Ttra};
+    const double Ub[3] = {U0, U1, U2};
+    long long slot = cellOff[c];
+    unsigned err = 0;
+    for (int m = 0; m < cs.nSpecies; ++m) {
+        const SpeciesDev& sp = cs.sp[m];
+        for (int q = 0; q < per[m]; ++q, ++slot) {
+            const uint32_t pid = (uint32_t)slot;
+            Rng r(cs, pid, 0, TAG_INIT_PARTICLE);
+            double x[3];
+            for (int a = 0; a < 3; ++a) x[a] = fma(r.u01(), cs.dx[a], cl[a]);
+            double g[4];
+            r.gauss2(&g[0], &g[1]);
+            r.gauss2(&g[2], &g[3]);
+            double U[3];
+            for (int a = 0; a < 3; ++a) U[a] = sqrt(kB * Ta[a] / sp.m) * g[a] + Ub[a];
+            const double erot = eq_rot(r, Trot, sp.rotDof, &err);
+            const int vib = eq_vib(r, Tvib, sp);
+            int sb = 0, ci[3];
+            for (int a = 0; a < 3; ++a) {
+                int c2 = floor2_coord(cs, x[a], a);
+                c2 = min(max(c2, 0), 2 * cs.n[a] - 1);
+                ci[a] = c2 >> 1;
+                sb |= (c2 & 1) << a;
+            }
+            s.x[slot] = x[0]; s.y[slot] = x[1]; s.z[slot] = x[2];
+            s.ux[slot] = U[0]; s.uy[slot] = U[1]; s.uz[slot] = U[2];
+            s.erot[slot] = erot;
+            s.vib[slot] = vib;
+            s.cellw[slot] = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) | (uint32_t)sb;
+            s.spc[slot] = (uint32_t)m;
+            s.id[slot] = pid;
+        }
+    }
+    if (err) atomicOr(&ctr->err, err);
+}
+
+__global__ void k_cellw(CaseDev cs, Soa s, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double x[3] = {s.x[i], s.y[i], s.z[i]};
+    int sb = 0, ci[3];
+    for (int a = 0; a < 3; ++a) {
+        int c2 = floor2_coord(cs, x[a], a);
+        c2 = min(max(c2, 0), 2 * cs.n[a] - 1);
+        ci[a] = c2 >> 1;
+        sb |= (c2 & 1) << a;
+    }
+    const uint32_t fresh = s.cellw[i] & CELLW_FRESH;
+    s.cellw[i] = (((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) | (uint32_t)sb) | fresh;
+}
+
+__global__ void k_remainder_init(CaseDev cs, double* rem) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cs.C) return;
+    Rng r(cs, (uint32_t)c, 0, TAG_REMAINDER);
+    rem[c] = r.u01();
+}
+
+int grid_for(long long n, int threads, int perSmBlocks) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long need = (n + threads - 1) / threads;
+    const long long cap = (long long)sms * perSmBlocks;
+    long long g = need < cap ? need : cap;
+    return (int)(g < 1 ? 1 : g);
+}
+
+}  // namespace
+
+int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TILE) + 1; }
+
+void launch_move(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
+    const int grid = grid_for(B.capacity, MOVE_THREADS, 8);
+    k_move<<<grid, MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.bfPatch, B.wall, B.count);
+}
+
+void launch_count(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
+    (void)cs;
+    const int grid = grid_for(B.capacity, 256, 8);
+    k_count_dev<<<grid, 256, 0, st>>>(s, B.ctr, B.count);
+}
+
+void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st) {
+    const int nb = (int)((cs.C + SCAN_TILE - 1) / SCAN_TILE);
+    k_scan_reduce<<<nb, SCAN_THREADS, 0, st>>>(B.count, cs.C, B.blockSums);
+    k_scan_top<<<1, SCAN_THREADS, 0, st>>>(B.blockSums, nb, B.start, cs.C, B.ctr);
+    k_scan_down<<<nb, SCAN_THREADS, 0, st>>>(B.count, cs.C, B.blockSums, B.start);
+}
+
+void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Soa& src, const Soa& dst,
+                    cudaStream_t st) {
+    (void)cs;
+    const int grid = grid_for(B.capacity, 256, 8);
+    k_scatter<<<grid, 256, 0, st>>>(src, dst, B.ctr, B.start, B.count);
+}
+
+void launch_finish_sort(const StepBuffers& B, cudaStream_t st) {
+    k_finish_sort<<<1, 1, 0, st>>>(B.ctr);
+}
+
+void launch_end_step(const StepBuffers& B, int sampled, cudaStream_t st) {
+    k_end_step<<<1, 1, 0, st>>>(B.ctr, sampled);
+}
+
+void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Soa& s,
+                   cudaStream_t st) {
+    const int nt = B.nInflowFaces * cs.nSpecies;
+    if (nt == 0) return;
+    const int grid = (nt + 255) / 256;
+    k_inflow_count<<<grid, 256, 0, st>>>(cs, in, B.nInflowFaces, B.inflowFace, B.inflowSide, B.bfPatch,
+                                         B.inflowAcc, B.inflowCount, B.ctr);
+    k_inflow_scan<<<1, 1024, 0, st>>>(B.inflowCount, nt, B.inflowOff, B.ctr, B.capacity);
+    k_inflow_fill<<<grid, 256, 0, st>>>(cs, in, B.nInflowFaces, B.inflowFace, B.inflowSide, B.inflowCell,
+                                        B.bfPatch, B.inflowCount, B.inflowOff, s, B.ctr);
+    k_inflow_commit<<<1, 1, 0, st>>>(B.ctr);
+}
+
+void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Soa& s, const double* dnd,
+                      const unsigned char* solid, const int* cellOff, double Ttra, const double* Txyz,
+                      double Trot, double Tvib, const double* U, cudaStream_t st) {
+    const int grid = (int)((cs.C + 127) / 128);
+    k_init_fill<<<grid, 128, 0, st>>>(cs, dnd, solid, cellOff, s, Ttra, Txyz[0], Txyz[1], Txyz[2], Trot,
+                                      Tvib, U[0], U[1], U[2], B.ctr);
+}
+
+void launch_init_count(const CaseDev& cs, const double* dnd, const unsigned char* solid, int* cellCounts,
+                       cudaStream_t st) {
+    const int grid = (int)((cs.C + 255) / 256);
+    k_init_count<<<grid, 256, 0, st>>>(cs, dnd, solid, cellCounts);
+}
+
+void launch_cellw(const CaseDev& cs, const Soa& s, long long n, cudaStream_t st) {
+    if (n <= 0) return;
+    k_cellw<<<(int)((n + 255) / 256), 256, 0, st>>>(cs, s, n);
+}
+
+void launch_count_n(const Soa& s, long long n, int* count, cudaStream_t st) {
+    if (n <= 0) return;
+    const int grid = grid_for(n, 256, 8);
+    k_count<<<grid, 256, 0, st>>>(s, n, count);
+}
+
+void launch_remainder_init(const CaseDev& cs, double* rem, cudaStream_t st) {
+    k_remainder_init<<<(int)((cs.C + 255) / 256), 256, 0, st>>>(cs, rem);
+}
+
+}  // namespace dsmc

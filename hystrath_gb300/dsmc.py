@@ -1,0 +1,197 @@
+"""Python face of the GB300 dsmcFoam+ hot path, over the C ABI.
+
+``DsmcCloud`` mirrors the calls the dsmcFoam+ driver makes on a dsmcCloud
+(applications/solvers/discreteMethods/dsmc/dsmcFoam+/dsmcFoam+.C:92-180):
+construct from a case, ``evolve()`` once per time step, ``info()``, field
+output.  Every call goes to libhystrath_gb300.so; there is no CPU path, and a
+missing library or GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import spec as S
+
+_lib = None
+
+
+def _load() -> C.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    from . import build as _build
+    path = _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA library first (python -m hystrath_gb300.build)")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.dsmc_spec_defaults.argtypes = [C.POINTER(S.CaseSpec)]
+    L.dsmc_create_from_spec.argtypes = [C.POINTER(S.CaseSpec), C.POINTER(vp)]
+    L.dsmc_create.argtypes = [C.c_char_p, C.POINTER(vp)]
+    L.dsmc_parse_case.argtypes = [C.c_char_p, C.POINTER(S.CaseSpec)]
+    L.dsmc_initialise.argtypes = [vp]
+    L.dsmc_evolve.argtypes = [vp, C.c_longlong]
+    L.dsmc_run_phases.argtypes = [vp, C.c_uint]
+    L.dsmc_set_particles.argtypes = [vp, C.c_longlong, vp, vp, vp, vp, vp, vp]
+    L.dsmc_get_particles.argtypes = [vp, C.c_longlong, C.POINTER(C.c_longlong), vp, vp, vp, vp, vp, vp, vp]
+    L.dsmc_get_cell_array.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+    L.dsmc_set_cell_array.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+    L.dsmc_get_field.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+    L.dsmc_get_wall_field.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+    L.dsmc_n_boundary_faces.argtypes = [vp]
+    L.dsmc_n_boundary_faces.restype = C.c_longlong
+    L.dsmc_reset_sampling.argtypes = [vp]
+    L.dsmc_info.argtypes = [vp, C.POINTER(S.Info)]
+    L.dsmc_checkpoint.argtypes = [vp, C.c_char_p]
+    L.dsmc_restore.argtypes = [vp, C.c_char_p]
+    L.dsmc_phase_times.argtypes = [vp] + [C.POINTER(C.c_double)] * 5
+    L.dsmc_last_error.argtypes = [vp]
+    L.dsmc_last_error.restype = C.c_char_p
+    L.dsmc_last_global_error.restype = C.c_char_p
+    L.dsmc_destroy.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def lib() -> C.CDLL:
+    return _load()
+
+
+class DsmcError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[dsmc status {code}] {msg}")
+        self.code = code
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def parse_case(case_dir: str) -> S.CaseSpec:
+    """Resolve an OpenFOAM dsmcFoam+ case directory into a CaseSpec."""
+    s = S.CaseSpec()
+    rc = lib().dsmc_parse_case(case_dir.encode(), C.byref(s))
+    if rc != 0:
+        raise DsmcError(rc, lib().dsmc_last_global_error().decode())
+    return s
+
+
+class DsmcCloud:
+    """One DSMC cloud resident on the GPU (the dsmcCloud of dsmcFoam+)."""
+
+    def __init__(self, spec: S.CaseSpec | str):
+        L = lib()
+        h = C.c_void_p()
+        if isinstance(spec, str):
+            rc = L.dsmc_create(spec.encode(), C.byref(h))
+            self.spec = parse_case(spec) if rc == 0 else None
+        else:
+            rc = L.dsmc_create_from_spec(C.byref(spec), C.byref(h))
+            self.spec = spec
+        if rc != 0:
+            raise DsmcError(rc, L.dsmc_last_global_error().decode())
+        self.h = h
+        s = self.spec
+        self.n_cells = s.n_cells[0] * s.n_cells[1] * s.n_cells[2]
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dsmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise DsmcError(rc, lib().dsmc_last_error(self.h).decode())
+
+    # dsmcInitialise+ / dsmcMeshFill
+    def initialise(self):
+        self._chk(lib().dsmc_initialise(self.h))
+
+    # dsmcCloud::evolve, n times
+    def evolve(self, n: int = 1):
+        self._chk(lib().dsmc_evolve(self.h, n))
+
+    def run_phases(self, phases: int):
+        self._chk(lib().dsmc_run_phases(self.h, phases))
+
+    def phase_times(self):
+        v = [C.c_double() for _ in range(5)]
+        self._chk(lib().dsmc_phase_times(self.h, *[C.byref(x) for x in v]))
+        return dict(zip(("inflow", "move", "sort", "collide_sample", "end"), [x.value for x in v]))
+
+    def set_particles(self, pos, U, erot=None, vib=None, species=None, ids=None):
+        n = len(pos)
+        pos = np.ascontiguousarray(pos, dtype=np.float64)
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        erot = None if erot is None else np.ascontiguousarray(erot, dtype=np.float64)
+        vib = None if vib is None else np.ascontiguousarray(vib, dtype=np.int32)
+        species = None if species is None else np.ascontiguousarray(species, dtype=np.int32)
+        ids = np.arange(n, dtype=np.uint32) if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+        self._chk(lib().dsmc_set_particles(self.h, n, _p(pos), _p(U), _p(erot), _p(vib), _p(species), _p(ids)))
+
+    def n_particles(self) -> int:
+        return self.info().n_particles
+
+    def particles(self):
+        n = self.n_particles()
+        out = dict(pos=np.empty((n, 3)), U=np.empty((n, 3)), erot=np.empty(n),
+                   vib=np.empty(n, np.int32), species=np.empty(n, np.int32),
+                   id=np.empty(n, np.uint32), cell=np.empty(n, np.int32))
+        nn = C.c_longlong()
+        self._chk(lib().dsmc_get_particles(self.h, n, C.byref(nn), _p(out["pos"]), _p(out["U"]),
+                                           _p(out["erot"]), _p(out["vib"]), _p(out["species"]),
+                                           _p(out["id"]), _p(out["cell"])))
+        return out
+
+    def cell_array(self, name: str):
+        if name in ("count", "start"):
+            a = np.empty(self.n_cells, np.int32)
+        elif name == "accumulators":
+            n_acc = self.spec.n_species * 7 + 2
+            a = np.empty(self.n_cells * n_acc)
+        else:
+            a = np.empty(self.n_cells)
+        self._chk(lib().dsmc_get_cell_array(self.h, name.encode(), _p(a), a.size))
+        return a
+
+    def set_cell_array(self, name: str, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        self._chk(lib().dsmc_set_cell_array(self.h, name.encode(), _p(a), a.size))
+
+    def field(self, name: str):
+        a = np.empty(self.n_cells)
+        self._chk(lib().dsmc_get_field(self.h, name.encode(), _p(a), a.size))
+        return a
+
+    def wall_accumulators(self):
+        nf = lib().dsmc_n_boundary_faces(self.h)
+        a = np.empty((nf, 14))
+        self._chk(lib().dsmc_get_wall_field(self.h, b"wallAccumulators", _p(a), a.size))
+        return a
+
+    def wall_field(self, name: str):
+        nf = lib().dsmc_n_boundary_faces(self.h)
+        a = np.empty(nf)
+        self._chk(lib().dsmc_get_wall_field(self.h, name.encode(), _p(a), a.size))
+        return a
+
+    def reset_sampling(self):
+        self._chk(lib().dsmc_reset_sampling(self.h))
+
+    def info(self) -> S.Info:
+        i = S.Info()
+        self._chk(lib().dsmc_info(self.h, C.byref(i)))
+        return i
+
+    def checkpoint(self, path: str):
+        self._chk(lib().dsmc_checkpoint(self.h, path.encode()))
+
+    def restore(self, path: str):
+        self._chk(lib().dsmc_restore(self.h, path.encode()))

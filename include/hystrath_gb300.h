@@ -1,0 +1,265 @@
+/*
+ * hystrath_gb300.h -- C ABI of the GB300-native dsmcFoam+ particle hot path.
+ *
+ * One handle owns one DSMC cloud on one GPU: its structure-of-arrays particle
+ * state in HBM, per-cell collision and sampling state, the stream it runs on
+ * and its captured step graph.  The entry points replace the calls that the
+ * dsmcFoam+ driver makes on a dsmcCloud:
+ *
+ *   reference (path in hystrath/hyStrath)                         this ABI
+ *   dsmcCloud ctor  src/lagrangian/dsmc/clouds/dsmcCloud.C:586-691  dsmc_create / dsmc_create_from_spec
+ *   dsmcMeshFill    src/lagrangian/dsmc/initialiseDsmcParcels/
+ *                   derived/dsmcMeshFill/dsmcMeshFill.C:68-238      dsmc_initialise
+ *   dsmcCloud::evolve  dsmcCloud.C:819-902                         dsmc_evolve
+ *   dsmcCloud::info    dsmcCloud.C:935-985                         dsmc_info
+ *   dsmcVolFields::calculateField (output part)
+ *                   src/lagrangian/dsmc/macroscopicProperties/derived/
+ *                   combined/dsmcVolFields/dsmcVolFields.C:1365-1876 dsmc_get_field
+ *   lagrangian/dsmc parcel IO    src/lagrangian/dsmc/parcels/
+ *                   dsmcParcelIO.C:133-450                          dsmc_get_particles / dsmc_set_particles
+ *   sigmaTcRMax field (MUST_READ/AUTO_WRITE) dsmcCloud.C:625-636     dsmc_get_cell_array / dsmc_set_cell_array
+ *   runtime selection New() of BinaryCollisionModel
+ *                   (collisions/BinaryCollisionModel/.../BinaryCollisionModel.C:59-90),
+ *                   collisionPartnerSelection (collisionPartnerSelection.C:64-97),
+ *                   dsmcPatchBoundary (dsmcPatchBoundary.C:130-165)  the model fields of dsmc_case_spec,
+ *                                                                   resolved by name in dsmc_create
+ *
+ * Every call returns a status (DSMC_OK == 0).  The reference aborts with
+ * FatalError instead; here the message is kept per handle (dsmc_last_error) or
+ * per thread when no handle exists yet (dsmc_last_global_error).  A handle is
+ * not thread safe.  All pointers in this header are HOST pointers.
+ */
+#ifndef HYSTRATH_GB300_H
+#define HYSTRATH_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSMC_MAX_SPECIES 8
+#define DSMC_MAX_PATCHES 16
+#define DSMC_MAX_OBSTACLES 8
+#define DSMC_NAME_LEN 64
+
+/* Status codes. */
+enum {
+    DSMC_OK = 0,
+    DSMC_ERR_IO = 1,            /* a case file could not be read */
+    DSMC_ERR_PARSE = 2,         /* a dictionary could not be parsed */
+    DSMC_ERR_UNKNOWN_MODEL = 3, /* model name not in the runtime-selection table */
+    DSMC_ERR_INVALID = 4,       /* inconsistent or unsupported case description */
+    DSMC_ERR_CUDA = 5,          /* a CUDA call failed */
+    DSMC_ERR_DEVICE = 6,        /* a device loop hit its iteration cap or a bound check */
+    DSMC_ERR_CAPACITY = 7,      /* particle or buffer capacity exceeded */
+    DSMC_ERR_NO_DEVICE = 8      /* no usable GPU */
+};
+
+/* polyPatch types of the boundary mesh. */
+enum {
+    DSMC_PATCH_WALL = 0,     /* wall: dispatched to a dsmcPatchBoundary model */
+    DSMC_PATCH_PATCH = 1,    /* patch: dispatched to a dsmcPatchBoundary model */
+    DSMC_PATCH_SYMMETRY = 2, /* symmetry / symmetryPlane: specular transform */
+    DSMC_PATCH_CYCLIC = 3    /* cyclic: periodic translation to the opposite side */
+};
+
+/* dsmcPatchBoundary models (boundariesDict dsmcPatchBoundaries). */
+enum {
+    DSMC_BC_NONE = 0,
+    DSMC_BC_SPECULAR = 1,  /* dsmcSpecularWallPatch */
+    DSMC_BC_DIFFUSE = 2,   /* dsmcDiffuseWallPatch */
+    DSMC_BC_DELETION = 3   /* dsmcDeletionPatch */
+};
+
+/* BinaryCollisionModel and collisionPartnerSelectionModel selections. */
+enum {
+    DSMC_COLL_VHS = 0,     /* VariableHardSphere */
+    DSMC_COLL_LB_VHS = 1   /* LarsenBorgnakkeVariableHardSphere */
+};
+enum { DSMC_SEL_NTC = 0 }; /* noTimeCounter */
+
+/* Step phases, for dsmc_run_phases. */
+enum {
+    DSMC_PHASE_INFLOW = 1,   /* dsmcFreeStreamInflowPatch::controlParcelsBeforeMove */
+    DSMC_PHASE_MOVE = 2,     /* Cloud::move with patch interactions */
+    DSMC_PHASE_SORT = 4,     /* buildCellOccupancy (counting sort into cells) */
+    DSMC_PHASE_COLLIDE = 8,  /* noTimeCounter::collide */
+    DSMC_PHASE_SAMPLE = 16,  /* dsmcVolFields::calculateField sample loop */
+    DSMC_PHASE_ALL = 31
+};
+
+/* One species of moleculeProperties (dsmcParcelI.H:37-200). */
+typedef struct {
+    char name[DSMC_NAME_LEN];
+    double mass;
+    double diameter;
+    double omega;
+    double alpha;
+    double rotational_dof;
+    int n_vib_modes;      /* 0 or 1 on this path */
+    double theta_v;       /* characteristicVibrationalTemperature[0] */
+    double theta_d;       /* dissociationTemperature */
+    double zref;          /* Zref[0] */
+    double tref_zv;       /* referenceTempForZref[0] */
+} dsmc_species;
+
+/* One boundary patch with its patch model and optional freestream inflow. */
+typedef struct {
+    char name[DSMC_NAME_LEN];
+    int type;                      /* DSMC_PATCH_* */
+    int model;                     /* DSMC_BC_* (wall and patch types) */
+    double wall_temperature;       /* dsmcDiffuseWallPatchProperties.temperature */
+    double wall_velocity[3];       /* dsmcDiffuseWallPatchProperties.velocity */
+    int inflow;                    /* 1: dsmcFreeStreamInflowPatch on this patch */
+    double inflow_number_density[DSMC_MAX_SPECIES];
+    double inflow_t_tra;
+    double inflow_t_rot;
+    double inflow_t_vib;
+    double inflow_velocity[3];
+} dsmc_patch;
+
+/* An axis-aligned solid block of cells [lo, hi) excluded from the flow. */
+typedef struct {
+    int lo[3];
+    int hi[3];
+    int patch[6];   /* patch of its -x,+x,-y,+y,-z,+z faces */
+} dsmc_obstacle;
+
+/*
+ * Fully resolved case: a uniform Cartesian hexahedral mesh, its patches, the
+ * species, the dsmcProperties models and the dsmcMeshFill initial state.
+ * Side order everywhere is -x, +x, -y, +y, -z, +z.  The face grid of a side
+ * is indexed (a + na*b) with (a, b) = (y, z) for x sides, (x, z) for y sides
+ * and (x, y) for z sides.
+ */
+typedef struct {
+    int n_cells[3];
+    double origin[3];
+    double cell_size[3];
+    int side_patch[6];             /* patch of every face of a side ...          */
+    const int* face_patch[6];      /* ... unless a per-face patch map is given   */
+    int n_obstacles;
+    dsmc_obstacle obstacles[DSMC_MAX_OBSTACLES];
+    int n_patches;
+    dsmc_patch patches[DSMC_MAX_PATCHES];
+
+    int n_species;
+    dsmc_species species[DSMC_MAX_SPECIES];
+
+    double n_equivalent_particles;   /* nEquivalentParticles (FN) */
+    int binary_collision_model;      /* DSMC_COLL_* */
+    int partner_selection_model;     /* DSMC_SEL_* */
+    double tref;                     /* <Model>Coeffs.Tref, default 273 */
+    double zrot;                     /* rotationalRelaxationCollisionNumber, default 5 */
+    double fixed_zv;                 /* vibrationalRelaxationCollisionNumber, 0 = variable Zv */
+    int inv_zv_formulation;          /* 0 pre-2008, 1 2008, 2 default */
+    double delta_t;                  /* controlDict deltaT */
+    unsigned long long seed;         /* Philox key */
+
+    int measure_mean_free_path;      /* dsmcVolFieldsProperties.measureMeanFreePath */
+    double mfp_tref;                 /* mfpReferenceTemperature, default 273 */
+
+    /* dsmcInitialiseDict dsmcMeshFill configuration */
+    double init_number_density[DSMC_MAX_SPECIES];
+    double init_t_tra;
+    double init_t_rot;
+    double init_t_vib;
+    double init_velocity[3];
+    double init_t_tra_xyz[3];        /* >0: per-axis translational temperatures
+                                        (anisotropic start; not a reference key) */
+    long long max_particles;         /* capacity; 0 = 2x the initial fill + inflow margin */
+} dsmc_case_spec;
+
+/* Cloud totals, as printed by dsmcCloud::info (dsmcCloud.C:935-985). */
+typedef struct {
+    long long n_particles;
+    long long step;
+    double linear_ke;        /* sum of 0.5 m |U|^2 over parcels, times FN */
+    double rotational_e;     /* times FN */
+    double vibrational_e;    /* times FN */
+    double momentum[3];      /* times FN */
+    long long collisions_last_step;
+    long long candidates_last_step;
+    long long collisions_total;
+    long long candidates_total;
+    long long wall_hits_last_step;
+    long long inserted_last_step;
+    long long deleted_last_step;
+    long long sample_steps;
+} dsmc_info_t;
+
+typedef struct dsmc_handle dsmc_handle;
+
+/* Fill *spec with the reference's defaults (Tref 273, Zrot 5, ...). */
+void dsmc_spec_defaults(dsmc_case_spec* spec);
+
+/* Build a cloud from a resolved spec (replaces dsmcCloud ctor). */
+int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out);
+
+/* Build a cloud from an OpenFOAM case directory: constant/dsmcProperties,
+ * system/{controlDict,boundariesDict,fieldPropertiesDict,dsmcInitialiseDict}
+ * and an axis-aligned uniform system/blockMeshDict (or constant/polyMesh/blockMeshDict). */
+int dsmc_create(const char* case_dir, dsmc_handle** out);
+
+/* Parse a case directory into *spec without touching a GPU.  face_patch maps
+ * stay owned by the library until the next call on this thread. */
+int dsmc_parse_case(const char* case_dir, dsmc_case_spec* spec);
+
+/* dsmcMeshFill: fill every cell from the spec's initial state and set
+ * sigmaTcRMax to sigmaT * most probable speed. */
+int dsmc_initialise(dsmc_handle* h);
+
+/* Advance n full steps (dsmcCloud::evolve). */
+int dsmc_evolve(dsmc_handle* h, long long n_steps);
+
+/* Advance one step running only the given DSMC_PHASE_* bits (tests). */
+int dsmc_run_phases(dsmc_handle* h, unsigned phases);
+
+/* Replace the particle set.  pos and U are n x 3 interleaved; vib may be NULL;
+ * ids must be unique.  Particles are placed in their cells and sorted. */
+int dsmc_set_particles(dsmc_handle* h, long long n, const double* pos, const double* U,
+                       const double* erot, const int* vib, const int* species,
+                       const unsigned* id);
+
+/* Read the particle set in device order (cell order after a sort). Any output
+ * pointer may be NULL.  cell receives the cell index, or -1 if deleted. */
+int dsmc_get_particles(dsmc_handle* h, long long capacity, long long* n, double* pos, double* U,
+                       double* erot, int* vib, int* species, unsigned* id, int* cell);
+
+/* Per-cell arrays: "count" (int, parcels per cell after the last sort),
+ * "start" (int), "sigmaTcRMax", "collisionSelectionRemainder" (double). */
+int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n);
+int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long long n);
+
+/* Derived volume field by its dsmcVolFields name, e.g. "rhoN", "rhoM",
+ * "Ttra", "Trot", "Tvib", "Tov", "p", "Ux", "Uy", "Uz", "dsmcNMean",
+ * "nColls", "measuredCollisionRate", "meanCollisionRate", "mfp".
+ * n must equal the number of cells. */
+int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n);
+
+/* Per-boundary-face wall fields: "wallHeatFlux", "wallShearStress_x|y|z",
+ * "rhoN_wall"; n = number of boundary faces (dsmc_info boundary face count). */
+int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long n);
+long long dsmc_n_boundary_faces(const dsmc_handle* h);
+
+/* Restart the time averages (dsmcField resetAtOutput). */
+int dsmc_reset_sampling(dsmc_handle* h);
+
+int dsmc_info(dsmc_handle* h, dsmc_info_t* out);
+
+/* Binary checkpoint: particles, per-cell state, step and seed.  Together with
+ * the counter-based random stream this resumes bit for bit. */
+int dsmc_checkpoint(dsmc_handle* h, const char* path);
+int dsmc_restore(dsmc_handle* h, const char* path);
+
+/* Wall-clock of each phase of the last dsmc_evolve, milliseconds (CUDA events). */
+int dsmc_phase_times(dsmc_handle* h, double* ms_inflow, double* ms_move, double* ms_sort,
+                     double* ms_collide, double* ms_sample);
+
+const char* dsmc_last_error(const dsmc_handle* h);
+const char* dsmc_last_global_error(void);
+void dsmc_destroy(dsmc_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HYSTRATH_GB300_H */

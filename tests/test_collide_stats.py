@@ -1,0 +1,113 @@
+"""Statistical parity of GPU collisions and sampling with the analytic VHS
+rate and with the CPU replay (collisions use pow/log/sin/cos, whose last
+bits differ between CUDA and libm, so the streams diverge after the first
+collisions and only statistics can agree)."""
+import math
+
+import numpy as np
+import pytest
+
+from hystrath_gb300 import spec as S
+from test_oracle import vhs_rate
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gpu_vhs_rate_matches_analytic(gpu_lib):
+    """Config 0 (Ar VHS, relaxes to 300 K): collisions per step within 1% of
+    the analytic equilibrium rate."""
+    from hystrath_gb300.dsmc import DsmcCloud
+    s = S.config0(seed=1)
+    g = DsmcCloud(s)
+    g.initialise()
+    i = g.info()
+    N = i.n_particles
+    T = 2.0 * i.linear_ke / (3.0 * N * s.n_equivalent_particles * S.KB)
+    g.evolve(300)
+    c0 = g.info().collisions_total
+    nsteps = 3000
+    g.evolve(nsteps)
+    i1 = g.info()
+    c1 = i1.collisions_total
+    n = N * s.n_equivalent_particles / (1000 * 1e-9)
+    expected = 0.5 * N * vhs_rate(s, T, n) * s.delta_t * nsteps
+    assert abs((c1 - c0) / expected - 1.0) < 0.01
+    # elastic collisions and specular walls conserve energy exactly up to rounding
+    assert abs(i1.linear_ke / i.linear_ke - 1.0) < 1e-11
+    # sampled temperature is the equilibrium temperature
+    g.reset_sampling()
+    g.evolve(200)
+    Tf = g.field("Ttra")
+    assert abs(Tf.mean() / T - 1.0) < 0.01
+    mcr = g.field("measuredCollisionRate")
+    acr = g.field("meanCollisionRate")
+    # dsmcVolFields counts each collision once (symmFactor TODO at :1751): x2 vs nu
+    assert abs(2 * mcr.mean() / acr.mean() - 1.0) < 0.05
+
+
+def _lb_energies(cloud_factory, seeds, checkpoints):
+    out = []
+    for sd in seeds:
+        c = cloud_factory(sd)
+        row = []
+        last = 0
+        for t in checkpoints:
+            c.evolve(t - last)
+            last = t
+            i = c.info()
+            row.append((i.linear_ke, i.rotational_e, i.vibrational_e))
+        out.append(row)
+    return np.array(out)   # seeds x checkpoints x 3
+
+
+def test_gpu_lb_relaxation_matches_oracle(gpu_lib, oracle_mod):
+    """N2 heat bath (config 1 at 8^3 cells): translational, rotational and
+    vibrational energy histories of GPU and CPU agree within 2 standard
+    errors at every checkpoint (6 seeds each)."""
+    from hystrath_gb300.dsmc import DsmcCloud
+
+    def gpu(sd):
+        g = DsmcCloud(S.config1(seed=100 + sd, n=8))
+        g.initialise()
+        return g
+
+    def cpu(sd):
+        o = oracle_mod.OracleCloud(S.config1(seed=200 + sd, n=8), threads=4)
+        o.initialise()
+        return o
+
+    checkpoints = [20, 60, 150, 300]
+    seeds = range(6)
+    eg = _lb_energies(gpu, seeds, checkpoints)
+    ec = _lb_energies(cpu, seeds, checkpoints)
+    # normalise by the total energy of each run
+    tg = eg / eg.sum(axis=2, keepdims=True)
+    tc = ec / ec.sum(axis=2, keepdims=True)
+    for k in range(3):
+        mg, mc = tg[:, :, k].mean(0), tc[:, :, k].mean(0)
+        se = np.sqrt(tg[:, :, k].var(0, ddof=1) / len(seeds) + tc[:, :, k].var(0, ddof=1) / len(seeds))
+        assert np.all(np.abs(mg - mc) <= 2.5 * se + 1e-4), (k, mg, mc, se)
+    # energy is conserved by LB collisions in a specular box
+    tot = eg.sum(axis=2)
+    assert np.all(np.abs(tot / tot[:, :1] - 1.0) < 1e-10)
+
+
+def test_gpu_checkpoint_resume_is_bit_exact(gpu_lib, tmp_path):
+    from hystrath_gb300.dsmc import DsmcCloud
+    s = S.config1(seed=7, n=6)
+    a = DsmcCloud(s)
+    a.initialise()
+    a.evolve(10)
+    path = str(tmp_path / "ck.bin")
+    a.checkpoint(path)
+    a.evolve(15)
+    pa = a.particles()
+    b = DsmcCloud(s)
+    b.restore(path)
+    b.evolve(15)
+    pb = b.particles()
+    oa = np.lexsort((pa["id"], pa["cell"]))
+    ob = np.lexsort((pb["id"], pb["cell"]))
+    for k in ("pos", "U", "erot", "vib", "id", "cell"):
+        np.testing.assert_array_equal(pa[k][oa], pb[k][ob])
+    np.testing.assert_array_equal(a.field("Ttra"), b.field("Ttra"))
