@@ -38,10 +38,11 @@ def _nvcc() -> str:
 
 def _compile(src: str, extra: list[str]) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    cmd = [_nvcc(), GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    # host code must not contract either (aarch64 GCC contracts by default)
+    cmd = [_nvcc(), GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
            "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c", src, "-o", obj] + extra
     if src.endswith(".cpp"):
-        cmd = [_nvcc(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-x", "c++",
+        cmd = [_nvcc(), "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-x", "c++",
                "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -12,11 +12,14 @@
 // fields    dsmcVolFields.C:1242-1290 and 1365-1876 (output-time fields).
 // info      dsmcCloud::info (dsmcCloud.C:935-985).
 //
-// One warp owns one cell: the cell's parcels are staged in shared memory,
-// put in canonical (particle id) order, pair selection runs serially on lane
-// 0 as the reference requires (later candidates see earlier collisions), and
-// the sampling sums are warp-shuffle reductions in that canonical order, so
-// results do not depend on the order the sort scatter left in memory.
+// A warp takes a tile of 32 consecutive cells, one cell per lane.  Each lane
+// puts its cell's parcels in canonical (particle id) order, runs the cell's
+// candidate loop serially as the reference requires (later candidates see
+// earlier collisions) and sums the cell's samples in that order, so results
+// do not depend on the order the sort scatter left in memory.  GB300 issues
+// an FP64 instruction over the whole warp whatever the active mask, which is
+// why the serial work is spread over lanes rather than left to one lane.
+// Cells with more than BIGN parcels take a warp-per-cell path.
 
 #include "dsmc_kernels.h"
 
@@ -24,7 +27,6 @@ namespace dsmc {
 
 namespace {
 
-constexpr int CAP = 128;          // parcels staged per warp in shared memory
 constexpr int CWARPS = 4;         // warps per block
 
 struct StageView {
@@ -37,15 +39,6 @@ struct StageView {
     unsigned char* dirty;
 };
 
-struct WarpStage {
-    uint32_t sid[CAP];
-    int perm[CAP];
-    int scl[CAP];
-    double ux[CAP], uy[CAP], uz[CAP], erot[CAP];
-    int vib[CAP];
-    unsigned char spsub[CAP];
-    unsigned char dirty[CAP];
-};
 
 __device__ __forceinline__ double post_rot(Rng& r, double dof, double ChiB, unsigned* err) {
     if (dof == 2.0) return 1.0 - pow(r.u01(), 1.0 / ChiB);
@@ -114,7 +107,7 @@ __device__ __forceinline__ void redistribute(const CaseDev& cs, const SpeciesDev
 
 // Serial NTC over the candidates of one cell (lane 0 only).
 __device__ void ntc_cell(const CaseDev& cs, const Soa& s, long long c, int off, int n, const StageView& v,
-                         const int* subStart, double* smax, double* rem, double* accC, uint32_t step,
+                         const int* subStart, double* smax, double* rem, double* acc, uint32_t step,
                          long long nCand, double smax0, unsigned* err, unsigned long long* nColl) {
     Rng r(cs, (uint32_t)c, step, TAG_COLLIDE);
     double smaxRun = smax[c];
@@ -181,8 +174,8 @@ __device__ void ntc_cell(const CaseDev& cs, const Soa& s, long long c, int off, 
     }
     smax[c] = smaxRun;
     if (coll) {
-        accC[CACC_NCOLLS] += (double)coll;
-        accC[CACC_COLLSEP] += collSep;
+        acc[(cs.nSpecies * SACC + CACC_NCOLLS) * cs.C + c] += (double)coll;
+        acc[(cs.nSpecies * SACC + CACC_COLLSEP) * cs.C + c] += collSep;
     }
     *nColl += coll;
 }
@@ -208,11 +201,13 @@ __device__ void process_cell(const CaseDev& cs, const Soa& s, long long c, int o
     for (int j = lane; j < n; j += 32) {
         const uint32_t my = v.sid[j];
         int rk = 0;
-        for (int k = 0; k < n; ++k) rk += (v.sid[k] < my) ? 1 : 0;
+        for (int k = 0; k < n; ++k) {
+            const uint32_t o = v.sid[k];
+            rk += (o < my || (o == my && k < j)) ? 1 : 0;
+        }
         v.perm[rk] = j;
     }
     __syncwarp();
-    double* accC = acc + c * cs.nAcc + cs.nSpecies * SACC;
     if (doCollide && n > 1) {
         long long nCand = 0;
         double smax0 = 0.0;
@@ -256,7 +251,7 @@ __device__ void process_cell(const CaseDev& cs, const Soa& s, long long c, int o
             }
             __syncwarp();
             if (lane == 0) {
-                ntc_cell(cs, s, c, off, n, v, subStart, smax, rem, accC, step, nCand, smax0, err, nColl);
+                ntc_cell(cs, s, c, off, n, v, subStart, smax, rem, acc, step, nCand, smax0, err, nColl);
                 *nCandTot += (unsigned long long)nCand;
             }
             __syncwarp();
@@ -300,48 +295,15 @@ __device__ void process_cell(const CaseDev& cs, const Soa& s, long long c, int o
             if (lane < SACC && a0 > 0.0) {
                 const double val = lane == 0 ? a0 : lane == 1 ? a1 : lane == 2 ? a2 : lane == 3 ? a3
                                  : lane == 4 ? a4 : lane == 5 ? a5 : a6;
-                acc[c * cs.nAcc + sp * SACC + lane] += val;
+                acc[(sp * SACC + lane) * cs.C + c] += val;
             }
         }
     }
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(CWARPS * 32)
-k_collide_sample(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* rem, double* acc,
-                 Counters* ctr, int* bigList, int doCollide, int doSample) {
-    __shared__ WarpStage stage[CWARPS];
-    __shared__ int subStartS[CWARPS][9];
-    const int w = threadIdx.x >> 5;
-    const uint32_t step = (uint32_t)ctr->step;
-    unsigned err = 0;
-    unsigned long long nColl = 0, nCand = 0;
-    WarpStage& ws = stage[w];
-    StageView v{ws.sid, ws.perm, ws.scl, ws.ux, ws.uy, ws.uz, ws.erot, ws.vib, ws.spsub, ws.dirty};
-    const long long nWarps = (long long)gridDim.x * CWARPS;
-    for (long long c = (long long)blockIdx.x * CWARPS + w; c < cs.C; c += nWarps) {
-        const int off = start[c];
-        const int n = start[c + 1] - off;
-        if (n == 0) continue;
-        if (n > CAP) {
-            if (lane_id() == 0) {
-                const int idx = atomicAdd(&ctr->bigCells, 1);
-                bigList[idx] = (int)c;
-            }
-            continue;
-        }
-        process_cell(cs, s, c, off, n, v, subStartS[w], smax, rem, acc, step, doCollide, doSample, &err,
-                     &nColl, &nCand);
-    }
-    if (lane_id() == 0) {
-        if (nColl) atomicAdd(&ctr->coll, nColl);
-        if (nCand) atomicAdd(&ctr->cand, nCand);
-        if (err) atomicOr(&ctr->err, err);
-    }
-}
-
-// Cells beyond the shared-memory capacity: the same code with the staging
-// arrays in a slot-indexed global scratch.
+// Cells above BIGN parcels (or tiles beyond the shared-memory capacity): one
+// warp per cell with its staging arrays in a slot-indexed global scratch.
 __global__ void __launch_bounds__(CWARPS * 32)
 k_collide_big(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* rem, double* acc,
               Counters* ctr, const int* __restrict__ bigList, Soa stageSoa, int* permS, int* sclS,
@@ -371,6 +333,209 @@ k_collide_big(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, do
     }
 }
 
+// ---------------------------------------------------------------- tiles
+// A warp takes 32 consecutive cells (one per lane).  Their parcels are one
+// contiguous slot range; ids and sub-cell/species bytes are staged in shared
+// memory with coalesced loads, then every lane orders its own cell by id,
+// runs its cell's serial NTC loop and sums its cell's samples.  Serial work
+// is spread across lanes, so FP64 instructions run 32 lanes wide.
+constexpr int TCAP = 2048;     // staged parcels per warp tile
+constexpr int TWARPS = 4;      // warps per block
+constexpr int BIGN = 192;      // cells above this go to the warp-per-cell path
+
+struct TileStage {
+    uint32_t id[TCAP];
+    unsigned char perm[TCAP];   // within-cell canonical order (n <= BIGN < 256)
+    unsigned char spsub[TCAP];  // species << 3 | sub-cell
+};
+
+// r-th parcel (canonical order) of sub-cell sb
+__device__ __forceinline__ int nth_in_sub(const unsigned char* perm, const unsigned char* spsub, int n, int sb,
+                                          int r) {
+    for (int k = 0; k < n; ++k) {
+        if ((spsub[perm[k]] & 7) == sb) {
+            if (r == 0) return k;
+            --r;
+        }
+    }
+    return 0;
+}
+
+// noTimeCounter::collide for one cell, run by one lane on global state.
+__device__ void ntc_lane(const CaseDev& cs, const Soa& s, long long c, long long off, int n,
+                         const unsigned char* perm, const unsigned char* spsub, const int subCnt[8],
+                         double* smax, double* acc, uint32_t step, long long nCand, double smax0, unsigned* err,
+                         unsigned long long* nColl) {
+    Rng r(cs, (uint32_t)c, step, TAG_COLLIDE);
+    double smaxRun = smax0;
+    unsigned long long coll = 0;
+    double collSep = 0.0;
+    for (long long k = 0; k < nCand; ++k) {
+        const int iP = r.label(0, n - 1, err);
+        const int jP = perm[iP];
+        const int sub = spsub[jP] & 7;
+        const int nSC = subCnt[sub];
+        int iQ = -1, it = 0;
+        if (nSC > 1) {
+            do { iQ = nth_in_sub(perm, spsub, n, sub, r.label(0, nSC - 1, err)); }
+            while (iP == iQ && ++it < MAX_REJECTION);
+        } else {
+            do { iQ = r.label(0, n - 1, err); } while (iP == iQ && ++it < MAX_REJECTION);
+        }
+        if (it >= MAX_REJECTION) { *err |= ERRB_REJECTION; continue; }
+        const int jQ = perm[iQ];
+        const long long gP = off + jP, gQ = off + jQ;
+        const int tP = spsub[jP] >> 3, tQ = spsub[jQ] >> 3;
+        const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
+        double UP[3] = {s.ux[gP], s.uy[gP], s.uz[gP]};
+        double UQ[3] = {s.ux[gQ], s.uy[gQ], s.uz[gQ]};
+        const double d0 = UP[0] - UQ[0], d1 = UP[1] - UQ[1], d2 = UP[2] - UQ[2];
+        const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
+        double sigma = 0.0;
+        if (!(sqrt(cr2) < VSMALL)) sigma = pr.sigmaPrefactor * pow(cr2, pr.expo);
+        if (sigma > smaxRun) smaxRun = sigma;
+        if ((sigma / smax0) > r.u01()) {
+            double cR;
+            if (cs.collModel == DSMC_COLL_LB_VHS) {
+                double Et = 0.5 * pr.mR * cr2;
+                double eP = s.erot[gP], eQ = s.erot[gQ];
+                int vP = s.vib[gP], vQ = s.vib[gQ];
+                redistribute(cs, cs.sp[tP], &eP, &vP, Et, pr.omegaPQ, r, err);
+                redistribute(cs, cs.sp[tQ], &eQ, &vQ, Et, pr.omegaPQ, r, err);
+                s.erot[gP] = eP; s.erot[gQ] = eQ;
+                s.vib[gP] = vP; s.vib[gQ] = vQ;
+                cR = sqrt(2.0 * Et / pr.mR);
+            } else {
+                cR = sqrt(cr2);
+            }
+            double Ucm[3];
+            for (int a = 0; a < 3; ++a) Ucm[a] = pr.mPfrac * UP[a] + pr.mQfrac * UQ[a];
+            const double cosT = 2.0 * r.u01() - 1.0;
+            const double sinT = sqrt(1.0 - cosT * cosT);
+            const double phi = 2.0 * PI * r.u01();
+            double sph, cph;
+            sincos(phi, &sph, &cph);
+            const double prel[3] = {cR * cosT, cR * sinT * cph, cR * sinT * sph};
+            s.ux[gP] = Ucm[0] + prel[0] * pr.mQfrac;
+            s.uy[gP] = Ucm[1] + prel[1] * pr.mQfrac;
+            s.uz[gP] = Ucm[2] + prel[2] * pr.mQfrac;
+            s.ux[gQ] = Ucm[0] - prel[0] * pr.mPfrac;
+            s.uy[gQ] = Ucm[1] - prel[1] * pr.mPfrac;
+            s.uz[gQ] = Ucm[2] - prel[2] * pr.mPfrac;
+            const double dx = s.x[gP] - s.x[gQ];
+            const double dy = s.y[gP] - s.y[gQ];
+            const double dz = s.z[gP] - s.z[gQ];
+            collSep += sqrt(dx * dx + dy * dy + dz * dz);
+            ++coll;
+        }
+    }
+    smax[c] = smaxRun;
+    if (coll) {
+        acc[(cs.nSpecies * SACC + CACC_NCOLLS) * cs.C + c] += (double)coll;
+        acc[(cs.nSpecies * SACC + CACC_COLLSEP) * cs.C + c] += collSep;
+    }
+    *nColl += coll;
+}
+
+__global__ void __launch_bounds__(TWARPS * 32)
+k_collide_tile(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* rem, double* acc,
+               Counters* ctr, int* bigList, int doCollide, int doSample) {
+    extern __shared__ unsigned char smraw[];
+    TileStage& st = reinterpret_cast<TileStage*>(smraw)[threadIdx.x >> 5];
+    const unsigned lane = lane_id();
+    const uint32_t step = (uint32_t)ctr->step;
+    unsigned err = 0;
+    unsigned long long nColl = 0, nCand = 0;
+    const long long nTiles = (cs.C + 31) / 32;
+    const long long nWarps = (long long)gridDim.x * TWARPS;
+    for (long long t = (long long)blockIdx.x * TWARPS + (threadIdx.x >> 5); t < nTiles; t += nWarps) {
+        const long long c0 = t * 32;
+        const long long cEnd = (c0 + 32 < cs.C) ? c0 + 32 : cs.C;
+        const long long c = c0 + lane;
+        const bool valid = c < cEnd;
+        const int P0 = start[c0];
+        const int P1 = start[cEnd];
+        const int myStart = valid ? start[c] : P1;
+        const int n = valid ? start[c + 1] - myStart : 0;
+        const bool fits = (P1 - P0) <= TCAP;
+        const bool big = n > BIGN || (!fits && n > 0);
+        if (big) {
+            const int idx = atomicAdd(&ctr->bigCells, 1);
+            bigList[idx] = (int)c;
+        }
+        if (fits) {
+            for (int p = lane; p < P1 - P0; p += 32) {
+                const long long g = (long long)P0 + p;
+                st.id[p] = s.id[g];
+                st.spsub[p] = (unsigned char)((s.spc[g] << 3) | (s.cellw[g] & 7u));
+            }
+        }
+        __syncwarp();
+        if (fits && !big && n > 0) {
+            const int b = myStart - P0;
+            uint32_t* id = st.id + b;
+            unsigned char* perm = st.perm + b;
+            const unsigned char* spsub = st.spsub + b;
+            // insertion sort of the cell's local indices by particle id
+            perm[0] = 0;
+            for (int k = 1; k < n; ++k) {
+                const uint32_t key = id[k];
+                int m = k - 1;
+                while (m >= 0 && id[perm[m]] > key) {
+                    perm[m + 1] = perm[m];
+                    --m;
+                }
+                perm[m + 1] = (unsigned char)k;
+            }
+            if (doCollide && n > 1) {
+                const double smax0 = smax[c];
+                const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * smax0 * cs.dt / cs.V;
+                const long long nc = (long long)sel;
+                rem[c] = sel - (double)nc;
+                if (nc > 0) {
+                    int subCnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                    for (int j = 0; j < n; ++j) subCnt[spsub[j] & 7]++;
+                    ntc_lane(cs, s, c, myStart, n, perm, spsub, subCnt, smax, acc, step, nc, smax0, &err, &nColl);
+                    nCand += (unsigned long long)nc;
+                }
+            }
+            if (doSample) {
+                for (int sp = 0; sp < cs.nSpecies; ++sp) {
+                    double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0;
+                    for (int k = 0; k < n; ++k) {
+                        const int j = perm[k];
+                        if ((spsub[j] >> 3) != sp) continue;
+                        const long long g = (long long)myStart + j;
+                        const double ux = s.ux[g], uy = s.uy[g], uz = s.uz[g];
+                        a0 += 1.0;
+                        a1 += ux;
+                        a2 += uy;
+                        a3 += uz;
+                        a4 += ux * ux + uy * uy + uz * uz;
+                        a5 += s.erot[g];
+                        a6 += (double)s.vib[g];
+                    }
+                    if (a0 > 0.0) {
+                        const long long C = cs.C;
+                        double* A = acc + (long long)sp * SACC * C + c;
+                        A[SACC_N * C] += a0;
+                        A[SACC_UX * C] += a1;
+                        A[SACC_UY * C] += a2;
+                        A[SACC_UZ * C] += a3;
+                        A[SACC_UU * C] += a4;
+                        A[SACC_EROT * C] += a5;
+                        A[SACC_VIB * C] += a6;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    }
+    if (nColl) atomicAdd(&ctr->coll, nColl);
+    if (nCand) atomicAdd(&ctr->cand, nCand);
+    if (err) atomicOr(&ctr->err, err);
+}
+
 __global__ void k_zero_step(Counters* ctr) {
     ctr->nMoved = ctr->n;
     ctr->coll = 0;
@@ -388,10 +553,13 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
     if (c >= cs.C) return;
     const double nT = (double)ctr->sampleSteps;
     const double FN = cs.FN, V = cs.V;
-    const double* A = acc + c * cs.nAcc;
+    const long long C = cs.C;
+    // accumulator k of cell c lives at acc[k * C + c]
+    auto A = [&](int k) { return acc[(long long)k * C + c]; };
     double N = 0, M = 0, mom[3] = {0, 0, 0}, mcc = 0, Er = 0, zr = 0;
     for (int s = 0; s < cs.nSpecies; ++s) {
-        const double* S = A + s * SACC;
+        const double S[SACC] = {A(s * SACC + 0), A(s * SACC + 1), A(s * SACC + 2), A(s * SACC + 3),
+                                A(s * SACC + 4), A(s * SACC + 5), A(s * SACC + 6)};
         const double m = cs.sp[s].m;
         N += S[SACC_N];
         M += m * S[SACC_N];
@@ -416,7 +584,8 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
     const double Trot = zr > SMALL ? 2.0 * Er / (kB * zr) : 0.0;
     double Tvib = 0, zetaVib = 0, molRhoN = 0;
     for (int s = 0; s < cs.nSpecies; ++s) {
-        const double* S = A + s * SACC;
+        const double S[SACC] = {A(s * SACC + 0), A(s * SACC + 1), A(s * SACC + 2), A(s * SACC + 3),
+                                A(s * SACC + 4), A(s * SACC + 5), A(s * SACC + 6)};
         const SpeciesDev& sp = cs.sp[s];
         if (!sp.nVib) continue;
         const double Ev = sp.kThetaV * S[SACC_VIB];
@@ -437,7 +606,7 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
     }
     if (molRhoN > SMALL) { Tvib /= molRhoN; zetaVib /= molRhoN; }
     const double Tov = (3.0 * Ttra + zetaRotTot * Trot + zetaVib * Tvib) / (3.0 + zetaRotTot + zetaVib);
-    const double* CA = A + cs.nSpecies * SACC;
+    const double CA[CACC] = {A(cs.nSpecies * SACC + CACC_NCOLLS), A(cs.nSpecies * SACC + CACC_COLLSEP)};
     double v = 0;
     switch (which) {
     case F_RHON: v = rhoN; break;
@@ -460,7 +629,7 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
             for (int s = 0; s < cs.nSpecies; ++s) {
                 double smfp = 0, smcr = 0;
                 for (int q = 0; q < cs.nSpecies; ++q) {
-                    const double* Sq = A + q * SACC;
+                    const double Sq[1] = {A(q * SACC + SACC_N)};
                     const double dPQ = 0.5 * (cs.sp[s].d + cs.sp[q].d);
                     const double oPQ = 0.5 * (cs.sp[s].omega + cs.sp[q].omega);
                     const double mr = cs.sp[s].m / cs.sp[q].m;
@@ -473,7 +642,7 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
                     }
                 }
                 if (smfp > SMALL) smfp = 1.0 / smfp;
-                const double rhoNi = A[s * SACC + SACC_N] * FN;
+                const double rhoNi = A(s * SACC + SACC_N) * FN;
                 mfp += smfp * rhoNi / (N * FN);
                 mcr += smcr * rhoNi / (N * FN);
             }
@@ -525,12 +694,18 @@ int sm_count() {
 
 void launch_collide_sample(const CaseDev& cs, const StepBuffers& B, const Soa& s, int doCollide, int doSample,
                            cudaStream_t st) {
-    const long long warpsNeeded = cs.C;
-    long long blocks = (warpsNeeded + CWARPS - 1) / CWARPS;
-    const long long cap = (long long)sm_count() * 8;
+    static bool attrSet = false;
+    const int smem = (int)sizeof(TileStage) * TWARPS;
+    if (!attrSet) {
+        cudaFuncSetAttribute(k_collide_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attrSet = true;
+    }
+    const long long tiles = (cs.C + 31) / 32;
+    long long blocks = (tiles + TWARPS - 1) / TWARPS;
+    const long long cap = (long long)sm_count() * 4;
     if (blocks > cap) blocks = cap;
-    k_collide_sample<<<(int)blocks, CWARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.rem, B.acc, B.ctr,
-                                                          B.bigList, doCollide, doSample);
+    k_collide_tile<<<(int)blocks, TWARPS * 32, smem, st>>>(cs, s, B.start, B.smax, B.rem, B.acc, B.ctr, B.bigList,
+                                                          doCollide, doSample);
     k_collide_big<<<sm_count() * 2, CWARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.rem, B.acc, B.ctr,
                                                           B.bigList, B.stage, B.perm, B.scl, B.dirty,
                                                           doCollide, doSample);

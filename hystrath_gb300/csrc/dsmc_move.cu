@@ -475,7 +475,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
 }
 
 // ---------------------------------------------------------------- scatter
-__global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, const Counters* ctr,
+__global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, Counters* ctr,
                                                  const int* __restrict__ start, int* count) {
     const long long n = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -496,6 +496,11 @@ __global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, const Counter
         if (key >= 0) {
             const int rank = __popc(peers & ((1u << lane) - 1u));
             const long long slot = (long long)start[key] + old - 1 - rank;
+            if (slot < start[key] || slot >= start[key + 1]) {
+                // histogram and scatter disagree: record, never write out of range
+                atomicOr(&ctr->err, ERRB_BOUNDS);
+                continue;
+            }
             dst.x[slot] = src.x[i];
             dst.y[slot] = src.y[i];
             dst.z[slot] = src.z[i];

@@ -32,7 +32,10 @@ def _pair(spec, gpu_lib, oracle_mod, threads=4):
     return g, o, st
 
 
-def _check_step(g, o, before, phases, allow_resampled=True):
+def _check_step(g, o, before, phases, allow_resampled=True, tainted=None):
+    """One step on both sides.  ``tainted`` collects ids whose state went
+    through a transcendental function (inflow creation, diffuse wall) in
+    this or an earlier step; they are compared with a tolerance."""
     g.run_phases(phases)
     o.run_phases(phases)
     a = _canonical(g.particles())
@@ -48,6 +51,9 @@ def _check_step(g, o, before, phases, allow_resampled=True):
     old = idx >= 0
     exact = old.copy()
     exact[old] = np.all(np.abs(b["U"][old]) == np.abs(before["U"][idx[old]]), axis=1)
+    if tainted is not None:
+        tainted.update(int(i) for i in b["id"][~exact])
+        exact &= ~np.isin(b["id"], np.fromiter(tainted, dtype=np.uint32, count=len(tainted)))
     n_exact = int(exact.sum())
     assert n_exact > 0
     for k in ("pos", "U"):
@@ -94,9 +100,12 @@ def test_move_sort_inflow_obstacle_diffuse(gpu_lib, oracle_mod):
     s = S.config2(seed=14, scale=8)
     g, o, st = _pair(s, gpu_lib, oracle_mod)
     before = _canonical(st)
+    tainted = set()
     for _ in range(4):
-        a, b, exact = _check_step(g, o, before, S.PHASE_INFLOW | S.PHASE_MOVE | S.PHASE_SORT)
+        a, b, exact = _check_step(g, o, before, S.PHASE_INFLOW | S.PHASE_MOVE | S.PHASE_SORT,
+                                  tainted=tainted)
         before = b
+    assert exact.sum() > 0.9 * len(exact)
     gi, oi = g.info(), o.info()
     assert gi.inserted_last_step == oi.inserted_last_step > 0
     assert gi.deleted_last_step == oi.deleted_last_step
