@@ -543,6 +543,56 @@ int dsmc_evolve(dsmc_handle* h, long long n) {
     return check_device_error(h);
 }
 
+int dsmc_evolve_profiled(dsmc_handle* h, long long n, double* phase_ms, double* total_ms) {
+    if (n <= 0) return fail(h, DSMC_ERR_INVALID, "n must be positive");
+    std::vector<cudaEvent_t> ev((size_t)n * 6);
+    for (auto& e : ev) CUDA_TRY(h, cudaEventCreate(&e));
+    for (long long i = 0; i < n; ++i) {
+        enqueue_step(h, h->cur, DSMC_PHASE_ALL, &ev[(size_t)i * 6]);
+        h->cur ^= 1;
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    int rc = check_device_error(h);
+    double sums[5] = {0, 0, 0, 0, 0};
+    for (long long i = 0; i < n; ++i) {
+        for (int k = 0; k < 5; ++k) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, ev[(size_t)i * 6 + k], ev[(size_t)i * 6 + k + 1]);
+            sums[k] += ms;
+        }
+    }
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ev[0], ev[(size_t)(n - 1) * 6 + 5]);
+    for (auto& e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < 5; ++k) {
+        if (phase_ms) phase_ms[k] = sums[k];
+        h->phaseMs[k] = sums[k] / (double)n;
+    }
+    if (total_ms) *total_ms = tot;
+    return rc;
+}
+
+int dsmc_evolve_timed(dsmc_handle* h, long long n, double* total_ms) {
+    int rc = build_graphs(h);
+    if (rc) return rc;
+    cudaEvent_t e0, e1;
+    CUDA_TRY(h, cudaEventCreate(&e0));
+    CUDA_TRY(h, cudaEventCreate(&e1));
+    CUDA_TRY(h, cudaEventRecord(e0, h->stream));
+    for (long long i = 0; i < n; ++i) {
+        CUDA_TRY(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
+        h->cur ^= 1;
+    }
+    CUDA_TRY(h, cudaEventRecord(e1, h->stream));
+    rc = check_device_error(h);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (total_ms) *total_ms = ms;
+    return rc;
+}
+
 int dsmc_run_phases(dsmc_handle* h, unsigned phases) {
     cudaEvent_t ev[6];
     for (int k = 0; k < 6; ++k) cudaEventCreate(&ev[k]);

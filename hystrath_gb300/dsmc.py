@@ -36,6 +36,8 @@ def _load() -> C.CDLL:
     L.dsmc_initialise.argtypes = [vp]
     L.dsmc_evolve.argtypes = [vp, C.c_longlong]
     L.dsmc_run_phases.argtypes = [vp, C.c_uint]
+    L.dsmc_evolve_timed.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double)]
+    L.dsmc_evolve_profiled.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.dsmc_set_particles.argtypes = [vp, C.c_longlong, vp, vp, vp, vp, vp, vp]
     L.dsmc_get_particles.argtypes = [vp, C.c_longlong, C.POINTER(C.c_longlong), vp, vp, vp, vp, vp, vp, vp]
     L.dsmc_get_cell_array.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
@@ -117,6 +119,20 @@ class DsmcCloud:
     # dsmcCloud::evolve, n times
     def evolve(self, n: int = 1):
         self._chk(lib().dsmc_evolve(self.h, n))
+
+    def evolve_timed(self, n: int) -> float:
+        """n graph-launched steps; returns the CUDA-event time in ms."""
+        ms = C.c_double()
+        self._chk(lib().dsmc_evolve_timed(self.h, n, C.byref(ms)))
+        return ms.value
+
+    def evolve_profiled(self, n: int):
+        """n steps with CUDA events around every phase; returns (total ms,
+        dict of summed phase ms)."""
+        ph = (C.c_double * 5)()
+        tot = C.c_double()
+        self._chk(lib().dsmc_evolve_profiled(self.h, n, ph, C.byref(tot)))
+        return tot.value, dict(zip(("inflow", "move", "sort", "collide_sample", "end"), list(ph)))
 
     def run_phases(self, phases: int):
         self._chk(lib().dsmc_run_phases(self.h, phases))

@@ -214,6 +214,14 @@ int dsmc_evolve(dsmc_handle* h, long long n_steps);
 /* Advance one step running only the given DSMC_PHASE_* bits (tests). */
 int dsmc_run_phases(dsmc_handle* h, unsigned phases);
 
+/* dsmc_evolve with CUDA events on the handle's stream around the whole run
+ * (graph launches) and, for the profiled form, around every phase of every
+ * step: phase_ms[5] receives the summed inflow, move, sort, collide+sample
+ * and bookkeeping times, total_ms the first-to-last event time.  No host
+ * synchronisation happens inside the run. */
+int dsmc_evolve_timed(dsmc_handle* h, long long n_steps, double* total_ms);
+int dsmc_evolve_profiled(dsmc_handle* h, long long n_steps, double* phase_ms, double* total_ms);
+
 /* Replace the particle set.  pos and U are n x 3 interleaved; vib may be NULL;
  * ids must be unique.  Particles are placed in their cells and sorted. */
 int dsmc_set_particles(dsmc_handle* h, long long n, const double* pos, const double* U,
