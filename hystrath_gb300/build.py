@@ -25,6 +25,7 @@ UNITS = {
     "dsmc_move.cu": ["-fmad=false"],
     "dsmc_collide.cu": ["-fmad=false"],
     "dsmc_api.cu": [],
+    "dsmc_noalloc.cu": [],
     "case_parser.cpp": [],
 }
 

@@ -267,6 +267,24 @@ const char* dsmc_last_error(const dsmc_handle* h);
 const char* dsmc_last_global_error(void);
 void dsmc_destroy(dsmc_handle* h);
 
+/*
+ * Cell start offsets for callers that must not allocate device memory.  This
+ * entry point has no counterpart in the reference (whose occupancy lists live
+ * in host memory); it is the exclusive scan of the occupancy sort, offered to
+ * code that owns its device memory in a fixed pool or may not grow its
+ * footprint.  Unlike the rest of this header it takes DEVICE pointers:
+ * d_counts[n_cells] parcels per cell in, d_start[n_cells + 1] out (the last
+ * entry is the total), on the given cudaStream_t (NULL = legacy stream).
+ * No cudaMalloc/cudaFree: the block sums live in a 16 KiB static device array
+ * that every GPU loading the library holds until exit, which limits n_cells to
+ * 2^24.  The first call on a device resolves that array's address (call it
+ * before any stream capture).  Calls share the array: calls that overlap on
+ * the GPU race.  Errors: DSMC_ERR_INVALID beyond 2^24 cells or for null
+ * buffers, message in dsmc_noalloc_last_error().
+ */
+int dsmc_cell_starts_noalloc(const int* d_counts, long long n_cells, int* d_start, void* stream);
+const char* dsmc_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
