@@ -240,6 +240,8 @@ void fill_case_dev(dsmc_handle* h) {
                                std::exp(std::lgamma(2.5 - om));
             p.mPfrac = a.mass / (a.mass + b.mass);
             p.mQfrac = b.mass / (a.mass + b.mass);
+            p.sigmaPrefactorF = (float)p.sigmaPrefactor;
+            p.expoF = (float)p.expo;
         }
     }
     for (int p = 0; p < s.n_patches; ++p) {
@@ -446,6 +448,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.wall, cs.nBFaces * W_N))) return rc;
     if ((rc = dalloc(h, &B.bfPatch, cs.nBFaces))) return rc;
     if ((rc = dalloc(h, &B.bigList, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.slowList, cap))) return rc;
     if ((rc = dalloc(h, &B.ctr, 1))) return rc;
     if ((rc = dalloc(h, &h->solid, cs.C))) return rc;
     if ((rc = dalloc(h, &h->info6, 8))) return rc;
@@ -458,6 +461,31 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.inflowAcc, ni))) return rc;
     if ((rc = dalloc(h, &B.inflowCount, ni))) return rc;
     if ((rc = dalloc(h, &B.inflowOff, ni + 1))) return rc;
+    // 1/Zv by quantised level (postCollisionVibrationalEnergyLevel, dsmcCloud.C:1420-1490)
+    {
+        std::vector<double> tab((size_t)DSMC_MAX_SPECIES * DSMC_MAX_SPECIES * ZV_TAB, 0.0);
+        for (int p = 0; p < spec->n_species; ++p) {
+            const dsmc_species& sp = spec->species[p];
+            if (sp.n_vib_modes == 0) continue;
+            for (int q = 0; q < spec->n_species; ++q) {
+                const double omega = 0.5 * (sp.omega + spec->species[q].omega);
+                double* row = &tab[(size_t)(p * DSMC_MAX_SPECIES + q) * ZV_TAB];
+                for (int iMax = 1; iMax < ZV_TAB; ++iMax) {
+                    const double T = iMax * sp.theta_v / (3.5 - omega);
+                    const double pow1 = std::pow(sp.theta_d / T, 1. / 3.) - 1.0;
+                    const double pow2 = std::pow(sp.theta_d / sp.tref_zv, 1. / 3.) - 1.0;
+                    const double ZvP1 = std::pow(sp.theta_d / T, omega);
+                    const double ZvP2 = std::pow(sp.zref * std::pow(sp.theta_d / sp.tref_zv, -omega), pow1 / pow2);
+                    const double Zv = ZvP1 * ZvP2;
+                    row[iMax] = (spec->inv_zv_formulation == 2) ? 1.0 / (5.0 * Zv) : 1.0 / Zv;
+                }
+            }
+        }
+        double* dtab = nullptr;
+        if ((rc = dalloc(h, &dtab, (long long)tab.size()))) return rc;
+        CUDA_TRY(h, cudaMemcpy(dtab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+        cs.invZvTab = dtab;
+    }
     CUDA_TRY(h, cudaMemcpy(B.bfPatch, bfPatch.data(), sizeof(int) * bfPatch.size(), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemcpy(h->solid, solid.data(), cs.C, cudaMemcpyHostToDevice));
     if (B.nInflowFaces) {

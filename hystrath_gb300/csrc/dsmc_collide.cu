@@ -57,26 +57,35 @@ __device__ __forceinline__ double post_rot(Rng& r, double dof, double ChiB, unsi
     return 0.0;
 }
 
+// postCollisionVibrationalEnergyLevel, non-reacting branch.  1/Zv comes from
+// the per-pair table when iMax is tabulated.  The level acceptance
+// probability (Bird eq. 5.61) is only compared with a uniform deviate, so it
+// is evaluated in FP32.
 __device__ __forceinline__ int post_vib(const CaseDev& cs, Rng& r, int vib, int iMax, const SpeciesDev& s,
-                                        double omega, double Ec, unsigned* err) {
+                                        double omega, double Ec, const double* tab, unsigned* err) {
     double invZv;
     if (cs.fixedZv == 0) {
-        const double T = iMax * s.thetaV / (3.5 - omega);
-        const double pow1 = pow(s.thetaD / T, 1. / 3.) - 1.0;
-        const double pow2 = pow(s.thetaD / s.trefZv, 1. / 3.) - 1.0;
-        const double ZvP1 = pow(s.thetaD / T, omega);
-        const double ZvP2 = pow(s.zref * pow(s.thetaD / s.trefZv, -omega), pow1 / pow2);
-        const double Zv = ZvP1 * ZvP2;
-        invZv = (cs.invZvForm == 2) ? 1.0 / (5.0 * Zv) : 1.0 / Zv;
+        if (tab && iMax < ZV_TAB) {
+            invZv = tab[iMax];
+        } else {
+            const double T = iMax * s.thetaV / (3.5 - omega);
+            const double pow1 = pow(s.thetaD / T, 1. / 3.) - 1.0;
+            const double pow2 = pow(s.thetaD / s.trefZv, 1. / 3.) - 1.0;
+            const double ZvP1 = pow(s.thetaD / T, omega);
+            const double ZvP2 = pow(s.zref * pow(s.thetaD / s.trefZv, -omega), pow1 / pow2);
+            const double Zv = ZvP1 * ZvP2;
+            invZv = (cs.invZvForm == 2) ? 1.0 / (5.0 * Zv) : 1.0 / Zv;
+        }
     } else {
         invZv = 1.0 / cs.fixedZv;
     }
     if (invZv > r.u01()) {
+        const float ex = (float)(1.5 - omega);
         for (int it = 0; it < MAX_REJECTION; ++it) {
             const int iDash = r.label(0, iMax, err);
-            const double EVib = iDash * s.kThetaV;
-            const double func = pow(1.0 - EVib / Ec, 1.5 - omega);
-            if (!(func < r.u01())) return iDash;
+            const float base = (float)(1.0 - (iDash * s.kThetaV) / Ec);
+            const float func = powf(base > 0.0f ? base : 0.0f, ex);
+            if (!((double)func < r.u01())) return iDash;
         }
         *err |= ERRB_REJECTION;
     }
@@ -84,12 +93,13 @@ __device__ __forceinline__ int post_vib(const CaseDev& cs, Rng& r, int vib, int 
 }
 
 __device__ __forceinline__ void redistribute(const CaseDev& cs, const SpeciesDev& s, double* erot, int* vib,
-                                             double& Et, double omegaPQ, Rng& r, unsigned* err) {
+                                             double& Et, double omegaPQ, Rng& r, const double* tab,
+                                             unsigned* err) {
     if (s.nVib > 0) {
         const double EcP = Et + *vib * s.kThetaV;
         const int iMax = (int)(EcP / s.kThetaV);
         if (iMax > 0) {
-            *vib = post_vib(cs, r, *vib, iMax, s, omegaPQ, EcP, err);
+            *vib = post_vib(cs, r, *vib, iMax, s, omegaPQ, EcP, tab, err);
             Et = EcP - *vib * s.kThetaV;
         }
     }
@@ -103,6 +113,17 @@ __device__ __forceinline__ void redistribute(const CaseDev& cs, const SpeciesDev
             Et = EcP - *erot;
         }
     }
+}
+
+__device__ __forceinline__ const double* zv_row(const CaseDev& cs, int p, int q) {
+    return cs.invZvTab ? cs.invZvTab + (size_t)(p * DSMC_MAX_SPECIES + q) * ZV_TAB : nullptr;
+}
+
+// sigma_T c_R of VariableHardSphere::sigmaTcR.  It feeds only the acceptance
+// test and the running maximum, so it is evaluated in FP32.
+__device__ __forceinline__ double sigma_cr(const PairDev& pr, double cr2) {
+    if (sqrt(cr2) < VSMALL) return 0.0;
+    return (double)(pr.sigmaPrefactorF * powf((float)cr2, pr.expoF));
 }
 
 // Serial NTC over the candidates of one cell (lane 0 only).
@@ -132,17 +153,16 @@ __device__ void ntc_cell(const CaseDev& cs, const Soa& s, long long c, int off, 
         double UQ[3] = {v.ux[jQ], v.uy[jQ], v.uz[jQ]};
         const double d0 = UP[0] - UQ[0], d1 = UP[1] - UQ[1], d2 = UP[2] - UQ[2];
         const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
-        double sigma = 0.0;
-        if (!(sqrt(cr2) < VSMALL)) sigma = pr.sigmaPrefactor * pow(cr2, pr.expo);
+        const double sigma = sigma_cr(pr, cr2);
         if (sigma > smaxRun) smaxRun = sigma;
-        if ((sigma / smax0) > r.u01()) {
+        if (sigma > r.u01() * smax0) {      // (sigma/smax0) > U with smax0 > 0
             double cR;
             if (cs.collModel == DSMC_COLL_LB_VHS) {
                 double Et = 0.5 * pr.mR * cr2;
                 double eP = v.erot[jP], eQ = v.erot[jQ];
                 int vP = v.vib[jP], vQ = v.vib[jQ];
-                redistribute(cs, cs.sp[tP], &eP, &vP, Et, pr.omegaPQ, r, err);
-                redistribute(cs, cs.sp[tQ], &eQ, &vQ, Et, pr.omegaPQ, r, err);
+                redistribute(cs, cs.sp[tP], &eP, &vP, Et, pr.omegaPQ, r, zv_row(cs, tP, tQ), err);
+                redistribute(cs, cs.sp[tQ], &eQ, &vQ, Et, pr.omegaPQ, r, zv_row(cs, tQ, tP), err);
                 v.erot[jP] = eP; v.erot[jQ] = eQ;
                 v.vib[jP] = vP; v.vib[jQ] = vQ;
                 cR = sqrt(2.0 * Et / pr.mR);
@@ -391,17 +411,16 @@ __device__ void ntc_lane(const CaseDev& cs, const Soa& s, long long c, long long
         double UQ[3] = {s.ux[gQ], s.uy[gQ], s.uz[gQ]};
         const double d0 = UP[0] - UQ[0], d1 = UP[1] - UQ[1], d2 = UP[2] - UQ[2];
         const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
-        double sigma = 0.0;
-        if (!(sqrt(cr2) < VSMALL)) sigma = pr.sigmaPrefactor * pow(cr2, pr.expo);
+        const double sigma = sigma_cr(pr, cr2);
         if (sigma > smaxRun) smaxRun = sigma;
-        if ((sigma / smax0) > r.u01()) {
+        if (sigma > r.u01() * smax0) {      // (sigma/smax0) > U with smax0 > 0
             double cR;
             if (cs.collModel == DSMC_COLL_LB_VHS) {
                 double Et = 0.5 * pr.mR * cr2;
                 double eP = s.erot[gP], eQ = s.erot[gQ];
                 int vP = s.vib[gP], vQ = s.vib[gQ];
-                redistribute(cs, cs.sp[tP], &eP, &vP, Et, pr.omegaPQ, r, err);
-                redistribute(cs, cs.sp[tQ], &eQ, &vQ, Et, pr.omegaPQ, r, err);
+                redistribute(cs, cs.sp[tP], &eP, &vP, Et, pr.omegaPQ, r, zv_row(cs, tP, tQ), err);
+                redistribute(cs, cs.sp[tQ], &eQ, &vQ, Et, pr.omegaPQ, r, zv_row(cs, tQ, tP), err);
                 s.erot[gP] = eP; s.erot[gQ] = eQ;
                 s.vib[gP] = vP; s.vib[gQ] = vQ;
                 cR = sqrt(2.0 * Et / pr.mR);
@@ -500,31 +519,34 @@ k_collide_tile(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, d
                 }
             }
             if (doSample) {
+                // counts and vibrational levels are integers: summed on the
+                // integer pipe; 7 FP64 operations per parcel remain
                 for (int sp = 0; sp < cs.nSpecies; ++sp) {
-                    double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0;
+                    double a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0;
+                    int a0 = 0, a6 = 0;
                     for (int k = 0; k < n; ++k) {
                         const int j = perm[k];
                         if ((spsub[j] >> 3) != sp) continue;
                         const long long g = (long long)myStart + j;
                         const double ux = s.ux[g], uy = s.uy[g], uz = s.uz[g];
-                        a0 += 1.0;
+                        a0 += 1;
                         a1 += ux;
                         a2 += uy;
                         a3 += uz;
-                        a4 += ux * ux + uy * uy + uz * uz;
+                        a4 = fma(ux, ux, fma(uy, uy, fma(uz, uz, a4)));
                         a5 += s.erot[g];
-                        a6 += (double)s.vib[g];
+                        a6 += s.vib[g];
                     }
-                    if (a0 > 0.0) {
+                    if (a0 > 0) {
                         const long long C = cs.C;
                         double* A = acc + (long long)sp * SACC * C + c;
-                        A[SACC_N * C] += a0;
+                        A[SACC_N * C] += (double)a0;
                         A[SACC_UX * C] += a1;
                         A[SACC_UY * C] += a2;
                         A[SACC_UZ * C] += a3;
                         A[SACC_UU * C] += a4;
                         A[SACC_EROT * C] += a5;
-                        A[SACC_VIB * C] += a6;
+                        A[SACC_VIB * C] += (double)a6;
                     }
                 }
             }
@@ -544,6 +566,7 @@ __global__ void k_zero_step(Counters* ctr) {
     ctr->inserted = 0;
     ctr->deleted = 0;
     ctr->bigCells = 0;
+    ctr->nSlow = 0;
 }
 
 // ---------------------------------------------------------------- fields

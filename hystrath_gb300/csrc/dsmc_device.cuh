@@ -26,6 +26,7 @@ constexpr double GREAT = 1.0e15;
 // sets an error bit that the host turns into DSMC_ERR_DEVICE.
 constexpr int MAX_CROSSINGS = 64;
 constexpr int MAX_REJECTION = 100000;
+constexpr int ZV_TAB = 512;     // iMax values tabulated for 1/Zv
 
 // Error bits of the device error word.
 enum : unsigned {
@@ -57,6 +58,8 @@ struct SpeciesDev {
 struct PairDev {
     double sigmaPrefactor;  // pi dPQ^2 (2 kB Tref / mR)^(omegaPQ - 1/2) / Gamma(5/2 - omegaPQ)
     double expo;            // 1 - omegaPQ: sigma_T cR = prefactor * (cR^2)^expo
+    float sigmaPrefactorF;  // FP32 copies for the acceptance test
+    float expoF;
     double omegaPQ;
     double mR;
     double mPfrac;          // mP / (mP + mQ)
@@ -94,6 +97,10 @@ struct CaseDev {
     long long nBFaces;
     int nAcc;           // doubles per cell of sampling accumulators
     int hasWallMeasure;
+    // 1/Zv of the variable-Zv model by quantised collision level iMax
+    // (dsmcCloud.C:1420-1490 depends on iMax, species and pair omega only):
+    // invZvTab[((p * DSMC_MAX_SPECIES + q) * ZV_TAB) + iMax]
+    const double* invZvTab;
 };
 
 // Sampling accumulators: per cell, per species s at s*SACC + k.

@@ -21,6 +21,7 @@ struct Counters {
     unsigned err;
     int bigCells;
     long long inflowTotal;
+    unsigned long long nSlow;   // parcels deferred to the boundary-path kernel this step
 };
 
 struct StepBuffers {
@@ -38,6 +39,7 @@ struct StepBuffers {
     double* wall;             // [nBFaces][W_N]
     int* bfPatch;             // [nBFaces]
     int* bigList;             // [C]
+    int* slowList;            // [capacity] parcels that take the boundary path this step
     // inflow
     int nInflowFaces;
     long long* inflowFace;    // boundary face ids with inflow [nInflowFaces]

@@ -312,15 +312,19 @@ __device__ __forceinline__ void agg_count(int* count, int key) {
     if (key >= 0 && (int)lane_id() == leader) atomicAdd(&count[key], __popc(peers));
 }
 
-__global__ void __launch_bounds__(MOVE_THREADS)
-k_move(CaseDev cs, Soa s, Counters* ctr, const int* __restrict__ bfPatch, double* wall, int* count) {
+// Interior parcels finish here.  Parcels that are fresh or whose straight
+// move leaves the domain or approaches an obstacle are appended to slowList
+// and tracked by k_move_slow: on GB300 an FP64 instruction costs the whole
+// warp's pipe time, so the ~100-instruction boundary path must not be run by
+// the warp of every wall-adjacent cell for its one or two boundary lanes.
+__global__ void __launch_bounds__(MOVE_THREADS, 4)
+k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count) {
     const long long n = ctr->nMoved;
-    const uint32_t step = (uint32_t)ctr->step;
-    unsigned err = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
         const long long i = base + threadIdx.x;
         int key = -1;
+        bool slow = false;
         if (i < n) {
             const uint32_t w = s.cellw[i];
             bool fast = false;
@@ -357,13 +361,35 @@ k_move(CaseDev cs, Soa s, Counters* ctr, const int* __restrict__ bfPatch, double
                     fast = true;
                 }
             }
-            if (!fast) {
-                const uint32_t nw = move_slow(cs, s, i, step, w, bfPatch, wall, &err, &ctr->wallHits);
-                s.cellw[i] = nw;
-                key = (nw == CELLW_DELETED) ? -1 : (int)(nw >> 3);
-            }
+            slow = !fast;
         }
         agg_count(count, key);
+        // warp-aggregated append of the deferred parcels
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, slow);
+        if (m) {
+            const unsigned lane = lane_id();
+            unsigned long long base0 = 0;
+            if (lane == (unsigned)(__ffs(m) - 1)) base0 = atomicAdd(&ctr->nSlow, (unsigned long long)__popc(m));
+            base0 = __shfl_sync(0xFFFFFFFFu, base0, __ffs(m) - 1);
+            if (slow) slowList[base0 + __popc(m & ((1u << lane) - 1u))] = (int)i;
+        }
+    }
+}
+
+// The boundary path for the parcels k_move deferred, densely packed.
+__global__ void __launch_bounds__(MOVE_THREADS)
+k_move_slow(CaseDev cs, Soa s, Counters* ctr, const int* __restrict__ slowList, const int* __restrict__ bfPatch,
+            double* wall, int* count) {
+    const long long nSlow = (long long)ctr->nSlow;
+    const uint32_t step = (uint32_t)ctr->step;
+    unsigned err = 0;
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nSlow;
+         k += (long long)gridDim.x * blockDim.x) {
+        const long long i = slowList[k];
+        const uint32_t w = s.cellw[i];
+        const uint32_t nw = move_slow(cs, s, i, step, w, bfPatch, wall, &err, &ctr->wallHits);
+        s.cellw[i] = nw;
+        if (nw != CELLW_DELETED) atomicAdd(&count[nw >> 3], 1);
     }
     if (err) atomicOr(&ctr->err, err);
 }
@@ -485,8 +511,23 @@ __global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, Counters* ctr
         int key = -1;
         uint32_t w = CELLW_DELETED;
         if (i < n) {
-            w = src.cellw[i];
+            w = __ldg(src.cellw + i);
             key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
+        }
+        // the parcel's state does not depend on the slot: load it before the
+        // atomic so that the loads overlap the atomic's round trip
+        double x = 0, y = 0, z = 0, ux = 0, uy = 0, uz = 0, er = 0;
+        int vb = 0, lo = 0, hi = 0;
+        uint32_t sp = 0, id = 0;
+        if (key >= 0) {
+            x = __ldg(src.x + i); y = __ldg(src.y + i); z = __ldg(src.z + i);
+            ux = __ldg(src.ux + i); uy = __ldg(src.uy + i); uz = __ldg(src.uz + i);
+            er = __ldg(src.erot + i);
+            vb = __ldg(src.vib + i);
+            sp = __ldg(src.spc + i);
+            id = __ldg(src.id + i);
+            lo = __ldg(start + key);
+            hi = __ldg(start + key + 1);
         }
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
         const int leader = __ffs(peers) - 1;
@@ -495,23 +536,23 @@ __global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, Counters* ctr
         old = __shfl_sync(0xFFFFFFFFu, old, leader);
         if (key >= 0) {
             const int rank = __popc(peers & ((1u << lane) - 1u));
-            const long long slot = (long long)start[key] + old - 1 - rank;
-            if (slot < start[key] || slot >= start[key + 1]) {
+            const long long slot = (long long)lo + old - 1 - rank;
+            if (slot < lo || slot >= hi) {
                 // histogram and scatter disagree: record, never write out of range
                 atomicOr(&ctr->err, ERRB_BOUNDS);
                 continue;
             }
-            dst.x[slot] = src.x[i];
-            dst.y[slot] = src.y[i];
-            dst.z[slot] = src.z[i];
-            dst.ux[slot] = src.ux[i];
-            dst.uy[slot] = src.uy[i];
-            dst.uz[slot] = src.uz[i];
-            dst.erot[slot] = src.erot[i];
-            dst.vib[slot] = src.vib[i];
+            dst.x[slot] = x;
+            dst.y[slot] = y;
+            dst.z[slot] = z;
+            dst.ux[slot] = ux;
+            dst.uy[slot] = uy;
+            dst.uz[slot] = uz;
+            dst.erot[slot] = er;
+            dst.vib[slot] = vb;
             dst.cellw[slot] = w;
-            dst.spc[slot] = src.spc[i];
-            dst.id[slot] = src.id[i];
+            dst.spc[slot] = sp;
+            dst.id[slot] = id;
         }
     }
 }
@@ -796,7 +837,9 @@ int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TIL
 
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
     const int grid = grid_for(B.capacity, MOVE_THREADS, 8);
-    k_move<<<grid, MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.bfPatch, B.wall, B.count);
+    k_move<<<grid, MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList, B.count);
+    k_move_slow<<<grid_for(B.capacity, MOVE_THREADS, 2), MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList,
+                                                                               B.bfPatch, B.wall, B.count);
 }
 
 void launch_count(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
