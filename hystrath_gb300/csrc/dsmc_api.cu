@@ -358,6 +358,10 @@ int sort_current(dsmc_handle* h, long long n) {
 
 }  // namespace
 
+namespace dsmc {
+void set_global_error(const std::string& msg) { g_err = msg; }
+}
+
 extern "C" {
 
 void dsmc_spec_defaults(dsmc_case_spec* s) {
