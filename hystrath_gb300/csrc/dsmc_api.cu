@@ -285,6 +285,7 @@ int check_device_error(dsmc_handle* h) {
         if (e & ERRB_CAPACITY) m += " particle capacity exceeded;";
         if (e & ERRB_BOUNDS) m += " index out of bounds;";
         if (e & ERRB_PATCH) m += " boundary face without a patch;";
+        if (e & ERRB_DENSE) m += " a cell above 16384 parcels or 2^24 candidates (its collisions were skipped);";
         return fail(h, e & ERRB_CAPACITY ? DSMC_ERR_CAPACITY : DSMC_ERR_DEVICE, m);
     }
     return DSMC_OK;
@@ -299,9 +300,15 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
     Soa& b = h->buf[parity ^ 1];
     if (ev) cudaEventRecord(ev[0], st);
     launch_zero_step(B, st);
+    // a sample pending from the previous step is taken by the move kernel,
+    // or here when this step does not move
+    if (!(phases & DSMC_PHASE_MOVE)) launch_sample_flush(cs, B, a, 0, st);
     if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
     if (ev) cudaEventRecord(ev[1], st);
-    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st);
+    if (phases & DSMC_PHASE_MOVE) {
+        launch_move(cs, B, a, st);
+        launch_sample_commit(cs, B, 0, st);
+    }
     if (ev) cudaEventRecord(ev[2], st);
     if (phases & DSMC_PHASE_SORT) {
         if (!(phases & DSMC_PHASE_MOVE)) launch_count(cs, B, a, st);
@@ -312,13 +319,18 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
         cudaMemsetAsync(B.count, 0, sizeof(int) * cs.C, st);
     }
     if (ev) cudaEventRecord(ev[3], st);
-    const int doColl = (phases & DSMC_PHASE_COLLIDE) ? 1 : 0;
-    const int doSamp = (phases & DSMC_PHASE_SAMPLE) ? 1 : 0;
-    if (doColl || doSamp) launch_collide_sample(cs, B, (phases & DSMC_PHASE_SORT) ? b : a, doColl, doSamp, st);
+    if (phases & DSMC_PHASE_COLLIDE) launch_collide(cs, B, (phases & DSMC_PHASE_SORT) ? b : a, st);
+    // dsmcVolFields samples the state after the collisions; the sums are
+    // taken when that state is next streamed (the next move, or a flush)
+    if (phases & DSMC_PHASE_SAMPLE) launch_set_pending(B, st);
     if (ev) cudaEventRecord(ev[4], st);
-    launch_end_step(B, doSamp, st);
+    launch_end_step(B, st);
     if (ev) cudaEventRecord(ev[5], st);
 }
+
+// Takes a pending sample of the current state (before fields are read,
+// checkpointed or reset).
+void flush_sample(dsmc_handle* h) { launch_sample_flush(h->cs, h->B, h->buf[h->cur], 1, h->stream); }
 
 int build_graphs(dsmc_handle* h) {
     for (int p = 0; p < 2; ++p) {
@@ -429,29 +441,25 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     h->B.capacity = cap;
 
     CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    if (collide_init()) return fail(h, DSMC_ERR_CUDA, "cannot raise the shared-memory limit of the cell-order kernel");
     StepBuffers& B = h->B;
     if ((rc = alloc_soa(h, &h->buf[0], cap))) return rc;
     if ((rc = alloc_soa(h, &h->buf[1], cap))) return rc;
-    // big-cell staging: id, ux, uy, uz, erot, vib, cellw (as bytes) only
-    if ((rc = dalloc(h, &B.stage.id, cap))) return rc;
-    if ((rc = dalloc(h, &B.stage.ux, cap))) return rc;
-    if ((rc = dalloc(h, &B.stage.uy, cap))) return rc;
-    if ((rc = dalloc(h, &B.stage.uz, cap))) return rc;
-    if ((rc = dalloc(h, &B.stage.erot, cap))) return rc;
-    if ((rc = dalloc(h, &B.stage.vib, cap))) return rc;
-    if ((rc = dalloc(h, &B.stage.cellw, cap))) return rc;
-    if ((rc = dalloc(h, &B.perm, cap))) return rc;
-    if ((rc = dalloc(h, &B.scl, cap))) return rc;
-    if ((rc = dalloc(h, &B.dirty, cap))) return rc;
     if ((rc = dalloc(h, &B.count, cs.C))) return rc;
     if ((rc = dalloc(h, &B.start, cs.C + 1))) return rc;
     if ((rc = dalloc(h, &B.blockSums, scan_scratch_ints(cs.C) + 1))) return rc;
     if ((rc = dalloc(h, &B.smax, cs.C))) return rc;
     if ((rc = dalloc(h, &B.rem, cs.C))) return rc;
     if ((rc = dalloc(h, &B.acc, cs.C * cs.nAcc))) return rc;
+    if ((rc = dalloc(h, &B.sfix, cs.C * cs.nSpecies * SACC))) return rc;
     if ((rc = dalloc(h, &B.wall, cs.nBFaces * W_N))) return rc;
     if ((rc = dalloc(h, &B.bfPatch, cs.nBFaces))) return rc;
     if ((rc = dalloc(h, &B.bigList, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.work, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.ncCell, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.buckets, 32))) return rc;
+    if ((rc = dalloc(h, &B.perm, cap))) return rc;
+    if ((rc = dalloc(h, &B.subs, cs.C))) return rc;
     if ((rc = dalloc(h, &B.slowList, cap))) return rc;
     if ((rc = dalloc(h, &B.ctr, 1))) return rc;
     if ((rc = dalloc(h, &h->solid, cs.C))) return rc;
@@ -741,6 +749,8 @@ int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n
     }
     if (nm == "accumulators") {
         if (n != C * h->cs.nAcc) return fail(h, DSMC_ERR_INVALID, "n must equal cells x accumulators");
+        flush_sample(h);
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
         CUDA_TRY(h, cudaMemcpy(out, h->B.acc, sizeof(double) * n, cudaMemcpyDeviceToHost));
         return DSMC_OK;
     }
@@ -774,6 +784,7 @@ int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n) {
         return fail(h, DSMC_ERR_INVALID, std::string("unknown field ") + name + "; valid:" + valid);
     }
     if (n != h->cs.C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
+    flush_sample(h);
     launch_field(h->cs, h->B, which, h->fieldTmp, h->spec.measure_mean_free_path, h->spec.mfp_tref, h->stream);
     CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaMemcpyAsync(out, h->fieldTmp, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
@@ -812,17 +823,22 @@ int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long
 }
 
 int dsmc_reset_sampling(dsmc_handle* h) {
+    // a pending sample belongs to the window being discarded
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     CUDA_TRY(h, cudaMemset(h->B.acc, 0, sizeof(double) * h->cs.C * h->cs.nAcc));
+    CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
     CUDA_TRY(h, cudaMemset(h->B.wall, 0, sizeof(double) * h->cs.nBFaces * W_N));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
     h->ctrHost->sampleSteps = 0;
+    h->ctrHost->pendingSample = 0;
+    h->ctrHost->unflushed = 0;
     CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
     return DSMC_OK;
 }
 
 int dsmc_info(dsmc_handle* h, dsmc_info_t* o) {
     std::memset(o, 0, sizeof(*o));
+    flush_sample(h);
     launch_info(h->cs, cur_soa(h), h->B.ctr, h->info6, h->stream);
     CUDA_TRY(h, cudaGetLastError());
     double v[6];
@@ -851,6 +867,7 @@ int dsmc_info(dsmc_handle* h, dsmc_info_t* o) {
 // Checkpoint layout: magic, version, C, nAcc, nBFaces, nInflow, counters,
 // particles (SoA arrays of n), smax, rem, acc, wall, inflow accumulators.
 int dsmc_checkpoint(dsmc_handle* h, const char* path) {
+    flush_sample(h);
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
     const Counters c = *h->ctrHost;
@@ -925,6 +942,7 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
     *h->ctrHost = c;
     CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemset(h->B.count, 0, sizeof(int) * h->cs.C));
+    CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
     return DSMC_OK;
 }
 

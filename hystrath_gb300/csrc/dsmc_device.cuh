@@ -31,7 +31,7 @@ constexpr int ZV_TAB = 512;     // iMax values tabulated for 1/Zv
 // Error bits of the device error word.
 enum : unsigned {
     ERRB_CROSSINGS = 1u, ERRB_REJECTION = 2u, ERRB_CAPACITY = 4u, ERRB_BOUNDS = 8u,
-    ERRB_PATCH = 16u
+    ERRB_PATCH = 16u, ERRB_DENSE = 32u
 };
 
 // Random-stream tags (counter word 3) shared with the CPU replay.
@@ -202,6 +202,51 @@ __device__ __forceinline__ int floor2_bits(double t) {
 
 __device__ __forceinline__ int floor2_coord(const CaseDev& cs, double x, int a) {
     return floor2_bits(fma(x, cs.inv[a], cs.negOinv[a]));
+}
+
+// ------------------------------------------------------- sampling sums
+// The per-step sums of the dsmcVolFields sample loop are exact integer
+// fixed-point sums (value * 2^F), so they come out the same for any parcel
+// order and any grouping of partial sums; they are added to the FP64
+// accumulators once per cell.
+constexpr int F_U = 28;        // velocity: resolution 3.7e-9 m/s
+constexpr int F_UU = 14;       // |U|^2: resolution 6.1e-5 m^2/s^2
+constexpr int F_E = 100;       // rotational energy: resolution 7.9e-31 J
+
+// round(v 2^F), halves away from zero, from the bits on the integer pipe;
+// |v 2^F| must stay below 2^62 (saturates and flags otherwise)
+__device__ __forceinline__ long long fixp(double v, int F, unsigned* err) {
+    const long long b = __double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF);
+    if (e == 0) return 0;
+    const long long m = (b & 0x000FFFFFFFFFFFFFll) | 0x0010000000000000ll;
+    const int sh = e - 1075 + F;
+    long long r;
+    if (sh >= 0) {
+        if (sh > 9) { *err |= ERRB_BOUNDS; r = (1ll << 62); }
+        else r = m << sh;
+    } else if (sh > -63) {
+        const int rs = -sh;
+        r = (m >> rs) + ((m >> (rs - 1)) & 1);
+    } else {
+        r = 0;
+    }
+    return b < 0 ? -r : r;
+}
+
+__device__ __forceinline__ double unfix(long long s, int F) { return ldexp((double)s, -F); }
+
+// Sum of v over this lane's run of the warp (a run starts at every lane set
+// in headMask; lane 0 always starts one).  The run's last lane holds the total.
+__device__ __forceinline__ long long seg_sum(long long v, unsigned headMask) {
+    const int lane = (int)(threadIdx.x & 31u);
+    const int segStart = 31 - __clz(headMask & (0xFFFFFFFFu >> (31 - lane)));
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane - o >= segStart) v += y;
+    }
+    return v;
 }
 
 __device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }

@@ -19,26 +19,32 @@ struct Counters {
     long long nextId;
     long long sampleSteps;
     unsigned err;
-    int bigCells;
+    int bigCells;           // listed cells too large for one warp to order
     long long inflowTotal;
     unsigned long long nSlow;   // parcels deferred to the boundary-path kernel this step
+    int pendingSample;          // the state after the last collide is still to be sampled
+    int unflushed;              // samples held in the fixed-point sums
+    unsigned long long nWork;   // cells with candidates this step
+    unsigned long long nHeavy;  // of which one warp each (the first nHeavy of the work list)
 };
 
 struct StepBuffers {
     Soa a, b;                 // current / other particle buffers
-    Soa stage;                // slot-indexed staging for cells too big for shared memory
-    int* perm;                // slot-indexed scratch for big cells
-    int* scl;
-    unsigned char* dirty;
     int* count;               // [C]
     int* start;               // [C+1]
     int* blockSums;           // scan scratch
     double* smax;             // sigmaTcRMax [C]
     double* rem;              // collisionSelectionRemainder [C]
-    double* acc;              // sampling accumulators [C][nAcc]
+    double* acc;              // sampling accumulators, accumulator-major [nAcc][C]
+    long long* sfix;          // one sample's fixed-point sums [nSpecies*SACC][C]
     double* wall;             // [nBFaces][W_N]
     int* bfPatch;             // [nBFaces]
-    int* bigList;             // [C]
+    int2* work;               // [C] cells with candidates: (cell, candidates)
+    int* bigList;             // [C] work indices of cells ordered by one block
+    int* ncCell;              // [C] candidates of each cell this step
+    unsigned* buckets;        // [32] work-slot counts and cursors
+    uint16_t* perm;           // [capacity] canonical member order of the cells with candidates
+    uint4* subs;              // [C] sub-cell starts in that order, per work item
     int* slowList;            // [capacity] parcels that take the boundary path this step
     // inflow
     int nInflowFaces;
@@ -73,9 +79,20 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Soa& src, const Soa& dst,
                     cudaStream_t st);
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
-void launch_collide_sample(const CaseDev& cs, const StepBuffers& B, const Soa& s, int doCollide,
-                           int doSample, cudaStream_t st);
-void launch_end_step(const StepBuffers& B, int sampled, cudaStream_t st);
+void launch_collide(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st);
+// one-time kernel attributes (large dynamic shared memory); call before the
+// first capture
+int collide_init();
+// Sampling: the move kernel folds a pending sample of the pre-move state into
+// per-cell fixed-point sums; launch_sample_flush takes a pending sample of the
+// current state when no move follows.  Both then add the sums to the FP64
+// accumulators and count the sample.
+// force: add the fixed-point sums to the FP64 accumulators now (otherwise
+// every 32 samples).
+void launch_sample_commit(const CaseDev& cs, const StepBuffers& B, int force, cudaStream_t st);
+void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Soa& s, int force, cudaStream_t st);
+void launch_set_pending(const StepBuffers& B, cudaStream_t st);
+void launch_end_step(const StepBuffers& B, cudaStream_t st);
 void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Soa& s,
                    cudaStream_t st);
 void launch_init_count(const CaseDev& cs, const double* dnd, const unsigned char* solid, int* cellCounts,

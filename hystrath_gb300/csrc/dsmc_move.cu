@@ -312,25 +312,83 @@ __device__ __forceinline__ void agg_count(int* count, int key) {
     if (key >= 0 && (int)lane_id() == leader) atomicAdd(&count[key], __popc(peers));
 }
 
+// One parcel's contribution to the dsmcVolFields sample sums
+// (dsmcVolFields.C:1115-1239) per lane, valid when skey = cell * 8 + species
+// is not negative: summed over the warp's runs of equal keys and added to the
+// per-cell fixed-point sums with 64-bit integer atomics, so the result does
+// not depend on the order of parcels, warps or atomics.
+__device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int skey, double ux, double uy,
+                                               double uz, double er, int vb, unsigned* err) {
+    long long f[SACC] = {0, 0, 0, 0, 0, 0, 0};
+    if (skey >= 0) {
+        f[SACC_N] = 1;
+        f[SACC_UX] = fixp(ux, F_U, err);
+        f[SACC_UY] = fixp(uy, F_U, err);
+        f[SACC_UZ] = fixp(uz, F_U, err);
+        // |U|^2 in fixed point from the fixed-point components, on the
+        // integer pipe: (u 2^32)^2 >> 48 = u^2 2^16
+        unsigned long long uu = 0;
+#pragma unroll
+        for (int a = SACC_UX; a <= SACC_UZ; ++a) {
+            const unsigned long long m = (unsigned long long)(f[a] < 0 ? -f[a] : f[a]);
+            const unsigned long long hi = __umul64hi(m, m);
+            if (hi >> 46) *err |= ERRB_BOUNDS;
+            uu += (hi << (64 - (2 * F_U - F_UU))) | ((m * m) >> (2 * F_U - F_UU));
+        }
+        f[SACC_UU] = (long long)uu;
+        f[SACC_EROT] = fixp(er, F_E, err);
+        f[SACC_VIB] = vb;
+    }
+    const unsigned lane = lane_id();
+    const int prev = __shfl_up_sync(0xFFFFFFFFu, skey, 1);
+    const unsigned hm = __ballot_sync(0xFFFFFFFFu, lane == 0 || prev != skey);
+#pragma unroll
+    for (int k = 0; k < SACC; ++k) f[k] = seg_sum(f[k], hm);
+    const bool tail = lane == 31 || ((hm >> (lane + 1)) & 1u);
+    if (tail && skey >= 0) {
+        const long long c = skey >> 3;
+        const int sp = skey & 7;
+#pragma unroll
+        for (int k = 0; k < SACC; ++k)
+            if (f[k]) atomicAdd(reinterpret_cast<unsigned long long*>(sfix + (long long)(sp * SACC + k) * C + c),
+                                (unsigned long long)f[k]);
+    }
+}
+
 // Interior parcels finish here.  Parcels that are fresh or whose straight
 // move leaves the domain or approaches an obstacle are appended to slowList
 // and tracked by k_move_slow: on GB300 an FP64 instruction costs the whole
 // warp's pipe time, so the ~100-instruction boundary path must not be run by
 // the warp of every wall-adjacent cell for its one or two boundary lanes.
+// When a sample is pending, the kernel also folds the pre-move state (the
+// state after the previous step's collisions, which the reference samples at
+// the end of that step) into the per-cell sample sums: it streams the
+// velocities anyway, in cell order.
 __global__ void __launch_bounds__(MOVE_THREADS, 4)
-k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count) {
+k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count, long long* sfix) {
     const long long n = ctr->nMoved;
+    const int doSample = ctr->pendingSample;
+    unsigned err = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
         const long long i = base + threadIdx.x;
         int key = -1;
         bool slow = false;
+        int skey = -1;
+        double sux = 0, suy = 0, suz = 0, ser = 0;
+        int svb = 0;
         if (i < n) {
             const uint32_t w = s.cellw[i];
             bool fast = false;
             if (!(w & CELLW_FRESH)) {
                 const double x = s.x[i], y = s.y[i], z = s.z[i];
                 const double ux = s.ux[i], uy = s.uy[i], uz = s.uz[i];
+                if (doSample) {
+                    skey = (int)(cellw_cell(w) * 8u + s.spc[i]);
+                    sux = ux; suy = uy; suz = uz;
+                    ser = s.erot[i];
+                    svb = s.vib[i];
+                }
                 const double ex = fma(ux, cs.dt, x);
                 const double ey = fma(uy, cs.dt, y);
                 const double ez = fma(uz, cs.dt, z);
@@ -373,8 +431,71 @@ k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count) {
             base0 = __shfl_sync(0xFFFFFFFFu, base0, __ffs(m) - 1);
             if (slow) slowList[base0 + __popc(m & ((1u << lane) - 1u))] = (int)i;
         }
+        if (doSample) sample_contrib(sfix, cs.C, skey, sux, suy, suz, ser, svb, &err);
+    }
+    if (err) atomicOr(&ctr->err, err);
+}
+
+// A pending sample of the current state when no move follows.
+__global__ void __launch_bounds__(MOVE_THREADS)
+k_sample_pass(CaseDev cs, Soa s, Counters* ctr, long long* sfix) {
+    if (!ctr->pendingSample) return;
+    const long long n = ctr->n;
+    unsigned err = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
+        const long long i = base + threadIdx.x;
+        int skey = -1;
+        double ux = 0, uy = 0, uz = 0, er = 0;
+        int vb = 0;
+        if (i < n) {
+            const uint32_t w = s.cellw[i];
+            if (w != CELLW_DELETED && !(w & CELLW_FRESH)) {
+                skey = (int)(cellw_cell(w) * 8u + s.spc[i]);
+                ux = s.ux[i]; uy = s.uy[i]; uz = s.uz[i];
+                er = s.erot[i];
+                vb = s.vib[i];
+            }
+        }
+        sample_contrib(sfix, cs.C, skey, ux, uy, uz, er, vb, &err);
+    }
+    if (err) atomicOr(&ctr->err, err);
+}
+
+// Adds the fixed-point sums of the samples taken so far to the FP64
+// accumulators and clears them: every SAMPLES_PER_FLUSH samples and whenever
+// the fields are read.  32 samples of a cell of 2^16 parcels at 8 km/s stay
+// below 2^62 in every sum (2^41 per velocity component, 2^40 per |U|^2, 2^40
+// per rotational energy of 1e-18 J).
+constexpr int SAMPLES_PER_FLUSH = 32;
+
+__global__ void k_sample_finalize(CaseDev cs, const Counters* ctr, long long* sfix, double* acc, int force) {
+    if (ctr->unflushed == 0 || (!force && ctr->unflushed < SAMPLES_PER_FLUSH)) return;
+    const long long total = (long long)cs.nSpecies * SACC * cs.C;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const long long v = sfix[idx];
+        if (!v) continue;
+        const int k = (int)((idx / cs.C) % SACC);
+        const int F = (k == SACC_UU) ? F_UU : (k == SACC_EROT) ? F_E : F_U;
+        acc[idx] += (k == SACC_N || k == SACC_VIB) ? (double)v : unfix(v, F);
+        sfix[idx] = 0;
     }
 }
+
+__global__ void k_sample_done(Counters* ctr) {
+    if (ctr->pendingSample) {
+        ctr->sampleSteps += 1;
+        ctr->unflushed += 1;
+        ctr->pendingSample = 0;
+    }
+}
+
+__global__ void k_sample_flushed(Counters* ctr, int force) {
+    if (force || ctr->unflushed >= SAMPLES_PER_FLUSH) ctr->unflushed = 0;
+}
+
+__global__ void k_set_pending(Counters* ctr) { ctr->pendingSample = 1; }
 
 // The boundary path for the parcels k_move deferred, densely packed.
 __global__ void __launch_bounds__(MOVE_THREADS)
@@ -563,12 +684,11 @@ __global__ void k_finish_sort(Counters* ctr) {
     ctr->nMoved = ctr->nKept;
 }
 
-__global__ void k_end_step(Counters* ctr, int sampled) {
+__global__ void k_end_step(Counters* ctr) {
     ctr->collTot += ctr->coll;
     ctr->candTot += ctr->cand;
     ctr->bigCells = 0;
     ctr->step += 1;
-    if (sampled) ctr->sampleSteps += 1;
 }
 
 // ---------------------------------------------------------------- inflow
@@ -837,7 +957,7 @@ int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TIL
 
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
     const int grid = grid_for(B.capacity, MOVE_THREADS, 8);
-    k_move<<<grid, MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList, B.count);
+    k_move<<<grid, MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
     k_move_slow<<<grid_for(B.capacity, MOVE_THREADS, 2), MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList,
                                                                                B.bfPatch, B.wall, B.count);
 }
@@ -866,8 +986,22 @@ void launch_finish_sort(const StepBuffers& B, cudaStream_t st) {
     k_finish_sort<<<1, 1, 0, st>>>(B.ctr);
 }
 
-void launch_end_step(const StepBuffers& B, int sampled, cudaStream_t st) {
-    k_end_step<<<1, 1, 0, st>>>(B.ctr, sampled);
+void launch_sample_commit(const CaseDev& cs, const StepBuffers& B, int force, cudaStream_t st) {
+    const long long total = (long long)cs.nSpecies * SACC * cs.C;
+    k_sample_done<<<1, 1, 0, st>>>(B.ctr);
+    k_sample_finalize<<<grid_for(total, 256, 8), 256, 0, st>>>(cs, B.ctr, B.sfix, B.acc, force);
+    k_sample_flushed<<<1, 1, 0, st>>>(B.ctr, force);
+}
+
+void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Soa& s, int force, cudaStream_t st) {
+    k_sample_pass<<<grid_for(B.capacity, MOVE_THREADS, 8), MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.sfix);
+    launch_sample_commit(cs, B, force, st);
+}
+
+void launch_set_pending(const StepBuffers& B, cudaStream_t st) { k_set_pending<<<1, 1, 0, st>>>(B.ctr); }
+
+void launch_end_step(const StepBuffers& B, cudaStream_t st) {
+    k_end_step<<<1, 1, 0, st>>>(B.ctr);
 }
 
 void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Soa& s,

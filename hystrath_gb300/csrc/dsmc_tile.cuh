@@ -1,0 +1,451 @@
+// dsmc_tile.cuh -- the per-cell collision kernels (noTimeCounter::collide,
+// noTimeCounter.C:81-339).
+//
+// Order of work in one step:
+//   k_ntc_select    one thread per cell: the number of candidate pairs
+//                   (selectedPairs, noTimeCounter.C:146-153) and the
+//                   remainder update; counts cells per work class.
+//   k_ntc_buckets   offsets of the work classes.
+//   k_ntc_list      the cells with candidates, grouped by class.
+//   k_cell_order    one warp per listed cell (one block above ORDER_WARP_N
+//                   parcels): the cell's members sorted by (sub-cell, parcel
+//                   id).  This is the cell's canonical list: sub-cells are
+//                   contiguous in it and it does not depend on the order in
+//                   which the sort scatter left the parcels in memory.
+//   k_collide_heavy one warp per cell with many candidates or parcels.
+//   k_collide_light one lane per remaining cell.
+//
+// Every candidate k of cell c draws from its own counter-based stream
+// (cell, step, k): its pair (the reference's randomLabel draws over the
+// cell's list, with the redraw while Q == P, noTimeCounter.C:164-198), its
+// acceptance test and its post-collision draws.  A candidate therefore depends
+// only on the state of its own two parcels when it runs, so the heavy kernel
+// runs up to 32 candidates of one cell at once: each round runs every
+// candidate that shares no parcel with an earlier candidate still waiting,
+// which gives exactly the result of running them one after the other
+// (disjoint candidates commute).  The light kernel runs its cell's candidates
+// one after the other in one lane.  Both give the same result for a cell, so
+// the split between them is a matter of speed only.
+//
+// Serial work is spread across lanes because GB300 issues an FP64 instruction
+// over the whole warp whatever the active mask.
+#pragma once
+
+namespace tile {
+
+constexpr int WARPS = 4;             // warps per block
+constexpr int LIGHT_N = 64;          // light cells: at most this many parcels
+constexpr int LIGHT_CAND = 8;        //   and fewer candidates than this
+constexpr int ORDER_WARP_N = 1024;   // cells up to this size are ordered by one warp
+constexpr int ORDER_MAX_N = 16384;   // cells up to this size are ordered by one block
+constexpr int ORDER_BLOCK = 512;     // threads of the block that orders a large cell
+constexpr int NBUCKET = 8;           // candidate-count buckets per class
+constexpr int MAX_CAND = 1 << 24;    // candidates of one cell in one step
+
+// bucket b holds candidate counts in [2^b, 2^(b+1)); heavier buckets come
+// first in the work list so that they start first
+__device__ __forceinline__ int bucket_of(int nc) {
+    const int b = 31 - __clz(nc);
+    return b < NBUCKET - 1 ? b : NBUCKET - 1;
+}
+
+__device__ __forceinline__ bool is_heavy(int n, int nc) { return n > LIGHT_N || nc >= LIGHT_CAND; }
+
+__device__ __forceinline__ int slot_of(int n, int nc) { return (is_heavy(n, nc) ? NBUCKET : 0) + bucket_of(nc); }
+
+// the 16-bit field s (0..7) of a packed sub-cell start table
+__device__ __forceinline__ int get16(const uint4& w, int s) {
+    const unsigned x = s < 2 ? w.x : s < 4 ? w.y : s < 6 ? w.z : w.w;
+    return (int)((x >> ((s & 1) << 4)) & 0xFFFFu);
+}
+
+// ------------------------------------------------------------ selection
+// selectedPairs and the remainder, one thread per cell; the candidate count
+// of each cell is kept for k_ntc_list and counted per slot
+__global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const double* __restrict__ smax, double* rem,
+                             Counters* ctr, int* ncCell, unsigned* slotCount) {
+    __shared__ unsigned hist[2 * NBUCKET];
+    if (threadIdx.x < 2 * NBUCKET) hist[threadIdx.x] = 0;
+    __syncthreads();
+    const long long C = cs.C;
+    unsigned err = 0;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < C;
+         c += (long long)gridDim.x * blockDim.x) {
+        int nc = 0;
+        const int n = start[c + 1] - start[c];
+        if (n > 1) {
+            const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * smax[c] * cs.dt / cs.V;
+            const double whole = floor(sel);
+            rem[c] = sel - whole;
+            if (n > ORDER_MAX_N || whole >= (double)MAX_CAND) err |= ERRB_DENSE;
+            else nc = (int)whole;
+        }
+        ncCell[c] = nc;
+        if (nc > 0) atomicAdd(&hist[slot_of(n, nc)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * NBUCKET && hist[threadIdx.x]) atomicAdd(&slotCount[threadIdx.x], hist[threadIdx.x]);
+    if (err) atomicOr(&ctr->err, err);
+}
+
+// slot offsets: heavy slots first, heaviest first; resets the counts
+__global__ void k_ntc_buckets(Counters* ctr, unsigned* slotCount, unsigned* slotCursor) {
+    unsigned off = 0;
+    for (int b = 2 * NBUCKET - 1; b >= 0; --b) {
+        slotCursor[b] = off;
+        off += slotCount[b];
+        slotCount[b] = 0;
+        if (b == NBUCKET) ctr->nHeavy = off;
+    }
+    ctr->nWork = off;
+}
+
+// work list of the cells with candidates; cells too large for one warp to
+// order are also listed (by work index) for k_cell_order_big
+__global__ void k_ntc_list(long long C, const int* __restrict__ start, const int* __restrict__ ncCell,
+                           unsigned* slotCursor, int2* work, int* bigList, Counters* ctr) {
+    const unsigned lane = threadIdx.x & 31u;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < C; base += (long long)gridDim.x * blockDim.x) {
+        const long long c = base + threadIdx.x;
+        int nc = 0, n = 0;
+        if (c < C) {
+            nc = ncCell[c];
+            if (nc > 0) n = start[c + 1] - start[c];
+        }
+        if (!__ballot_sync(0xFFFFFFFFu, nc > 0)) continue;
+        const int slot = nc > 0 ? slot_of(n, nc) : -1;
+        // one atomic per slot present in the warp
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, slot);
+        const int leader = __ffs(peers) - 1;
+        unsigned q0 = 0;
+        if (nc > 0 && (int)lane == leader) q0 = atomicAdd(&slotCursor[slot], (unsigned)__popc(peers));
+        q0 = __shfl_sync(0xFFFFFFFFu, q0, leader);
+        if (nc > 0) {
+            const unsigned q = q0 + __popc(peers & ((1u << lane) - 1u));
+            work[q] = make_int2((int)c, nc);
+            if (n > ORDER_WARP_N) bigList[atomicAdd(&ctr->bigCells, 1)] = (int)q;
+        }
+    }
+}
+
+// ------------------------------------------------------------ ordering
+// Key of member j: (sub-cell, parcel id, j).  Ids are unique, so the order is
+// total and j rides in the low bits.
+__device__ __forceinline__ unsigned long long order_key(uint32_t cellw, uint32_t id, int j) {
+    return ((unsigned long long)(cellw & 7u) << 48) | ((unsigned long long)id << 16) | (unsigned long long)j;
+}
+
+// bitonic sort of keys[0, N) (N a power of two) by the nt threads of a group
+// (thread t) that all call it; bar() synchronises the group
+template <class Bar>
+__device__ __forceinline__ void bitonic(unsigned long long* keys, int N, int t, int nt, Bar bar) {
+    for (int k = 2; k <= N; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = t; i < (N >> 1); i += nt) {
+                const int lo = ((i & ~(j - 1)) << 1) | (i & (j - 1));
+                const int hi = lo + j;
+                const unsigned long long a = keys[lo], b = keys[hi];
+                const bool up = (lo & k) == 0;
+                if ((a > b) == up) { keys[lo] = b; keys[hi] = a; }
+            }
+            bar();
+        }
+    }
+}
+
+__device__ __forceinline__ uint4 pack_starts(const int* cnt) {
+    int so[8];
+    int acc = 0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) { so[b] = acc; acc += cnt[b]; }
+    return make_uint4((unsigned)so[0] | ((unsigned)so[1] << 16), (unsigned)so[2] | ((unsigned)so[3] << 16),
+                      (unsigned)so[4] | ((unsigned)so[5] << 16), (unsigned)so[6] | ((unsigned)so[7] << 16));
+}
+
+struct WarpBar {
+    __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+struct BlockBar {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+
+// one warp per listed cell of at most ORDER_WARP_N parcels: perm[off + r] is
+// the local index of the r-th member in canonical order, subs[q] the start
+// of each sub-cell in it
+__global__ void __launch_bounds__(WARPS * 32)
+k_cell_order(Soa s, const int* __restrict__ start, const Counters* ctr, const int2* __restrict__ work,
+             uint16_t* perm, uint4* subs) {
+    __shared__ unsigned long long keysAll[WARPS][ORDER_WARP_N];
+    unsigned long long* keys = keysAll[threadIdx.x >> 5];
+    const int lane = (int)(threadIdx.x & 31u);
+    const long long nWork = (long long)ctr->nWork;
+    const long long nWarps = (long long)gridDim.x * WARPS;
+    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nWork; q += nWarps) {
+        const int c = work[q].x;
+        const long long off = start[c];
+        const int n = start[c + 1] - (int)off;
+        if (n > ORDER_WARP_N) continue;
+        int N = 32;
+        while (N < n) N <<= 1;
+        int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int j0 = 0; j0 < N; j0 += 32) {
+            const int j = j0 + lane;
+            unsigned long long key = ~0ull;
+            int sb = 8;
+            if (j < n) {
+                const uint32_t w = s.cellw[off + j];
+                sb = (int)(w & 7u);
+                key = order_key(w, s.id[off + j], j);
+            }
+            keys[j] = key;
+#pragma unroll
+            for (int b = 0; b < 8; ++b) cnt[b] += __popc(__ballot_sync(0xFFFFFFFFu, sb == b));
+        }
+        __syncwarp();
+        bitonic(keys, N, lane, 32, WarpBar());
+        for (int r = lane; r < n; r += 32) perm[off + r] = (uint16_t)(keys[r] & 0xFFFFu);
+        if (lane == 0) subs[q] = pack_starts(cnt);
+        __syncwarp();
+    }
+}
+
+// one block per listed cell above ORDER_WARP_N parcels (dynamic shared
+// memory of ORDER_MAX_N keys)
+__global__ void __launch_bounds__(ORDER_BLOCK)
+k_cell_order_big(Soa s, const int* __restrict__ start, const Counters* ctr, const int2* __restrict__ work,
+                 const int* __restrict__ bigList, uint16_t* perm, uint4* subs) {
+    extern __shared__ unsigned long long keysBig[];
+    __shared__ int cnt[8];
+    const int nBig = ctr->bigCells;
+    for (int b = blockIdx.x; b < nBig; b += gridDim.x) {
+        const int q = bigList[b];
+        const int c = work[q].x;
+        const long long off = start[c];
+        const int n = start[c + 1] - (int)off;
+        int N = 32;
+        while (N < n) N <<= 1;
+        if (threadIdx.x < 8) cnt[threadIdx.x] = 0;
+        __syncthreads();
+        for (int j = threadIdx.x; j < N; j += blockDim.x) {
+            unsigned long long key = ~0ull;
+            if (j < n) {
+                const uint32_t w = s.cellw[off + j];
+                atomicAdd(&cnt[w & 7u], 1);
+                key = order_key(w, s.id[off + j], j);
+            }
+            keysBig[j] = key;
+        }
+        __syncthreads();
+        bitonic(keysBig, N, (int)threadIdx.x, (int)blockDim.x, BlockBar());
+        for (int r = threadIdx.x; r < n; r += blockDim.x) perm[off + r] = (uint16_t)(keysBig[r] & 0xFFFFu);
+        if (threadIdx.x == 0) {
+            int c8[8];
+            for (int k = 0; k < 8; ++k) c8[k] = cnt[k];
+            subs[q] = pack_starts(c8);
+        }
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------ candidates
+// One accepted collision: Larsen-Borgnakke redistribution (or plain VHS) and
+// the isotropic centre-of-mass scatter (VariableHardSphere.C:191-228).
+struct Post {
+    double UP[3], UQ[3];
+    double eP, eQ;
+    int vP, vQ;
+};
+
+__device__ __forceinline__ void collide_pair(const CaseDev& cs, Rng& r, const PairDev& pr, int tP, int tQ,
+                                             double cr2, Post& o, unsigned* err) {
+    double cR;
+    if (cs.collModel == DSMC_COLL_LB_VHS) {
+        double Et = 0.5 * pr.mR * cr2;
+        redistribute(cs, cs.sp[tP], &o.eP, &o.vP, Et, pr.omegaPQ, r, zv_row(cs, tP, tQ), err);
+        redistribute(cs, cs.sp[tQ], &o.eQ, &o.vQ, Et, pr.omegaPQ, r, zv_row(cs, tQ, tP), err);
+        cR = sqrt(2.0 * Et / pr.mR);
+    } else {
+        cR = sqrt(cr2);
+    }
+    double Ucm[3];
+    for (int a = 0; a < 3; ++a) Ucm[a] = pr.mPfrac * o.UP[a] + pr.mQfrac * o.UQ[a];
+    const double cosT = 2.0 * r.u01() - 1.0;
+    const double sinT = sqrt(1.0 - cosT * cosT);
+    const double phi = 2.0 * PI * r.u01();
+    double sph, cph;
+    sincos(phi, &sph, &cph);
+    const double prel[3] = {cR * cosT, cR * sinT * cph, cR * sinT * sph};
+    for (int a = 0; a < 3; ++a) {
+        o.UP[a] = Ucm[a] + prel[a] * pr.mQfrac;
+        o.UQ[a] = Ucm[a] - prel[a] * pr.mPfrac;
+    }
+}
+
+// Positions (in the canonical list of n members with sub-cell starts so) of
+// candidate pair P, Q: P uniform over the cell, Q uniform over P's sub-cell
+// when it holds another member, else over the cell; Q != P.
+__device__ __forceinline__ void draw_pair(Rng& r, int n, const uint4& so, int* pP, int* pQ, unsigned* err) {
+    const int p = r.label(0, n - 1, err);
+    int sub = 0;
+#pragma unroll
+    for (int b = 1; b < 8; ++b) sub += (get16(so, b) <= p) ? 1 : 0;
+    const int lo = get16(so, sub);
+    const int hi = sub < 7 ? get16(so, sub + 1) : n;
+    int q = p;
+    if (hi - lo > 1) {
+        for (int it = 0; it < MAX_REJECTION && q == p; ++it) q = lo + r.label(0, hi - lo - 1, err);
+    } else {
+        for (int it = 0; it < MAX_REJECTION && q == p; ++it) q = r.label(0, n - 1, err);
+    }
+    if (q == p) {
+        *err |= ERRB_REJECTION;
+        q = p == 0 ? 1 : 0;
+    }
+    *pP = p;
+    *pQ = q;
+}
+
+// Candidate (gP, gQ): sigma_T c_R, the running maximum, the acceptance test
+// against the maximum the candidate count was based on, and the collision.
+__device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Soa& s, Rng& r, long long gP, long long gQ,
+                                              double smax0, double* smaxRun, double* collSep, unsigned* err) {
+    const int tP = (int)s.spc[gP], tQ = (int)s.spc[gQ];
+    const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
+    Post o;
+    o.UP[0] = s.ux[gP]; o.UP[1] = s.uy[gP]; o.UP[2] = s.uz[gP];
+    o.UQ[0] = s.ux[gQ]; o.UQ[1] = s.uy[gQ]; o.UQ[2] = s.uz[gQ];
+    const double d0 = o.UP[0] - o.UQ[0], d1 = o.UP[1] - o.UQ[1], d2 = o.UP[2] - o.UQ[2];
+    const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
+    const double sigma = sigma_cr(pr, cr2);
+    if (sigma > *smaxRun) *smaxRun = sigma;
+    if (!(sigma > r.u01() * smax0)) return false;      // (sigma/smax0) > U with smax0 > 0
+    o.eP = s.erot[gP]; o.eQ = s.erot[gQ];
+    o.vP = s.vib[gP]; o.vQ = s.vib[gQ];
+    collide_pair(cs, r, pr, tP, tQ, cr2, o, err);
+    s.ux[gP] = o.UP[0]; s.uy[gP] = o.UP[1]; s.uz[gP] = o.UP[2];
+    s.ux[gQ] = o.UQ[0]; s.uy[gQ] = o.UQ[1]; s.uz[gQ] = o.UQ[2];
+    s.erot[gP] = o.eP; s.erot[gQ] = o.eQ;
+    s.vib[gP] = o.vP; s.vib[gQ] = o.vQ;
+    const double dx = s.x[gP] - s.x[gQ];
+    const double dy = s.y[gP] - s.y[gQ];
+    const double dz = s.z[gP] - s.z[gQ];
+    *collSep += sqrt(dx * dx + dy * dy + dz * dz);
+    return true;
+}
+
+__device__ __forceinline__ uint32_t cand_tag(int k) { return (uint32_t)TAG_COLLIDE | ((uint32_t)k << 8); }
+
+// one warp per heavy cell, up to 32 candidates at a time
+__global__ void __launch_bounds__(WARPS * 32)
+k_collide_heavy(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
+                const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs) {
+    const unsigned lane = lane_id();
+    const uint32_t step = (uint32_t)ctr->step;
+    const long long nHeavy = (long long)ctr->nHeavy;
+    const long long C = cs.C;
+    unsigned err = 0;
+    unsigned long long nColl = 0, nCandTot = 0;
+    const long long nWarps = (long long)gridDim.x * WARPS;
+    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nHeavy; q += nWarps) {
+        const int2 it = work[q];
+        const long long c = it.x;
+        const int nCand = it.y;
+        const long long off = start[c];
+        const int n = start[c + 1] - (int)off;
+        const uint4 so = subs[q];
+        const double smax0 = smax[c];
+        double smaxRun = smax0, collSep = 0.0;
+        unsigned coll = 0;
+        for (int base = 0; base < nCand; base += 32) {
+            const int k = base + (int)lane;
+            Rng r(cs, (uint32_t)c, step, cand_tag(k));
+            long long gP = 0, gQ = 0;
+            int pP = -1, pQ = -1;
+            if (k < nCand) {
+                draw_pair(r, n, so, &pP, &pQ, &err);
+                gP = off + perm[off + pP];
+                gQ = off + perm[off + pQ];
+            }
+            unsigned pend = __ballot_sync(0xFFFFFFFFu, k < nCand);
+            while (pend) {
+                // ready: no earlier waiting candidate shares a parcel
+                bool ready = (pend >> lane) & 1u;
+                unsigned m = pend;
+                while (m) {
+                    const int j = __ffs(m) - 1;
+                    m &= m - 1u;
+                    const int a = __shfl_sync(0xFFFFFFFFu, pP, j);
+                    const int b = __shfl_sync(0xFFFFFFFFu, pQ, j);
+                    if (j < (int)lane && (a == pP || a == pQ || b == pP || b == pQ)) ready = false;
+                }
+                if (ready && run_candidate(cs, s, r, gP, gQ, smax0, &smaxRun, &collSep, &err)) ++coll;
+                __syncwarp();
+                pend &= ~__ballot_sync(0xFFFFFFFFu, ready);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            collSep += __shfl_xor_sync(0xFFFFFFFFu, collSep, o);
+            smaxRun = fmax(smaxRun, __shfl_xor_sync(0xFFFFFFFFu, smaxRun, o));
+            coll += __shfl_xor_sync(0xFFFFFFFFu, coll, o);
+        }
+        if (lane == 0) {
+            smax[c] = smaxRun;
+            if (coll) {
+                acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
+                acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
+            }
+            nColl += coll;
+            nCandTot += (unsigned long long)nCand;
+        }
+    }
+    if (lane == 0) {
+        if (nColl) atomicAdd(&ctr->coll, nColl);
+        if (nCandTot) atomicAdd(&ctr->cand, nCandTot);
+    }
+    if (err) atomicOr(&ctr->err, err);
+}
+
+// one lane per light cell, its candidates one after the other
+__global__ void __launch_bounds__(WARPS * 32, 4)
+k_collide_light(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
+                const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs) {
+    const uint32_t step = (uint32_t)ctr->step;
+    const long long nWork = (long long)ctr->nWork;
+    const long long nHeavy = (long long)ctr->nHeavy;
+    const long long C = cs.C;
+    unsigned err = 0;
+    unsigned long long nColl = 0, nCandTot = 0;
+    for (long long q = nHeavy + (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nWork;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int2 it = work[q];
+        const long long c = it.x;
+        const int nCand = it.y;
+        const long long off = start[c];
+        const int n = start[c + 1] - (int)off;
+        const uint4 so = subs[q];
+        const double smax0 = smax[c];
+        double smaxRun = smax0, collSep = 0.0;
+        unsigned coll = 0;
+        for (int k = 0; k < nCand; ++k) {
+            Rng r(cs, (uint32_t)c, step, cand_tag(k));
+            int pP, pQ;
+            draw_pair(r, n, so, &pP, &pQ, &err);
+            const long long gP = off + perm[off + pP];
+            const long long gQ = off + perm[off + pQ];
+            if (run_candidate(cs, s, r, gP, gQ, smax0, &smaxRun, &collSep, &err)) ++coll;
+        }
+        smax[c] = smaxRun;
+        if (coll) {
+            acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
+            acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
+        }
+        nColl += coll;
+        nCandTot += (unsigned long long)nCand;
+    }
+    if (nColl) atomicAdd(&ctr->coll, nColl);
+    if (nCandTot) atomicAdd(&ctr->cand, nCandTot);
+    if (err) atomicOr(&ctr->err, err);
+}
+
+}  // namespace tile
