@@ -461,6 +461,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.perm, cap))) return rc;
     if ((rc = dalloc(h, &B.subs, cs.C))) return rc;
     if ((rc = dalloc(h, &B.slowList, cap))) return rc;
+    if ((rc = dalloc(h, &B.sortIdx, cap))) return rc;
     if ((rc = dalloc(h, &B.ctr, 1))) return rc;
     if ((rc = dalloc(h, &h->solid, cs.C))) return rc;
     if ((rc = dalloc(h, &h->info6, 8))) return rc;

@@ -292,8 +292,7 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaS
         s, B.start, B.ctr, B.work, B.bigList, B.perm, B.subs);
     tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
                                                                 B.perm, B.subs);
-    tile::k_collide_light<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
-                                                                B.perm, B.subs);
+    tile::k_collide_light<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work);
 }
 
 void launch_zero_step(const StepBuffers& B, cudaStream_t st) { k_zero_step<<<1, 1, 0, st>>>(B.ctr); }

@@ -46,6 +46,7 @@ struct StepBuffers {
     uint16_t* perm;           // [capacity] canonical member order of the cells with candidates
     uint4* subs;              // [C] sub-cell starts in that order, per work item
     int* slowList;            // [capacity] parcels that take the boundary path this step
+    int* sortIdx;             // [capacity] source index of each destination slot of the sort
     // inflow
     int nInflowFaces;
     long long* inflowFace;    // boundary face ids with inflow [nInflowFaces]

@@ -622,31 +622,29 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
 }
 
 // ---------------------------------------------------------------- scatter
-__global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, Counters* ctr,
-                                                 const int* __restrict__ start, int* count) {
+// The counting sort runs in two passes.  k_scatter_index gives every kept
+// parcel its slot in cell order (a warp-aggregated atomic per cell present in
+// the warp) and writes only the parcel's source index there.  k_gather then
+// walks the destination slots in order and pulls each parcel's state from its
+// source: every store is coalesced, and the loads of one warp come from a few
+// runs of neighbouring source cells.  Storing the payload from the source side
+// instead leaves most sectors partly written (parcels that changed cell land
+// in short runs all over the destination).
+__global__ void __launch_bounds__(256) k_scatter_index(const uint32_t* __restrict__ cellw, Counters* ctr,
+                                                       const int* __restrict__ start, int* count,
+                                                       int* __restrict__ sortIdx) {
     const long long n = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const unsigned lane = lane_id();
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
         const long long i = base + threadIdx.x;
         int key = -1;
-        uint32_t w = CELLW_DELETED;
         if (i < n) {
-            w = __ldg(src.cellw + i);
+            const uint32_t w = __ldg(cellw + i);
             key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
         }
-        // the parcel's state does not depend on the slot: load it before the
-        // atomic so that the loads overlap the atomic's round trip
-        double x = 0, y = 0, z = 0, ux = 0, uy = 0, uz = 0, er = 0;
-        int vb = 0, lo = 0, hi = 0;
-        uint32_t sp = 0, id = 0;
+        int lo = 0, hi = 0;
         if (key >= 0) {
-            x = __ldg(src.x + i); y = __ldg(src.y + i); z = __ldg(src.z + i);
-            ux = __ldg(src.ux + i); uy = __ldg(src.uy + i); uz = __ldg(src.uz + i);
-            er = __ldg(src.erot + i);
-            vb = __ldg(src.vib + i);
-            sp = __ldg(src.spc + i);
-            id = __ldg(src.id + i);
             lo = __ldg(start + key);
             hi = __ldg(start + key + 1);
         }
@@ -663,18 +661,33 @@ __global__ void __launch_bounds__(256) k_scatter(Soa src, Soa dst, Counters* ctr
                 atomicOr(&ctr->err, ERRB_BOUNDS);
                 continue;
             }
-            dst.x[slot] = x;
-            dst.y[slot] = y;
-            dst.z[slot] = z;
-            dst.ux[slot] = ux;
-            dst.uy[slot] = uy;
-            dst.uz[slot] = uz;
-            dst.erot[slot] = er;
-            dst.vib[slot] = vb;
-            dst.cellw[slot] = w;
-            dst.spc[slot] = sp;
-            dst.id[slot] = id;
+            sortIdx[slot] = (int)i;
         }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_gather(Soa src, Soa dst, Counters* ctr, const int* __restrict__ sortIdx) {
+    const long long n = ctr->nKept;
+    const long long nSrc = ctr->nMoved;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const long long i = __ldg(sortIdx + j);
+        if (i < 0 || i >= nSrc) {
+            atomicOr(&ctr->err, ERRB_BOUNDS);
+            continue;
+        }
+        const double x = __ldg(src.x + i), y = __ldg(src.y + i), z = __ldg(src.z + i);
+        const double ux = __ldg(src.ux + i), uy = __ldg(src.uy + i), uz = __ldg(src.uz + i);
+        const double er = __ldg(src.erot + i);
+        const int vb = __ldg(src.vib + i);
+        const uint32_t w = __ldg(src.cellw + i), sp = __ldg(src.spc + i), id = __ldg(src.id + i);
+        __stcs(dst.x + j, x); __stcs(dst.y + j, y); __stcs(dst.z + j, z);
+        __stcs(dst.ux + j, ux); __stcs(dst.uy + j, uy); __stcs(dst.uz + j, uz);
+        __stcs(dst.erot + j, er);
+        dst.vib[j] = vb;
+        dst.cellw[j] = w;
+        dst.spc[j] = sp;
+        dst.id[j] = id;
     }
 }
 
@@ -979,7 +992,8 @@ void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Soa& src, con
                     cudaStream_t st) {
     (void)cs;
     const int grid = grid_for(B.capacity, 256, 8);
-    k_scatter<<<grid, 256, 0, st>>>(src, dst, B.ctr, B.start, B.count);
+    k_scatter_index<<<grid, 256, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortIdx);
+    k_gather<<<grid, 256, 0, st>>>(src, dst, B.ctr, B.sortIdx);
 }
 
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st) {

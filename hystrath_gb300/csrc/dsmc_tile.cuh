@@ -6,29 +6,41 @@
 //                   (selectedPairs, noTimeCounter.C:146-153) and the
 //                   remainder update; counts cells per work class.
 //   k_ntc_buckets   offsets of the work classes.
-//   k_ntc_list      the cells with candidates, grouped by class.
-//   k_cell_order    one warp per listed cell (one block above ORDER_WARP_N
+//   k_ntc_list      the cells with candidates, grouped by class: heavy cells
+//                   (many parcels or candidates) first, then light cells,
+//                   each class heaviest first.
+//   k_cell_order    one warp per heavy cell (one block above ORDER_WARP_N
 //                   parcels): the cell's members sorted by (sub-cell, parcel
 //                   id).  This is the cell's canonical list: sub-cells are
 //                   contiguous in it and it does not depend on the order in
 //                   which the sort scatter left the parcels in memory.
-//   k_collide_heavy one warp per cell with many candidates or parcels.
-//   k_collide_light one lane per remaining cell.
+//   k_collide_heavy one warp per heavy cell.
+//   k_collide_light one lane per light cell.
 //
-// Every candidate k of cell c draws from its own counter-based stream
-// (cell, step, k): its pair (the reference's randomLabel draws over the
-// cell's list, with the redraw while Q == P, noTimeCounter.C:164-198), its
-// acceptance test and its post-collision draws.  A candidate therefore depends
-// only on the state of its own two parcels when it runs, so the heavy kernel
-// runs up to 32 candidates of one cell at once: each round runs every
-// candidate that shares no parcel with an earlier candidate still waiting,
-// which gives exactly the result of running them one after the other
-// (disjoint candidates commute).  The light kernel runs its cell's candidates
-// one after the other in one lane.  Both give the same result for a cell, so
-// the split between them is a matter of speed only.
+// Every candidate k of cell c draws its acceptance test and post-collision
+// deviates from its own counter-based stream (cell, step, k).
 //
-// Serial work is spread across lanes because GB300 issues an FP64 instruction
-// over the whole warp whatever the active mask.
+// Heavy cells pick the pair as the reference does (randomLabel draws over
+// the cell's list, with the redraw while Q == P, noTimeCounter.C:164-198) over
+// the canonical list.  A candidate then depends only on the state of its own
+// two parcels when it runs, so the warp runs up to 32 candidates of the cell
+// at once: each round runs every candidate that shares no parcel with an
+// earlier candidate still waiting, which gives exactly the result of running
+// them one after the other (disjoint candidates commute).
+//
+// Light cells (at most LIGHT_N parcels, fewer than LIGHT_CAND candidates)
+// run their candidates one after the other in one lane and pick without a
+// list: P is the member whose id has the smallest keyed 32-bit hash, Q the
+// member of P's sub-cell (or of the cell when P is alone there) other than P
+// with the smallest hash under a second key.  For a given key the hash is a
+// bijection of the id, so every member is equally likely and picks under
+// different keys are independent: the same distribution as the list draws,
+// for a few passes over the cell instead of a sort.
+//
+// Both paths give results that do not depend on the parcels' order in
+// memory, so a run is reproducible.  Serial work is spread across lanes
+// because GB300 issues an FP64 instruction over the whole warp whatever the
+// active mask.
 #pragma once
 
 namespace tile {
@@ -169,7 +181,7 @@ struct BlockBar {
     __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
 
-// one warp per listed cell of at most ORDER_WARP_N parcels: perm[off + r] is
+// one warp per heavy cell of at most ORDER_WARP_N parcels: perm[off + r] is
 // the local index of the r-th member in canonical order, subs[q] the start
 // of each sub-cell in it
 __global__ void __launch_bounds__(WARPS * 32)
@@ -178,9 +190,9 @@ k_cell_order(Soa s, const int* __restrict__ start, const Counters* ctr, const in
     __shared__ unsigned long long keysAll[WARPS][ORDER_WARP_N];
     unsigned long long* keys = keysAll[threadIdx.x >> 5];
     const int lane = (int)(threadIdx.x & 31u);
-    const long long nWork = (long long)ctr->nWork;
+    const long long nHeavy = (long long)ctr->nHeavy;
     const long long nWarps = (long long)gridDim.x * WARPS;
-    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nWork; q += nWarps) {
+    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nHeavy; q += nWarps) {
         const int c = work[q].x;
         const long long off = start[c];
         const int n = start[c + 1] - (int)off;
@@ -406,10 +418,42 @@ k_collide_heavy(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, 
     if (err) atomicOr(&ctr->err, err);
 }
 
+// MurmurHash3's 32-bit finaliser (Appleby): a bijection with full avalanche.
+__device__ __forceinline__ uint32_t fmix32(uint32_t h) {
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
+
+__device__ __forceinline__ uint32_t pick_key(const CaseDev& cs, uint32_t cell, uint32_t step, uint32_t draw) {
+    uint32_t h = fmix32(cs.seedHi ^ 0x51ED270Bu);
+    h = fmix32(h ^ cell);
+    h = fmix32(h ^ step);
+    h = fmix32(h ^ draw);
+    return h ^ cs.seedLo;
+}
+
+// member of the cell [off, off+n) with the smallest hash under key; sub < 0:
+// any sub-cell; skip: excluded member
+__device__ __forceinline__ int hash_pick(const Soa& s, long long off, int n, uint32_t key, int sub, int skip) {
+    uint32_t best = 0xFFFFFFFFu;
+    int arg = -1;
+    for (int j = 0; j < n; ++j) {
+        if (j == skip) continue;
+        if (sub >= 0 && (int)(__ldg(s.cellw + off + j) & 7u) != sub) continue;
+        const uint32_t h = fmix32(key ^ __ldg(s.id + off + j));
+        if (arg < 0 || h < best) { best = h; arg = j; }
+    }
+    return arg;
+}
+
 // one lane per light cell, its candidates one after the other
 __global__ void __launch_bounds__(WARPS * 32, 4)
 k_collide_light(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
-                const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs) {
+                const int2* __restrict__ work) {
     const uint32_t step = (uint32_t)ctr->step;
     const long long nWork = (long long)ctr->nWork;
     const long long nHeavy = (long long)ctr->nHeavy;
@@ -423,17 +467,19 @@ k_collide_light(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, 
         const int nCand = it.y;
         const long long off = start[c];
         const int n = start[c + 1] - (int)off;
-        const uint4 so = subs[q];
+        // sub-cell occupancy, 8 bits per sub-cell (n <= LIGHT_N < 256)
+        unsigned long long subCnt = 0;
+        for (int j = 0; j < n; ++j) subCnt += 1ull << (8u * (__ldg(s.cellw + off + j) & 7u));
         const double smax0 = smax[c];
         double smaxRun = smax0, collSep = 0.0;
         unsigned coll = 0;
         for (int k = 0; k < nCand; ++k) {
+            const int jP = hash_pick(s, off, n, pick_key(cs, (uint32_t)c, step, 2u * k), -1, -1);
+            const int sub = (int)(__ldg(s.cellw + off + jP) & 7u);
+            const bool inSub = ((subCnt >> (8 * sub)) & 0xFFu) > 1;
+            const int jQ = hash_pick(s, off, n, pick_key(cs, (uint32_t)c, step, 2u * k + 1u), inSub ? sub : -1, jP);
             Rng r(cs, (uint32_t)c, step, cand_tag(k));
-            int pP, pQ;
-            draw_pair(r, n, so, &pP, &pQ, &err);
-            const long long gP = off + perm[off + pP];
-            const long long gQ = off + perm[off + pQ];
-            if (run_candidate(cs, s, r, gP, gQ, smax0, &smaxRun, &collSep, &err)) ++coll;
+            if (run_candidate(cs, s, r, off + jP, off + jQ, smax0, &smaxRun, &collSep, &err)) ++coll;
         }
         smax[c] = smaxRun;
         if (coll) {
