@@ -8,6 +8,7 @@
 // dsmcCloud::evolve.  One step is captured once per buffer parity as a CUDA
 // graph and replayed; nothing in a step waits on the host.
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -26,7 +27,7 @@ struct dsmc_handle {
     CaseDev cs{};
     InflowDev inflow{};
     StepBuffers B{};
-    Soa buf[2]{};
+    Parcels buf[2]{};
     int cur = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -73,19 +74,10 @@ int dalloc(dsmc_handle* h, T** p, long long count) {
     return DSMC_OK;
 }
 
-int alloc_soa(dsmc_handle* h, Soa* s, long long cap) {
+int alloc_soa(dsmc_handle* h, Parcels* s, long long cap) {
     int rc;
-    if ((rc = dalloc(h, &s->x, cap))) return rc;
-    if ((rc = dalloc(h, &s->y, cap))) return rc;
-    if ((rc = dalloc(h, &s->z, cap))) return rc;
-    if ((rc = dalloc(h, &s->ux, cap))) return rc;
-    if ((rc = dalloc(h, &s->uy, cap))) return rc;
-    if ((rc = dalloc(h, &s->uz, cap))) return rc;
-    if ((rc = dalloc(h, &s->erot, cap))) return rc;
-    if ((rc = dalloc(h, &s->vib, cap))) return rc;
+    if ((rc = dalloc(h, &s->r, cap))) return rc;
     if ((rc = dalloc(h, &s->cellw, cap))) return rc;
-    if ((rc = dalloc(h, &s->spc, cap))) return rc;
-    if ((rc = dalloc(h, &s->id, cap))) return rc;
     return DSMC_OK;
 }
 
@@ -272,7 +264,7 @@ void fill_case_dev(dsmc_handle* h) {
     cs.nAcc = s.n_species * SACC + CACC;
 }
 
-Soa& cur_soa(dsmc_handle* h) { return h->buf[h->cur]; }
+Parcels& cur_soa(dsmc_handle* h) { return h->buf[h->cur]; }
 
 int check_device_error(dsmc_handle* h) {
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -296,8 +288,8 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
     const CaseDev& cs = h->cs;
     StepBuffers& B = h->B;
     cudaStream_t st = h->stream;
-    Soa& a = h->buf[parity];
-    Soa& b = h->buf[parity ^ 1];
+    Parcels& a = h->buf[parity];
+    Parcels& b = h->buf[parity ^ 1];
     if (ev) cudaEventRecord(ev[0], st);
     launch_zero_step(B, st);
     // a sample pending from the previous step is taken by the move kernel,
@@ -461,7 +453,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.perm, cap))) return rc;
     if ((rc = dalloc(h, &B.subs, cs.C))) return rc;
     if ((rc = dalloc(h, &B.slowList, cap))) return rc;
-    if ((rc = dalloc(h, &B.sortIdx, cap))) return rc;
+    if ((rc = dalloc(h, &B.sortSrc, cap))) return rc;
     if ((rc = dalloc(h, &B.ctr, 1))) return rc;
     if ((rc = dalloc(h, &h->solid, cs.C))) return rc;
     if ((rc = dalloc(h, &h->info6, 8))) return rc;
@@ -660,36 +652,41 @@ int dsmc_phase_times(dsmc_handle* h, double* a, double* b, double* c, double* d,
     return DSMC_OK;
 }
 
+// Host <-> device parcel transfers go through pinned-free chunks of packed
+// records (PACK_CHUNK parcels at a time).
+constexpr long long PACK_CHUNK = 1 << 20;
+
 int dsmc_set_particles(dsmc_handle* h, long long n, const double* pos, const double* U, const double* erot,
                        const int* vib, const int* species, const unsigned* id) {
     if (n < 0 || n > h->B.capacity) return fail(h, DSMC_ERR_CAPACITY, "particle count exceeds capacity");
-    Soa& s = cur_soa(h);
-    std::vector<double> tmp(n);
-    auto put = [&](double* dst, const double* src, int stride, int k) -> int {
-        for (long long i = 0; i < n; ++i) tmp[i] = src ? src[stride * i + k] : 0.0;
-        CUDA_TRY(h, cudaMemcpy(dst, tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
-        return DSMC_OK;
-    };
-    int rc;
-    if ((rc = put(s.x, pos, 3, 0)) || (rc = put(s.y, pos, 3, 1)) || (rc = put(s.z, pos, 3, 2))) return rc;
-    if ((rc = put(s.ux, U, 3, 0)) || (rc = put(s.uy, U, 3, 1)) || (rc = put(s.uz, U, 3, 2))) return rc;
-    if ((rc = put(s.erot, erot, 1, 0))) return rc;
-    std::vector<int> iv(n, 0);
-    std::vector<uint32_t> uv(n, 0);
-    uint32_t maxId = 0;
     for (long long i = 0; i < n; ++i) {
-        iv[i] = vib ? vib[i] : 0;
         if (species && (species[i] < 0 || species[i] >= h->spec.n_species))
             return fail(h, DSMC_ERR_INVALID, "species index out of range");
+        if (vib && (vib[i] < 0 || vib[i] > SV_MAX_VIB))
+            return fail(h, DSMC_ERR_INVALID, "vibrational level out of range");
     }
-    CUDA_TRY(h, cudaMemcpy(s.vib, iv.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
-    for (long long i = 0; i < n; ++i) uv[i] = species ? (uint32_t)species[i] : 0u;
-    CUDA_TRY(h, cudaMemcpy(s.spc, uv.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
-    for (long long i = 0; i < n; ++i) {
-        uv[i] = id ? id[i] : (uint32_t)i;
-        if (uv[i] + 1 > maxId) maxId = uv[i] + 1;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    Parcels& s = cur_soa(h);
+    std::vector<Rec> rec((size_t)std::min(n, PACK_CHUNK));
+    uint32_t maxId = 0;
+    for (long long c0 = 0; c0 < n; c0 += PACK_CHUNK) {
+        const long long m = std::min(PACK_CHUNK, n - c0);
+        for (long long k = 0; k < m; ++k) {
+            const long long i = c0 + k;
+            Rec& r = rec[k];
+            r.x = pos ? pos[3 * i] : 0.0;
+            r.y = pos ? pos[3 * i + 1] : 0.0;
+            r.z = pos ? pos[3 * i + 2] : 0.0;
+            r.ux = U ? U[3 * i] : 0.0;
+            r.uy = U ? U[3 * i + 1] : 0.0;
+            r.uz = U ? U[3 * i + 2] : 0.0;
+            r.erot = erot ? erot[i] : 0.0;
+            r.id = id ? id[i] : (uint32_t)i;
+            r.sv = make_sv(species ? species[i] : 0, vib ? vib[i] : 0);
+            if (r.id + 1 > maxId) maxId = r.id + 1;
+        }
+        CUDA_TRY(h, cudaMemcpy(s.r + c0, rec.data(), sizeof(Rec) * m, cudaMemcpyHostToDevice));
     }
-    CUDA_TRY(h, cudaMemcpy(s.id, uv.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemset(s.cellw, 0, sizeof(uint32_t) * n));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
     h->ctrHost->nextId = maxId;
@@ -704,28 +701,24 @@ int dsmc_get_particles(dsmc_handle* h, long long capacity, long long* n_out, dou
     const long long n = h->ctrHost->n;
     if (n_out) *n_out = n;
     if (capacity < n) return fail(h, DSMC_ERR_CAPACITY, "output capacity smaller than the particle count");
-    Soa& s = cur_soa(h);
-    std::vector<double> tmp(n);
-    auto get = [&](double* dst, const double* src, int stride, int k) -> int {
-        if (!dst) return DSMC_OK;
-        CUDA_TRY(h, cudaMemcpy(tmp.data(), src, sizeof(double) * n, cudaMemcpyDeviceToHost));
-        for (long long i = 0; i < n; ++i) dst[stride * i + k] = tmp[i];
-        return DSMC_OK;
-    };
-    int rc;
-    if ((rc = get(pos, s.x, 3, 0)) || (rc = get(pos, s.y, 3, 1)) || (rc = get(pos, s.z, 3, 2))) return rc;
-    if ((rc = get(U, s.ux, 3, 0)) || (rc = get(U, s.uy, 3, 1)) || (rc = get(U, s.uz, 3, 2))) return rc;
-    if ((rc = get(erot, s.erot, 1, 0))) return rc;
-    if (vib) CUDA_TRY(h, cudaMemcpy(vib, s.vib, sizeof(int) * n, cudaMemcpyDeviceToHost));
-    std::vector<uint32_t> uv(n);
-    if (species) {
-        CUDA_TRY(h, cudaMemcpy(uv.data(), s.spc, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
-        for (long long i = 0; i < n; ++i) species[i] = (int)uv[i];
-    }
-    if (id) CUDA_TRY(h, cudaMemcpy(id, s.id, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
-    if (cell) {
-        CUDA_TRY(h, cudaMemcpy(uv.data(), s.cellw, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
-        for (long long i = 0; i < n; ++i) cell[i] = uv[i] == CELLW_DELETED ? -1 : (int)cellw_cell(uv[i]);
+    Parcels& s = cur_soa(h);
+    std::vector<Rec> rec((size_t)std::min(n, PACK_CHUNK));
+    std::vector<uint32_t> cw((size_t)std::min(n, PACK_CHUNK));
+    for (long long c0 = 0; c0 < n; c0 += PACK_CHUNK) {
+        const long long m = std::min(PACK_CHUNK, n - c0);
+        CUDA_TRY(h, cudaMemcpy(rec.data(), s.r + c0, sizeof(Rec) * m, cudaMemcpyDeviceToHost));
+        if (cell) CUDA_TRY(h, cudaMemcpy(cw.data(), s.cellw + c0, sizeof(uint32_t) * m, cudaMemcpyDeviceToHost));
+        for (long long k = 0; k < m; ++k) {
+            const long long i = c0 + k;
+            const Rec& r = rec[k];
+            if (pos) { pos[3 * i] = r.x; pos[3 * i + 1] = r.y; pos[3 * i + 2] = r.z; }
+            if (U) { U[3 * i] = r.ux; U[3 * i + 1] = r.uy; U[3 * i + 2] = r.uz; }
+            if (erot) erot[i] = r.erot;
+            if (vib) vib[i] = sv_vib(r.sv);
+            if (species) species[i] = sv_species(r.sv);
+            if (id) id[i] = r.id;
+            if (cell) cell[i] = cw[k] == CELLW_DELETED ? -1 : (int)cellw_cell(cw[k]);
+        }
     }
     return DSMC_OK;
 }
@@ -866,7 +859,7 @@ int dsmc_info(dsmc_handle* h, dsmc_info_t* o) {
 }
 
 // Checkpoint layout: magic, version, C, nAcc, nBFaces, nInflow, counters,
-// particles (SoA arrays of n), smax, rem, acc, wall, inflow accumulators.
+// parcels (n 64-byte records, then n cell words), smax, rem, acc, wall, inflow accumulators.
 int dsmc_checkpoint(dsmc_handle* h, const char* path) {
     flush_sample(h);
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -874,12 +867,12 @@ int dsmc_checkpoint(dsmc_handle* h, const char* path) {
     const Counters c = *h->ctrHost;
     std::ofstream f(path, std::ios::binary);
     if (!f) return fail(h, DSMC_ERR_IO, std::string("cannot write ") + path);
-    const long long hdr[6] = {0x44534D4347423330LL, 1, h->cs.C, h->cs.nAcc, h->cs.nBFaces,
+    const long long hdr[6] = {0x44534D4347423330LL, 2, h->cs.C, h->cs.nAcc, h->cs.nBFaces,
                               (long long)h->B.nInflowFaces * h->spec.n_species};
     f.write(reinterpret_cast<const char*>(hdr), sizeof(hdr));
     f.write(reinterpret_cast<const char*>(&c), sizeof(c));
     const long long n = c.n;
-    Soa& s = cur_soa(h);
+    Parcels& s = cur_soa(h);
     std::vector<char> buf;
     auto dump = [&](const void* dptr, size_t bytes) -> int {
         buf.resize(bytes);
@@ -888,12 +881,8 @@ int dsmc_checkpoint(dsmc_handle* h, const char* path) {
         return DSMC_OK;
     };
     int rc;
-    const double* d8[7] = {s.x, s.y, s.z, s.ux, s.uy, s.uz, s.erot};
-    for (int k = 0; k < 7; ++k)
-        if ((rc = dump(d8[k], sizeof(double) * n))) return rc;
-    const void* d4[4] = {s.vib, s.cellw, s.spc, s.id};
-    for (int k = 0; k < 4; ++k)
-        if ((rc = dump(d4[k], 4 * n))) return rc;
+    if ((rc = dump(s.r, sizeof(Rec) * n))) return rc;
+    if ((rc = dump(s.cellw, sizeof(uint32_t) * n))) return rc;
     if ((rc = dump(h->B.start, sizeof(int) * (h->cs.C + 1)))) return rc;
     if ((rc = dump(h->B.smax, sizeof(double) * h->cs.C))) return rc;
     if ((rc = dump(h->B.rem, sizeof(double) * h->cs.C))) return rc;
@@ -910,14 +899,14 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
     if (!f) return fail(h, DSMC_ERR_IO, std::string("cannot read ") + path);
     long long hdr[6];
     f.read(reinterpret_cast<char*>(hdr), sizeof(hdr));
-    if (!f || hdr[0] != 0x44534D4347423330LL || hdr[1] != 1 || hdr[2] != h->cs.C || hdr[3] != h->cs.nAcc ||
+    if (!f || hdr[0] != 0x44534D4347423330LL || hdr[1] != 2 || hdr[2] != h->cs.C || hdr[3] != h->cs.nAcc ||
         hdr[4] != h->cs.nBFaces || hdr[5] != (long long)h->B.nInflowFaces * h->spec.n_species)
         return fail(h, DSMC_ERR_INVALID, "checkpoint does not match this case");
     Counters c;
     f.read(reinterpret_cast<char*>(&c), sizeof(c));
     const long long n = c.n;
     if (n > h->B.capacity) return fail(h, DSMC_ERR_CAPACITY, "checkpoint holds more parcels than the capacity");
-    Soa& s = cur_soa(h);
+    Parcels& s = cur_soa(h);
     std::vector<char> buf;
     auto load = [&](void* dptr, size_t bytes) -> int {
         buf.resize(bytes);
@@ -927,12 +916,8 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
         return DSMC_OK;
     };
     int rc;
-    double* d8[7] = {s.x, s.y, s.z, s.ux, s.uy, s.uz, s.erot};
-    for (int k = 0; k < 7; ++k)
-        if ((rc = load(d8[k], sizeof(double) * n))) return rc;
-    void* d4[4] = {s.vib, s.cellw, s.spc, s.id};
-    for (int k = 0; k < 4; ++k)
-        if ((rc = load(d4[k], 4 * n))) return rc;
+    if ((rc = load(s.r, sizeof(Rec) * n))) return rc;
+    if ((rc = load(s.cellw, sizeof(uint32_t) * n))) return rc;
     if ((rc = load(h->B.start, sizeof(int) * (h->cs.C + 1)))) return rc;
     if ((rc = load(h->B.smax, sizeof(double) * h->cs.C))) return rc;
     if ((rc = load(h->B.rem, sizeof(double) * h->cs.C))) return rc;

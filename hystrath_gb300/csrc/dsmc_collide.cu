@@ -240,16 +240,17 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
 }
 
 // Totals for dsmcCloud::info: KE, Erot, Evib, momentum (times FN on the host).
-__global__ void k_info(CaseDev cs, Soa s, const Counters* ctr, double* out) {
+__global__ void k_info(CaseDev cs, Parcels s, const Counters* ctr, double* out) {
     const long long n = ctr->n;
     double v[6] = {0, 0, 0, 0, 0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        const SpeciesDev& sp = cs.sp[s.spc[i]];
-        const double ux = s.ux[i], uy = s.uy[i], uz = s.uz[i];
+        const Rec p = ldg_rec(s.r + i);
+        const SpeciesDev& sp = cs.sp[sv_species(p.sv)];
+        const double ux = p.ux, uy = p.uy, uz = p.uz;
         v[0] += 0.5 * sp.m * (ux * ux + uy * uy + uz * uz);
-        v[1] += s.erot[i];
-        v[2] += sp.nVib ? s.vib[i] * sp.kThetaV : 0.0;
+        v[1] += p.erot;
+        v[2] += sp.nVib ? sv_vib(p.sv) * sp.kThetaV : 0.0;
         v[3] += sp.m * ux;
         v[4] += sp.m * uy;
         v[5] += sp.m * uz;
@@ -278,7 +279,7 @@ int collide_init() {
     return e == cudaSuccess ? 0 : (int)e;
 }
 
-void launch_collide(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
+void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
     const int sms = sm_count();
     long long selBlocks = (cs.C + 255) / 256;
     if (selBlocks > (long long)sms * 8) selBlocks = (long long)sms * 8;
@@ -302,7 +303,7 @@ void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* ou
     k_field<<<(int)((cs.C + 255) / 256), 256, 0, st>>>(cs, B.acc, B.ctr, which, out, measureMfp, mfpTref);
 }
 
-void launch_info(const CaseDev& cs, const Soa& s, const Counters* ctr, double* out6, cudaStream_t st) {
+void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, double* out6, cudaStream_t st) {
     cudaMemsetAsync(out6, 0, sizeof(double) * 6, st);
     k_info<<<sm_count() * 4, 256, 0, st>>>(cs, s, ctr, out6);
 }

@@ -111,14 +111,68 @@ enum { CACC_NCOLLS = 0, CACC_COLLSEP, CACC };
 enum { W_RHON = 0, W_RHOM, W_LINKE, W_MCC, W_MOMX, W_MOMY, W_MOMZ, W_EROT, W_ZETAROT, W_EVIB,
        W_Q, W_FDX, W_FDY, W_FDZ, W_N };
 
-// Structure-of-arrays particle state.
-struct Soa {
-    double *x, *y, *z, *ux, *uy, *uz, *erot;
-    int* vib;
-    uint32_t* cellw;
-    uint32_t* spc;   // species index
-    uint32_t* id;
+// Parcel state: one 64-byte record per parcel, aligned so that it is two
+// whole sectors, plus the cell word in its own array (the sort key).  A parcel
+// that changes cell is moved by the sort as two sectors instead of one sector
+// per field, and the collision kernels reach a parcel's velocity, energy and
+// species in one record.
+struct __align__(16) Rec {
+    double x, y, z;
+    double ux, uy, uz;
+    double erot;
+    uint32_t id;
+    uint32_t sv;     // species index (bits 0-7) | vibrational level << 8
 };
+static_assert(sizeof(Rec) == 64, "parcel record must be 64 bytes");
+
+constexpr int SV_MAX_VIB = (1 << 24) - 1;
+__host__ __device__ inline int sv_species(uint32_t sv) { return (int)(sv & 0xFFu); }
+__host__ __device__ inline int sv_vib(uint32_t sv) { return (int)(sv >> 8); }
+__host__ __device__ inline uint32_t make_sv(int species, int vib) { return (uint32_t)species | ((uint32_t)vib << 8); }
+
+struct Parcels {
+    Rec* r;            // [capacity]
+    uint32_t* cellw;   // [capacity]
+};
+
+// Whole-record access with four 16-byte loads or stores.
+__device__ __forceinline__ Rec rec_from(double2 a, double2 b, double2 c, double2 d) {
+    Rec v;
+    v.x = a.x; v.y = a.y; v.z = b.x;
+    v.ux = b.y; v.uy = c.x; v.uz = c.y;
+    v.erot = d.x;
+    const unsigned long long t = (unsigned long long)__double_as_longlong(d.y);
+    v.id = (uint32_t)t;
+    v.sv = (uint32_t)(t >> 32);
+    return v;
+}
+__device__ __forceinline__ double tail_word(const Rec& v) {
+    return __longlong_as_double((long long)(((unsigned long long)v.sv << 32) | v.id));
+}
+__device__ __forceinline__ Rec ld_rec(const Rec* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    return rec_from(q[0], q[1], q[2], q[3]);
+}
+// read-only path: for kernels that do not write the record
+__device__ __forceinline__ Rec ldg_rec(const Rec* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    return rec_from(__ldg(q), __ldg(q + 1), __ldg(q + 2), __ldg(q + 3));
+}
+__device__ __forceinline__ void st_rec(Rec* p, const Rec& v) {
+    double2* q = reinterpret_cast<double2*>(p);
+    q[0] = make_double2(v.x, v.y);
+    q[1] = make_double2(v.z, v.ux);
+    q[2] = make_double2(v.uy, v.uz);
+    q[3] = make_double2(v.erot, tail_word(v));
+}
+// streaming store (the record is not read again soon)
+__device__ __forceinline__ void st_rec_cs(Rec* p, const Rec& v) {
+    double2* q = reinterpret_cast<double2*>(p);
+    __stcs(q, make_double2(v.x, v.y));
+    __stcs(q + 1, make_double2(v.z, v.ux));
+    __stcs(q + 2, make_double2(v.uy, v.uz));
+    __stcs(q + 3, make_double2(v.erot, tail_word(v)));
+}
 
 // ------------------------------------------------------------------ Philox
 // Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): two 32x32->64

@@ -29,7 +29,7 @@ struct Counters {
 };
 
 struct StepBuffers {
-    Soa a, b;                 // current / other particle buffers
+    Parcels a, b;                 // current / other particle buffers
     int* count;               // [C]
     int* start;               // [C+1]
     int* blockSums;           // scan scratch
@@ -46,7 +46,7 @@ struct StepBuffers {
     uint16_t* perm;           // [capacity] canonical member order of the cells with candidates
     uint4* subs;              // [C] sub-cell starts in that order, per work item
     int* slowList;            // [capacity] parcels that take the boundary path this step
-    int* sortIdx;             // [capacity] source index of each destination slot of the sort
+    int2* sortSrc;            // [capacity] (source index, cell word) of each destination slot of the sort
     // inflow
     int nInflowFaces;
     long long* inflowFace;    // boundary face ids with inflow [nInflowFaces]
@@ -74,13 +74,13 @@ struct InflowDev {
 
 int scan_scratch_ints(long long C);
 
-void launch_count(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st);
-void launch_move(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st);
+void launch_count(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
+void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
 void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
-void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Soa& src, const Soa& dst,
+void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
                     cudaStream_t st);
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
-void launch_collide(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st);
+void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
 // one-time kernel attributes (large dynamic shared memory); call before the
 // first capture
 int collide_init();
@@ -91,23 +91,23 @@ int collide_init();
 // force: add the fixed-point sums to the FP64 accumulators now (otherwise
 // every 32 samples).
 void launch_sample_commit(const CaseDev& cs, const StepBuffers& B, int force, cudaStream_t st);
-void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Soa& s, int force, cudaStream_t st);
+void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int force, cudaStream_t st);
 void launch_set_pending(const StepBuffers& B, cudaStream_t st);
 void launch_end_step(const StepBuffers& B, cudaStream_t st);
-void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Soa& s,
+void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Parcels& s,
                    cudaStream_t st);
 void launch_init_count(const CaseDev& cs, const double* dnd, const unsigned char* solid, int* cellCounts,
                        cudaStream_t st);
-void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Soa& s, const double* dnd,
+void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Parcels& s, const double* dnd,
                       const unsigned char* solid, const int* cellOff, double Ttra, const double* Txyz,
                       double Trot, double Tvib, const double* U, cudaStream_t st);
-void launch_count_n(const Soa& s, long long n, int* count, cudaStream_t st);
+void launch_count_n(const Parcels& s, long long n, int* count, cudaStream_t st);
 void launch_zero_step(const StepBuffers& B, cudaStream_t st);
-void launch_cellw(const CaseDev& cs, const Soa& s, long long n, cudaStream_t st);
+void launch_cellw(const CaseDev& cs, const Parcels& s, long long n, cudaStream_t st);
 void launch_remainder_init(const CaseDev& cs, double* rem, cudaStream_t st);
 void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* out,
                   int measureMfp, double mfpTref, cudaStream_t st);
-void launch_info(const CaseDev& cs, const Soa& s, const Counters* ctr, double* out7,
+void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, double* out7,
                  cudaStream_t st);
 
 // field selectors of launch_field

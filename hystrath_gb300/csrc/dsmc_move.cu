@@ -123,18 +123,17 @@ __device__ void diffuse_reflect(const CaseDev& cs, Rng& r, int axis, double sgn,
 
 // Full Cartesian tracking of one parcel: the same steps as the CPU replay.
 // Returns the new cell word (CELLW_DELETED when removed).
-__device__ uint32_t move_slow(const CaseDev& cs, const Soa& s, long long i, uint32_t step,
+__device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, uint32_t step,
                               uint32_t w, const int* bfPatch, double* wall, unsigned* err,
                               unsigned long long* hits) {
-    double x[3] = {s.x[i], s.y[i], s.z[i]};
-    double U[3] = {s.ux[i], s.uy[i], s.uz[i]};
-    const uint32_t pid = s.id[i];
-    const int type = (int)s.spc[i];
+    Rec p = ld_rec(s.r + i);
+    double x[3] = {p.x, p.y, p.z};
+    double U[3] = {p.ux, p.uy, p.uz};
+    const uint32_t pid = p.id;
+    const int type = sv_species(p.sv);
     const SpeciesDev& sp = cs.sp[type];
-    double erot = 0.0;
-    int vib = 0;
-    bool internalLoaded = false;
-    bool internalChanged = false;
+    double erot = p.erot;
+    int vib = sv_vib(p.sv);
     Rng r(cs, pid, step, TAG_MOVE);
     double tr = cs.dt;
     if (w & CELLW_FRESH) {
@@ -258,11 +257,6 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Soa& s, long long i, uint
         } else if (pt.type == DSMC_PATCH_CYCLIC) {
             if (hitKind == 0) x[axis] = (hitSide & 1) ? cs.lo[axis] : cs.hi[axis];
         } else if (pt.model == DSMC_BC_SPECULAR || pt.model == DSMC_BC_DIFFUSE) {
-            if (!internalLoaded) {
-                erot = s.erot[i];
-                vib = s.vib[i];
-                internalLoaded = true;
-            }
             double preE, preM[3];
             if (cs.hasWallMeasure)
                 wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, false, &preE, preM);
@@ -270,7 +264,6 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Soa& s, long long i, uint
                 if (U[axis] * sgn > 0.0) U[axis] = -U[axis];
             } else {
                 diffuse_reflect(cs, r, axis, sgn, pt, sp, U, &erot, &vib, err);
-                internalChanged = true;
             }
             if (cs.hasWallMeasure)
                 wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, true, &preE, preM);
@@ -296,12 +289,12 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Soa& s, long long i, uint
         }
         result = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) | (uint32_t)sb;
     }
-    s.x[i] = x[0]; s.y[i] = x[1]; s.z[i] = x[2];
-    s.ux[i] = U[0]; s.uy[i] = U[1]; s.uz[i] = U[2];
-    if (internalChanged) {
-        s.erot[i] = erot;
-        s.vib[i] = vib;
-    }
+    if (vib < 0 || vib > SV_MAX_VIB) { *err |= ERRB_BOUNDS; vib = 0; }
+    p.x = x[0]; p.y = x[1]; p.z = x[2];
+    p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
+    p.erot = erot;
+    p.sv = make_sv(type, vib);
+    st_rec(s.r + i, p);
     return result;
 }
 
@@ -365,7 +358,7 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
 // the end of that step) into the per-cell sample sums: it streams the
 // velocities anyway, in cell order.
 __global__ void __launch_bounds__(MOVE_THREADS, 4)
-k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count, long long* sfix) {
+k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix) {
     const long long n = ctr->nMoved;
     const int doSample = ctr->pendingSample;
     unsigned err = 0;
@@ -381,13 +374,17 @@ k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count, long long* s
             const uint32_t w = s.cellw[i];
             bool fast = false;
             if (!(w & CELLW_FRESH)) {
-                const double x = s.x[i], y = s.y[i], z = s.z[i];
-                const double ux = s.ux[i], uy = s.uy[i], uz = s.uz[i];
+                double2* q = reinterpret_cast<double2*>(s.r + i);
+                const double2 q0 = q[0], q1 = q[1], q2 = q[2];
+                const double x = q0.x, y = q0.y, z = q1.x;
+                const double ux = q1.y, uy = q2.x, uz = q2.y;
                 if (doSample) {
-                    skey = (int)(cellw_cell(w) * 8u + s.spc[i]);
+                    const double2 q3 = q[3];
+                    const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q3.y) >> 32);
+                    skey = (int)(cellw_cell(w) * 8u + (uint32_t)sv_species(sv));
                     sux = ux; suy = uy; suz = uz;
-                    ser = s.erot[i];
-                    svb = s.vib[i];
+                    ser = q3.x;
+                    svb = sv_vib(sv);
                 }
                 const double ex = fma(ux, cs.dt, x);
                 const double ey = fma(uy, cs.dt, y);
@@ -411,7 +408,8 @@ k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count, long long* s
                     }
                 }
                 if (inside) {
-                    s.x[i] = ex; s.y[i] = ey; s.z[i] = ez;
+                    q[0] = make_double2(ex, ey);
+                    s.r[i].z = ez;
                     const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
                                         (uint32_t)((c2x & 1) | ((c2y & 1) << 1) | ((c2z & 1) << 2));
                     s.cellw[i] = nw;
@@ -438,7 +436,7 @@ k_move(CaseDev cs, Soa s, Counters* ctr, int* slowList, int* count, long long* s
 
 // A pending sample of the current state when no move follows.
 __global__ void __launch_bounds__(MOVE_THREADS)
-k_sample_pass(CaseDev cs, Soa s, Counters* ctr, long long* sfix) {
+k_sample_pass(CaseDev cs, Parcels s, Counters* ctr, long long* sfix) {
     if (!ctr->pendingSample) return;
     const long long n = ctr->n;
     unsigned err = 0;
@@ -451,10 +449,11 @@ k_sample_pass(CaseDev cs, Soa s, Counters* ctr, long long* sfix) {
         if (i < n) {
             const uint32_t w = s.cellw[i];
             if (w != CELLW_DELETED && !(w & CELLW_FRESH)) {
-                skey = (int)(cellw_cell(w) * 8u + s.spc[i]);
-                ux = s.ux[i]; uy = s.uy[i]; uz = s.uz[i];
-                er = s.erot[i];
-                vb = s.vib[i];
+                const Rec p = ldg_rec(s.r + i);
+                skey = (int)(cellw_cell(w) * 8u + (uint32_t)sv_species(p.sv));
+                ux = p.ux; uy = p.uy; uz = p.uz;
+                er = p.erot;
+                vb = sv_vib(p.sv);
             }
         }
         sample_contrib(sfix, cs.C, skey, ux, uy, uz, er, vb, &err);
@@ -499,7 +498,7 @@ __global__ void k_set_pending(Counters* ctr) { ctr->pendingSample = 1; }
 
 // The boundary path for the parcels k_move deferred, densely packed.
 __global__ void __launch_bounds__(MOVE_THREADS)
-k_move_slow(CaseDev cs, Soa s, Counters* ctr, const int* __restrict__ slowList, const int* __restrict__ bfPatch,
+k_move_slow(CaseDev cs, Parcels s, Counters* ctr, const int* __restrict__ slowList, const int* __restrict__ bfPatch,
             double* wall, int* count) {
     const long long nSlow = (long long)ctr->nSlow;
     const uint32_t step = (uint32_t)ctr->step;
@@ -515,7 +514,7 @@ k_move_slow(CaseDev cs, Soa s, Counters* ctr, const int* __restrict__ slowList, 
     if (err) atomicOr(&ctr->err, err);
 }
 
-__global__ void k_count(Soa s, long long n, int* count) {
+__global__ void k_count(Parcels s, long long n, int* count) {
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
         const long long i = base + threadIdx.x;
@@ -528,7 +527,7 @@ __global__ void k_count(Soa s, long long n, int* count) {
     }
 }
 
-__global__ void k_count_dev(Soa s, const Counters* ctr, int* count) {
+__global__ void k_count_dev(Parcels s, const Counters* ctr, int* count) {
     const long long n = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
@@ -632,15 +631,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
 // in short runs all over the destination).
 __global__ void __launch_bounds__(256) k_scatter_index(const uint32_t* __restrict__ cellw, Counters* ctr,
                                                        const int* __restrict__ start, int* count,
-                                                       int* __restrict__ sortIdx) {
+                                                       int2* __restrict__ sortSrc) {
     const long long n = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
     const unsigned lane = lane_id();
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
         const long long i = base + threadIdx.x;
         int key = -1;
+        uint32_t w = CELLW_DELETED;
         if (i < n) {
-            const uint32_t w = __ldg(cellw + i);
+            w = __ldg(cellw + i);
             key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
         }
         int lo = 0, hi = 0;
@@ -661,33 +661,25 @@ __global__ void __launch_bounds__(256) k_scatter_index(const uint32_t* __restric
                 atomicOr(&ctr->err, ERRB_BOUNDS);
                 continue;
             }
-            sortIdx[slot] = (int)i;
+            sortSrc[slot] = make_int2((int)i, (int)w);
         }
     }
 }
 
-__global__ void __launch_bounds__(256) k_gather(Soa src, Soa dst, Counters* ctr, const int* __restrict__ sortIdx) {
+__global__ void __launch_bounds__(256) k_gather(Parcels src, Parcels dst, Counters* ctr,
+                                                const int2* __restrict__ sortSrc) {
     const long long n = ctr->nKept;
     const long long nSrc = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
-        const long long i = __ldg(sortIdx + j);
+        const int2 sk = __ldg(sortSrc + j);
+        const long long i = sk.x;
         if (i < 0 || i >= nSrc) {
             atomicOr(&ctr->err, ERRB_BOUNDS);
             continue;
         }
-        const double x = __ldg(src.x + i), y = __ldg(src.y + i), z = __ldg(src.z + i);
-        const double ux = __ldg(src.ux + i), uy = __ldg(src.uy + i), uz = __ldg(src.uz + i);
-        const double er = __ldg(src.erot + i);
-        const int vb = __ldg(src.vib + i);
-        const uint32_t w = __ldg(src.cellw + i), sp = __ldg(src.spc + i), id = __ldg(src.id + i);
-        __stcs(dst.x + j, x); __stcs(dst.y + j, y); __stcs(dst.z + j, z);
-        __stcs(dst.ux + j, ux); __stcs(dst.uy + j, uy); __stcs(dst.uz + j, uz);
-        __stcs(dst.erot + j, er);
-        dst.vib[j] = vb;
-        dst.cellw[j] = w;
-        dst.spc[j] = sp;
-        dst.id[j] = id;
+        st_rec_cs(dst.r + j, ldg_rec(src.r + i));
+        __stcs(dst.cellw + j, (uint32_t)sk.y);
     }
 }
 
@@ -767,7 +759,7 @@ __global__ void k_inflow_scan(const int* cnt, int n, int* off, Counters* ctr, lo
 __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long long* __restrict__ face,
                               const int* __restrict__ side, const int* __restrict__ cellOf,
                               const int* __restrict__ bfPatch, const int* __restrict__ cnt,
-                              const int* __restrict__ off, Soa s, Counters* ctr) {
+                              const int* __restrict__ off, Parcels s, Counters* ctr) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int ns = cs.nSpecies;
     if (off[nFaces * ns] < 0) return;     // capacity exceeded: nothing inserted
@@ -827,13 +819,14 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
                 const double erot = eq_rot(r, pt.Trot, sp.rotDof, &err);
                 const int vib = eq_vib(r, pt.Tvib, sp);
                 const long long slot = base + q;
-                s.x[slot] = x[0]; s.y[slot] = x[1]; s.z[slot] = x[2];
-                s.ux[slot] = U[0]; s.uy[slot] = U[1]; s.uz[slot] = U[2];
-                s.erot[slot] = erot;
-                s.vib[slot] = vib;
+                Rec p;
+                p.x = x[0]; p.y = x[1]; p.z = x[2];
+                p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
+                p.erot = erot;
+                p.id = (uint32_t)(id0 + q);
+                p.sv = make_sv(m, vib);
+                st_rec(s.r + slot, p);
                 s.cellw[slot] = ((uint32_t)cell << 3) | CELLW_FRESH;
-                s.spc[slot] = (uint32_t)m;
-                s.id[slot] = (uint32_t)(id0 + q);
             }
             if (err) atomicOr(&ctr->err, err);
         }
@@ -873,7 +866,7 @@ __global__ void k_init_count(CaseDev cs, const double* __restrict__ nd, const un
 // Per-species counts again (same draws) so that parcels come out grouped by
 // species inside a cell, in the replay's order.
 __global__ void k_init_fill(CaseDev cs, const double* __restrict__ nd, const unsigned char* __restrict__ solid,
-                            const int* __restrict__ cellOff, Soa s, double Ttra, double Tx, double Ty, double Tz,
+                            const int* __restrict__ cellOff, Parcels s, double Ttra, double Tx, double Ty, double Tz,
                             double Trot, double Tvib, double U0, double U1, double U2, Counters* ctr) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cs.C || solid[c]) return;
@@ -920,22 +913,24 @@ __global__ void k_init_fill(CaseDev cs, const double* __restrict__ nd, const uns
                 ci[a] = c2 >> 1;
                 sb |= (c2 & 1) << a;
             }
-            s.x[slot] = x[0]; s.y[slot] = x[1]; s.z[slot] = x[2];
-            s.ux[slot] = U[0]; s.uy[slot] = U[1]; s.uz[slot] = U[2];
-            s.erot[slot] = erot;
-            s.vib[slot] = vib;
+            Rec p;
+            p.x = x[0]; p.y = x[1]; p.z = x[2];
+            p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
+            p.erot = erot;
+            p.id = pid;
+            p.sv = make_sv(m, vib);
+            st_rec(s.r + slot, p);
             s.cellw[slot] = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) | (uint32_t)sb;
-            s.spc[slot] = (uint32_t)m;
-            s.id[slot] = pid;
         }
     }
     if (err) atomicOr(&ctr->err, err);
 }
 
-__global__ void k_cellw(CaseDev cs, Soa s, long long n) {
+__global__ void k_cellw(CaseDev cs, Parcels s, long long n) {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double x[3] = {s.x[i], s.y[i], s.z[i]};
+    const Rec p = ldg_rec(s.r + i);
+    const double x[3] = {p.x, p.y, p.z};
     int sb = 0, ci[3];
     for (int a = 0; a < 3; ++a) {
         int c2 = floor2_coord(cs, x[a], a);
@@ -968,14 +963,14 @@ int grid_for(long long n, int threads, int perSmBlocks) {
 
 int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TILE) + 1; }
 
-void launch_move(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
+void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
     const int grid = grid_for(B.capacity, MOVE_THREADS, 8);
     k_move<<<grid, MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
     k_move_slow<<<grid_for(B.capacity, MOVE_THREADS, 2), MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList,
                                                                                B.bfPatch, B.wall, B.count);
 }
 
-void launch_count(const CaseDev& cs, const StepBuffers& B, const Soa& s, cudaStream_t st) {
+void launch_count(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
     (void)cs;
     const int grid = grid_for(B.capacity, 256, 8);
     k_count_dev<<<grid, 256, 0, st>>>(s, B.ctr, B.count);
@@ -988,12 +983,12 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st) {
     k_scan_down<<<nb, SCAN_THREADS, 0, st>>>(B.count, cs.C, B.blockSums, B.start);
 }
 
-void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Soa& src, const Soa& dst,
+void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
                     cudaStream_t st) {
     (void)cs;
     const int grid = grid_for(B.capacity, 256, 8);
-    k_scatter_index<<<grid, 256, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortIdx);
-    k_gather<<<grid, 256, 0, st>>>(src, dst, B.ctr, B.sortIdx);
+    k_scatter_index<<<grid, 256, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortSrc);
+    k_gather<<<grid, 256, 0, st>>>(src, dst, B.ctr, B.sortSrc);
 }
 
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st) {
@@ -1007,7 +1002,7 @@ void launch_sample_commit(const CaseDev& cs, const StepBuffers& B, int force, cu
     k_sample_flushed<<<1, 1, 0, st>>>(B.ctr, force);
 }
 
-void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Soa& s, int force, cudaStream_t st) {
+void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int force, cudaStream_t st) {
     k_sample_pass<<<grid_for(B.capacity, MOVE_THREADS, 8), MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.sfix);
     launch_sample_commit(cs, B, force, st);
 }
@@ -1018,7 +1013,7 @@ void launch_end_step(const StepBuffers& B, cudaStream_t st) {
     k_end_step<<<1, 1, 0, st>>>(B.ctr);
 }
 
-void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Soa& s,
+void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B, const Parcels& s,
                    cudaStream_t st) {
     const int nt = B.nInflowFaces * cs.nSpecies;
     if (nt == 0) return;
@@ -1031,7 +1026,7 @@ void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B,
     k_inflow_commit<<<1, 1, 0, st>>>(B.ctr);
 }
 
-void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Soa& s, const double* dnd,
+void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Parcels& s, const double* dnd,
                       const unsigned char* solid, const int* cellOff, double Ttra, const double* Txyz,
                       double Trot, double Tvib, const double* U, cudaStream_t st) {
     const int grid = (int)((cs.C + 127) / 128);
@@ -1045,12 +1040,12 @@ void launch_init_count(const CaseDev& cs, const double* dnd, const unsigned char
     k_init_count<<<grid, 256, 0, st>>>(cs, dnd, solid, cellCounts);
 }
 
-void launch_cellw(const CaseDev& cs, const Soa& s, long long n, cudaStream_t st) {
+void launch_cellw(const CaseDev& cs, const Parcels& s, long long n, cudaStream_t st) {
     if (n <= 0) return;
     k_cellw<<<(int)((n + 255) / 256), 256, 0, st>>>(cs, s, n);
 }
 
-void launch_count_n(const Soa& s, long long n, int* count, cudaStream_t st) {
+void launch_count_n(const Parcels& s, long long n, int* count, cudaStream_t st) {
     if (n <= 0) return;
     const int grid = grid_for(n, 256, 8);
     k_count<<<grid, 256, 0, st>>>(s, n, count);

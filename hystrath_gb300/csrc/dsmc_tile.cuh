@@ -185,7 +185,7 @@ struct BlockBar {
 // the local index of the r-th member in canonical order, subs[q] the start
 // of each sub-cell in it
 __global__ void __launch_bounds__(WARPS * 32)
-k_cell_order(Soa s, const int* __restrict__ start, const Counters* ctr, const int2* __restrict__ work,
+k_cell_order(Parcels s, const int* __restrict__ start, const Counters* ctr, const int2* __restrict__ work,
              uint16_t* perm, uint4* subs) {
     __shared__ unsigned long long keysAll[WARPS][ORDER_WARP_N];
     unsigned long long* keys = keysAll[threadIdx.x >> 5];
@@ -207,7 +207,7 @@ k_cell_order(Soa s, const int* __restrict__ start, const Counters* ctr, const in
             if (j < n) {
                 const uint32_t w = s.cellw[off + j];
                 sb = (int)(w & 7u);
-                key = order_key(w, s.id[off + j], j);
+                key = order_key(w, s.r[off + j].id, j);
             }
             keys[j] = key;
 #pragma unroll
@@ -224,7 +224,7 @@ k_cell_order(Soa s, const int* __restrict__ start, const Counters* ctr, const in
 // one block per listed cell above ORDER_WARP_N parcels (dynamic shared
 // memory of ORDER_MAX_N keys)
 __global__ void __launch_bounds__(ORDER_BLOCK)
-k_cell_order_big(Soa s, const int* __restrict__ start, const Counters* ctr, const int2* __restrict__ work,
+k_cell_order_big(Parcels s, const int* __restrict__ start, const Counters* ctr, const int2* __restrict__ work,
                  const int* __restrict__ bigList, uint16_t* perm, uint4* subs) {
     extern __shared__ unsigned long long keysBig[];
     __shared__ int cnt[8];
@@ -243,7 +243,7 @@ k_cell_order_big(Soa s, const int* __restrict__ start, const Counters* ctr, cons
             if (j < n) {
                 const uint32_t w = s.cellw[off + j];
                 atomicAdd(&cnt[w & 7u], 1);
-                key = order_key(w, s.id[off + j], j);
+                key = order_key(w, s.r[off + j].id, j);
             }
             keysBig[j] = key;
         }
@@ -319,28 +319,33 @@ __device__ __forceinline__ void draw_pair(Rng& r, int n, const uint4& so, int* p
 
 // Candidate (gP, gQ): sigma_T c_R, the running maximum, the acceptance test
 // against the maximum the candidate count was based on, and the collision.
-__device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Soa& s, Rng& r, long long gP, long long gQ,
-                                              double smax0, double* smaxRun, double* collSep, unsigned* err) {
-    const int tP = (int)s.spc[gP], tQ = (int)s.spc[gQ];
+__device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
+                                              long long gQ, double smax0, double* smaxRun, double* collSep,
+                                              unsigned* err) {
+    Rec P = ld_rec(s.r + gP), Q = ld_rec(s.r + gQ);
+    const int tP = sv_species(P.sv), tQ = sv_species(Q.sv);
     const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
     Post o;
-    o.UP[0] = s.ux[gP]; o.UP[1] = s.uy[gP]; o.UP[2] = s.uz[gP];
-    o.UQ[0] = s.ux[gQ]; o.UQ[1] = s.uy[gQ]; o.UQ[2] = s.uz[gQ];
+    o.UP[0] = P.ux; o.UP[1] = P.uy; o.UP[2] = P.uz;
+    o.UQ[0] = Q.ux; o.UQ[1] = Q.uy; o.UQ[2] = Q.uz;
     const double d0 = o.UP[0] - o.UQ[0], d1 = o.UP[1] - o.UQ[1], d2 = o.UP[2] - o.UQ[2];
     const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
     const double sigma = sigma_cr(pr, cr2);
     if (sigma > *smaxRun) *smaxRun = sigma;
     if (!(sigma > r.u01() * smax0)) return false;      // (sigma/smax0) > U with smax0 > 0
-    o.eP = s.erot[gP]; o.eQ = s.erot[gQ];
-    o.vP = s.vib[gP]; o.vQ = s.vib[gQ];
+    o.eP = P.erot; o.eQ = Q.erot;
+    o.vP = sv_vib(P.sv); o.vQ = sv_vib(Q.sv);
     collide_pair(cs, r, pr, tP, tQ, cr2, o, err);
-    s.ux[gP] = o.UP[0]; s.uy[gP] = o.UP[1]; s.uz[gP] = o.UP[2];
-    s.ux[gQ] = o.UQ[0]; s.uy[gQ] = o.UQ[1]; s.uz[gQ] = o.UQ[2];
-    s.erot[gP] = o.eP; s.erot[gQ] = o.eQ;
-    s.vib[gP] = o.vP; s.vib[gQ] = o.vQ;
-    const double dx = s.x[gP] - s.x[gQ];
-    const double dy = s.y[gP] - s.y[gQ];
-    const double dz = s.z[gP] - s.z[gQ];
+    if (o.vP > SV_MAX_VIB || o.vQ > SV_MAX_VIB) *err |= ERRB_BOUNDS;
+    P.ux = o.UP[0]; P.uy = o.UP[1]; P.uz = o.UP[2];
+    Q.ux = o.UQ[0]; Q.uy = o.UQ[1]; Q.uz = o.UQ[2];
+    P.erot = o.eP; Q.erot = o.eQ;
+    P.sv = make_sv(tP, o.vP); Q.sv = make_sv(tQ, o.vQ);
+    st_rec(s.r + gP, P);
+    st_rec(s.r + gQ, Q);
+    const double dx = P.x - Q.x;
+    const double dy = P.y - Q.y;
+    const double dz = P.z - Q.z;
     *collSep += sqrt(dx * dx + dy * dy + dz * dz);
     return true;
 }
@@ -349,7 +354,7 @@ __device__ __forceinline__ uint32_t cand_tag(int k) { return (uint32_t)TAG_COLLI
 
 // one warp per heavy cell, up to 32 candidates at a time
 __global__ void __launch_bounds__(WARPS * 32)
-k_collide_heavy(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
+k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs) {
     const unsigned lane = lane_id();
     const uint32_t step = (uint32_t)ctr->step;
@@ -436,15 +441,23 @@ __device__ __forceinline__ uint32_t pick_key(const CaseDev& cs, uint32_t cell, u
     return h ^ cs.seedLo;
 }
 
-// member of the cell [off, off+n) with the smallest hash under key; sub < 0:
-// any sub-cell; skip: excluded member
-__device__ __forceinline__ int hash_pick(const Soa& s, long long off, int n, uint32_t key, int sub, int skip) {
+// Light cells stage their members' ids and sub-cells in shared memory, one
+// column per lane (member j of lane l at [j][l]: the lanes of a warp read
+// consecutive words).
+struct LightStage {
+    uint32_t id[LIGHT_N][32];
+    uint8_t sub[LIGHT_N][32];
+};
+
+// member of the staged cell of n members with the smallest hash under key;
+// sub < 0: any sub-cell; skip: excluded member
+__device__ __forceinline__ int hash_pick(const LightStage& st, int lane, int n, uint32_t key, int sub, int skip) {
     uint32_t best = 0xFFFFFFFFu;
     int arg = -1;
     for (int j = 0; j < n; ++j) {
         if (j == skip) continue;
-        if (sub >= 0 && (int)(__ldg(s.cellw + off + j) & 7u) != sub) continue;
-        const uint32_t h = fmix32(key ^ __ldg(s.id + off + j));
+        if (sub >= 0 && (int)st.sub[j][lane] != sub) continue;
+        const uint32_t h = fmix32(key ^ st.id[j][lane]);
         if (arg < 0 || h < best) { best = h; arg = j; }
     }
     return arg;
@@ -452,8 +465,11 @@ __device__ __forceinline__ int hash_pick(const Soa& s, long long off, int n, uin
 
 // one lane per light cell, its candidates one after the other
 __global__ void __launch_bounds__(WARPS * 32, 4)
-k_collide_light(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
+k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work) {
+    __shared__ LightStage stage[WARPS];
+    LightStage& st = stage[threadIdx.x >> 5];
+    const int lane = (int)(threadIdx.x & 31u);
     const uint32_t step = (uint32_t)ctr->step;
     const long long nWork = (long long)ctr->nWork;
     const long long nHeavy = (long long)ctr->nHeavy;
@@ -469,15 +485,20 @@ k_collide_light(CaseDev cs, Soa s, const int* __restrict__ start, double* smax, 
         const int n = start[c + 1] - (int)off;
         // sub-cell occupancy, 8 bits per sub-cell (n <= LIGHT_N < 256)
         unsigned long long subCnt = 0;
-        for (int j = 0; j < n; ++j) subCnt += 1ull << (8u * (__ldg(s.cellw + off + j) & 7u));
+        for (int j = 0; j < n; ++j) {
+            const uint32_t sb = __ldg(s.cellw + off + j) & 7u;
+            st.sub[j][lane] = (uint8_t)sb;
+            st.id[j][lane] = s.r[off + j].id;
+            subCnt += 1ull << (8u * sb);
+        }
         const double smax0 = smax[c];
         double smaxRun = smax0, collSep = 0.0;
         unsigned coll = 0;
         for (int k = 0; k < nCand; ++k) {
-            const int jP = hash_pick(s, off, n, pick_key(cs, (uint32_t)c, step, 2u * k), -1, -1);
-            const int sub = (int)(__ldg(s.cellw + off + jP) & 7u);
+            const int jP = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k), -1, -1);
+            const int sub = (int)st.sub[jP][lane];
             const bool inSub = ((subCnt >> (8 * sub)) & 0xFFu) > 1;
-            const int jQ = hash_pick(s, off, n, pick_key(cs, (uint32_t)c, step, 2u * k + 1u), inSub ? sub : -1, jP);
+            const int jQ = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k + 1u), inSub ? sub : -1, jP);
             Rng r(cs, (uint32_t)c, step, cand_tag(k));
             if (run_candidate(cs, s, r, off + jP, off + jQ, smax0, &smaxRun, &collSep, &err)) ++coll;
         }
