@@ -106,11 +106,31 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# parcel state: a 64-byte record (pos, U, ERot, id, species|vib) + a 4-byte cell word
+STATE_BYTES = 68
+
+# kernels of one heat-bath step (no inflow): zero_step; move, move_slow;
+# sample_done, sample_finalize, sample_flushed; scan_reduce, scan_top,
+# scan_down; scatter_index, gather, finish_sort; ntc_select, ntc_buckets,
+# ntc_list, cell_order, cell_order_big, collide_heavy, collide_light;
+# set_pending; end_step
+KERNELS_PER_STEP = 21
+
+
 def bytes_model(N, C, coll, n_acc):
-    """Algorithmic bytes per step (per-parcel and per-cell figures)."""
-    move = 80.0 * N                                 # read pos,U (48) + cell word (4); write pos (24) + cell word (4)
-    sort = 144.0 * N + 16.0 * C                     # scatter 72 B read + 72 B write; scan 12 B + start 4 B per cell
-    collide = 48.0 * N + (32.0 + 16.0 * n_acc + 4.0) * C + 80.0 * coll
+    """Algorithmic bytes per step, per phase.
+
+    move:    read pos,U (48) + cell word (4); write pos (24) + cell word (4)
+    sort:    stable counting sort of the state, read + write (2 x 68), plus
+             the per-cell count and offset (8 B per cell)
+    collide: per cell the sigmaTcRMax, remainder and counts (32 B) and the
+             sampling accumulators (8 B per accumulator, read + write every
+             32 samples, 16/32 per step); per collision the two records
+             read and written (4 x 64 B)
+    """
+    move = 80.0 * N
+    sort = 2.0 * STATE_BYTES * N + 8.0 * C
+    collide = (32.0 + 0.5 * n_acc) * C + 256.0 * coll
     return move, sort, collide
 
 
@@ -185,7 +205,7 @@ def gpu_arm(args, rank, world, local):
     per = {k: v / args.steps for k, v in phases.items()}
     dominant = max(("move", "sort", "collide_sample"), key=lambda k: per[k])
     algo = {"move": mv, "sort": so, "collide_sample": co}
-    kern = {"move": "k_move", "sort": "k_scatter", "collide_sample": "k_collide_tile"}
+    kern = {"move": "k_move", "sort": "k_gather", "collide_sample": "k_collide_light"}
 
     def roof(k):
         achieved = algo[k] / (per[k] * 1e-3) / 1e9
@@ -210,7 +230,7 @@ def gpu_arm(args, rank, world, local):
         "dtype": "f64",
         "data": "synthetic (dsmcMeshFill of the heat bath from the seed)",
         "config": {"workload": WORKLOAD.format(n=args.cells), "cells": C, "parcels": N, "parcels_total": int(tot_N),
-                   "l2": "inputs larger than L2 (0.94 GB of parcel state per GPU)",
+                   "l2": "inputs larger than L2 (0.89 GB of parcel state per buffer)",
                    "parallelism": f"{world} independent replicas" if world > 1 else "1 GPU",
                    "phase_ms_per_step": {k: round(v, 4) for k, v in per.items()}},
         "roofline": roof(dominant),
@@ -218,7 +238,7 @@ def gpu_arm(args, rank, world, local):
                                "peak": peak, "unit": "GB/s",
                                "frac": round((mv + so) / (ms_ms * 1e-3) / 1e9 / peak, 4),
                                "bytes_per_parcel_step": round((mv + so) / N, 1)},
-        "gpu_launches": int(args.steps * 10),
+        "gpu_launches": int(args.steps * KERNELS_PER_STEP),
         "e2e": e2e,
         "clocks": clocks,
     }
