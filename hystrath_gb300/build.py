@@ -28,6 +28,7 @@ UNITS = {
     "dsmc_collide.cu": [],
     "dsmc_api.cu": [],
     "dsmc_noalloc.cu": [],
+    "dsmc_mlp.cu": [],
     "case_parser.cpp": [],
 }
 

@@ -41,6 +41,10 @@ struct dsmc_handle {
     double phaseMs[5] = {0, 0, 0, 0, 0};
     bool hasInflow = false;
     long long expectedN = 0;
+    // learned selection
+    const MlpModel* model = nullptr;
+    int learnEvery = 0;
+    float learnMargin = 0.f;
 };
 
 namespace {
@@ -208,6 +212,7 @@ void fill_case_dev(dsmc_handle* h) {
     cs.fixedZv = s.fixed_zv;
     cs.invZvForm = s.inv_zv_formulation;
     cs.nPatches = s.n_patches;
+    for (int i = 0; i < s.n_species; ++i) cs.mRel[i] = (float)(s.species[i].mass / s.species[0].mass);
     for (int i = 0; i < s.n_species; ++i) {
         const dsmc_species& q = s.species[i];
         SpeciesDev& d = cs.sp[i];
@@ -311,7 +316,14 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
         cudaMemsetAsync(B.count, 0, sizeof(int) * cs.C, st);
     }
     if (ev) cudaEventRecord(ev[3], st);
-    if (phases & DSMC_PHASE_COLLIDE) launch_collide(cs, B, (phases & DSMC_PHASE_SORT) ? b : a, st);
+    if (phases & DSMC_PHASE_COLLIDE) {
+        const Parcels& cur = (phases & DSMC_PHASE_SORT) ? b : a;
+        if (h->model) {
+            launch_cell_features(cs, B, cur, h->learnEvery, 1, st);
+            mlp_launch_infer(h->model, B.feat, cs.C, B.pred, h->learnMargin, &B.ctr->step, h->learnEvery, st);
+        }
+        launch_collide(cs, B, cur, h->model ? 1 : 0, st);
+    }
     // dsmcVolFields samples the state after the collisions; the sums are
     // taken when that state is next streamed (the next move, or a flush)
     if (phases & DSMC_PHASE_SAMPLE) launch_set_pending(B, st);
@@ -452,6 +464,11 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.buckets, 32))) return rc;
     if ((rc = dalloc(h, &B.perm, cap))) return rc;
     if ((rc = dalloc(h, &B.subs, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.obsMax, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.feat, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.pred, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.useR, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.smaxSel, cs.C))) return rc;
     if ((rc = dalloc(h, &B.slowList, cap))) return rc;
     if ((rc = dalloc(h, &B.sortSrc, cap))) return rc;
     if ((rc = dalloc(h, &B.ctr, 1))) return rc;
@@ -929,6 +946,51 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
     CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemset(h->B.count, 0, sizeof(int) * h->cs.C));
     CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
+    return DSMC_OK;
+}
+
+// ------------------------------------------------------- learned selection
+int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float margin) {
+    if (every < 1) return fail(h, DSMC_ERR_INVALID, "every must be at least 1");
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->model = reinterpret_cast<const MlpModel*>(model);
+    h->learnEvery = every;
+    h->learnMargin = margin;
+    // the step graphs hold the selection mode: capture them again
+    for (int p = 0; p < 2; ++p)
+        if (h->graph[p]) {
+            cudaGraphExecDestroy(h->graph[p]);
+            h->graph[p] = nullptr;
+        }
+    // every cell starts on the running maximum until the first prediction
+    CUDA_TRY(h, cudaMemset(h->B.pred, 0, sizeof(float) * h->cs.C));
+    CUDA_TRY(h, cudaMemset(h->B.useR, 1, h->cs.C));
+    return DSMC_OK;
+}
+
+int dsmc_learn_record(dsmc_handle* h, long long max_rows, float* X, float* Y, long long* n_out) {
+    if (n_out) *n_out = 0;
+    if (max_rows <= 0) return DSMC_OK;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    float *dX = nullptr, *dY = nullptr;
+    unsigned long long* dn = nullptr;
+    CUDA_TRY(h, cudaMalloc(&dX, sizeof(float) * 3 * max_rows));
+    CUDA_TRY(h, cudaMalloc(&dY, sizeof(float) * max_rows));
+    CUDA_TRY(h, cudaMalloc(&dn, sizeof(unsigned long long)));
+    launch_cell_features(h->cs, h->B, cur_soa(h), 0, 0, h->stream);
+    launch_learn_compact(h->cs, h->B, max_rows, dX, dY, dn, h->stream);
+    unsigned long long n = 0;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&n, dn, sizeof(n), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    const long long m = (long long)n < max_rows ? (long long)n : max_rows;
+    if (e == cudaSuccess && m > 0) e = cudaMemcpy(X, dX, sizeof(float) * 3 * m, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && m > 0) e = cudaMemcpy(Y, dY, sizeof(float) * m, cudaMemcpyDeviceToHost);
+    cudaFree(dX);
+    cudaFree(dY);
+    cudaFree(dn);
+    if (e != cudaSuccess) return fail(h, DSMC_ERR_CUDA, std::string("dsmc_learn_record: ") + cudaGetErrorString(e));
+    if (n_out) *n_out = m;
     return DSMC_OK;
 }
 

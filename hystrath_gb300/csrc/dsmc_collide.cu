@@ -264,6 +264,68 @@ __global__ void k_info(CaseDev cs, Parcels s, const Counters* ctr, double* out) 
     }
 }
 
+// ------------------------------------------------------- learned maximum
+// Features of the learned (sigma_T c_R)max, one thread per cell: log number
+// density, log translational temperature of the cell's parcels and their
+// speed ratio |U| / sqrt(2 k T / m), with m the mean parcel mass.  Features
+// need three digits: the sums run in FP32 on velocities converted on the
+// integer pipe, with masses relative to species 0.
+__global__ void k_cell_features(CaseDev cs, Parcels s, const int* __restrict__ start, const Counters* ctr,
+                                int every, float4* feat, unsigned char* useR) {
+    if (every > 0 && (ctr->step % every) != 0) return;
+    const float kOverM0 = (float)(kB / cs.sp[0].m);
+    const float ndScale = (float)(cs.FN / cs.V);
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cs.C;
+         c += (long long)gridDim.x * blockDim.x) {
+        const long long off = start[c];
+        const int n = start[c + 1] - (int)off;
+        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (n >= 2) {
+            float M = 0.f, Mu0 = 0.f, Mu1 = 0.f, Mu2 = 0.f, Muu = 0.f;
+            for (int j = 0; j < n; ++j) {
+                const double2* q = reinterpret_cast<const double2*>(s.r + off + j);
+                const double2 b = __ldg(q + 1), d = __ldg(q + 2), e = __ldg(q + 3);
+                const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(e.y) >> 32);
+                const float m = cs.mRel[sv_species(sv)];
+                const float ux = d2f_bits(b.y), uy = d2f_bits(d.x), uz = d2f_bits(d.y);
+                M += m;
+                Mu0 = fmaf(m, ux, Mu0);
+                Mu1 = fmaf(m, uy, Mu1);
+                Mu2 = fmaf(m, uz, Mu2);
+                Muu = fmaf(m, ux * ux + uy * uy + uz * uz, Muu);
+            }
+            const float U2 = (Mu0 * Mu0 + Mu1 * Mu1 + Mu2 * Mu2) / (M * M);
+            // T = m0 (sum m_rel u^2 - M U^2) / (3 k n)
+            const float T = (Muu - M * U2) / (3.0f * kOverM0 * (float)n);
+            if (T > 0.f) {
+                const float cmp = sqrtf(2.0f * kOverM0 * T / (M / (float)n));
+                f = make_float4(logf(ndScale * (float)n), logf(T), sqrtf(U2) / cmp, 1.f);
+            }
+        }
+        feat[c] = f;
+        if (useR) useR[c] = 0;
+    }
+}
+
+// (features, log observed maximum) of the cells that had candidates in the
+// last step, compacted in any order
+__global__ void k_learn_compact(CaseDev cs, const int* __restrict__ ncCell, const float4* __restrict__ feat,
+                                const float* __restrict__ obsMax, long long maxRows, float* X, float* Y,
+                                unsigned long long* nOut) {
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cs.C;
+         c += (long long)gridDim.x * blockDim.x) {
+        const float4 f = feat[c];
+        const float o = obsMax[c];
+        if (ncCell[c] <= 0 || f.w == 0.f || !(o > 0.f)) continue;
+        const unsigned long long q = atomicAdd(nOut, 1ull);
+        if ((long long)q >= maxRows) continue;
+        X[3 * q] = f.x;
+        X[3 * q + 1] = f.y;
+        X[3 * q + 2] = f.z;
+        Y[q] = logf(o);
+    }
+}
+
 int sm_count() {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -279,21 +341,40 @@ int collide_init() {
     return e == cudaSuccess ? 0 : (int)e;
 }
 
-void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
+void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st) {
     const int sms = sm_count();
     long long selBlocks = (cs.C + 255) / 256;
     if (selBlocks > (long long)sms * 8) selBlocks = (long long)sms * 8;
     unsigned* slotCount = B.buckets;
     unsigned* slotCursor = B.buckets + 2 * tile::NBUCKET;
-    tile::k_ntc_select<<<(int)selBlocks, 256, 0, st>>>(cs, B.start, B.smax, B.rem, B.ctr, B.ncCell, slotCount);
+    tile::k_ntc_select<<<(int)selBlocks, 256, 0, st>>>(cs, B.start, B.smax, B.rem, B.ctr, B.ncCell, slotCount,
+                                                        learned, B.pred, B.useR, B.smaxSel);
     tile::k_ntc_buckets<<<1, 1, 0, st>>>(B.ctr, slotCount, slotCursor);
     tile::k_ntc_list<<<(int)selBlocks, 256, 0, st>>>(cs.C, B.start, B.ncCell, slotCursor, B.work, B.bigList, B.ctr);
     tile::k_cell_order<<<sms * 8, tile::WARPS * 32, 0, st>>>(s, B.start, B.ctr, B.work, B.perm, B.subs);
     tile::k_cell_order_big<<<sms, tile::ORDER_BLOCK, tile::ORDER_MAX_N * sizeof(unsigned long long), st>>>(
         s, B.start, B.ctr, B.work, B.bigList, B.perm, B.subs);
     tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
-                                                                B.perm, B.subs);
-    tile::k_collide_light<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work);
+                                                                B.perm, B.subs, learned, B.smaxSel, B.useR,
+                                                                B.obsMax);
+    tile::k_collide_light<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
+                                                                learned, B.smaxSel, B.useR, B.obsMax);
+}
+
+void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,
+                          cudaStream_t st) {
+    long long blocks = (cs.C + 255) / 256;
+    if (blocks > (long long)sm_count() * 16) blocks = (long long)sm_count() * 16;
+    k_cell_features<<<(int)blocks, 256, 0, st>>>(cs, s, B.start, B.ctr, every, B.feat,
+                                                 resetFallback ? B.useR : nullptr);
+}
+
+void launch_learn_compact(const CaseDev& cs, const StepBuffers& B, long long maxRows, float* X, float* Y,
+                          unsigned long long* nOut, cudaStream_t st) {
+    long long blocks = (cs.C + 255) / 256;
+    if (blocks > (long long)sm_count() * 16) blocks = (long long)sm_count() * 16;
+    cudaMemsetAsync(nOut, 0, sizeof(unsigned long long), st);
+    k_learn_compact<<<(int)blocks, 256, 0, st>>>(cs, B.ncCell, B.feat, B.obsMax, maxRows, X, Y, nOut);
 }
 
 void launch_zero_step(const StepBuffers& B, cudaStream_t st) { k_zero_step<<<1, 1, 0, st>>>(B.ctr); }

@@ -88,6 +88,7 @@ struct CaseDev {
     int invZvForm;
     int nPatches;
     SpeciesDev sp[DSMC_MAX_SPECIES];
+    float mRel[DSMC_MAX_SPECIES];   // species mass / mass of species 0 (FP32 feature sums)
     PairDev pair[DSMC_MAX_SPECIES * DSMC_MAX_SPECIES];
     PatchDev patch[DSMC_MAX_PATCHES];
     int obLoI[DSMC_MAX_OBSTACLES][3], obHiI[DSMC_MAX_OBSTACLES][3];
@@ -252,6 +253,17 @@ __device__ __forceinline__ int floor2_bits(double t) {
     const int ip = (int)(m >> sh);
     const int frac = (m << (64 - sh)) != 0ull;
     return b < 0 ? -(ip + frac) : ip;
+}
+
+// float(v) truncated, from the bits of v on the integer pipe (normal range;
+// values below FLT_MIN become 0)
+__device__ __forceinline__ float d2f_bits(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+    if (e <= 0) return 0.0f;
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    if (e >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
 }
 
 __device__ __forceinline__ int floor2_coord(const CaseDev& cs, double x, int a) {

@@ -45,6 +45,12 @@ struct StepBuffers {
     unsigned* buckets;        // [32] work-slot counts and cursors
     uint16_t* perm;           // [capacity] canonical member order of the cells with candidates
     uint4* subs;              // [C] sub-cell starts in that order, per work item
+    float* obsMax;            // [C] largest sigma_T c_R among this step's candidates of the cell
+    // learned selection (used when a model is attached)
+    float4* feat;             // [C] log n, log T_tr, speed ratio, valid
+    float* pred;              // [C] predicted (sigma_T c_R)max
+    unsigned char* useR;      // [C] 1: the cell has fallen back to the running maximum
+    double* smaxSel;          // [C] the maximum this step's selection used
     int* slowList;            // [capacity] parcels that take the boundary path this step
     int2* sortSrc;            // [capacity] (source index, cell word) of each destination slot of the sort
     // inflow
@@ -80,7 +86,24 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
                     cudaStream_t st);
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
-void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
+// learned != 0: the selection uses the prediction (or the running maximum of
+// cells that fell back to it) instead of the running maximum alone
+void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st);
+// per-cell features of the learned maximum; every > 0: only on steps that are
+// multiples of every, every == 0: always; resetFallback: the cells go back to
+// the prediction
+void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,
+                          cudaStream_t st);
+// compacts (features, log observed maximum) of the cells with candidates in
+// the last step; returns the count in *nOut (device)
+void launch_learn_compact(const CaseDev& cs, const StepBuffers& B, long long maxRows, float* X, float* Y,
+                          unsigned long long* nOut, cudaStream_t st);
+
+struct MlpModel;
+// prediction for n rows of features: out = exp(net + margin); with step !=
+// nullptr and every > 0 only when *step is a multiple of every
+void mlp_launch_infer(const MlpModel* m, const float4* X, long long n, float* out, float margin,
+                      const long long* step, int every, cudaStream_t st);
 // one-time kernel attributes (large dynamic shared memory); call before the
 // first capture
 int collide_init();

@@ -74,8 +74,13 @@ __device__ __forceinline__ int get16(const uint4& w, int s) {
 // ------------------------------------------------------------ selection
 // selectedPairs and the remainder, one thread per cell; the candidate count
 // of each cell is kept for k_ntc_list and counted per slot
+// learned: the maximum is the prediction unless the cell has fallen back to
+// the running maximum (or has no prediction); it is kept in smaxSel for the
+// acceptance tests of this step
 __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const double* __restrict__ smax, double* rem,
-                             Counters* ctr, int* ncCell, unsigned* slotCount) {
+                             Counters* ctr, int* ncCell, unsigned* slotCount, int learned,
+                             const float* __restrict__ pred, const unsigned char* __restrict__ useR,
+                             double* smaxSel) {
     __shared__ unsigned hist[2 * NBUCKET];
     if (threadIdx.x < 2 * NBUCKET) hist[threadIdx.x] = 0;
     __syncthreads();
@@ -86,7 +91,13 @@ __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const do
         int nc = 0;
         const int n = start[c + 1] - start[c];
         if (n > 1) {
-            const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * smax[c] * cs.dt / cs.V;
+            double sm = smax[c];
+            if (learned) {
+                const float pv = pred[c];
+                if (!useR[c] && pv > 0.f && pv < 3.0e38f) sm = (double)pv;
+                smaxSel[c] = sm;
+            }
+            const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cs.V;
             const double whole = floor(sel);
             rem[c] = sel - whole;
             if (n > ORDER_MAX_N || whole >= (double)MAX_CAND) err |= ERRB_DENSE;
@@ -320,7 +331,7 @@ __device__ __forceinline__ void draw_pair(Rng& r, int n, const uint4& so, int* p
 // Candidate (gP, gQ): sigma_T c_R, the running maximum, the acceptance test
 // against the maximum the candidate count was based on, and the collision.
 __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
-                                              long long gQ, double smax0, double* smaxRun, double* collSep,
+                                              long long gQ, double smax0, double* stepMax, double* collSep,
                                               unsigned* err) {
     Rec P = ld_rec(s.r + gP), Q = ld_rec(s.r + gQ);
     const int tP = sv_species(P.sv), tQ = sv_species(Q.sv);
@@ -331,7 +342,7 @@ __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& 
     const double d0 = o.UP[0] - o.UQ[0], d1 = o.UP[1] - o.UQ[1], d2 = o.UP[2] - o.UQ[2];
     const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
     const double sigma = sigma_cr(pr, cr2);
-    if (sigma > *smaxRun) *smaxRun = sigma;
+    if (sigma > *stepMax) *stepMax = sigma;
     if (!(sigma > r.u01() * smax0)) return false;      // (sigma/smax0) > U with smax0 > 0
     o.eP = P.erot; o.eQ = Q.erot;
     o.vP = sv_vib(P.sv); o.vQ = sv_vib(Q.sv);
@@ -350,12 +361,24 @@ __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& 
     return true;
 }
 
+// After a cell's candidates: the running maximum takes the largest product
+// seen (noTimeCounter.C:243-246), the step's largest product is kept for
+// training, and a learned cell whose prediction was exceeded falls back to
+// the running maximum until the next prediction.
+__device__ __forceinline__ void cell_epilogue(double* smax, long long c, double R, double smax0, double stepMax,
+                                              int learned, unsigned char* useR, float* obsMax) {
+    if (stepMax > R) smax[c] = stepMax;
+    obsMax[c] = (float)stepMax;
+    if (learned && stepMax > smax0) useR[c] = 1;
+}
+
 __device__ __forceinline__ uint32_t cand_tag(int k) { return (uint32_t)TAG_COLLIDE | ((uint32_t)k << 8); }
 
 // one warp per heavy cell, up to 32 candidates at a time
 __global__ void __launch_bounds__(WARPS * 32)
 k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
-                const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs) {
+                const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs,
+                int learned, const double* __restrict__ smaxSel, unsigned char* useR, float* obsMax) {
     const unsigned lane = lane_id();
     const uint32_t step = (uint32_t)ctr->step;
     const long long nHeavy = (long long)ctr->nHeavy;
@@ -370,8 +393,9 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
         const long long off = start[c];
         const int n = start[c + 1] - (int)off;
         const uint4 so = subs[q];
-        const double smax0 = smax[c];
-        double smaxRun = smax0, collSep = 0.0;
+        const double R = smax[c];
+        const double smax0 = learned ? smaxSel[c] : R;
+        double stepMax = 0.0, collSep = 0.0;
         unsigned coll = 0;
         for (int base = 0; base < nCand; base += 32) {
             const int k = base + (int)lane;
@@ -395,7 +419,7 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
                     const int b = __shfl_sync(0xFFFFFFFFu, pQ, j);
                     if (j < (int)lane && (a == pP || a == pQ || b == pP || b == pQ)) ready = false;
                 }
-                if (ready && run_candidate(cs, s, r, gP, gQ, smax0, &smaxRun, &collSep, &err)) ++coll;
+                if (ready && run_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &collSep, &err)) ++coll;
                 __syncwarp();
                 pend &= ~__ballot_sync(0xFFFFFFFFu, ready);
             }
@@ -403,11 +427,11 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             collSep += __shfl_xor_sync(0xFFFFFFFFu, collSep, o);
-            smaxRun = fmax(smaxRun, __shfl_xor_sync(0xFFFFFFFFu, smaxRun, o));
+            stepMax = fmax(stepMax, __shfl_xor_sync(0xFFFFFFFFu, stepMax, o));
             coll += __shfl_xor_sync(0xFFFFFFFFu, coll, o);
         }
         if (lane == 0) {
-            smax[c] = smaxRun;
+            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax);
             if (coll) {
                 acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
                 acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
@@ -466,7 +490,8 @@ __device__ __forceinline__ int hash_pick(const LightStage& st, int lane, int n, 
 // one lane per light cell, its candidates one after the other
 __global__ void __launch_bounds__(WARPS * 32, 4)
 k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
-                const int2* __restrict__ work) {
+                const int2* __restrict__ work, int learned, const double* __restrict__ smaxSel, unsigned char* useR,
+                float* obsMax) {
     __shared__ LightStage stage[WARPS];
     LightStage& st = stage[threadIdx.x >> 5];
     const int lane = (int)(threadIdx.x & 31u);
@@ -491,8 +516,9 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
             st.id[j][lane] = s.r[off + j].id;
             subCnt += 1ull << (8u * sb);
         }
-        const double smax0 = smax[c];
-        double smaxRun = smax0, collSep = 0.0;
+        const double R = smax[c];
+        const double smax0 = learned ? smaxSel[c] : R;
+        double stepMax = 0.0, collSep = 0.0;
         unsigned coll = 0;
         for (int k = 0; k < nCand; ++k) {
             const int jP = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k), -1, -1);
@@ -500,9 +526,9 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
             const bool inSub = ((subCnt >> (8 * sub)) & 0xFFu) > 1;
             const int jQ = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k + 1u), inSub ? sub : -1, jP);
             Rng r(cs, (uint32_t)c, step, cand_tag(k));
-            if (run_candidate(cs, s, r, off + jP, off + jQ, smax0, &smaxRun, &collSep, &err)) ++coll;
+            if (run_candidate(cs, s, r, off + jP, off + jQ, smax0, &stepMax, &collSep, &err)) ++coll;
         }
-        smax[c] = smaxRun;
+        cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax);
         if (coll) {
             acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
             acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;

@@ -55,6 +55,20 @@ def _load() -> C.CDLL:
     L.dsmc_last_error.restype = C.c_char_p
     L.dsmc_last_global_error.restype = C.c_char_p
     L.dsmc_destroy.argtypes = [vp]
+    L.dsmc_mlp_create.argtypes = [C.POINTER(vp)]
+    L.dsmc_mlp_destroy.argtypes = [vp]
+    L.dsmc_mlp_destroy.restype = None
+    L.dsmc_mlp_last_error.argtypes = [vp]
+    L.dsmc_mlp_last_error.restype = C.c_char_p
+    L.dsmc_mlp_set_params.argtypes = [vp, vp, vp]
+    L.dsmc_mlp_get_params.argtypes = [vp, vp, vp]
+    L.dsmc_mlp_set_data.argtypes = [vp, vp, vp, C.c_longlong]
+    L.dsmc_mlp_set_loss.argtypes = [vp, C.c_float]
+    L.dsmc_mlp_train.argtypes = [vp, C.c_int, C.c_int, C.c_float, C.c_ulonglong, vp]
+    L.dsmc_mlp_grad.argtypes = [vp, vp, vp, C.c_int, vp, vp]
+    L.dsmc_mlp_predict.argtypes = [vp, vp, C.c_longlong, vp]
+    L.dsmc_set_learned.argtypes = [vp, vp, C.c_int, C.c_float]
+    L.dsmc_learn_record.argtypes = [vp, C.c_longlong, vp, vp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -211,3 +225,87 @@ class DsmcCloud:
 
     def restore(self, path: str):
         self._chk(lib().dsmc_restore(self.h, path.encode()))
+
+    # learned (sigma_T c_R)max
+    def set_learned(self, model: "Mlp | None", every: int = 1, margin: float = 0.0):
+        """Attach a trained model (None: the plain running maximum)."""
+        self._learned = model   # keep the model alive while attached
+        self._chk(lib().dsmc_set_learned(self.h, model.h if model else None, int(every), float(margin)))
+
+    def learn_record(self, max_rows: int):
+        """(features[n,3], log observed maximum[n]) of the cells that had
+        candidates in the last step."""
+        X = np.empty((max_rows, 3), dtype=np.float32)
+        Y = np.empty(max_rows, dtype=np.float32)
+        n = C.c_longlong()
+        self._chk(lib().dsmc_learn_record(self.h, int(max_rows), _p(X), _p(Y), C.byref(n)))
+        return X[:n.value].copy(), Y[:n.value].copy()
+
+
+NPARAM = 4481
+
+
+class Mlp:
+    """The 3-64-64-1 BF16 perceptron of the learned (sigma_T c_R)max, on the
+    GPU: training, gradients and predictions run in the library's kernels."""
+
+    def __init__(self):
+        L = lib()
+        h = C.c_void_p()
+        rc = L.dsmc_mlp_create(C.byref(h))
+        if rc != 0:
+            raise DsmcError(rc, L.dsmc_mlp_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().dsmc_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def _chk(self, rc):
+        if rc != 0:
+            raise DsmcError(rc, lib().dsmc_mlp_last_error(self.h).decode())
+
+    def set_params(self, params=None, norm=None):
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        q = None if norm is None else np.ascontiguousarray(norm, dtype=np.float32)
+        if p is not None and p.size != NPARAM:
+            raise ValueError(f"expected {NPARAM} parameters")
+        self._chk(lib().dsmc_mlp_set_params(self.h, _p(p), _p(q)))
+
+    def params(self):
+        p = np.empty(NPARAM, dtype=np.float32)
+        q = np.empty(8, dtype=np.float32)
+        self._chk(lib().dsmc_mlp_get_params(self.h, _p(p), _p(q)))
+        return p, q
+
+    def set_loss(self, tau: float = 0.0):
+        """0: mean squared error; tau in (0, 1): pinball loss (tau-quantile)."""
+        self._chk(lib().dsmc_mlp_set_loss(self.h, float(tau)))
+
+    def set_data(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        self._chk(lib().dsmc_mlp_set_data(self.h, _p(X), _p(Y), len(Y)))
+
+    def train(self, steps: int, batch: int, lr: float = 1e-3, seed: int = 1):
+        loss = np.empty(max(steps, 1), dtype=np.float32)
+        self._chk(lib().dsmc_mlp_train(self.h, int(steps), int(batch), float(lr), int(seed), _p(loss)))
+        return loss[:steps]
+
+    def grad(self, X, Y):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.ascontiguousarray(Y, dtype=np.float32)
+        g = np.empty(NPARAM, dtype=np.float32)
+        loss = np.empty(1, dtype=np.float32)
+        self._chk(lib().dsmc_mlp_grad(self.h, _p(X), _p(Y), len(Y), _p(g), _p(loss)))
+        return g, float(loss[0])
+
+    def predict(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        out = np.empty(len(X), dtype=np.float32)
+        self._chk(lib().dsmc_mlp_predict(self.h, _p(X), len(X), _p(out)))
+        return out

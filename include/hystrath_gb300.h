@@ -1,9 +1,9 @@
 /*
  * hystrath_gb300.h -- C ABI of the GB300-native dsmcFoam+ particle hot path.
  *
- * One handle owns one DSMC cloud on one GPU: its structure-of-arrays particle
- * state in HBM, per-cell collision and sampling state, the stream it runs on
- * and its captured step graph.  The entry points replace the calls that the
+ * One handle owns one DSMC cloud on one GPU: its parcel state in HBM (one
+ * 64-byte record per parcel plus a cell word), per-cell collision and sampling
+ * state, the stream it runs on and its captured step graph.  The entry points replace the calls that the
  * dsmcFoam+ driver makes on a dsmcCloud:
  *
  *   reference (path in hystrath/hyStrath)                         this ABI
@@ -284,6 +284,50 @@ void dsmc_destroy(dsmc_handle* h);
  */
 int dsmc_cell_starts_noalloc(const int* d_counts, long long n_cells, int* d_start, void* stream);
 const char* dsmc_noalloc_last_error(void);
+
+/*
+ * Learned (sigma_T c_R)max.  No counterpart in the reference, which keeps only
+ * the running maximum of noTimeCounter (noTimeCounter.C:243-246).  A
+ * 3-64-64-1 SiLU perceptron (BF16 weights and activations, FP32 sums) maps a
+ * cell's (log n, log T_tr, speed ratio) to log (sigma_T c_R)max.  It is
+ * trained on the GPU with Adam on (state, observed maximum) rows recorded
+ * from plain runs; attached to a cloud, it replaces the running maximum in
+ * the candidate count and the acceptance test of each cell until a product
+ * exceeds it, after which the cell uses the running maximum again until the
+ * next prediction.
+ *
+ * Parameter vector (DSMC_MLP_NPARAM floats): W1[64][3], b1[64], W2[64][64]
+ * (row = output), b2[64], w3[64], b3.  norm8: input means (3), input scales
+ * (3), output mean, output scale: the net sees (x - mean) / scale and its
+ * output y maps to ymean + yscale * y.
+ */
+#define DSMC_MLP_NPARAM 4481
+typedef struct dsmc_mlp dsmc_mlp;
+int dsmc_mlp_nparam(void);
+int dsmc_mlp_create(dsmc_mlp** out);
+void dsmc_mlp_destroy(dsmc_mlp* m);
+const char* dsmc_mlp_last_error(const dsmc_mlp* m);
+int dsmc_mlp_set_params(dsmc_mlp* m, const float* params, const float* norm8);
+int dsmc_mlp_get_params(dsmc_mlp* m, float* params, float* norm8);
+/* loss of dsmc_mlp_train and dsmc_mlp_grad: tau 0 (default) the mean squared
+   error, tau in (0, 1) the pinball loss whose minimiser is the tau-quantile */
+int dsmc_mlp_set_loss(dsmc_mlp* m, float tau);
+/* training rows: X[n][3] features, Y[n] log maxima */
+int dsmc_mlp_set_data(dsmc_mlp* m, const float* X, const float* Y, long long n);
+/* steps Adam steps (beta 0.9/0.999) on minibatches of batch rows drawn with
+   replacement from the data by a Philox stream of seed; loss_out[steps] or
+   NULL receives the minibatch mean loss (normalised units) */
+int dsmc_mlp_train(dsmc_mlp* m, int steps, int batch, float lr, unsigned long long seed, float* loss_out);
+/* gradient of the mean loss over rows [0, n) (no update) */
+int dsmc_mlp_grad(dsmc_mlp* m, const float* X, const float* Y, int n, float* grad_out, float* loss_out);
+/* log-maximum predictions for n rows */
+int dsmc_mlp_predict(dsmc_mlp* m, const float* X, long long n, float* out);
+/* attach a model (NULL: plain running maximum); predictions every `every`
+   steps, used as exp(prediction + margin) */
+int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float margin);
+/* after a step: (features, log largest product among the step's candidates)
+   of the cells that had candidates, at most max_rows of them */
+int dsmc_learn_record(dsmc_handle* h, long long max_rows, float* X, float* Y, long long* n_out);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,151 @@
+"""The learned (sigma_T c_R)max: the oracle's gradient formulas against finite
+differences (CPU), the GPU kernels against the oracle (forward, gradient),
+training, and what the trained network gains inside noTimeCounter (GPU)."""
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as MO
+
+
+def _data(n, seed=0):
+    rng = np.random.default_rng(seed)
+    X = np.stack([rng.uniform(40.0, 48.0, n), rng.uniform(5.0, 10.0, n), rng.uniform(0.0, 12.0, n)], 1)
+    # a smooth target in the range of log (sigma_T c_R)max
+    Y = -40.0 + 0.26 * X[:, 1] + 0.05 * np.sin(X[:, 2]) + 0.01 * (X[:, 0] - 44.0) ** 2
+    return X.astype(np.float32), Y.astype(np.float32)
+
+
+def _norm(X, Y):
+    from hystrath_gb300.learn import fit_norm
+    return fit_norm(X, Y)
+
+
+def _params(seed=0):
+    from hystrath_gb300.learn import init_params
+    return init_params(seed)
+
+
+def test_bf16_rounding():
+    v = np.array([1.0, 1.0 + 2 ** -9, 1.0 + 3 * 2 ** -9, -2.5, 3.14159265], dtype=np.float32)
+    r = MO.bf16(v)
+    assert r[0] == 1.0
+    assert r[1] == 1.0                     # halfway: ties to even
+    assert r[2] == np.float32(1.0 + 2 ** -7)
+    assert r[3] == -2.5
+    assert abs(r[4] - 3.140625) < 1e-7
+
+
+def test_oracle_gradient_matches_finite_differences():
+    X, Y = _data(64, 1)
+    nm = _norm(X, Y)
+    p = _params(3).astype(np.float64)
+    loss, g = MO.loss_grad(p, nm, X, Y, exact=True)
+    rng = np.random.default_rng(0)
+    idx = np.concatenate([rng.choice(np.arange(MO.OFF_W1, MO.OFF_B1), 6, replace=False),
+                          rng.choice(np.arange(MO.OFF_W2, MO.OFF_B2), 10, replace=False),
+                          [MO.OFF_B1 + 5, MO.OFF_B2 + 7, MO.OFF_W3 + 9, MO.OFF_B3]])
+    h = 1e-6
+    for i in idx:
+        pp = p.copy(); pp[i] += h
+        pm = p.copy(); pm[i] -= h
+        fd = (MO.loss_grad(pp, nm, X, Y, exact=True)[0] - MO.loss_grad(pm, nm, X, Y, exact=True)[0]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])) + 1e-8, (i, fd, g[i])
+
+
+def test_learn_module_needs_no_gpu_to_import():
+    from hystrath_gb300 import learn
+    p = learn.init_params(0)
+    assert p.shape == (MO.NPARAM,) and np.all(np.abs(p[MO.OFF_W2:MO.OFF_B2]) <= 0.125 + 1e-7)
+
+
+@pytest.mark.gpu
+def test_gpu_forward_matches_oracle():
+    from hystrath_gb300.dsmc import Mlp
+    X, Y = _data(1000, 2)
+    nm = _norm(X, Y)
+    p = _params(1)
+    m = Mlp()
+    m.set_params(p, nm)
+    got = m.predict(X)
+    want = MO.predict(p, nm, X)
+    # same bf16 roundings; FP32 sums in a different order can move a rounding
+    # by one bf16 step
+    assert np.max(np.abs(got - want)) < 2e-2 * nm[7]
+    assert np.mean(np.abs(got - want)) < 2e-3 * nm[7]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [64, 1000, 4099])
+def test_gpu_gradient_matches_oracle(n):
+    from hystrath_gb300.dsmc import Mlp
+    X, Y = _data(n, 5)
+    nm = _norm(X, Y)
+    p = _params(2)
+    m = Mlp()
+    m.set_params(p, nm)
+    g, loss = m.grad(X, Y)
+    lo, go = MO.loss_grad(p, nm, X, Y)
+    assert abs(loss - lo) <= 1e-3 * lo
+    rel = np.linalg.norm(g - go) / np.linalg.norm(go)
+    assert rel < 1e-2, rel
+    # every parameter block carries its own gradient
+    for a, b in ((MO.OFF_W1, MO.OFF_B1), (MO.OFF_B1, MO.OFF_W2), (MO.OFF_W2, MO.OFF_B2),
+                 (MO.OFF_B2, MO.OFF_W3), (MO.OFF_W3, MO.OFF_B3)):
+        assert np.linalg.norm(g[a:b] - go[a:b]) <= 2e-2 * np.linalg.norm(go[a:b]) + 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_training_fits_and_is_reproducible():
+    from hystrath_gb300.dsmc import Mlp
+    from hystrath_gb300.learn import init_params
+    X, Y = _data(200_000, 7)
+    nm = _norm(X, Y)
+    losses = []
+    params = []
+    for _ in range(2):
+        m = Mlp()
+        m.set_params(init_params(0), nm)
+        m.set_data(X, Y)
+        loss = m.train(600, 4096, 1e-3, seed=5)
+        losses.append(loss)
+        params.append(m.params()[0])
+    assert np.mean(losses[0][-50:]) < 0.05 * np.mean(losses[0][:10])
+    assert np.array_equal(params[0], params[1])            # no atomics in the reduction
+    assert np.array_equal(losses[0], losses[1])
+
+
+@pytest.mark.gpu
+def test_learned_selection_draws_fewer_candidates_at_the_same_rate():
+    """A network trained on a plain heat bath's recorded maxima: the learned
+    run of the same heat bath draws fewer candidates per accepted collision and
+    keeps the collision count of the plain run."""
+    from hystrath_gb300 import learn
+    from hystrath_gb300 import spec as S
+    from hystrath_gb300.dsmc import DsmcCloud
+
+    def make(seed):
+        return S.config1(seed=seed, n=24)
+
+    X, Y = learn.collect(make, [0, 1], [5, 20, 40, 80, 160])
+    # the 0.95-quantile of the recorded maxima given the cell state
+    model, loss = learn.train(X, Y, steps=1500, batch=8192, seed=0, tau=0.95)
+    margin = 0.0
+    steps = 300
+
+    def run(learned):
+        g = DsmcCloud(make(9))
+        g.initialise()
+        g.evolve(100)
+        if learned:
+            g.set_learned(model, 10, margin)
+        i0 = g.info()
+        g.evolve(steps)
+        i1 = g.info()
+        g.close()
+        return i1.collisions_total - i0.collisions_total, i1.candidates_total - i0.candidates_total
+
+    cp, kp = run(False)
+    cl, kl = run(True)
+    assert kl / cl < 0.95 * (kp / cp), (kp / cp, kl / cl)
+    # both are Poisson-like counts of about 1e6: 1% is several standard errors
+    assert abs(cl / cp - 1) < 0.01, (cp, cl)
