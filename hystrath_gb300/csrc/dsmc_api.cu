@@ -32,6 +32,7 @@ struct dsmc_handle {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraph_t graphT[2] = {nullptr, nullptr};   // the captured steps (child graphs of a batch)
     unsigned char* solid = nullptr;
     double* info6 = nullptr;
     double* fieldTmp = nullptr;
@@ -344,9 +345,20 @@ int build_graphs(dsmc_handle* h) {
         enqueue_step(h, p, DSMC_PHASE_ALL, nullptr);
         CUDA_TRY(h, cudaStreamEndCapture(h->stream, &g));
         CUDA_TRY(h, cudaGraphInstantiate(&h->graph[p], g, 0));
-        cudaGraphDestroy(g);
+        h->graphT[p] = g;
     }
     return DSMC_OK;
+}
+
+// The step graphs hold the launch shape and the selection mode: drop them
+// when either changes (they are captured again on the next step).
+void drop_graphs(dsmc_handle* h) {
+    for (int p = 0; p < 2; ++p) {
+        if (h->graph[p]) cudaGraphExecDestroy(h->graph[p]);
+        if (h->graphT[p]) cudaGraphDestroy(h->graphT[p]);
+        h->graph[p] = nullptr;
+        h->graphT[p] = nullptr;
+    }
 }
 
 int sort_current(dsmc_handle* h, long long n) {
@@ -532,8 +544,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
 void dsmc_destroy(dsmc_handle* h) {
     if (!h) return;
     if (h->stream) cudaStreamSynchronize(h->stream);
-    for (int p = 0; p < 2; ++p)
-        if (h->graph[p]) cudaGraphExecDestroy(h->graph[p]);
+    drop_graphs(h);
     for (void* q : h->allocs) cudaFree(q);
     if (h->ctrHost) cudaFreeHost(h->ctrHost);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -956,12 +967,7 @@ int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float mar
     h->model = reinterpret_cast<const MlpModel*>(model);
     h->learnEvery = every;
     h->learnMargin = margin;
-    // the step graphs hold the selection mode: capture them again
-    for (int p = 0; p < 2; ++p)
-        if (h->graph[p]) {
-            cudaGraphExecDestroy(h->graph[p]);
-            h->graph[p] = nullptr;
-        }
+    drop_graphs(h);
     // every cell starts on the running maximum until the first prediction
     CUDA_TRY(h, cudaMemset(h->B.pred, 0, sizeof(float) * h->cs.C));
     CUDA_TRY(h, cudaMemset(h->B.useR, 1, h->cs.C));
@@ -993,5 +999,172 @@ int dsmc_learn_record(dsmc_handle* h, long long max_rows, float* X, float* Y, lo
     if (n_out) *n_out = m;
     return DSMC_OK;
 }
+
+// ------------------------------------------------------- launch shape
+int dsmc_set_launch(dsmc_handle* h, int cta_threads, int cells_per_cta) {
+    if (cta_threads != 128 && cta_threads != 256 && cta_threads != 512)
+        return fail(h, DSMC_ERR_INVALID, "cta_threads must be 128, 256 or 512");
+    if (cells_per_cta != 32 && cells_per_cta != 64 && cells_per_cta != 128)
+        return fail(h, DSMC_ERR_INVALID, "cells_per_cta must be 32, 64 or 128");
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->B.cfg.streamThreads = cta_threads;
+    h->B.cfg.streamCtasPerSm = 2048 / cta_threads;
+    h->B.cfg.lightCells = cells_per_cta;
+    drop_graphs(h);
+    return DSMC_OK;
+}
+
+int dsmc_get_launch(dsmc_handle* h, int* cta_threads, int* cells_per_cta) {
+    if (cta_threads) *cta_threads = h->B.cfg.streamThreads;
+    if (cells_per_cta) *cells_per_cta = h->B.cfg.lightCells;
+    return DSMC_OK;
+}
+
+// ------------------------------------------------------- batch of clouds
+struct dsmc_batch {
+    std::vector<dsmc_handle*> cases;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    std::string err;
+};
+
+static thread_local std::string g_batch_err;
+
+static int bfail(dsmc_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    g_batch_err = msg;
+    return code;
+}
+
+static void drop_batch_graphs(dsmc_batch* b) {
+    for (int p = 0; p < 2; ++p) {
+        if (b->graph[p]) cudaGraphExecDestroy(b->graph[p]);
+        b->graph[p] = nullptr;
+    }
+}
+
+// One graph per parity holding every case's captured step as an independent
+// child: a batched step is one launch, and the cases' kernels run side by
+// side as the GPU has room.
+static int build_batch_graphs(dsmc_batch* b) {
+    for (int p = 0; p < 2; ++p) {
+        if (b->graph[p]) continue;
+        for (dsmc_handle* h : b->cases) {
+            int rc = build_graphs(h);
+            if (rc) return bfail(b, rc, std::string("case graph: ") + h->err);
+        }
+        cudaGraph_t pg;
+        cudaError_t e = cudaGraphCreate(&pg, 0);
+        for (size_t i = 0; e == cudaSuccess && i < b->cases.size(); ++i) {
+            cudaGraphNode_t node;
+            e = cudaGraphAddChildGraphNode(&node, pg, nullptr, 0, b->cases[i]->graphT[p]);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph[p], pg, 0);
+        cudaGraphDestroy(pg);
+        if (e != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    }
+    return DSMC_OK;
+}
+
+
+int dsmc_batch_create(int n, const dsmc_case_spec* specs, dsmc_batch** out) {
+    *out = nullptr;
+    if (n < 1) return bfail(nullptr, DSMC_ERR_INVALID, "a batch needs at least one case");
+    auto b = std::make_unique<dsmc_batch>();
+    for (int i = 0; i < n; ++i) {
+        dsmc_handle* h = nullptr;
+        int rc = dsmc_create_from_spec(&specs[i], &h);
+        if (rc) {
+            const std::string m = "case " + std::to_string(i) + ": " + dsmc_last_global_error();
+            for (dsmc_handle* q : b->cases) dsmc_destroy(q);
+            return bfail(nullptr, rc, m);
+        }
+        b->cases.push_back(h);
+    }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        for (dsmc_handle* q : b->cases) dsmc_destroy(q);
+        return bfail(nullptr, DSMC_ERR_CUDA, "cannot create the batch stream");
+    }
+    *out = b.release();
+    return DSMC_OK;
+}
+
+void dsmc_batch_destroy(dsmc_batch* b) {
+    if (!b) return;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_batch_graphs(b);
+    for (dsmc_handle* h : b->cases) dsmc_destroy(h);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+}
+
+const char* dsmc_batch_last_error(const dsmc_batch* b) { return b ? b->err.c_str() : g_batch_err.c_str(); }
+
+int dsmc_batch_size(const dsmc_batch* b) { return (int)b->cases.size(); }
+
+dsmc_handle* dsmc_batch_case(dsmc_batch* b, int i) {
+    if (i < 0 || i >= (int)b->cases.size()) return nullptr;
+    return b->cases[i];
+}
+
+int dsmc_batch_initialise(dsmc_batch* b) {
+    for (size_t i = 0; i < b->cases.size(); ++i) {
+        int rc = dsmc_initialise(b->cases[i]);
+        if (rc) return bfail(b, rc, "case " + std::to_string(i) + ": " + b->cases[i]->err);
+    }
+    drop_batch_graphs(b);
+    return DSMC_OK;
+}
+
+int dsmc_batch_set_launch(dsmc_batch* b, int i, int cta_threads, int cells_per_cta) {
+    if (i < 0 || i >= (int)b->cases.size()) return bfail(b, DSMC_ERR_INVALID, "case index out of range");
+    int rc = dsmc_set_launch(b->cases[i], cta_threads, cells_per_cta);
+    if (rc) return bfail(b, rc, b->cases[i]->err);
+    drop_batch_graphs(b);
+    return DSMC_OK;
+}
+
+int dsmc_batch_evolve_timed(dsmc_batch* b, long long n, double* total_ms) {
+    // the cases are stepped together, so they share the buffer parity
+    const int cur = b->cases[0]->cur;
+    for (dsmc_handle* h : b->cases)
+        if (h->cur != cur) return bfail(b, DSMC_ERR_INVALID, "cases of a batch must be at the same buffer parity");
+    int rc = build_batch_graphs(b);
+    if (rc) return rc;
+    // the cases' own streams may still hold work (initialisation, reads)
+    for (dsmc_handle* h : b->cases)
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, "case stream");
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (total_ms) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, b->stream);
+    }
+    int p = cur;
+    for (long long s = 0; s < n; ++s) {
+        const cudaError_t e = cudaGraphLaunch(b->graph[p], b->stream);
+        if (e != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+        p ^= 1;
+    }
+    if (total_ms) cudaEventRecord(e1, b->stream);
+    const cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (total_ms) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *total_ms = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if (e != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, std::string("batch step: ") + cudaGetErrorString(e));
+    for (size_t i = 0; i < b->cases.size(); ++i) {
+        dsmc_handle* h = b->cases[i];
+        if (n & 1) h->cur ^= 1;
+        rc = check_device_error(h);
+        if (rc) return bfail(b, rc, "case " + std::to_string(i) + ": " + h->err);
+    }
+    return DSMC_OK;
+}
+
+int dsmc_batch_evolve(dsmc_batch* b, long long n) { return dsmc_batch_evolve_timed(b, n, nullptr); }
 
 }  // extern "C"

@@ -357,8 +357,9 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
     tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
                                                                 B.perm, B.subs, learned, B.smaxSel, B.useR,
                                                                 B.obsMax);
-    tile::k_collide_light<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
-                                                                learned, B.smaxSel, B.useR, B.obsMax);
+    const int L = B.cfg.lightCells;
+    tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * sizeof(tile::LightStage), st>>>(
+        cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.obsMax);
 }
 
 void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,

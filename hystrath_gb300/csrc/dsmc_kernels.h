@@ -28,7 +28,17 @@ struct Counters {
     unsigned long long nHeavy;  // of which one warp each (the first nHeavy of the work list)
 };
 
+// Launch shape of one cloud's step, chosen by the autotuner: threads per CTA
+// of the parcel-streaming kernels (move, sample, sort) and their CTAs per
+// SM, and cells per CTA of the one-lane-per-cell collision kernel.
+struct LaunchCfg {
+    int streamThreads = 256;     // 128, 256 or 512
+    int streamCtasPerSm = 8;
+    int lightCells = 128;        // 32, 64 or 128 (one warp per 32 cells)
+};
+
 struct StepBuffers {
+    LaunchCfg cfg;
     Parcels a, b;                 // current / other particle buffers
     int* count;               // [C]
     int* start;               // [C+1]

@@ -22,7 +22,7 @@ namespace dsmc {
 
 namespace {
 
-constexpr int MOVE_THREADS = 256;
+constexpr int MAX_STREAM_THREADS = 512;   // largest CTA of the parcel-streaming kernels
 
 __device__ __forceinline__ double eq_rot(Rng& r, double T, double dof, unsigned* err) {
     if (dof < SMALL) return 0.0;
@@ -357,7 +357,7 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
 // state after the previous step's collisions, which the reference samples at
 // the end of that step) into the per-cell sample sums: it streams the
 // velocities anyway, in cell order.
-__global__ void __launch_bounds__(MOVE_THREADS, 4)
+__global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix) {
     const long long n = ctr->nMoved;
     const int doSample = ctr->pendingSample;
@@ -435,7 +435,7 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
 }
 
 // A pending sample of the current state when no move follows.
-__global__ void __launch_bounds__(MOVE_THREADS)
+__global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_sample_pass(CaseDev cs, Parcels s, Counters* ctr, long long* sfix) {
     if (!ctr->pendingSample) return;
     const long long n = ctr->n;
@@ -497,7 +497,7 @@ __global__ void k_sample_flushed(Counters* ctr, int force) {
 __global__ void k_set_pending(Counters* ctr) { ctr->pendingSample = 1; }
 
 // The boundary path for the parcels k_move deferred, densely packed.
-__global__ void __launch_bounds__(MOVE_THREADS)
+__global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_move_slow(CaseDev cs, Parcels s, Counters* ctr, const int* __restrict__ slowList, const int* __restrict__ bfPatch,
             double* wall, int* count) {
     const long long nSlow = (long long)ctr->nSlow;
@@ -629,7 +629,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
 // runs of neighbouring source cells.  Storing the payload from the source side
 // instead leaves most sectors partly written (parcels that changed cell land
 // in short runs all over the destination).
-__global__ void __launch_bounds__(256) k_scatter_index(const uint32_t* __restrict__ cellw, Counters* ctr,
+__global__ void __launch_bounds__(MAX_STREAM_THREADS) k_scatter_index(const uint32_t* __restrict__ cellw, Counters* ctr,
                                                        const int* __restrict__ start, int* count,
                                                        int2* __restrict__ sortSrc) {
     const long long n = ctr->nMoved;
@@ -666,7 +666,7 @@ __global__ void __launch_bounds__(256) k_scatter_index(const uint32_t* __restric
     }
 }
 
-__global__ void __launch_bounds__(256) k_gather(Parcels src, Parcels dst, Counters* ctr,
+__global__ void __launch_bounds__(MAX_STREAM_THREADS) k_gather(Parcels src, Parcels dst, Counters* ctr,
                                                 const int2* __restrict__ sortSrc) {
     const long long n = ctr->nKept;
     const long long nSrc = ctr->nMoved;
@@ -964,9 +964,10 @@ int grid_for(long long n, int threads, int perSmBlocks) {
 int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TILE) + 1; }
 
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
-    const int grid = grid_for(B.capacity, MOVE_THREADS, 8);
-    k_move<<<grid, MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
-    k_move_slow<<<grid_for(B.capacity, MOVE_THREADS, 2), MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.slowList,
+    const int T = B.cfg.streamThreads;
+    const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
+    k_move<<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
+    k_move_slow<<<grid_for(B.capacity, T, 2), T, 0, st>>>(cs, s, B.ctr, B.slowList,
                                                                                B.bfPatch, B.wall, B.count);
 }
 
@@ -986,9 +987,10 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st) {
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
                     cudaStream_t st) {
     (void)cs;
-    const int grid = grid_for(B.capacity, 256, 8);
-    k_scatter_index<<<grid, 256, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortSrc);
-    k_gather<<<grid, 256, 0, st>>>(src, dst, B.ctr, B.sortSrc);
+    const int T = B.cfg.streamThreads;
+    const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
+    k_scatter_index<<<grid, T, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortSrc);
+    k_gather<<<grid, T, 0, st>>>(src, dst, B.ctr, B.sortSrc);
 }
 
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st) {
@@ -1003,7 +1005,8 @@ void launch_sample_commit(const CaseDev& cs, const StepBuffers& B, int force, cu
 }
 
 void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int force, cudaStream_t st) {
-    k_sample_pass<<<grid_for(B.capacity, MOVE_THREADS, 8), MOVE_THREADS, 0, st>>>(cs, s, B.ctr, B.sfix);
+    const int T = B.cfg.streamThreads;
+    k_sample_pass<<<grid_for(B.capacity, T, B.cfg.streamCtasPerSm), T, 0, st>>>(cs, s, B.ctr, B.sfix);
     launch_sample_commit(cs, B, force, st);
 }
 

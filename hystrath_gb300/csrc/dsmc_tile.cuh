@@ -487,13 +487,15 @@ __device__ __forceinline__ int hash_pick(const LightStage& st, int lane, int n, 
     return arg;
 }
 
-// one lane per light cell, its candidates one after the other
-__global__ void __launch_bounds__(WARPS * 32, 4)
+// one lane per light cell, its candidates one after the other; blockDim.x
+// (the cells per CTA) is 32, 64 or 128, with one LightStage per warp in
+// dynamic shared memory
+__global__ void __launch_bounds__(128, 4)
 k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, int learned, const double* __restrict__ smaxSel, unsigned char* useR,
                 float* obsMax) {
-    __shared__ LightStage stage[WARPS];
-    LightStage& st = stage[threadIdx.x >> 5];
+    extern __shared__ __align__(16) unsigned char lightSmem[];
+    LightStage& st = reinterpret_cast<LightStage*>(lightSmem)[threadIdx.x >> 5];
     const int lane = (int)(threadIdx.x & 31u);
     const uint32_t step = (uint32_t)ctr->step;
     const long long nWork = (long long)ctr->nWork;

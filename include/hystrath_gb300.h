@@ -329,6 +329,37 @@ int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float mar
    of the cells that had candidates, at most max_rows of them */
 int dsmc_learn_record(dsmc_handle* h, long long max_rows, float* X, float* Y, long long* n_out);
 
+/*
+ * Launch shape of a cloud's step (no counterpart in the reference, which runs
+ * on CPU threads): threads per CTA of the parcel-streaming kernels (move,
+ * sample, sort; 128, 256 or 512) and cells per CTA of the one-lane-per-cell
+ * collision kernel (32, 64 or 128).  Chosen by the autotuner of
+ * hystrath_gb300/batch.py.
+ */
+int dsmc_set_launch(dsmc_handle* h, int cta_threads, int cells_per_cta);
+int dsmc_get_launch(dsmc_handle* h, int* cta_threads, int* cells_per_cta);
+
+/*
+ * A batch of independent clouds stepped together (no counterpart in the
+ * reference, which runs one case per process).  Every batched step is ONE
+ * launch of a CUDA graph that holds each case's captured step as an
+ * independent child graph.  The cases are created and initialised as by
+ * dsmc_create_from_spec / dsmc_initialise; dsmc_batch_case gives each case's
+ * handle for reads (dsmc_info, dsmc_get_field, ...), which must not step it
+ * on its own.  Errors: dsmc_batch_last_error.
+ */
+typedef struct dsmc_batch dsmc_batch;
+int dsmc_batch_create(int n, const dsmc_case_spec* specs, dsmc_batch** out);
+void dsmc_batch_destroy(dsmc_batch* b);
+const char* dsmc_batch_last_error(const dsmc_batch* b);
+int dsmc_batch_size(const dsmc_batch* b);
+dsmc_handle* dsmc_batch_case(dsmc_batch* b, int i);
+int dsmc_batch_initialise(dsmc_batch* b);
+int dsmc_batch_set_launch(dsmc_batch* b, int i, int cta_threads, int cells_per_cta);
+int dsmc_batch_evolve(dsmc_batch* b, long long n_steps);
+/* the same, with the device time of the n steps in *total_ms */
+int dsmc_batch_evolve_timed(dsmc_batch* b, long long n_steps, double* total_ms);
+
 #ifdef __cplusplus
 }
 #endif

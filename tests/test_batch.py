@@ -1,0 +1,92 @@
+"""Batched clouds and launch shapes: a batched step gives every case exactly
+the state it reaches when stepped alone, and no launch shape changes a
+result (the step is deterministic).  The workload generator draws the
+batched heat-bath distribution."""
+import math
+
+import numpy as np
+import pytest
+
+from hystrath_gb300 import spec as S
+
+
+def test_workload_generator_draws_the_batched_distribution():
+    from hystrath_gb300.batch import heat_bath_cases, mean_collision_time, size_classes
+    specs, meta = heat_bath_cases(0, 256)
+    edges = np.array([m["edge"] for m in meta])
+    ppc = np.array([m["ppc"] for m in meta])
+    T = np.array([m["T"] for m in meta])
+    assert edges.min() >= 8 and edges.max() <= 48
+    assert ppc.min() >= 5 and ppc.max() <= 60
+    assert T.min() >= 500 and T.max() <= 20000
+    assert 0.35 < np.mean([m["species"] == "N2" for m in meta]) < 0.65
+    for s, m in zip(specs, meta):
+        sp = S.N2 if m["species"] == "N2" else S.AR
+        assert math.isclose(s.delta_t, 0.2 * mean_collision_time(sp, m["T"], 1e20), rel_tol=1e-12)
+        assert all(s.patches[s.side_patch[q]].type == S.PATCH_CYCLIC for q in range(6))
+    assert sum(len(c) for c in size_classes(specs)) == 256
+
+
+def _state(g):
+    st = g.particles()
+    order = np.argsort(st["id"])
+    return {k: v[order] for k, v in st.items() if k != "cell"}
+
+
+@pytest.mark.gpu
+def test_batched_steps_equal_steps_alone():
+    from hystrath_gb300.batch import BatchCloud, heat_bath_cases
+    from hystrath_gb300.dsmc import DsmcCloud
+    specs, _ = heat_bath_cases(3, 256)
+    small = [s for s in specs if s.n_cells[0] <= 12][:4]
+    assert len(small) >= 2
+    b = BatchCloud(small)
+    b.initialise()
+    b.evolve(7)
+    for i, s in enumerate(small):
+        g = DsmcCloud(s)
+        g.initialise()
+        g.evolve(7)
+        ib, ig = b.info(i), g.info()
+        assert ib.collisions_total == ig.collisions_total
+        assert ib.n_particles == ig.n_particles
+        sb = _state_of_case(b, i)
+        sg = _state(g)
+        for k in sb:
+            assert np.array_equal(sb[k], sg[k]), k
+        g.close()
+    b.close()
+
+
+def _state_of_case(b, i):
+    import ctypes as C
+    from hystrath_gb300.dsmc import DsmcCloud, lib
+    view = DsmcCloud.__new__(DsmcCloud)
+    view.h = C.c_void_p(lib().dsmc_batch_case(b.h, i))
+    view.spec = b.specs[i]
+    s = view.spec
+    view.n_cells = s.n_cells[0] * s.n_cells[1] * s.n_cells[2]
+    try:
+        return _state(view)
+    finally:
+        view.h = None       # owned by the batch
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(128, 32), (512, 64)])
+def test_launch_shape_does_not_change_results(shape):
+    from hystrath_gb300.batch import _bind
+    from hystrath_gb300.dsmc import DsmcCloud
+    s = S.config1(seed=4, n=16)
+    ref = DsmcCloud(s)
+    ref.initialise()
+    ref.evolve(6)
+    g = DsmcCloud(s)
+    g.initialise()
+    assert _bind().dsmc_set_launch(g.h, *shape) == 0
+    g.evolve(6)
+    assert g.info().collisions_total == ref.info().collisions_total
+    a, b = _state(ref), _state(g)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    np.testing.assert_array_equal(ref.field("Ttra"), g.field("Ttra"))
