@@ -81,6 +81,7 @@ struct CaseDev {
     double lo[3], hi[3], dx[3], inv[3], negOinv[3];
     double V;
     double FN, dt;
+    double invDtFa[3];   // 1 / (dt * area of a face normal to each axis)
     uint32_t seedLo, seedHi;
     int nSpecies;
     int collModel;

@@ -48,6 +48,7 @@ __device__ void wall_measure(const CaseDev& cs, double* wall, long long bf, int 
     const int ax1 = (axis == 0) ? 1 : 0;
     const int ax2 = (axis == 2) ? 1 : 2;
     const double fA = cs.dx[ax1] * cs.dx[ax2];
+    const double invDtFa = cs.invDtFa[axis];      // 1 / (dt fA), one division per case
     const double Un = U[axis] * sgn;
     double Ut[3] = {U[0], U[1], U[2]};
     Ut[axis] = U[axis] - Un * sgn;
@@ -71,10 +72,10 @@ __device__ void wall_measure(const CaseDev& cs, double* wall, long long bf, int 
         *preE = E;
         for (int a = 0; a < 3; ++a) preMom[a] = s.m * U[a];
     } else {
-        atomicAdd(W + W_Q, cs.FN * (*preE - E) / (cs.dt * fA));
-        atomicAdd(W + W_FDX, cs.FN * (preMom[0] - s.m * U[0]) / (cs.dt * fA));
-        atomicAdd(W + W_FDY, cs.FN * (preMom[1] - s.m * U[1]) / (cs.dt * fA));
-        atomicAdd(W + W_FDZ, cs.FN * (preMom[2] - s.m * U[2]) / (cs.dt * fA));
+        atomicAdd(W + W_Q, cs.FN * (*preE - E) * invDtFa);
+        atomicAdd(W + W_FDX, cs.FN * (preMom[0] - s.m * U[0]) * invDtFa);
+        atomicAdd(W + W_FDY, cs.FN * (preMom[1] - s.m * U[1]) * invDtFa);
+        atomicAdd(W + W_FDZ, cs.FN * (preMom[2] - s.m * U[2]) * invDtFa);
     }
 }
 
