@@ -37,6 +37,7 @@
 
 namespace dsmc {
 void set_global_error(const std::string& msg);   // dsmc_api.cu
+bool foam_cell_order(const std::string& dir, std::vector<long long>& order, std::string& err);
 }
 
 namespace {
@@ -567,10 +568,13 @@ void readCase(const std::string& dir, dsmc_case_spec* s) {
     const std::string bcm = word(dp.get(), "BinaryCollisionModel", dpPath);
     if (bcm == "VariableHardSphere") s->binary_collision_model = DSMC_COLL_VHS;
     else if (bcm == "LarsenBorgnakkeVariableHardSphere") s->binary_collision_model = DSMC_COLL_LB_VHS;
+    else if (bcm == "VariableSoftSphere") s->binary_collision_model = DSMC_COLL_VSS;
+    else if (bcm == "LarsenBorgnakkeVariableSoftSphere") s->binary_collision_model = DSMC_COLL_LB_VSS;
     else
         throw ParseError(DSMC_ERR_UNKNOWN_MODEL, "Unknown BinaryCollisionModel type " + bcm +
-                                                     ". Valid BinaryCollisionModel types are: 2(VariableHardSphere "
-                                                     "LarsenBorgnakkeVariableHardSphere)");
+                                                     ". Valid BinaryCollisionModel types are: 4(VariableHardSphere "
+                                                     "LarsenBorgnakkeVariableHardSphere VariableSoftSphere "
+                                                     "LarsenBorgnakkeVariableSoftSphere)");
     if (const Node* co = dp->find(bcm + "Coeffs")) {
         s->tref = scalarOr(co, "Tref", 273.0);
         s->zrot = scalarOr(co, "rotationalRelaxationCollisionNumber", 5.0);
@@ -726,6 +730,50 @@ void readCase(const std::string& dir, dsmc_case_spec* s) {
 }
 
 }  // namespace
+
+// OpenFOAM's cell order of the case's blockMesh (block by block in the
+// blocks list, i fastest within a block) as Cartesian indices
+// i + nx (j + ny k) of the merged uniform grid.
+bool dsmc::foam_cell_order(const std::string& dir, std::vector<long long>& order, std::string& err) {
+    try {
+        dsmc_case_spec s{};
+        std::map<std::string, int> patchIds;
+        std::vector<std::string> patchTypes;
+        readMesh(dir, &s, patchIds, patchTypes);
+        const std::string path = fileIn(dir, "system/blockMeshDict", "constant/polyMesh/blockMeshDict");
+        auto bm = readDict(path);
+        const double scale = scalarOr(bm.get(), "convertToMeters", scalarOr(bm.get(), "scale", 1.0));
+        const Node& vn = need(bm.get(), "vertices", path);
+        std::vector<std::array<double, 3>> V;
+        for (auto& it : vn.items) {
+            auto c = numList(*it, "vertex");
+            V.push_back({c[0] * scale, c[1] * scale, c[2] * scale});
+        }
+        const Node& bn = need(bm.get(), "blocks", path);
+        order.clear();
+        for (size_t i = 0; i < bn.items.size(); ++i) {
+            const Node& it = *bn.items[i];
+            if (!(it.kind == Node::VALUE && !it.words.empty() && it.words[0] == "hex")) continue;
+            auto ids = numList(*bn.items[i + 1], "hex vertices");
+            auto cnt = numList(*bn.items[i + 2], "hex cell counts");
+            double lo[3] = {1e300, 1e300, 1e300};
+            for (double id : ids)
+                for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], V.at((size_t)id)[a]);
+            int o[3];
+            for (int a = 0; a < 3; ++a) o[a] = (int)std::lround((lo[a] - s.origin[a]) / s.cell_size[a]);
+            for (int k = 0; k < (int)cnt[2]; ++k)
+                for (int j = 0; j < (int)cnt[1]; ++j)
+                    for (int ii = 0; ii < (int)cnt[0]; ++ii)
+                        order.push_back((o[0] + ii) +
+                                        (long long)s.n_cells[0] * ((o[1] + j) + (long long)s.n_cells[1] * (o[2] + k)));
+            i += 2;
+        }
+        return true;
+    } catch (const std::exception& e) {
+        err = e.what();
+        return false;
+    }
+}
 
 extern "C" int dsmc_parse_case(const char* case_dir, dsmc_case_spec* spec) {
     try {

@@ -17,7 +17,13 @@
 #include <string>
 #include <vector>
 
+#include <sys/stat.h>
+
 #include "dsmc_kernels.h"
+
+namespace dsmc {
+bool foam_cell_order(const std::string& dir, std::vector<long long>& order, std::string& err);   // case_parser.cpp
+}
 
 using namespace dsmc;
 
@@ -105,10 +111,16 @@ int validate(dsmc_handle* h, const dsmc_case_spec& s) {
             return fail(h, DSMC_ERR_INVALID, std::string("species ") + q.name +
                                                  ": nVibrationalModes > 1 is not supported on this path");
     }
-    if (s.binary_collision_model != DSMC_COLL_VHS && s.binary_collision_model != DSMC_COLL_LB_VHS)
+    if (s.binary_collision_model < DSMC_COLL_VHS || s.binary_collision_model > DSMC_COLL_LB_VSS)
         return fail(h, DSMC_ERR_UNKNOWN_MODEL,
                     "Unknown BinaryCollisionModel type. Valid BinaryCollisionModel types are: "
-                    "2(VariableHardSphere LarsenBorgnakkeVariableHardSphere)");
+                    "4(VariableHardSphere LarsenBorgnakkeVariableHardSphere VariableSoftSphere "
+                    "LarsenBorgnakkeVariableSoftSphere)");
+    if (s.binary_collision_model == DSMC_COLL_VSS || s.binary_collision_model == DSMC_COLL_LB_VSS)
+        for (int i = 0; i < s.n_species; ++i)
+            if (!(s.species[i].alpha > 0))
+                return fail(h, DSMC_ERR_INVALID, std::string("species ") + s.species[i].name +
+                                                     ": VariableSoftSphere needs alpha > 0");
     if (s.partner_selection_model != DSMC_SEL_NTC)
         return fail(h, DSMC_ERR_UNKNOWN_MODEL,
                     "Unknown collisionPartnerSelectionModel type. Valid types are: 1(noTimeCounter)");
@@ -240,6 +252,7 @@ void fill_case_dev(dsmc_handle* h) {
                                std::exp(std::lgamma(2.5 - om));
             p.mPfrac = a.mass / (a.mass + b.mass);
             p.mQfrac = b.mass / (a.mass + b.mass);
+            p.invAlphaPQ = 1.0 / (0.5 * (a.alpha + b.alpha));
             p.sigmaPrefactorF = (float)p.sigmaPrefactor;
             p.expoF = (float)p.expo;
         }
@@ -1168,5 +1181,103 @@ int dsmc_batch_evolve_timed(dsmc_batch* b, long long n, double* total_ms) {
 }
 
 int dsmc_batch_evolve(dsmc_batch* b, long long n) { return dsmc_batch_evolve_timed(b, n, nullptr); }
+
+// ------------------------------------------------------- OpenFOAM output
+// volScalarField / volVectorField files as dsmcVolFields::writeField writes
+// them (dsmcVolFields.C:1878-2380): ASCII, nonuniform internal field in
+// OpenFOAM's cell order, constraint types on constraint patches.
+namespace {
+
+const char* FOAM_BANNER =
+    "/*--------------------------------*- C++ -*----------------------------------*\\\n"
+    "  written by libhystrath_gb300 (GB300 dsmcFoam+ particle step)\n"
+    "\\*---------------------------------------------------------------------------*/\n";
+
+void foam_write(const std::string& path, const std::string& cls, const std::string& object,
+                const std::string& location, const char* dims, const std::vector<const double*>& comps,
+                const std::vector<long long>& order, const dsmc_case_spec& spec, bool* ok) {
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) { *ok = false; return; }
+    const bool vec = comps.size() == 3;
+    std::fprintf(f, "%sFoamFile\n{\n    version     2.0;\n    format      ascii;\n    class       %s;\n"
+                    "    location    \"%s\";\n    object      %s;\n}\n\ndimensions      %s;\n\n"
+                    "internalField   nonuniform List<%s> \n%lld\n(\n",
+                 FOAM_BANNER, cls.c_str(), location.c_str(), object.c_str(), dims, vec ? "vector" : "scalar",
+                 (long long)order.size());
+    for (long long c : order) {
+        if (vec) std::fprintf(f, "(%.10g %.10g %.10g)\n", comps[0][c], comps[1][c], comps[2][c]);
+        else std::fprintf(f, "%.10g\n", comps[0][c]);
+    }
+    std::fprintf(f, ")\n;\n\nboundaryField\n{\n");
+    for (int p = 0; p < spec.n_patches; ++p) {
+        const dsmc_patch& pt = spec.patches[p];
+        std::fprintf(f, "    %s\n    {\n", pt.name);
+        if (pt.type == DSMC_PATCH_CYCLIC) std::fprintf(f, "        type            cyclic;\n");
+        else if (pt.type == DSMC_PATCH_SYMMETRY) std::fprintf(f, "        type            symmetryPlane;\n");
+        else std::fprintf(f, "        type            calculated;\n        value           uniform %s;\n",
+                          vec ? "(0 0 0)" : "0");
+        std::fprintf(f, "    }\n");
+    }
+    std::fprintf(f, "}\n");
+    if (std::fclose(f) != 0) *ok = false;
+}
+
+}  // namespace
+
+int dsmc_write_fields(dsmc_handle* h, const char* case_dir, const char* time_name, const char* field_name) {
+    const long long C = h->cs.C;
+    std::vector<long long> order;
+    std::string err;
+    std::string bm = std::string(case_dir) + "/system/blockMeshDict";
+    std::ifstream probe(bm);
+    if (!probe) probe.open(std::string(case_dir) + "/constant/polyMesh/blockMeshDict");
+    if (probe) {
+        if (!foam_cell_order(case_dir, order, err)) return fail(h, DSMC_ERR_PARSE, "cell order: " + err);
+        for (long long c : order)
+            if (c < 0 || c >= C) return fail(h, DSMC_ERR_INVALID, "the case's blockMeshDict does not match this cloud");
+    } else {
+        for (long long c = 0; c < C; ++c)
+            order.push_back(c);
+    }
+    const std::string dir = std::string(case_dir) + "/" + time_name;
+    mkdir(dir.c_str(), 0755);
+    struct FieldOut {
+        const char* name;   // dsmc_get_field name(s)
+        const char* file;   // file prefix
+        const char* dims;
+        bool vec;
+    };
+    const FieldOut fields[] = {
+        {"rhoN", "rhoN", "[0 -3 0 0 0 0 0]", false}, {"rhoM", "rhoM", "[1 -3 0 0 0 0 0]", false},
+        {"Ttra", "Ttra", "[0 0 0 1 0 0 0]", false},  {"Trot", "Trot", "[0 0 0 1 0 0 0]", false},
+        {"Tvib", "Tvib", "[0 0 0 1 0 0 0]", false},  {"Tov", "Tov", "[0 0 0 1 0 0 0]", false},
+        {"p", "p", "[1 -1 -2 0 0 0 0]", false},       {"dsmcNMean", "dsmcNMean", "[0 0 0 0 0 0 0]", false},
+        {"U", "U", "[0 1 -1 0 0 0 0]", true},
+    };
+    std::vector<double> a(C), b(C), c(C);
+    bool ok = true;
+    const std::string suffix = (field_name && *field_name) ? std::string("_") + field_name : std::string();
+    for (const FieldOut& fo : fields) {
+        int rc;
+        std::vector<const double*> comps;
+        if (fo.vec) {
+            if ((rc = dsmc_get_field(h, "Ux", a.data(), C)) || (rc = dsmc_get_field(h, "Uy", b.data(), C)) ||
+                (rc = dsmc_get_field(h, "Uz", c.data(), C)))
+                return rc;
+            comps = {a.data(), b.data(), c.data()};
+        } else {
+            if ((rc = dsmc_get_field(h, fo.name, a.data(), C))) return rc;
+            comps = {a.data()};
+        }
+        foam_write(dir + "/" + fo.file + suffix, fo.vec ? "volVectorField" : "volScalarField", fo.file + suffix,
+                   time_name, fo.dims, comps, order, h->spec, &ok);
+    }
+    int rc = dsmc_get_cell_array(h, "sigmaTcRMax", a.data(), C);
+    if (rc) return rc;
+    foam_write(dir + "/dsmcSigmaTcRMax", "volScalarField", "dsmcSigmaTcRMax", time_name, "[0 3 -1 0 0 0 0]",
+               {a.data()}, order, h->spec, &ok);
+    if (!ok) return fail(h, DSMC_ERR_IO, "cannot write fields under " + dir);
+    return DSMC_OK;
+}
 
 }  // extern "C"

@@ -64,6 +64,7 @@ struct PairDev {
     double mR;
     double mPfrac;          // mP / (mP + mQ)
     double mQfrac;          // mQ / (mP + mQ)
+    double invAlphaPQ;      // 1 / alphaPQ, alphaPQ = (alphaP + alphaQ) / 2 (VariableSoftSphere)
 };
 
 struct PatchDev {

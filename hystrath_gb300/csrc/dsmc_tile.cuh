@@ -282,7 +282,7 @@ struct Post {
 __device__ __forceinline__ void collide_pair(const CaseDev& cs, Rng& r, const PairDev& pr, int tP, int tQ,
                                              double cr2, Post& o, unsigned* err) {
     double cR;
-    if (cs.collModel == DSMC_COLL_LB_VHS) {
+    if (cs.collModel == DSMC_COLL_LB_VHS || cs.collModel == DSMC_COLL_LB_VSS) {
         double Et = 0.5 * pr.mR * cr2;
         redistribute(cs, cs.sp[tP], &o.eP, &o.vP, Et, pr.omegaPQ, r, zv_row(cs, tP, tQ), err);
         redistribute(cs, cs.sp[tQ], &o.eQ, &o.vQ, Et, pr.omegaPQ, r, zv_row(cs, tQ, tP), err);
@@ -292,12 +292,41 @@ __device__ __forceinline__ void collide_pair(const CaseDev& cs, Rng& r, const Pa
     }
     double Ucm[3];
     for (int a = 0; a < 3; ++a) Ucm[a] = pr.mPfrac * o.UP[a] + pr.mQfrac * o.UQ[a];
-    const double cosT = 2.0 * r.u01() - 1.0;
-    const double sinT = sqrt(1.0 - cosT * cosT);
-    const double phi = 2.0 * PI * r.u01();
-    double sph, cph;
-    sincos(phi, &sph, &cph);
-    const double prel[3] = {cR * cosT, cR * sinT * cph, cR * sinT * sph};
+    double prel[3];
+    if (cs.collModel == DSMC_COLL_VSS || cs.collModel == DSMC_COLL_LB_VSS) {
+        // VariableSoftSphere::postCollisionVelocities (VariableSoftSphere.C:191-233):
+        // deflection cos(chi) = 2 U^(1/alpha) - 1 about the pre-collision
+        // relative velocity, Bird eq. 2.22.  Its components are first scaled
+        // to the post-exchange speed cR (equal for plain VSS), so the
+        // Larsen-Borgnakke variant keeps the energy it computed.
+        const double cosT = 2.0 * pow(r.u01(), pr.invAlphaPQ) - 1.0;
+        const double sinT = sqrt(1.0 - cosT * cosT);
+        const double phi = 2.0 * PI * r.u01();
+        double sph, cph;
+        sincos(phi, &sph, &cph);
+        const double cpre = sqrt(cr2);
+        const double k = cpre > 0.0 ? cR / cpre : 0.0;
+        const double c0 = k * (o.UP[0] - o.UQ[0]), c1 = k * (o.UP[1] - o.UQ[1]), c2 = k * (o.UP[2] - o.UQ[2]);
+        const double D = sqrt(c1 * c1 + c2 * c2);
+        if (D > 1e-12 * cR) {
+            prel[0] = cosT * c0 + sinT * sph * D;
+            prel[1] = cosT * c1 + sinT * (cR * c2 * cph - c0 * c1 * sph) / D;
+            prel[2] = cosT * c2 - sinT * (cR * c1 * cph + c0 * c2 * sph) / D;
+        } else {   // relative velocity along x
+            prel[0] = cosT * c0;
+            prel[1] = cR * sinT * cph;
+            prel[2] = cR * sinT * sph;
+        }
+    } else {
+        const double cosT = 2.0 * r.u01() - 1.0;
+        const double sinT = sqrt(1.0 - cosT * cosT);
+        const double phi = 2.0 * PI * r.u01();
+        double sph, cph;
+        sincos(phi, &sph, &cph);
+        prel[0] = cR * cosT;
+        prel[1] = cR * sinT * cph;
+        prel[2] = cR * sinT * sph;
+    }
     for (int a = 0; a < 3; ++a) {
         o.UP[a] = Ucm[a] + prel[a] * pr.mQfrac;
         o.UQ[a] = Ucm[a] - prel[a] * pr.mPfrac;

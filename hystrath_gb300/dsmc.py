@@ -47,6 +47,7 @@ def _load() -> C.CDLL:
     L.dsmc_n_boundary_faces.argtypes = [vp]
     L.dsmc_n_boundary_faces.restype = C.c_longlong
     L.dsmc_reset_sampling.argtypes = [vp]
+    L.dsmc_write_fields.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p]
     L.dsmc_info.argtypes = [vp, C.POINTER(S.Info)]
     L.dsmc_checkpoint.argtypes = [vp, C.c_char_p]
     L.dsmc_restore.argtypes = [vp, C.c_char_p]
@@ -214,6 +215,10 @@ class DsmcCloud:
 
     def reset_sampling(self):
         self._chk(lib().dsmc_reset_sampling(self.h))
+
+    def write_fields(self, case_dir: str, time_name: str, field_name: str = ""):
+        """The averaged fields as OpenFOAM files in case_dir/time_name."""
+        self._chk(lib().dsmc_write_fields(self.h, case_dir.encode(), time_name.encode(), field_name.encode()))
 
     def info(self) -> S.Info:
         i = S.Info()

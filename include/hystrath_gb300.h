@@ -73,7 +73,9 @@ enum {
 /* BinaryCollisionModel and collisionPartnerSelectionModel selections. */
 enum {
     DSMC_COLL_VHS = 0,     /* VariableHardSphere */
-    DSMC_COLL_LB_VHS = 1   /* LarsenBorgnakkeVariableHardSphere */
+    DSMC_COLL_LB_VHS = 1,  /* LarsenBorgnakkeVariableHardSphere */
+    DSMC_COLL_VSS = 2,     /* VariableSoftSphere */
+    DSMC_COLL_LB_VSS = 3   /* LarsenBorgnakkeVariableSoftSphere */
 };
 enum { DSMC_SEL_NTC = 0 }; /* noTimeCounter */
 
@@ -251,6 +253,14 @@ long long dsmc_n_boundary_faces(const dsmc_handle* h);
 
 /* Restart the time averages (dsmcField resetAtOutput). */
 int dsmc_reset_sampling(dsmc_handle* h);
+
+/* dsmcVolFields::writeField (dsmcVolFields.C:1878-2380): the averaged fields
+ * as OpenFOAM ASCII files in case_dir/time_name/ -- rhoN, rhoM, Ttra, Trot,
+ * Tvib, Tov, p, dsmcNMean and U (each with the suffix "_" field_name, as the
+ * fieldName of fieldPropertiesDict) and dsmcSigmaTcRMax.  Cells are written
+ * in the order of the case's blockMeshDict when case_dir has one (block by
+ * block, i fastest), else in the Cartesian order i + nx (j + ny k). */
+int dsmc_write_fields(dsmc_handle* h, const char* case_dir, const char* time_name, const char* field_name);
 
 int dsmc_info(dsmc_handle* h, dsmc_info_t* out);
 

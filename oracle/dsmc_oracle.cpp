@@ -173,6 +173,7 @@ struct Parcel {
 struct Species {
     double m, d, omega, rotDof, thetaV, thetaD, zref, trefZv;
     int nVib;
+    double alpha;   // VariableSoftSphere deflection exponent
 };
 
 struct WallAcc {   // per boundary face, dsmcPatchBoundary.C:263-482
@@ -287,7 +288,7 @@ struct Oracle {
         for (int i = 0; i < s->n_species; ++i) {
             const dsmc_species& q = s->species[i];
             sp[i] = Species{q.mass, q.diameter, q.omega, q.rotational_dof, q.theta_v, q.theta_d,
-                            q.zref, q.tref_zv, q.n_vib_modes};
+                            q.zref, q.tref_zv, q.n_vib_modes, q.alpha};
         }
         solid.assign(C, 0);
         for (int o = 0; o < s->n_obstacles; ++o) {
@@ -814,14 +815,45 @@ struct Oracle {
     }
 
     // VariableHardSphere::postCollisionVelocities
+    // VariableHardSphere::postCollisionVelocities (VariableHardSphere.C:191-228),
+    // or for the soft-sphere models VariableSoftSphere::postCollisionVelocities
+    // (VariableSoftSphere.C:191-233, Bird eq. 2.22) with the pre-collision
+    // relative velocity scaled to the post-exchange speed cR.
     void scatter(Parcel& p, Parcel& q, double cR, Rng& r) {
         const double mP = sp[p.type].m, mQ = sp[q.type].m;
         double Ucm[3];
         for (int a = 0; a < 3; ++a) Ucm[a] = (mP * p.U[a] + mQ * q.U[a]) / (mP + mQ);
-        const double cosT = 2.0 * r.u01() - 1.0;
-        const double sinT = std::sqrt(1.0 - cosT * cosT);
-        const double phi = 2.0 * PI * r.u01();
-        const double pr[3] = {cR * cosT, cR * sinT * std::cos(phi), cR * sinT * std::sin(phi)};
+        double pr[3];
+        const int cm = spec.binary_collision_model;
+        if (cm == DSMC_COLL_VSS || cm == DSMC_COLL_LB_VSS) {
+            const double alpha = 0.5 * (sp[p.type].alpha + sp[q.type].alpha);
+            const double cosT = 2.0 * std::pow(r.u01(), 1.0 / alpha) - 1.0;
+            const double sinT = std::sqrt(1.0 - cosT * cosT);
+            const double phi = 2.0 * PI * r.u01();
+            double c[3], cpre2 = 0;
+            for (int a = 0; a < 3; ++a) { c[a] = p.U[a] - q.U[a]; cpre2 += c[a] * c[a]; }
+            const double cpre = std::sqrt(cpre2);
+            const double k = cpre > 0.0 ? cR / cpre : 0.0;
+            for (int a = 0; a < 3; ++a) c[a] *= k;
+            const double D = std::sqrt(c[1] * c[1] + c[2] * c[2]);
+            const double sph = std::sin(phi), cph = std::cos(phi);
+            if (D > 1e-12 * cR) {
+                pr[0] = cosT * c[0] + sinT * sph * D;
+                pr[1] = cosT * c[1] + sinT * (cR * c[2] * cph - c[0] * c[1] * sph) / D;
+                pr[2] = cosT * c[2] - sinT * (cR * c[1] * cph + c[0] * c[2] * sph) / D;
+            } else {
+                pr[0] = cosT * c[0];
+                pr[1] = cR * sinT * cph;
+                pr[2] = cR * sinT * sph;
+            }
+        } else {
+            const double cosT = 2.0 * r.u01() - 1.0;
+            const double sinT = std::sqrt(1.0 - cosT * cosT);
+            const double phi = 2.0 * PI * r.u01();
+            pr[0] = cR * cosT;
+            pr[1] = cR * sinT * std::cos(phi);
+            pr[2] = cR * sinT * std::sin(phi);
+        }
         for (int a = 0; a < 3; ++a) {
             p.U[a] = Ucm[a] + pr[a] * mQ / (mP + mQ);
             q.U[a] = Ucm[a] - pr[a] * mP / (mP + mQ);
@@ -863,7 +895,8 @@ struct Oracle {
                 const Species& a = sp[p.type];
                 const Species& b = sp[q.type];
                 double cR;
-                if (spec.binary_collision_model == DSMC_COLL_LB_VHS) {
+                if (spec.binary_collision_model == DSMC_COLL_LB_VHS ||
+                    spec.binary_collision_model == DSMC_COLL_LB_VSS) {
                     const double mR = a.m * b.m / (a.m + b.m);
                     double cr2 = 0;
                     for (int d = 0; d < 3; ++d) cr2 += (p.U[d] - q.U[d]) * (p.U[d] - q.U[d]);

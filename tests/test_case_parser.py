@@ -95,9 +95,18 @@ def _expect(tmp_case, code, needle):
 
 def test_unknown_binary_collision_model(gpu_lib, tmp_path):
     d = _copy_case(tmp_path)
-    _edit(d / "constant/dsmcProperties", "VariableHardSphere;", "VariableSoftSphere;")
-    _expect(d, S.ERR_UNKNOWN_MODEL, "Valid BinaryCollisionModel types are: 2(VariableHardSphere "
-                                    "LarsenBorgnakkeVariableHardSphere)")
+    _edit(d / "constant/dsmcProperties", "VariableHardSphere;", "GeneralisedHardSphere;")
+    _expect(d, S.ERR_UNKNOWN_MODEL, "Valid BinaryCollisionModel types are: 4(VariableHardSphere "
+                                    "LarsenBorgnakkeVariableHardSphere VariableSoftSphere "
+                                    "LarsenBorgnakkeVariableSoftSphere)")
+
+
+def test_soft_sphere_models_are_selected_by_name(gpu_lib, tmp_path):
+    from hystrath_gb300.dsmc import parse_case
+    for name, code in (("VariableSoftSphere", S.COLL_VSS), ("LarsenBorgnakkeVariableSoftSphere", S.COLL_LB_VSS)):
+        d = _copy_case(tmp_path / name)
+        _edit(d / "constant/dsmcProperties", "VariableHardSphere;", name + ";")
+        assert parse_case(str(d)).binary_collision_model == code
 
 
 def test_unknown_partner_selection(gpu_lib, tmp_path):
