@@ -117,20 +117,22 @@ STATE_BYTES = 68
 KERNELS_PER_STEP = 21
 
 
-def bytes_model(N, C, coll, n_acc):
+def bytes_model(N, C, coll, cand, n_acc):
     """Algorithmic bytes per step, per phase.
 
     move:    read pos,U (48) + cell word (4); write pos (24) + cell word (4)
     sort:    stable counting sort of the state, read + write (2 x 68), plus
              the per-cell count and offset (8 B per cell)
-    collide: per cell the sigmaTcRMax, remainder and counts (32 B) and the
-             sampling accumulators (8 B per accumulator, read + write every
-             32 samples, 16/32 per step); per collision the two records
-             read and written (4 x 64 B)
+    collide: per cell the candidate count (start, sigmaTcRMax, remainder,
+             count: 36 B) and the sampling accumulators (8 B each, read and
+             written every 32 samples: 0.5 B per accumulator and step); per
+             parcel the id and cell word of a cell's members for the pair
+             draw (8 B); per candidate the two velocities and species words
+             (2 x 32 B); per collision the energies written back (2 x 64 B)
     """
     move = 80.0 * N
     sort = 2.0 * STATE_BYTES * N + 8.0 * C
-    collide = (32.0 + 0.5 * n_acc) * C + 256.0 * coll
+    collide = (36.0 + 0.5 * n_acc) * C + 8.0 * N + 64.0 * cand + 128.0 * coll
     return move, sort, collide
 
 
@@ -163,6 +165,7 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.synchronize()
     clocks = clk.stop() if clk else None
     coll = i1.collisions_total - i0.collisions_total
+    cand = i1.candidates_total - i0.candidates_total
     t = torch.tensor([total_ms, float(coll), float(N)], dtype=torch.float64, device="cuda")
     if dist:
         tm = t.clone()
@@ -200,7 +203,7 @@ def gpu_arm(args, rank, world, local):
         if dist:
             dist.destroy_process_group()
         return
-    mv, so, co = bytes_model(N, C, coll / args.steps, s.n_species * 7 + 2)
+    mv, so, co = bytes_model(N, C, coll / args.steps, cand / args.steps, s.n_species * 7 + 2)
     peak, peak_kind = read_peaks()
     per = {k: v / args.steps for k, v in phases.items()}
     dominant = max(("move", "sort", "collide_sample"), key=lambda k: per[k])

@@ -583,10 +583,12 @@ void readCase(const std::string& dir, dsmc_case_spec* s) {
         s->inv_zv_formulation = (f == "pre-2008") ? 0 : (f == "2008") ? 1 : 2;
     }
     const std::string sel = word(dp.get(), "collisionPartnerSelectionModel", dpPath);
-    if (sel != "noTimeCounter")
+    if (sel == "noTimeCounter") s->partner_selection_model = DSMC_SEL_NTC;
+    else if (sel == "simplifiedBernoulliTrials") s->partner_selection_model = DSMC_SEL_SBT;
+    else
         throw ParseError(DSMC_ERR_UNKNOWN_MODEL, "Unknown collisionPartnerSelectionModel type " + sel +
-                                                     ". Valid collisionPartnerSelectionModel types are: 1(noTimeCounter)");
-    s->partner_selection_model = DSMC_SEL_NTC;
+                                                     ". Valid collisionPartnerSelectionModel types are: "
+                                                     "2(noTimeCounter simplifiedBernoulliTrials)");
     s->seed = (unsigned long long)scalarOr(dp.get(), "seedNumber", 0.0);
     const std::vector<std::string> types = wordList(need(dp.get(), "typeIdList", dpPath));
     if (types.empty() || types.size() > DSMC_MAX_SPECIES)

@@ -121,9 +121,10 @@ int validate(dsmc_handle* h, const dsmc_case_spec& s) {
             if (!(s.species[i].alpha > 0))
                 return fail(h, DSMC_ERR_INVALID, std::string("species ") + s.species[i].name +
                                                      ": VariableSoftSphere needs alpha > 0");
-    if (s.partner_selection_model != DSMC_SEL_NTC)
+    if (s.partner_selection_model != DSMC_SEL_NTC && s.partner_selection_model != DSMC_SEL_SBT)
         return fail(h, DSMC_ERR_UNKNOWN_MODEL,
-                    "Unknown collisionPartnerSelectionModel type. Valid types are: 1(noTimeCounter)");
+                    "Unknown collisionPartnerSelectionModel type. Valid types are: "
+                    "2(noTimeCounter simplifiedBernoulliTrials)");
     if (s.n_patches < 1 || s.n_patches > DSMC_MAX_PATCHES)
         return fail(h, DSMC_ERR_INVALID, "n_patches must be 1.." + std::to_string(DSMC_MAX_PATCHES));
     for (int p = 0; p < s.n_patches; ++p) {
@@ -223,6 +224,7 @@ void fill_case_dev(dsmc_handle* h) {
     cs.seedHi = (uint32_t)(s.seed >> 32);
     cs.nSpecies = s.n_species;
     cs.collModel = s.binary_collision_model;
+    cs.selModel = s.partner_selection_model;
     cs.zrot = s.zrot;
     cs.fixedZv = s.fixed_zv;
     cs.invZvForm = s.inv_zv_formulation;
@@ -978,6 +980,8 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
 // ------------------------------------------------------- learned selection
 int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float margin) {
     if (every < 1) return fail(h, DSMC_ERR_INVALID, "every must be at least 1");
+    if (model && h->spec.partner_selection_model != DSMC_SEL_NTC)
+        return fail(h, DSMC_ERR_INVALID, "the learned maximum applies to noTimeCounter selection only");
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     h->model = reinterpret_cast<const MlpModel*>(model);
     h->learnEvery = every;

@@ -347,13 +347,22 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
     if (selBlocks > (long long)sms * 8) selBlocks = (long long)sms * 8;
     unsigned* slotCount = B.buckets;
     unsigned* slotCursor = B.buckets + 2 * tile::NBUCKET;
-    tile::k_ntc_select<<<(int)selBlocks, 256, 0, st>>>(cs, B.start, B.smax, B.rem, B.ctr, B.ncCell, slotCount,
-                                                        learned, B.pred, B.useR, B.smaxSel);
+    const bool sbt = cs.selModel == DSMC_SEL_SBT;
+    if (sbt)
+        tile::k_sbt_select<<<(int)selBlocks, 256, 0, st>>>(cs, B.start, B.ctr, B.ncCell, slotCount);
+    else
+        tile::k_ntc_select<<<(int)selBlocks, 256, 0, st>>>(cs, B.start, B.smax, B.rem, B.ctr, B.ncCell, slotCount,
+                                                            learned, B.pred, B.useR, B.smaxSel);
     tile::k_ntc_buckets<<<1, 1, 0, st>>>(B.ctr, slotCount, slotCursor);
-    tile::k_ntc_list<<<(int)selBlocks, 256, 0, st>>>(cs.C, B.start, B.ncCell, slotCursor, B.work, B.bigList, B.ctr);
+    tile::k_ntc_list<<<(int)selBlocks, 256, 0, st>>>(cs.C, B.start, B.ncCell, slotCursor, B.work, B.bigList, B.ctr,
+                                                      sbt ? 1 : 0);
     tile::k_cell_order<<<sms * 8, tile::WARPS * 32, 0, st>>>(s, B.start, B.ctr, B.work, B.perm, B.subs);
     tile::k_cell_order_big<<<sms, tile::ORDER_BLOCK, tile::ORDER_MAX_N * sizeof(unsigned long long), st>>>(
         s, B.start, B.ctr, B.work, B.bigList, B.perm, B.subs);
+    if (sbt) {
+        tile::k_sbt_collide<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.acc, B.ctr, B.work, B.perm);
+        return;
+    }
     tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
                                                                 B.perm, B.subs, learned, B.smaxSel, B.useR,
                                                                 B.obsMax);

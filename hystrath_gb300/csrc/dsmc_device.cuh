@@ -86,6 +86,7 @@ struct CaseDev {
     uint32_t seedLo, seedHi;
     int nSpecies;
     int collModel;
+    int selModel;       // DSMC_SEL_*
     double zrot, fixedZv;
     int invZvForm;
     int nPatches;

@@ -125,8 +125,10 @@ __global__ void k_ntc_buckets(Counters* ctr, unsigned* slotCount, unsigned* slot
 
 // work list of the cells with candidates; cells too large for one warp to
 // order are also listed (by work index) for k_cell_order_big
+// allHeavy: every listed cell is ordered and takes a heavy slot (the
+// Bernoulli-trial selection walks the canonical list of every cell)
 __global__ void k_ntc_list(long long C, const int* __restrict__ start, const int* __restrict__ ncCell,
-                           unsigned* slotCursor, int2* work, int* bigList, Counters* ctr) {
+                           unsigned* slotCursor, int2* work, int* bigList, Counters* ctr, int allHeavy) {
     const unsigned lane = threadIdx.x & 31u;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < C; base += (long long)gridDim.x * blockDim.x) {
         const long long c = base + threadIdx.x;
@@ -136,7 +138,7 @@ __global__ void k_ntc_list(long long C, const int* __restrict__ start, const int
             if (nc > 0) n = start[c + 1] - start[c];
         }
         if (!__ballot_sync(0xFFFFFFFFu, nc > 0)) continue;
-        const int slot = nc > 0 ? slot_of(n, nc) : -1;
+        const int slot = nc > 0 ? (allHeavy ? NBUCKET + bucket_of(nc) : slot_of(n, nc)) : -1;
         // one atomic per slot present in the warp
         const unsigned peers = __match_any_sync(0xFFFFFFFFu, slot);
         const int leader = __ffs(peers) - 1;
@@ -569,6 +571,72 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
     }
     if (nColl) atomicAdd(&ctr->coll, nColl);
     if (nCandTot) atomicAdd(&ctr->cand, nCandTot);
+    if (err) atomicOr(&ctr->err, err);
+}
+
+// ------------------------------------------------------------ Bernoulli trials
+// simplifiedBernoulliTrials::collide (simplifiedBernoulliTrials.C:88-190):
+// every cell with two or more parcels has nC - 1 trials; trial p pairs the
+// p-th member of the cell's list with one of the k = nC - 1 - p members after
+// it (randomLabel(1, k)) and collides them with probability
+// k FN dt / V sigma_T c_R.  There is no maximum and no sub-cell.
+__global__ void k_sbt_select(CaseDev cs, const int* __restrict__ start, Counters* ctr, int* ncCell,
+                             unsigned* slotCount) {
+    __shared__ unsigned hist[2 * NBUCKET];
+    if (threadIdx.x < 2 * NBUCKET) hist[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned err = 0;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cs.C;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int n = start[c + 1] - start[c];
+        int nt = 0;
+        if (n > 1) {
+            if (n > ORDER_MAX_N) err |= ERRB_DENSE;
+            else nt = n - 1;
+        }
+        ncCell[c] = nt;
+        if (nt > 0) atomicAdd(&hist[NBUCKET + bucket_of(nt)], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 2 * NBUCKET && hist[threadIdx.x]) atomicAdd(&slotCount[threadIdx.x], hist[threadIdx.x]);
+    if (err) atomicOr(&ctr->err, err);
+}
+
+// one lane per listed cell, its trials one after the other in list order
+__global__ void __launch_bounds__(WARPS * 32, 4)
+k_sbt_collide(CaseDev cs, Parcels s, const int* __restrict__ start, double* acc, Counters* ctr,
+              const int2* __restrict__ work, const uint16_t* __restrict__ perm) {
+    const uint32_t step = (uint32_t)ctr->step;
+    const long long nWork = (long long)ctr->nWork;
+    const long long C = cs.C;
+    const double prob1 = cs.FN * cs.dt / cs.V;
+    unsigned err = 0;
+    unsigned long long nColl = 0, nTrials = 0;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nWork;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int c = work[q].x;
+        const long long off = start[c];
+        const int n = start[c + 1] - (int)off;
+        double stepMax = 0.0, collSep = 0.0;
+        unsigned coll = 0;
+        for (int p = 0; p < n - 1; ++p) {
+            Rng r(cs, (uint32_t)c, step, cand_tag(p));
+            const int k = n - 1 - p;
+            const int qq = p + r.label(1, k, &err);
+            const long long gP = off + perm[off + p];
+            const long long gQ = off + perm[off + qq];
+            // accept when k prob1 sigma > U, i.e. sigma > U / (k prob1)
+            if (run_candidate(cs, s, r, gP, gQ, 1.0 / (k * prob1), &stepMax, &collSep, &err)) ++coll;
+        }
+        if (coll) {
+            acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
+            acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
+        }
+        nColl += coll;
+        nTrials += (unsigned long long)(n - 1);
+    }
+    if (nColl) atomicAdd(&ctr->coll, nColl);
+    if (nTrials) atomicAdd(&ctr->cand, nTrials);
     if (err) atomicOr(&ctr->err, err);
 }
 

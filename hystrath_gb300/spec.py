@@ -26,7 +26,7 @@ ERR_IO, ERR_PARSE, ERR_UNKNOWN_MODEL, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_CAP
 PATCH_WALL, PATCH_PATCH, PATCH_SYMMETRY, PATCH_CYCLIC = range(4)
 BC_NONE, BC_SPECULAR, BC_DIFFUSE, BC_DELETION = range(4)
 COLL_VHS, COLL_LB_VHS, COLL_VSS, COLL_LB_VSS = range(4)
-SEL_NTC = 0
+SEL_NTC, SEL_SBT = 0, 1
 
 PHASE_INFLOW, PHASE_MOVE, PHASE_SORT, PHASE_COLLIDE, PHASE_SAMPLE = 1, 2, 4, 8, 16
 PHASE_ALL = 31

@@ -77,7 +77,10 @@ enum {
     DSMC_COLL_VSS = 2,     /* VariableSoftSphere */
     DSMC_COLL_LB_VSS = 3   /* LarsenBorgnakkeVariableSoftSphere */
 };
-enum { DSMC_SEL_NTC = 0 }; /* noTimeCounter */
+enum {
+    DSMC_SEL_NTC = 0,      /* noTimeCounter */
+    DSMC_SEL_SBT = 1       /* simplifiedBernoulliTrials */
+};
 
 /* Step phases, for dsmc_run_phases. */
 enum {

@@ -920,13 +920,58 @@ struct Oracle {
         }
     }
 
+    // simplifiedBernoulliTrials::collide for one cell
+    // (simplifiedBernoulliTrials.C:88-190): nC - 1 trials in list order
+    void bernoulliCell(long long c, long long* nColl, long long* nCand, int* e) {
+        const int nC = cellCount[c];
+        if (nC <= 1) return;
+        Parcel* cp = &P[cellStart[c]];
+        Rng r(spec.seed, (uint32_t)c, (uint32_t)step, TAG_COLLIDE);
+        const double prob1 = spec.n_equivalent_particles * spec.delta_t / V;
+        double* A = &acc[c * nAcc];
+        for (int ip = 0; ip < nC - 1; ++ip) {
+            const int k = nC - 1 - ip;
+            const int iq = ip + r.label(1, k, e);
+            Parcel& p = cp[ip];
+            Parcel& q = cp[iq];
+            const double s = sigmaTcR(p, q);
+            ++*nCand;
+            if (k * prob1 * s > r.u01()) {
+                const Species& a = sp[p.type];
+                const Species& b = sp[q.type];
+                double cr2 = 0;
+                for (int d = 0; d < 3; ++d) cr2 += (p.U[d] - q.U[d]) * (p.U[d] - q.U[d]);
+                double cR;
+                if (spec.binary_collision_model == DSMC_COLL_LB_VHS ||
+                    spec.binary_collision_model == DSMC_COLL_LB_VSS) {
+                    const double mR = a.m * b.m / (a.m + b.m);
+                    double Et = 0.5 * mR * cr2;
+                    const double omegaPQ = 0.5 * (a.omega + b.omega);
+                    redistribute(p, Et, omegaPQ, r, e);
+                    redistribute(q, Et, omegaPQ, r, e);
+                    cR = std::sqrt(2.0 * Et / mR);
+                } else {
+                    cR = std::sqrt(cr2);
+                }
+                scatter(p, q, cR, r);
+                A[ACC_COLLSEP] += std::sqrt((p.x[0] - q.x[0]) * (p.x[0] - q.x[0]) +
+                                            (p.x[1] - q.x[1]) * (p.x[1] - q.x[1]) +
+                                            (p.x[2] - q.x[2]) * (p.x[2] - q.x[2]));
+                A[ACC_NCOLLS] += 1.0;
+                ++*nColl;
+            }
+        }
+    }
+
     void collide() {
         long long nColl = 0, nCand = 0;
         int e = 0;
+        const bool sbt = spec.partner_selection_model == DSMC_SEL_SBT;
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : nColl, nCand) reduction(| : e) num_threads(nThreads)
         for (long long c = 0; c < C; ++c) {
             int ee = 0;
-            collideCell(c, &nColl, &nCand, &ee);
+            if (sbt) bernoulliCell(c, &nColl, &nCand, &ee);
+            else collideCell(c, &nColl, &nCand, &ee);
             e |= ee;
         }
         collLast = nColl;

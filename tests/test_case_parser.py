@@ -111,8 +111,14 @@ def test_soft_sphere_models_are_selected_by_name(gpu_lib, tmp_path):
 
 def test_unknown_partner_selection(gpu_lib, tmp_path):
     d = _copy_case(tmp_path)
+    _edit(d / "constant/dsmcProperties", "noTimeCounter;", "noRepeatCollisions;")
+    _expect(d, S.ERR_UNKNOWN_MODEL, "2(noTimeCounter simplifiedBernoulliTrials)")
+
+
+def test_bernoulli_trials_selected_by_name(gpu_lib, tmp_path):
+    d = _copy_case(tmp_path)
     _edit(d / "constant/dsmcProperties", "noTimeCounter;", "simplifiedBernoulliTrials;")
-    _expect(d, S.ERR_UNKNOWN_MODEL, "noTimeCounter")
+    assert parse(str(d)).partner_selection_model == S.SEL_SBT
 
 
 def test_unknown_patch_model(gpu_lib, tmp_path):
