@@ -136,6 +136,20 @@ def bytes_model(N, C, coll, cand, n_acc):
     return move, sort, collide
 
 
+def reduce_ranks(total_ms, coll, n_parcels, dist, device):
+    """Whole-job figures over the replicas: the slowest rank's time, the
+    summed collisions and parcels (dist None: one rank)."""
+    import torch
+    t = torch.tensor([total_ms, float(coll), float(n_parcels)], dtype=torch.float64, device=device)
+    if dist:
+        tm = t[:1].clone()
+        rest = t[1:].clone()
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        dist.all_reduce(rest, op=dist.ReduceOp.SUM)
+        t = torch.cat([tm, rest])
+    return float(t[0]), float(t[1]), float(t[2])
+
+
 def gpu_arm(args, rank, world, local):
     import numpy as np  # noqa: F401
     from hystrath_gb300 import spec as S
@@ -166,15 +180,7 @@ def gpu_arm(args, rank, world, local):
     clocks = clk.stop() if clk else None
     coll = i1.collisions_total - i0.collisions_total
     cand = i1.candidates_total - i0.candidates_total
-    t = torch.tensor([total_ms, float(coll), float(N)], dtype=torch.float64, device="cuda")
-    if dist:
-        tm = t.clone()
-        dist.all_reduce(tm[:1], op=dist.ReduceOp.MAX)
-        dist.all_reduce(t[1:], op=dist.ReduceOp.SUM)
-        t[0] = tm[0]
-    max_ms = float(t[0])
-    tot_coll = float(t[1])
-    tot_N = float(t[2])
+    max_ms, tot_coll, tot_N = reduce_ranks(total_ms, coll, N, dist, "cuda")
 
     # end-to-end through the C ABI with host buffers: upload the state,
     # K steps each returning the cloud totals, read a field back.
