@@ -305,14 +305,23 @@ __device__ __forceinline__ long long fixp(double v, int F, unsigned* err) {
 
 __device__ __forceinline__ double unfix(long long s, int F) { return ldexp((double)s, -F); }
 
-// Sum of v over this lane's run of the warp (a run starts at every lane set
-// in headMask; lane 0 always starts one).  The run's last lane holds the total.
-__device__ __forceinline__ long long seg_sum(long long v, unsigned headMask) {
+// Sum of v over this lane's run of the warp (the run starts at lane
+// segStart).  The run's last lane holds the total.
+__device__ __forceinline__ long long seg_sum(long long v, int segStart) {
     const int lane = (int)(threadIdx.x & 31u);
-    const int segStart = 31 - __clz(headMask & (0xFFFFFFFFu >> (31 - lane)));
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const long long y = __shfl_up_sync(0xFFFFFFFFu, v, o);
+        if (lane - o >= segStart) v += y;
+    }
+    return v;
+}
+
+__device__ __forceinline__ int seg_sum32(int v, int segStart) {
+    const int lane = (int)(threadIdx.x & 31u);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xFFFFFFFFu, v, o);
         if (lane - o >= segStart) v += y;
     }
     return v;

@@ -336,8 +336,12 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
     const unsigned lane = lane_id();
     const int prev = __shfl_up_sync(0xFFFFFFFFu, skey, 1);
     const unsigned hm = __ballot_sync(0xFFFFFFFFu, lane == 0 || prev != skey);
+    const int segStart = 31 - __clz(hm & (0xFFFFFFFFu >> (31 - (int)lane)));
+    // the count is the run's length; vibrational levels sum in 32 bits
+    f[SACC_N] = (long long)((int)lane - segStart + 1);
+    f[SACC_VIB] = seg_sum32((int)f[SACC_VIB], segStart);
 #pragma unroll
-    for (int k = 0; k < SACC; ++k) f[k] = seg_sum(f[k], hm);
+    for (int k = SACC_UX; k <= SACC_EROT; ++k) f[k] = seg_sum(f[k], segStart);
     const bool tail = lane == 31 || ((hm >> (lane + 1)) & 1u);
     if (tail && skey >= 0) {
         const long long c = skey >> 3;
