@@ -211,6 +211,8 @@ void fill_case_dev(dsmc_handle* h) {
         cs.dx[a] = s.cell_size[a];
         cs.inv[a] = 1.0 / s.cell_size[a];
         cs.negOinv[a] = -(s.origin[a] * cs.inv[a]);
+        cs.invF[a] = (float)cs.inv[a];
+        cs.negOinvF[a] = (float)cs.negOinv[a];
         cs.lo[a] = s.origin[a];
         cs.hi[a] = s.origin[a] + s.n_cells[a] * s.cell_size[a];
     }

@@ -80,6 +80,7 @@ struct CaseDev {
     int nObst;
     long long C;
     double lo[3], hi[3], dx[3], inv[3], negOinv[3];
+    float invF[3], negOinvF[3];   // FP32 roundings of inv and negOinv (cell index screen)
     double V;
     double FN, dt;
     double invDtFa[3];   // 1 / (dt * area of a face normal to each axis)
@@ -271,6 +272,25 @@ __device__ __forceinline__ float d2f_bits(double v) {
 
 __device__ __forceinline__ int floor2_coord(const CaseDev& cs, double x, int a) {
     return floor2_bits(fma(x, cs.inv[a], cs.negOinv[a]));
+}
+
+// floor2_coord with the FP64 multiply-add replaced, where it cannot change
+// the result, by an FP32 one.  t32 = fmaf(float(x), float(inv), float(negOinv))
+// differs from the FP64 coordinate t by at most 2^-21 (|x inv| + |negOinv| +
+// |t|) (truncation of x: 2^-23, roundings of the constants and of the fmaf:
+// 2^-24 each), so when 2 t32 lies farther than twice that bound from an
+// integer both floors agree; otherwise (about one coordinate in 10^4, and
+// every exact integer) the FP64 path decides.  The result is bit for bit that
+// of floor2_coord.
+__device__ __forceinline__ int floor2_coord_fast(const CaseDev& cs, double x, int a) {
+    const float xf = d2f_bits(x);
+    const float p = xf * cs.invF[a];
+    const float t = fmaf(xf, cs.invF[a], cs.negOinvF[a]);
+    const float u = 2.0f * t;
+    const float f = floorf(u);
+    const float margin = 1.9073486e-6f * (fabsf(p) + fabsf(cs.negOinvF[a]) + fabsf(t));   // 2 x 2^-20 x (...)
+    if (fabsf(u) < 4194304.0f && u - f > margin && (f + 1.0f) - u > margin) return (int)f;
+    return floor2_coord(cs, x, a);
 }
 
 // ------------------------------------------------------- sampling sums

@@ -394,9 +394,9 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                 const double ex = fma(ux, cs.dt, x);
                 const double ey = fma(uy, cs.dt, y);
                 const double ez = fma(uz, cs.dt, z);
-                const int c2x = floor2_coord(cs, ex, 0);
-                const int c2y = floor2_coord(cs, ey, 1);
-                const int c2z = floor2_coord(cs, ez, 2);
+                const int c2x = floor2_coord_fast(cs, ex, 0);
+                const int c2y = floor2_coord_fast(cs, ey, 1);
+                const int c2z = floor2_coord_fast(cs, ez, 2);
                 const int cx = c2x >> 1, cy = c2y >> 1, cz = c2z >> 1;
                 bool inside = (unsigned)cx < (unsigned)cs.n[0] && (unsigned)cy < (unsigned)cs.n[1] &&
                               (unsigned)cz < (unsigned)cs.n[2];
