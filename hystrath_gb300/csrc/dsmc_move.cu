@@ -683,7 +683,7 @@ __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_gather(Parcels src, Parc
             atomicOr(&ctr->err, ERRB_BOUNDS);
             continue;
         }
-        st_rec_cs(dst.r + j, ldg_rec(src.r + i));
+        st_rec(dst.r + j, ldg_rec(src.r + i));
         __stcs(dst.cellw + j, (uint32_t)sk.y);
     }
 }
