@@ -173,9 +173,16 @@ void build_faces(dsmc_handle* h, std::vector<int>& bfPatch, std::vector<long lon
         const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
         cs.sideOff[q] = off;
         const long long nf = (long long)s.n_cells[b] * s.n_cells[c];
+        // a side deletes when every face's patch removes what reaches it
+        // (not symmetry or cyclic, no specular or diffuse model)
+        cs.sideDeletes[q] = 1;
         for (long long f = 0; f < nf; ++f) {
             const int p = s.face_patch[q] ? s.face_patch[q][f] : s.side_patch[q];
             bfPatch.push_back(p);
+            if (p < 0 || p >= s.n_patches || s.patches[p].type == DSMC_PATCH_SYMMETRY ||
+                s.patches[p].type == DSMC_PATCH_CYCLIC || s.patches[p].model == DSMC_BC_SPECULAR ||
+                s.patches[p].model == DSMC_BC_DIFFUSE)
+                cs.sideDeletes[q] = 0;
             if (p >= 0 && p < s.n_patches && s.patches[p].inflow) {
                 inflowFace.push_back(off + f);
                 inflowSide.push_back(q);

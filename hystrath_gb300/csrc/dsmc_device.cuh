@@ -81,6 +81,7 @@ struct CaseDev {
     long long C;
     double lo[3], hi[3], dx[3], inv[3], negOinv[3];
     float invF[3], negOinvF[3];   // FP32 roundings of inv and negOinv (cell index screen)
+    int sideDeletes[6];           // every face of the domain side deletes (dsmcDeletionPatch)
     double V;
     double FN, dt;
     double invDtFa[3];   // 1 / (dt * area of a face normal to each axis)

@@ -365,6 +365,7 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix) {
     const long long n = ctr->nMoved;
+    const uint32_t step = (uint32_t)ctr->step;
     const int doSample = ctr->pendingSample;
     unsigned err = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -378,12 +379,20 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
         if (i < n) {
             const uint32_t w = s.cellw[i];
             bool fast = false;
-            if (!(w & CELLW_FRESH)) {
+            {
+                const bool fresh = (w & CELLW_FRESH) != 0;
                 double2* q = reinterpret_cast<double2*>(s.r + i);
                 const double2 q0 = q[0], q1 = q[1], q2 = q[2];
                 const double x = q0.x, y = q0.y, z = q1.x;
                 const double ux = q1.y, uy = q2.x, uz = q2.y;
-                if (doSample) {
+                double tr = cs.dt;
+                if (fresh) {
+                    // a parcel inserted this step moves for (1 - U) dt
+                    // (dsmcParcel.C:52-59), with the draw of the boundary path
+                    const uint32_t pid = (uint32_t)__double_as_longlong(q[3].y);
+                    Rng r(cs, pid, step, TAG_MOVE);
+                    tr = (1.0 - r.u01()) * cs.dt;
+                } else if (doSample) {
                     const double2 q3 = q[3];
                     const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q3.y) >> 32);
                     skey = (int)(cellw_cell(w) * 8u + (uint32_t)sv_species(sv));
@@ -391,16 +400,27 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     ser = q3.x;
                     svb = sv_vib(sv);
                 }
-                const double ex = fma(ux, cs.dt, x);
-                const double ey = fma(uy, cs.dt, y);
-                const double ez = fma(uz, cs.dt, z);
+                const double ex = fma(ux, tr, x);
+                const double ey = fma(uy, tr, y);
+                const double ez = fma(uz, tr, z);
                 const int c2x = floor2_coord_fast(cs, ex, 0);
                 const int c2y = floor2_coord_fast(cs, ey, 1);
                 const int c2z = floor2_coord_fast(cs, ez, 2);
                 const int cx = c2x >> 1, cy = c2y >> 1, cz = c2z >> 1;
-                bool inside = (unsigned)cx < (unsigned)cs.n[0] && (unsigned)cy < (unsigned)cs.n[1] &&
-                              (unsigned)cz < (unsigned)cs.n[2];
-                if (inside && cs.nObst) {
+                const bool inX = (unsigned)cx < (unsigned)cs.n[0], inY = (unsigned)cy < (unsigned)cs.n[1],
+                           inZ = (unsigned)cz < (unsigned)cs.n[2];
+                bool inside = inX && inY && inZ;
+                // leaving through exactly one side whose every face deletes
+                // (dsmcDeletionPatch, no wall measurement): the straight path
+                // stays inside the other two slabs, so that side is the one hit
+                int delSide = -1;
+                if (!inside && (int)inX + (int)inY + (int)inZ == 2) {
+                    const int a = !inX ? 0 : !inY ? 1 : 2;
+                    const int c2a = a == 0 ? c2x : a == 1 ? c2y : c2z;
+                    const int side = 2 * a + (c2a < 0 ? 0 : 1);
+                    if (cs.sideDeletes[side]) delSide = side;
+                }
+                if ((inside || delSide >= 0) && cs.nObst) {
                     const uint32_t c = cellw_cell(w);
                     const int sx = (int)(c % (uint32_t)cs.n[0]);
                     const int sy = (int)((c / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]);
@@ -408,11 +428,16 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     for (int o = 0; o < cs.nObst; ++o) {
                         if (max(sx, cx) + 1 >= cs.obLoI[o][0] && min(sx, cx) - 1 <= cs.obHiI[o][0] - 1 &&
                             max(sy, cy) + 1 >= cs.obLoI[o][1] && min(sy, cy) - 1 <= cs.obHiI[o][1] - 1 &&
-                            max(sz, cz) + 1 >= cs.obLoI[o][2] && min(sz, cz) - 1 <= cs.obHiI[o][2] - 1)
+                            max(sz, cz) + 1 >= cs.obLoI[o][2] && min(sz, cz) - 1 <= cs.obHiI[o][2] - 1) {
                             inside = false;
+                            delSide = -1;
+                        }
                     }
                 }
-                if (inside) {
+                if (delSide >= 0) {
+                    s.cellw[i] = CELLW_DELETED;
+                    fast = true;
+                } else if (inside) {
                     q[0] = make_double2(ex, ey);
                     s.r[i].z = ez;
                     const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
