@@ -521,6 +521,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.inflowAcc, ni))) return rc;
     if ((rc = dalloc(h, &B.inflowCount, ni))) return rc;
     if ((rc = dalloc(h, &B.inflowOff, ni + 1))) return rc;
+    if ((rc = dalloc(h, &B.inflowTerm, ni))) return rc;
     // 1/Zv by quantised level (postCollisionVibrationalEnergyLevel, dsmcCloud.C:1420-1490)
     {
         std::vector<double> tab((size_t)DSMC_MAX_SPECIES * DSMC_MAX_SPECIES * ZV_TAB, 0.0);
@@ -555,6 +556,30 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
                                cudaMemcpyHostToDevice));
         CUDA_TRY(h, cudaMemcpy(B.inflowCell, inflowCell.data(), sizeof(int) * inflowCell.size(),
                                cudaMemcpyHostToDevice));
+        // the Bird eq. 4.22 number of parcels per step through each inflow
+        // face (dsmcFreeStreamInflowPatch.C:96-141): constant in time, so it
+        // is evaluated once, here
+        std::vector<double> term((size_t)ni, 0.0);
+        const double sqrtPi = std::sqrt(PI);
+        for (size_t f = 0; f < inflowFace.size(); ++f) {
+            const int sd = inflowSide[f];
+            const int a = sd / 2;
+            const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+            const double sgnOut = (sd & 1) ? 1.0 : -1.0;
+            const double fA = spec->cell_size[b] * spec->cell_size[c];
+            const int pi = bfPatch[(size_t)inflowFace[f]];
+            const dsmc_patch& pt = spec->patches[pi];
+            for (int m = 0; m < spec->n_species; ++m) {
+                const double nd = pt.inflow_number_density[m];
+                if (!(nd > 0)) continue;
+                const double cmp = std::sqrt(2.0 * kB * pt.inflow_t_tra / spec->species[m].mass);
+                const double sCos = (pt.inflow_velocity[a] * (-sgnOut)) / cmp;
+                term[f * spec->n_species + m] =
+                    (fA * nd * spec->delta_t * cmp * (std::exp(-sCos * sCos) + sqrtPi * sCos * (1 + std::erf(sCos)))) /
+                    (2.0 * sqrtPi * spec->n_equivalent_particles);
+            }
+        }
+        CUDA_TRY(h, cudaMemcpy(B.inflowTerm, term.data(), sizeof(double) * term.size(), cudaMemcpyHostToDevice));
     }
     void* pinned = nullptr;
     CUDA_TRY(h, cudaMallocHost(&pinned, sizeof(Counters)));

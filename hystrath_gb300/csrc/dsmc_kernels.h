@@ -69,6 +69,7 @@ struct StepBuffers {
     int* inflowSide;          // side of each inflow face
     int* inflowCell;          // owner cell
     double* inflowAcc;        // [nInflowFaces * nSpecies]
+    double* inflowTerm;       // [nInflowFaces * nSpecies] parcels per step (Bird eq. 4.22)
     int* inflowCount;         // [nInflowFaces * nSpecies]
     int* inflowOff;           // [nInflowFaces * nSpecies + 1]
     double inflowND[DSMC_MAX_PATCHES][DSMC_MAX_SPECIES];

@@ -729,31 +729,19 @@ __global__ void k_end_step(Counters* ctr) {
 // ---------------------------------------------------------------- inflow
 // One thread per (inflow face, species): Bird eq. 4.22 flux accumulation and
 // the integer-plus-remainder count (dsmcFreeStreamInflowPatch.C:96-141,226-236).
-__global__ void k_inflow_count(CaseDev cs, InflowDev in, int nFaces, const long long* __restrict__ face,
-                               const int* __restrict__ side, const int* __restrict__ bfPatch,
-                               double* accum, int* cnt, const Counters* ctr) {
+// One thread per (inflow face, species): the flux accumulation and the
+// integer-plus-remainder count (dsmcFreeStreamInflowPatch.C:96-141,226-236).
+__global__ void k_inflow_count(CaseDev cs, int nFaces, const long long* __restrict__ face,
+                               const double* __restrict__ term, double* accum, int* cnt, const Counters* ctr) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int ns = cs.nSpecies;
     if (t >= nFaces * ns) return;
-    const int f = t / ns, m = t % ns;
-    const long long bf = face[f];
-    const int sd = side[f];
-    const int a = sd / 2;
-    const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
-    const double sgnOut = (sd & 1) ? 1.0 : -1.0;
-    const InflowPatchDev& pt = in.p[bfPatch[bf]];
-    const double nd = pt.nd[m];
     int nI = 0;
-    if (nd > 0) {
-        const SpeciesDev& s = cs.sp[m];
-        const double fA = cs.dx[b] * cs.dx[c];
-        const double cmp = sqrt(2.0 * kB * pt.Ttra / s.m);
-        const double sCos = (pt.U[a] * (-sgnOut)) / cmp;
-        const double sqrtPi = sqrt(PI);
-        double A = accum[t];
-        A += (fA * nd * cs.dt * cmp * (exp(-sCos * sCos) + sqrtPi * sCos * (1 + erf(sCos)))) /
-             (2.0 * sqrtPi * cs.FN);
-        Rng r(cs, (uint32_t)bf, (uint32_t)ctr->step, TAG_INFLOW | ((uint32_t)m << 8));
+    const double add = term[t];
+    if (add > 0) {
+        const int m = t % ns;
+        double A = accum[t] + add;
+        Rng r(cs, (uint32_t)face[t / ns], (uint32_t)ctr->step, TAG_INFLOW | ((uint32_t)m << 8));
         nI = (int)A;
         if (nI < 0) nI = 0;
         if ((A - nI) > r.u01()) nI++;
@@ -786,81 +774,86 @@ __global__ void k_inflow_scan(const int* cnt, int n, int* off, Counters* ctr, lo
     }
 }
 
+// One thread per inserted parcel (dsmcFreeStreamInflowPatch.C:237-364): the
+// parcel's (face, species) is found by bisection of the count offsets, and
+// every parcel draws from its own stream (face, step, species, parcel).
 __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long long* __restrict__ face,
                               const int* __restrict__ side, const int* __restrict__ cellOf,
-                              const int* __restrict__ bfPatch, const int* __restrict__ cnt,
-                              const int* __restrict__ off, Parcels s, Counters* ctr) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+                              const int* __restrict__ bfPatch, const int* __restrict__ off, Parcels s,
+                              Counters* ctr) {
     const int ns = cs.nSpecies;
-    if (off[nFaces * ns] < 0) return;     // capacity exceeded: nothing inserted
-    if (t < nFaces * ns) {
-        const int nI = cnt[t];
-        if (nI > 0) {
-            unsigned err = 0;
-            const int f = t / ns, m = t % ns;
-            const long long bf = face[f];
-            const int sd = side[f];
-            const int a = sd / 2;
-            const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
-            const double sgnOut = (sd & 1) ? 1.0 : -1.0;
-            const InflowPatchDev& pt = in.p[bfPatch[bf]];
-            const SpeciesDev& sp = cs.sp[m];
-            const double cmp = sqrt(2.0 * kB * pt.Ttra / sp.m);
-            const double sCos = (pt.U[a] * (-sgnOut)) / cmp;
-            const double coeffA = sCos + sqrt(sCos * sCos + 2.0);
-            const double coeffB = 0.5 * (1.0 + sCos * (sCos - sqrt(sCos * sCos + 2.0)));
-            double scaling = 3.0;
-            if (sCos < -3) scaling = fabs(sCos) + 1;
-            const long long fl = bf - cs.sideOff[sd];
-            const long long ib = fl % cs.n[b], ic = fl / cs.n[b];
-            const double lob = cs.lo[b] + (double)ib * cs.dx[b];
-            const double loc = cs.lo[c] + (double)ic * cs.dx[c];
-            const int cell = cellOf[f];
-            const double scT = sqrt(kB * pt.Ttra / sp.m);
-            Rng r(cs, (uint32_t)bf, (uint32_t)ctr->step, TAG_INFLOW | ((uint32_t)m << 8));
-            (void)r.u01();   // the remainder draw of k_inflow_count
-            const long long base = ctr->n + off[t];
-            const long long id0 = ctr->nextId + off[t];
-            for (int q = 0; q < nI; ++q) {
-                double x[3], U[3];
-                x[a] = (sd & 1) ? cs.hi[a] : cs.lo[a];
-                x[b] = fma(r.u01(), cs.dx[b], lob);
-                x[c] = fma(r.u01(), cs.dx[c], loc);
-                double uNormal = 0;
-                if (fabs(pt.U[a]) > VSMALL) {
-                    int it = 0;
-                    for (;;) {
-                        const double uth = scaling * (2.0 * r.u01() - 1);
-                        uNormal = uth + sCos;
-                        double Pr;
-                        if (uNormal < 0.0) Pr = -1;
-                        else Pr = 2.0 * uNormal / coeffA * exp(coeffB - uth * uth);
-                        if (!(Pr < r.u01())) break;
-                        if (++it >= MAX_REJECTION) { err |= ERRB_REJECTION; break; }
-                    }
-                } else {
-                    uNormal = sqrt(-log(r.u01()));
-                }
-                double g1, g2;
-                r.gauss2(&g1, &g2);
-                U[a] = cmp * uNormal * (-sgnOut);
-                U[b] = scT * g1 + pt.U[b];
-                U[c] = scT * g2 + pt.U[c];
-                const double erot = eq_rot(r, pt.Trot, sp.rotDof, &err);
-                const int vib = eq_vib(r, pt.Tvib, sp);
-                const long long slot = base + q;
-                Rec p;
-                p.x = x[0]; p.y = x[1]; p.z = x[2];
-                p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
-                p.erot = erot;
-                p.id = (uint32_t)(id0 + q);
-                p.sv = make_sv(m, vib);
-                st_rec(s.r + slot, p);
-                s.cellw[slot] = ((uint32_t)cell << 3) | CELLW_FRESH;
-            }
-            if (err) atomicOr(&ctr->err, err);
+    const int nt = nFaces * ns;
+    const long long total = off[nt];
+    if (total <= 0) return;     // nothing inserted (or capacity exceeded: -1)
+    unsigned err = 0;
+    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+         g += (long long)gridDim.x * blockDim.x) {
+        // the (face, species) slot t with off[t] <= g < off[t + 1]
+        int lo = 0, hi = nt;
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (off[mid] <= g) lo = mid; else hi = mid;
         }
+        const int t = lo;
+        const int q = (int)(g - off[t]);
+        const int f = t / ns, m = t % ns;
+        const long long bf = face[f];
+        const int sd = side[f];
+        const int a = sd / 2;
+        const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+        const double sgnOut = (sd & 1) ? 1.0 : -1.0;
+        const InflowPatchDev& pt = in.p[bfPatch[bf]];
+        const SpeciesDev& sp = cs.sp[m];
+        const double cmp = sqrt(2.0 * kB * pt.Ttra / sp.m);
+        const double sCos = (pt.U[a] * (-sgnOut)) / cmp;
+        const double coeffA = sCos + sqrt(sCos * sCos + 2.0);
+        const double coeffB = 0.5 * (1.0 + sCos * (sCos - sqrt(sCos * sCos + 2.0)));
+        double scaling = 3.0;
+        if (sCos < -3) scaling = fabs(sCos) + 1;
+        const long long fl = bf - cs.sideOff[sd];
+        const long long ib = fl % cs.n[b], ic = fl / cs.n[b];
+        const double lob = cs.lo[b] + (double)ib * cs.dx[b];
+        const double loc = cs.lo[c] + (double)ic * cs.dx[c];
+        const double scT = sqrt(kB * pt.Ttra / sp.m);
+        Rng r(cs, (uint32_t)bf, (uint32_t)ctr->step,
+              TAG_INFLOW | ((uint32_t)m << 8) | ((uint32_t)(q + 1) << 11));
+        double x[3], U[3];
+        x[a] = (sd & 1) ? cs.hi[a] : cs.lo[a];
+        x[b] = fma(r.u01(), cs.dx[b], lob);
+        x[c] = fma(r.u01(), cs.dx[c], loc);
+        double uNormal = 0;
+        if (fabs(pt.U[a]) > VSMALL) {
+            int it = 0;
+            for (;;) {
+                const double uth = scaling * (2.0 * r.u01() - 1);
+                uNormal = uth + sCos;
+                double Pr;
+                if (uNormal < 0.0) Pr = -1;
+                else Pr = 2.0 * uNormal / coeffA * exp(coeffB - uth * uth);
+                if (!(Pr < r.u01())) break;
+                if (++it >= MAX_REJECTION) { err |= ERRB_REJECTION; break; }
+            }
+        } else {
+            uNormal = sqrt(-log(r.u01()));
+        }
+        double g1, g2;
+        r.gauss2(&g1, &g2);
+        U[a] = cmp * uNormal * (-sgnOut);
+        U[b] = scT * g1 + pt.U[b];
+        U[c] = scT * g2 + pt.U[c];
+        const double erot = eq_rot(r, pt.Trot, sp.rotDof, &err);
+        const int vib = eq_vib(r, pt.Tvib, sp);
+        const long long slot = ctr->n + g;
+        Rec p;
+        p.x = x[0]; p.y = x[1]; p.z = x[2];
+        p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
+        p.erot = erot;
+        p.id = (uint32_t)(ctr->nextId + g);
+        p.sv = make_sv(m, vib);
+        st_rec(s.r + slot, p);
+        s.cellw[slot] = ((uint32_t)cellOf[f] << 3) | CELLW_FRESH;
     }
+    if (err) atomicOr(&ctr->err, err);
 }
 
 __global__ void k_inflow_commit(Counters* ctr) {
@@ -1051,11 +1044,12 @@ void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B,
     const int nt = B.nInflowFaces * cs.nSpecies;
     if (nt == 0) return;
     const int grid = (nt + 255) / 256;
-    k_inflow_count<<<grid, 256, 0, st>>>(cs, in, B.nInflowFaces, B.inflowFace, B.inflowSide, B.bfPatch,
-                                         B.inflowAcc, B.inflowCount, B.ctr);
+    k_inflow_count<<<grid, 256, 0, st>>>(cs, B.nInflowFaces, B.inflowFace, B.inflowTerm, B.inflowAcc,
+                                         B.inflowCount, B.ctr);
     k_inflow_scan<<<1, 1024, 0, st>>>(B.inflowCount, nt, B.inflowOff, B.ctr, B.capacity);
-    k_inflow_fill<<<grid, 256, 0, st>>>(cs, in, B.nInflowFaces, B.inflowFace, B.inflowSide, B.inflowCell,
-                                        B.bfPatch, B.inflowCount, B.inflowOff, s, B.ctr);
+    k_inflow_fill<<<grid_for(B.capacity, 256, 8), 256, 0, st>>>(cs, in, B.nInflowFaces, B.inflowFace,
+                                                                B.inflowSide, B.inflowCell, B.bfPatch,
+                                                                B.inflowOff, s, B.ctr);
     k_inflow_commit<<<1, 1, 0, st>>>(B.ctr);
 }
 

@@ -694,6 +694,9 @@ struct Oracle {
                     double scaling = 3.0;
                     if (sCos < -3) scaling = std::fabs(sCos) + 1;
                     for (int i = 0; i < nI; ++i) {
+                        // every parcel has its own stream (face, step, species, parcel)
+                        Rng r(spec.seed, (uint32_t)bf, (uint32_t)step,
+                              TAG_INFLOW | ((uint32_t)m << 8) | ((uint32_t)(i + 1) << 11));
                         Parcel p{};
                         p.x[a] = (side & 1) ? hi[a] : lo[a];
                         p.x[b] = std::fma(r.u01(), dx[b], lo[b] + ib * dx[b]);
