@@ -477,11 +477,10 @@ void readMesh(const std::string& dir, dsmc_case_spec* s, std::map<std::string, i
         else if (p.type == "patch") type = DSMC_PATCH_PATCH;
         else if (p.type == "symmetry" || p.type == "symmetryPlane") type = DSMC_PATCH_SYMMETRY;
         else if (p.type == "cyclic") type = DSMC_PATCH_CYCLIC;
-        else if (p.type == "empty")
-            throw ParseError(DSMC_ERR_INVALID, "patch " + p.name + ": empty (reduced-D) patches are not supported on this path");
+        else if (p.type == "empty") type = DSMC_PATCH_EMPTY;
         else
             throw ParseError(DSMC_ERR_INVALID, "patch " + p.name + ": unsupported patch type " + p.type +
-                                                   "; valid: wall patch symmetry symmetryPlane cyclic");
+                                                   "; valid: wall patch symmetry symmetryPlane cyclic empty");
         if (s->n_patches >= DSMC_MAX_PATCHES) throw ParseError(DSMC_ERR_INVALID, "more than 16 patches");
         const int pid = s->n_patches++;
         copyName(s->patches[pid].name, p.name);

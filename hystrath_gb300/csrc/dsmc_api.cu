@@ -34,6 +34,7 @@ struct dsmc_handle {
     InflowDev inflow{};
     StepBuffers B{};
     Parcels buf[2]{};
+    double* faceBuf = nullptr;   // face tracker sums, kept while tracking is off
     int cur = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -92,7 +93,7 @@ int alloc_soa(dsmc_handle* h, Parcels* s, long long cap) {
     return DSMC_OK;
 }
 
-const char* patch_type_names[] = {"wall", "patch", "symmetry", "cyclic"};
+const char* patch_type_names[] = {"wall", "patch", "symmetry", "cyclic", "empty"};
 
 int validate(dsmc_handle* h, const dsmc_case_spec& s) {
     for (int a = 0; a < 3; ++a) {
@@ -129,7 +130,10 @@ int validate(dsmc_handle* h, const dsmc_case_spec& s) {
         return fail(h, DSMC_ERR_INVALID, "n_patches must be 1.." + std::to_string(DSMC_MAX_PATCHES));
     for (int p = 0; p < s.n_patches; ++p) {
         const dsmc_patch& pt = s.patches[p];
-        if (pt.type < 0 || pt.type > 3) return fail(h, DSMC_ERR_INVALID, std::string("patch ") + pt.name + ": bad type");
+        if (pt.type < 0 || pt.type > DSMC_PATCH_EMPTY)
+            return fail(h, DSMC_ERR_INVALID, std::string("patch ") + pt.name + ": bad type");
+        if (pt.type == DSMC_PATCH_EMPTY && pt.inflow)
+            return fail(h, DSMC_ERR_INVALID, std::string("patch ") + pt.name + ": an empty patch takes no inflow");
         if ((pt.type == DSMC_PATCH_WALL || pt.type == DSMC_PATCH_PATCH) &&
             (pt.model < DSMC_BC_SPECULAR || pt.model > DSMC_BC_DELETION))
             return fail(h, DSMC_ERR_UNKNOWN_MODEL,
@@ -146,6 +150,34 @@ int validate(dsmc_handle* h, const dsmc_case_spec& s) {
                 return fail(h, DSMC_ERR_INVALID, "a cyclic side needs a cyclic opposite side");
         }
     }
+    // an empty direction: both sides empty on every face, one cell thick
+    // (OpenFOAM's emptyPolyPatch rules)
+    int nEmpty = 0;
+    for (int q = 0; q < 6; ++q) {
+        const int a = q / 2, b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
+        const long long nf = (long long)s.n_cells[b] * s.n_cells[c];
+        int ne = 0;
+        for (long long f = 0; f < nf; ++f) {
+            const int p = s.face_patch[q] ? s.face_patch[q][f] : s.side_patch[q];
+            if (p >= 0 && p < s.n_patches && s.patches[p].type == DSMC_PATCH_EMPTY) ++ne;
+        }
+        if (ne && ne != nf)
+            return fail(h, DSMC_ERR_INVALID, "an empty patch must cover a whole side of the mesh");
+        if (ne && s.n_cells[a] != 1)
+            return fail(h, DSMC_ERR_INVALID, "an empty direction must be one cell thick");
+        if (ne && (q & 1) == 0) {
+            const int p = s.face_patch[q ^ 1] ? s.face_patch[q ^ 1][0] : s.side_patch[q ^ 1];
+            if (s.patches[p].type != DSMC_PATCH_EMPTY)
+                return fail(h, DSMC_ERR_INVALID, "an empty side needs an empty opposite side");
+            ++nEmpty;
+        }
+    }
+    if (nEmpty == 3) return fail(h, DSMC_ERR_INVALID, "every direction is empty");
+    for (int o = 0; o < s.n_obstacles; ++o)
+        for (int q = 0; q < 6; ++q)
+            if (s.patches[s.obstacles[o].patch[q]].type == DSMC_PATCH_EMPTY &&
+                !((q & 1) ? s.obstacles[o].hi[q / 2] == s.n_cells[q / 2] : s.obstacles[o].lo[q / 2] == 0))
+                return fail(h, DSMC_ERR_INVALID, "a solid box face cannot be empty");
     if (s.n_obstacles < 0 || s.n_obstacles > DSMC_MAX_OBSTACLES)
         return fail(h, DSMC_ERR_INVALID, "too many obstacles");
     for (int o = 0; o < s.n_obstacles; ++o) {
@@ -222,7 +254,11 @@ void fill_case_dev(dsmc_handle* h) {
         cs.negOinvF[a] = (float)cs.negOinv[a];
         cs.lo[a] = s.origin[a];
         cs.hi[a] = s.origin[a] + s.n_cells[a] * s.cell_size[a];
+        cs.mid[a] = 0.5 * (cs.lo[a] + cs.hi[a]);
+        const int p = s.face_patch[2 * a] ? s.face_patch[2 * a][0] : s.side_patch[2 * a];
+        cs.emptyAx[a] = s.patches[p].type == DSMC_PATCH_EMPTY;
     }
+    cs.anyEmpty = cs.emptyAx[0] | cs.emptyAx[1] | cs.emptyAx[2];
     cs.C = (long long)cs.n[0] * cs.n[1] * cs.n[2];
     cs.V = cs.dx[0] * cs.dx[1] * cs.dx[2];
     cs.FN = s.n_equivalent_particles;
@@ -844,7 +880,7 @@ int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long l
     return fail(h, DSMC_ERR_INVALID, "unknown settable cell array " + nm);
 }
 
-int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n) {
+int dsmc_get_species_field(dsmc_handle* h, const char* name, unsigned species_mask, double* out, long long n) {
     static const char* names[F_COUNT_FIELDS] = {"rhoN", "rhoM", "Ux", "Uy", "Uz", "Ttra", "p", "Trot", "Tvib",
                                                 "Tov", "dsmcNMean", "nColls", "measuredCollisionRate",
                                                 "meanCollisionRate", "mfp"};
@@ -857,12 +893,20 @@ int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n) {
         return fail(h, DSMC_ERR_INVALID, std::string("unknown field ") + name + "; valid:" + valid);
     }
     if (n != h->cs.C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
+    const unsigned all = (1u << h->cs.nSpecies) - 1u;
+    if (!(species_mask & all) || (species_mask & ~all))
+        return fail(h, DSMC_ERR_INVALID, "species_mask must select species of the case");
     flush_sample(h);
-    launch_field(h->cs, h->B, which, h->fieldTmp, h->spec.measure_mean_free_path, h->spec.mfp_tref, h->stream);
+    launch_field(h->cs, h->B, which, h->fieldTmp, h->spec.measure_mean_free_path, h->spec.mfp_tref, species_mask,
+                 h->stream);
     CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaMemcpyAsync(out, h->fieldTmp, sizeof(double) * n, cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     return DSMC_OK;
+}
+
+int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n) {
+    return dsmc_get_species_field(h, name, (1u << h->cs.nSpecies) - 1u, out, n);
 }
 
 long long dsmc_n_boundary_faces(const dsmc_handle* h) { return h->cs.nBFaces; }
@@ -901,6 +945,8 @@ int dsmc_reset_sampling(dsmc_handle* h) {
     CUDA_TRY(h, cudaMemset(h->B.acc, 0, sizeof(double) * h->cs.C * h->cs.nAcc));
     CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
     CUDA_TRY(h, cudaMemset(h->B.wall, 0, sizeof(double) * h->cs.nBFaces * W_N));
+    if (h->cs.faceFlux)
+        CUDA_TRY(h, cudaMemset(h->cs.faceFlux, 0, sizeof(double) * 2 * h->cs.nSpecies * h->cs.nFacesAll));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
     h->ctrHost->sampleSteps = 0;
     h->ctrHost->pendingSample = 0;
@@ -1252,6 +1298,7 @@ void foam_write(const std::string& path, const std::string& cls, const std::stri
         std::fprintf(f, "    %s\n    {\n", pt.name);
         if (pt.type == DSMC_PATCH_CYCLIC) std::fprintf(f, "        type            cyclic;\n");
         else if (pt.type == DSMC_PATCH_SYMMETRY) std::fprintf(f, "        type            symmetryPlane;\n");
+        else if (pt.type == DSMC_PATCH_EMPTY) std::fprintf(f, "        type            empty;\n");
         else std::fprintf(f, "        type            calculated;\n        value           uniform %s;\n",
                           vec ? "(0 0 0)" : "0");
         std::fprintf(f, "    }\n");
@@ -1315,6 +1362,47 @@ int dsmc_write_fields(dsmc_handle* h, const char* case_dir, const char* time_nam
     foam_write(dir + "/dsmcSigmaTcRMax", "volScalarField", "dsmcSigmaTcRMax", time_name, "[0 3 -1 0 0 0 0]",
                {a.data()}, order, h->spec, &ok);
     if (!ok) return fail(h, DSMC_ERR_IO, "cannot write fields under " + dir);
+    return DSMC_OK;
+}
+
+// ------------------------------------------------------- face tracker
+int dsmc_set_face_tracking(dsmc_handle* h, int on) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CaseDev& cs = h->cs;
+    const long long nx = cs.n[0], ny = cs.n[1], nz = cs.n[2];
+    cs.faceOff[0] = 0;
+    cs.faceOff[1] = (nx + 1) * ny * nz;
+    cs.faceOff[2] = cs.faceOff[1] + nx * (ny + 1) * nz;
+    cs.nFacesAll = cs.faceOff[2] + nx * ny * (nz + 1);
+    const long long n = 2 * (long long)cs.nSpecies * cs.nFacesAll;
+    if (on && !h->faceBuf) {
+        int rc;
+        if ((rc = dalloc(h, &h->faceBuf, n))) return rc;
+    }
+    if (on && !cs.faceFlux) CUDA_TRY(h, cudaMemset(h->faceBuf, 0, sizeof(double) * n));
+    cs.faceFlux = on ? h->faceBuf : nullptr;
+    drop_graphs(h);
+    return DSMC_OK;
+}
+
+long long dsmc_n_faces(const dsmc_handle* h) {
+    const long long nx = h->cs.n[0], ny = h->cs.n[1], nz = h->cs.n[2];
+    return (nx + 1) * ny * nz + nx * (ny + 1) * nz + nx * ny * (nz + 1);
+}
+
+int dsmc_get_face_flux(dsmc_handle* h, const char* name, int species, double* out, long long n) {
+    const std::string nm(name);
+    const CaseDev& cs = h->cs;
+    if (!cs.faceFlux) return fail(h, DSMC_ERR_INVALID, "face tracking is off (dsmc_set_face_tracking)");
+    if (n != cs.nFacesAll) return fail(h, DSMC_ERR_INVALID, "n must equal dsmc_n_faces");
+    if (species < 0 || species >= cs.nSpecies) return fail(h, DSMC_ERR_INVALID, "species index out of range");
+    int k;
+    if (nm == "parcelIdFlux") k = 0;
+    else if (nm == "massIdFlux") k = 1;
+    else return fail(h, DSMC_ERR_INVALID, "unknown face flux " + nm + " (parcelIdFlux, massIdFlux)");
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaMemcpy(out, cs.faceFlux + ((long long)k * cs.nSpecies + species) * cs.nFacesAll,
+                           sizeof(double) * n, cudaMemcpyDeviceToHost));
     return DSMC_OK;
 }
 

@@ -127,8 +127,10 @@ __global__ void k_zero_step(Counters* ctr) {
 }
 
 // ---------------------------------------------------------------- fields
+// Species outside mask are left out of every sum (a dsmcVolFields typeIds
+// subset, dsmcVolFields.C:841).
 __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counters* ctr, int which, double* out,
-                        int measureMfp, double mfpTref) {
+                        int measureMfp, double mfpTref, unsigned mask) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cs.C) return;
     const double nT = (double)ctr->sampleSteps;
@@ -138,6 +140,7 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
     auto A = [&](int k) { return acc[(long long)k * C + c]; };
     double N = 0, M = 0, mom[3] = {0, 0, 0}, mcc = 0, Er = 0, zr = 0;
     for (int s = 0; s < cs.nSpecies; ++s) {
+        if (!((mask >> s) & 1u)) continue;
         const double S[SACC] = {A(s * SACC + 0), A(s * SACC + 1), A(s * SACC + 2), A(s * SACC + 3),
                                 A(s * SACC + 4), A(s * SACC + 5), A(s * SACC + 6)};
         const double m = cs.sp[s].m;
@@ -167,7 +170,7 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
         const double S[SACC] = {A(s * SACC + 0), A(s * SACC + 1), A(s * SACC + 2), A(s * SACC + 3),
                                 A(s * SACC + 4), A(s * SACC + 5), A(s * SACC + 6)};
         const SpeciesDev& sp = cs.sp[s];
-        if (!sp.nVib) continue;
+        if (!sp.nVib || !((mask >> s) & 1u)) continue;
         const double Ev = sp.kThetaV * S[SACC_VIB];
         double zeta = 0, Ts = 0;
         if (Ev > VSMALL && S[SACC_N] > SMALL) {
@@ -207,8 +210,10 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
         double mfp = 0, mcr = 0;
         if (Ttra > 1.0 && nT > 0) {
             for (int s = 0; s < cs.nSpecies; ++s) {
+                if (!((mask >> s) & 1u)) continue;
                 double smfp = 0, smcr = 0;
                 for (int q = 0; q < cs.nSpecies; ++q) {
+                    if (!((mask >> q) & 1u)) continue;
                     const double Sq[1] = {A(q * SACC + SACC_N)};
                     const double dPQ = 0.5 * (cs.sp[s].d + cs.sp[q].d);
                     const double oPQ = 0.5 * (cs.sp[s].omega + cs.sp[q].omega);
@@ -390,8 +395,8 @@ void launch_learn_compact(const CaseDev& cs, const StepBuffers& B, long long max
 void launch_zero_step(const StepBuffers& B, cudaStream_t st) { k_zero_step<<<1, 1, 0, st>>>(B.ctr); }
 
 void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* out, int measureMfp,
-                  double mfpTref, cudaStream_t st) {
-    k_field<<<(int)((cs.C + 255) / 256), 256, 0, st>>>(cs, B.acc, B.ctr, which, out, measureMfp, mfpTref);
+                  double mfpTref, unsigned mask, cudaStream_t st) {
+    k_field<<<(int)((cs.C + 255) / 256), 256, 0, st>>>(cs, B.acc, B.ctr, which, out, measureMfp, mfpTref, mask);
 }
 
 void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, double* out6, cudaStream_t st) {

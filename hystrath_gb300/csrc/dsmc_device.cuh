@@ -82,6 +82,16 @@ struct CaseDev {
     double lo[3], hi[3], dx[3], inv[3], negOinv[3];
     float invF[3], negOinvF[3];   // FP32 roundings of inv and negOinv (cell index screen)
     int sideDeletes[6];           // every face of the domain side deletes (dsmcDeletionPatch)
+    // reduced-D: an axis whose two sides are empty is tracked at the mesh
+    // centre with no velocity along it (dsmcParcel.C:73-84)
+    int emptyAx[3];
+    int anyEmpty;
+    double mid[3];                // mesh bounding-box midpoint
+    // dsmcFaceTracker: per face and species the signed parcel count and mass
+    // through every cell face (x faces, then y faces, then z faces), or null
+    double* faceFlux;             // [2][nSpecies][nFacesAll]
+    long long faceOff[3];
+    long long nFacesAll;
     double V;
     double FN, dt;
     double invDtFa[3];   // 1 / (dt * area of a face normal to each axis)

@@ -140,7 +140,7 @@ void launch_zero_step(const StepBuffers& B, cudaStream_t st);
 void launch_cellw(const CaseDev& cs, const Parcels& s, long long n, cudaStream_t st);
 void launch_remainder_init(const CaseDev& cs, double* rem, cudaStream_t st);
 void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* out,
-                  int measureMfp, double mfpTref, cudaStream_t st);
+                  int measureMfp, double mfpTref, unsigned speciesMask, cudaStream_t st);
 void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, double* out7,
                  cudaStream_t st);
 

@@ -122,6 +122,55 @@ __device__ void diffuse_reflect(const CaseDev& cs, Rng& r, int axis, double sgn,
     for (int a = 0; a < 3; ++a) U[a] += pt.Uwall[a];
 }
 
+// ---------------------------------------------------------------- face tracker
+// dsmcFaceTracker::trackFaceTransition (dsmcFaceTracker.C:124-190): every face
+// a parcel crosses gets sign(U . S) and sign(U . S) m, with S the face's
+// area vector (+axis for a face between two cells, outward for a boundary
+// face), and a cyclic crossing gets +1 on the face it leaves through.
+
+// face on axis a at plane index p, the other two cell indices from cell[]
+__device__ __forceinline__ long long face_index(const CaseDev& cs, int a, int p, const int* cell) {
+    const long long nx = cs.n[0], ny = cs.n[1];
+    if (a == 0) return cs.faceOff[0] + p + (nx + 1) * (cell[1] + ny * cell[2]);
+    if (a == 1) return cs.faceOff[1] + cell[0] + nx * (p + (ny + 1) * cell[2]);
+    return cs.faceOff[2] + cell[0] + nx * (cell[1] + ny * p);
+}
+
+__device__ __forceinline__ void face_add(const CaseDev& cs, long long f, int sp, double sgn) {
+    atomicAdd(cs.faceFlux + (long long)sp * cs.nFacesAll + f, sgn);
+    atomicAdd(cs.faceFlux + ((long long)cs.nSpecies + sp) * cs.nFacesAll + f, sgn * cs.sp[sp].m);
+}
+
+// the cell faces crossed on the straight path from x (in cell sc) to cell te,
+// in the order of their crossing times (ties: lower axis first)
+__device__ void track_internal(const CaseDev& cs, const double* x, const double* U, const int* sc, const int* te,
+                               int sp) {
+    int cur[3] = {sc[0], sc[1], sc[2]};
+    int left[3], dir[3];
+    double t[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < 3; ++a) {
+        const int d = te[a] - sc[a];
+        left[a] = d < 0 ? -d : d;
+        dir[a] = d > 0 ? 1 : -1;
+        if (left[a]) {
+            const int p = d > 0 ? sc[a] + 1 : sc[a];
+            t[a] = (cs.lo[a] + p * cs.dx[a] - x[a]) / U[a];
+        }
+    }
+    while (left[0] + left[1] + left[2] > 0) {
+        int a = -1;
+        for (int b = 0; b < 3; ++b)
+            if (left[b] && (a < 0 || t[b] < t[a])) a = b;
+        const int p = dir[a] > 0 ? cur[a] + 1 : cur[a];
+        face_add(cs, face_index(cs, a, p, cur), sp, dir[a] > 0 ? 1.0 : -1.0);
+        cur[a] += dir[a];
+        if (--left[a]) {
+            const int pn = dir[a] > 0 ? cur[a] + 1 : cur[a];
+            t[a] = (cs.lo[a] + pn * cs.dx[a] - x[a]) / U[a];
+        }
+    }
+}
+
 // Full Cartesian tracking of one parcel: the same steps as the CPU replay.
 // Returns the new cell word (CELLW_DELETED when removed).
 __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, uint32_t step,
@@ -153,11 +202,17 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
     for (int it = 0; !done; ++it) {
         if (!(tr > ROOTVSMALL)) break;
         if (it >= MAX_CROSSINGS) { *err |= ERRB_CROSSINGS; break; }
+        // tracking velocity: none along an empty (reduced-D) axis, whose
+        // coordinate is held at the mesh centre; U keeps all three components
+        double V[3] = {U[0], U[1], U[2]};
+        if (cs.anyEmpty)
+            for (int a = 0; a < 3; ++a)
+                if (cs.emptyAx[a]) { x[a] = cs.mid[a]; V[a] = 0.0; }
         double ex[3];
         int c2[3], ci[3];
         bool out = false;
         for (int a = 0; a < 3; ++a) {
-            ex[a] = fma(U[a], tr, x[a]);
+            ex[a] = fma(V[a], tr, x[a]);
             c2[a] = floor2_coord(cs, ex[a], a);
             ci[a] = c2[a] >> 1;
             if (ci[a] < 0 || ci[a] >= cs.n[a]) out = true;
@@ -173,6 +228,7 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             obst = ov;
         }
         if (!out && !obst) {
+            if (cs.faceFlux) track_internal(cs, x, V, sc, ci, type);
             x[0] = ex[0]; x[1] = ex[1]; x[2] = ex[2];
             result = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) |
                      (uint32_t)((c2[0] & 1) | ((c2[1] & 1) << 1) | ((c2[2] & 1) << 2));
@@ -183,12 +239,12 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
         int hitKind = -1, hitSide = -1;
         for (int a = 0; a < 3; ++a) {
             if (ci[a] < 0) {
-                double t = (cs.lo[a] - x[a]) / U[a];
+                double t = (cs.lo[a] - x[a]) / V[a];
                 if (!(t >= 0.0)) t = 0.0;
                 if (t > tr) t = tr;
                 if (t < tHit) { tHit = t; hitKind = 0; hitSide = 2 * a; }
             } else if (ci[a] >= cs.n[a]) {
-                double t = (cs.hi[a] - x[a]) / U[a];
+                double t = (cs.hi[a] - x[a]) / V[a];
                 if (!(t >= 0.0)) t = 0.0;
                 if (t > tr) t = tr;
                 if (t < tHit) { tHit = t; hitKind = 0; hitSide = 2 * a + 1; }
@@ -199,9 +255,9 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             int ax = -1;
             bool miss = false;
             for (int a = 0; a < 3; ++a) {
-                if (U[a] != 0.0) {
-                    const double t1 = (cs.obLo[o][a] - x[a]) / U[a];
-                    const double t2 = (cs.obHi[o][a] - x[a]) / U[a];
+                if (V[a] != 0.0) {
+                    const double t1 = (cs.obLo[o][a] - x[a]) / V[a];
+                    const double t2 = (cs.obHi[o][a] - x[a]) / V[a];
                     const double ta = dmin(t1, t2), tb = dmax(t1, t2);
                     if (ta > tin) { tin = ta; ax = a; }
                     if (tb < tout) tout = tb;
@@ -212,10 +268,11 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             if (!miss && ax >= 0 && tin >= 0.0 && tin < tout && tin <= tr && tin < tHit) {
                 tHit = tin;
                 hitKind = 1 + o;
-                hitSide = 2 * ax + (U[ax] > 0.0 ? 0 : 1);
+                hitSide = 2 * ax + (V[ax] > 0.0 ? 0 : 1);
             }
         }
         if (hitKind < 0) {
+            if (cs.faceFlux) track_internal(cs, x, V, sc, ci, type);
             x[0] = ex[0]; x[1] = ex[1]; x[2] = ex[2];
             result = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) |
                      (uint32_t)((c2[0] & 1) | ((c2[1] & 1) << 1) | ((c2[2] & 1) << 2));
@@ -226,7 +283,22 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
         double plane;
         if (hitKind == 0) plane = (hitSide & 1) ? cs.hi[axis] : cs.lo[axis];
         else plane = (hitSide & 1) ? cs.obHi[hitKind - 1][axis] : cs.obLo[hitKind - 1][axis];
-        for (int a = 0; a < 3; ++a) x[a] = (a == axis) ? plane : fma(U[a], tHit, x[a]);
+        double x0[3] = {x[0], x[1], x[2]};
+        for (int a = 0; a < 3; ++a) x[a] = (a == axis) ? plane : fma(V[a], tHit, x[a]);
+        // the fluid cell at the hit point and the plane index of the face hit
+        int hitCell[3], facePlane;
+        for (int a = 0; a < 3; ++a) {
+            const int cc = floor2_coord(cs, x[a], a) >> 1;
+            hitCell[a] = min(max(cc, 0), cs.n[a] - 1);
+        }
+        if (hitKind == 0) {
+            facePlane = (hitSide & 1) ? cs.n[axis] : 0;
+            hitCell[axis] = (hitSide & 1) ? cs.n[axis] - 1 : 0;
+        } else {
+            facePlane = (hitSide & 1) ? cs.obHiI[hitKind - 1][axis] : cs.obLoI[hitKind - 1][axis];
+            hitCell[axis] = (hitSide & 1) ? facePlane : facePlane - 1;
+        }
+        if (cs.faceFlux) track_internal(cs, x0, V, sc, hitCell, type);
         tr = tr - tHit;
         const int b = (axis == 0) ? 1 : 0;
         const int c = (axis == 2) ? 1 : 2;
@@ -257,6 +329,9 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             U[axis] = -U[axis];
         } else if (pt.type == DSMC_PATCH_CYCLIC) {
             if (hitKind == 0) x[axis] = (hitSide & 1) ? cs.lo[axis] : cs.hi[axis];
+            // hitCyclicPatch moves the parcel onto the receiving face, and
+            // the tracker adds +1 to that face's coupled face: the exit face
+            if (cs.faceFlux && hitKind == 0) face_add(cs, face_index(cs, axis, facePlane, hitCell), type, 1.0);
         } else if (pt.model == DSMC_BC_SPECULAR || pt.model == DSMC_BC_DIFFUSE) {
             double preE, preM[3];
             if (cs.hasWallMeasure)
@@ -271,10 +346,15 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             atomicAdd(hits, 1ull);
         } else {
             // deletion (and any patch without a model) removes the parcel
+            if (cs.faceFlux)
+                face_add(cs, face_index(cs, axis, facePlane, hitCell), type, U[axis] * sgn > 0.0 ? 1.0 : -1.0);
             result = CELLW_DELETED;
             done = true;
             break;
         }
+        // a reflected parcel is counted on the face with its new velocity
+        if (cs.faceFlux && pt.type != DSMC_PATCH_CYCLIC)
+            face_add(cs, face_index(cs, axis, facePlane, hitCell), type, U[axis] * sgn > 0.0 ? 1.0 : -1.0);
         for (int a = 0; a < 3; ++a) {
             int cc = floor2_coord(cs, x[a], a) >> 1;
             sc[a] = min(max(cc, 0), cs.n[a] - 1);
@@ -383,8 +463,16 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                 const bool fresh = (w & CELLW_FRESH) != 0;
                 double2* q = reinterpret_cast<double2*>(s.r + i);
                 const double2 q0 = q[0], q1 = q[1], q2 = q[2];
-                const double x = q0.x, y = q0.y, z = q1.x;
+                double x = q0.x, y = q0.y, z = q1.x;
                 const double ux = q1.y, uy = q2.x, uz = q2.y;
+                // tracking velocity (zero along an empty axis, whose coordinate
+                // is held at the mesh centre: dsmcParcel.C:73-84)
+                double tux = ux, tuy = uy, tuz = uz;
+                if (cs.anyEmpty) {
+                    if (cs.emptyAx[0]) { x = cs.mid[0]; tux = 0.0; }
+                    if (cs.emptyAx[1]) { y = cs.mid[1]; tuy = 0.0; }
+                    if (cs.emptyAx[2]) { z = cs.mid[2]; tuz = 0.0; }
+                }
                 double tr = cs.dt;
                 if (fresh) {
                     // a parcel inserted this step moves for (1 - U) dt
@@ -400,9 +488,9 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     ser = q3.x;
                     svb = sv_vib(sv);
                 }
-                const double ex = fma(ux, tr, x);
-                const double ey = fma(uy, tr, y);
-                const double ez = fma(uz, tr, z);
+                const double ex = fma(tux, tr, x);
+                const double ey = fma(tuy, tr, y);
+                const double ez = fma(tuz, tr, z);
                 const int c2x = floor2_coord_fast(cs, ex, 0);
                 const int c2y = floor2_coord_fast(cs, ey, 1);
                 const int c2z = floor2_coord_fast(cs, ez, 2);
@@ -418,7 +506,7 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     const int a = !inX ? 0 : !inY ? 1 : 2;
                     const int c2a = a == 0 ? c2x : a == 1 ? c2y : c2z;
                     const int side = 2 * a + (c2a < 0 ? 0 : 1);
-                    if (cs.sideDeletes[side]) delSide = side;
+                    if (cs.sideDeletes[side] && !cs.faceFlux) delSide = side;
                 }
                 if ((inside || delSide >= 0) && cs.nObst) {
                     const uint32_t c = cellw_cell(w);
@@ -438,6 +526,16 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     s.cellw[i] = CELLW_DELETED;
                     fast = true;
                 } else if (inside) {
+                    if (cs.faceFlux) {
+                        const uint32_t c0 = cellw_cell(w);
+                        const int sc[3] = {(int)(c0 % (uint32_t)cs.n[0]),
+                                           (int)((c0 / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]),
+                                           (int)(c0 / ((uint32_t)cs.n[0] * (uint32_t)cs.n[1]))};
+                        const int te[3] = {cx, cy, cz};
+                        const double xs[3] = {x, y, z}, Us[3] = {tux, tuy, tuz};
+                        const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q[3].y) >> 32);
+                        track_internal(cs, xs, Us, sc, te, sv_species(sv));
+                    }
                     q[0] = make_double2(ex, ey);
                     s.r[i].z = ez;
                     const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
@@ -852,6 +950,13 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
         p.sv = make_sv(m, vib);
         st_rec(s.r + slot, p);
         s.cellw[slot] = ((uint32_t)cellOf[f] << 3) | CELLW_FRESH;
+        if (cs.faceFlux) {
+            // dsmcCloud::addNewParcel counts an inserted parcel on its face
+            // (dsmcCloud.C:425-437): moving inwards, against the outward normal
+            const int cc = cellOf[f];
+            const int cell3[3] = {(int)(cc % cs.n[0]), (int)((cc / cs.n[0]) % cs.n[1]), (int)(cc / (cs.n[0] * cs.n[1]))};
+            face_add(cs, face_index(cs, a, (sd & 1) ? cs.n[a] : 0, cell3), m, -1.0);
+        }
     }
     if (err) atomicOr(&ctr->err, err);
 }

@@ -43,11 +43,16 @@ def _load() -> C.CDLL:
     L.dsmc_get_cell_array.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
     L.dsmc_set_cell_array.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
     L.dsmc_get_field.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
+    L.dsmc_get_species_field.argtypes = [vp, C.c_char_p, C.c_uint, vp, C.c_longlong]
     L.dsmc_get_wall_field.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
     L.dsmc_n_boundary_faces.argtypes = [vp]
     L.dsmc_n_boundary_faces.restype = C.c_longlong
     L.dsmc_reset_sampling.argtypes = [vp]
     L.dsmc_write_fields.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p]
+    L.dsmc_set_face_tracking.argtypes = [vp, C.c_int]
+    L.dsmc_n_faces.argtypes = [vp]
+    L.dsmc_n_faces.restype = C.c_longlong
+    L.dsmc_get_face_flux.argtypes = [vp, C.c_char_p, C.c_int, vp, C.c_longlong]
     L.dsmc_info.argtypes = [vp, C.POINTER(S.Info)]
     L.dsmc_checkpoint.argtypes = [vp, C.c_char_p]
     L.dsmc_restore.argtypes = [vp, C.c_char_p]
@@ -196,9 +201,17 @@ class DsmcCloud:
         a = np.ascontiguousarray(a, dtype=np.float64)
         self._chk(lib().dsmc_set_cell_array(self.h, name.encode(), _p(a), a.size))
 
-    def field(self, name: str):
+    def field(self, name: str, species=None):
+        """A dsmcVolFields field over all species, or over the species
+        indices in ``species`` (the entry's typeIds)."""
         a = np.empty(self.n_cells)
-        self._chk(lib().dsmc_get_field(self.h, name.encode(), _p(a), a.size))
+        if species is None:
+            self._chk(lib().dsmc_get_field(self.h, name.encode(), _p(a), a.size))
+        else:
+            mask = 0
+            for s in ([species] if isinstance(species, int) else species):
+                mask |= 1 << int(s)
+            self._chk(lib().dsmc_get_species_field(self.h, name.encode(), mask, _p(a), a.size))
         return a
 
     def wall_accumulators(self):
@@ -215,6 +228,15 @@ class DsmcCloud:
 
     def reset_sampling(self):
         self._chk(lib().dsmc_reset_sampling(self.h))
+
+    def set_face_tracking(self, on: bool = True):
+        self._chk(lib().dsmc_set_face_tracking(self.h, 1 if on else 0))
+
+    def face_flux(self, name: str = "parcelIdFlux", species: int = 0):
+        n = lib().dsmc_n_faces(self.h)
+        out = np.empty(n)
+        self._chk(lib().dsmc_get_face_flux(self.h, name.encode(), int(species), _p(out), n))
+        return out
 
     def write_fields(self, case_dir: str, time_name: str, field_name: str = ""):
         """The averaged fields as OpenFOAM files in case_dir/time_name."""

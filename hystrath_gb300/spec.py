@@ -23,7 +23,7 @@ NAME_LEN = 64
 OK = 0
 ERR_IO, ERR_PARSE, ERR_UNKNOWN_MODEL, ERR_INVALID, ERR_CUDA, ERR_DEVICE, ERR_CAPACITY, ERR_NO_DEVICE = range(1, 9)
 
-PATCH_WALL, PATCH_PATCH, PATCH_SYMMETRY, PATCH_CYCLIC = range(4)
+PATCH_WALL, PATCH_PATCH, PATCH_SYMMETRY, PATCH_CYCLIC, PATCH_EMPTY = range(5)
 BC_NONE, BC_SPECULAR, BC_DIFFUSE, BC_DELETION = range(4)
 COLL_VHS, COLL_LB_VHS, COLL_VSS, COLL_LB_VSS = range(4)
 SEL_NTC, SEL_SBT = 0, 1

@@ -59,7 +59,8 @@ enum {
     DSMC_PATCH_WALL = 0,     /* wall: dispatched to a dsmcPatchBoundary model */
     DSMC_PATCH_PATCH = 1,    /* patch: dispatched to a dsmcPatchBoundary model */
     DSMC_PATCH_SYMMETRY = 2, /* symmetry / symmetryPlane: specular transform */
-    DSMC_PATCH_CYCLIC = 3    /* cyclic: periodic translation to the opposite side */
+    DSMC_PATCH_CYCLIC = 3,   /* cyclic: periodic translation to the opposite side */
+    DSMC_PATCH_EMPTY = 4     /* empty: reduced-D axis, one cell thick, both sides */
 };
 
 /* dsmcPatchBoundary models (boundariesDict dsmcPatchBoundaries). */
@@ -249,6 +250,11 @@ int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long l
  * n must equal the number of cells. */
 int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n);
 
+/* The same field over a subset of the species (bit s of species_mask selects
+ * species s): a dsmcVolFields entry with its own typeIds list
+ * (dsmcVolFields.C:841), e.g. Ttra_N2 of the N2/O2 Couette case. */
+int dsmc_get_species_field(dsmc_handle* h, const char* name, unsigned species_mask, double* out, long long n);
+
 /* Per-boundary-face wall fields: "wallHeatFlux", "wallShearStress_x|y|z",
  * "rhoN_wall"; n = number of boundary faces (dsmc_info boundary face count). */
 int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long n);
@@ -264,6 +270,21 @@ int dsmc_reset_sampling(dsmc_handle* h);
  * in the order of the case's blockMeshDict when case_dir has one (block by
  * block, i fastest), else in the Cartesian order i + nx (j + ny k). */
 int dsmc_write_fields(dsmc_handle* h, const char* case_dir, const char* time_name, const char* field_name);
+
+/* dsmcFaceTracker (faceTracker/dsmcFaceTracker.C:124-190, dsmcCloud.C:425-437):
+ * with tracking on, every cell face a parcel crosses in the move gets
+ * sign(U . S) ("parcelIdFlux") and sign(U . S) m ("massIdFlux") for the
+ * parcel's species, S the face's area vector (+axis between two cells,
+ * outward on a boundary face, the velocity after a wall or symmetry
+ * interaction); a cyclic crossing counts +1 on the face it leaves through
+ * and an inserted parcel counts -1 on its inflow face.  Sums over the steps
+ * since the last dsmc_reset_sampling (the reference clears them every step).
+ * Faces: x faces i + (nx+1)(j + ny k), then y faces i + nx(j + (ny+1) k),
+ * then z faces i + nx(j + ny k), n = dsmc_n_faces.  Off by default (it adds
+ * a division per crossing and two atomics per face). */
+int dsmc_set_face_tracking(dsmc_handle* h, int on);
+long long dsmc_n_faces(const dsmc_handle* h);
+int dsmc_get_face_flux(dsmc_handle* h, const char* name, int species, double* out, long long n);
 
 int dsmc_info(dsmc_handle* h, dsmc_info_t* out);
 

@@ -190,6 +190,8 @@ struct Oracle {
     int n[3];
     long long C;
     double lo[3], hi[3], dx[3], inv[3], negOinv[3];
+    double mid[3];          // mesh bounding-box midpoint
+    int emptyAx[3];         // reduced-D: both sides of the axis are empty patches
     double V;
     std::vector<Species> sp;
     std::vector<uint8_t> solid;
@@ -208,6 +210,8 @@ struct Oracle {
     int nAcc;
     std::vector<WallAcc> wall;
     std::vector<double> inflowAcc;              // [nBFaces][nSpecies]
+    std::vector<double> faceFlux;               // [2][nSpecies][nFacesAll]; empty: tracking off
+    long long faceOff[3], nFacesAll;
     long long step;
     uint32_t nextId;
     long long sampleSteps;
@@ -235,6 +239,46 @@ struct Oracle {
         *cell = ci[0] + n[0] * (ci[1] + n[1] * ci[2]);
         *sub = sb;
     }
+    // ------------------------------------------------------------ face tracker
+    // dsmcFaceTracker::trackFaceTransition (dsmcFaceTracker.C:124-190):
+    // sign(U . S) and sign(U . S) m on every face crossed, S = +axis inside
+    // and outward on the boundary.  Faces: x faces, then y, then z.
+    long long faceIndex(int a, long long p, const int* cell) const {
+        const long long nx = n[0], ny = n[1];
+        if (a == 0) return faceOff[0] + p + (nx + 1) * (cell[1] + ny * cell[2]);
+        if (a == 1) return faceOff[1] + cell[0] + nx * (p + (ny + 1) * cell[2]);
+        return faceOff[2] + cell[0] + nx * (cell[1] + ny * p);
+    }
+    void faceAdd(long long f, int m, double sgn) {
+        double* a = &faceFlux[(size_t)m * nFacesAll + f];
+        double* b = &faceFlux[((size_t)spec.n_species + m) * nFacesAll + f];
+        const double dm = sgn * sp[m].m;
+#pragma omp atomic
+        *a += sgn;
+#pragma omp atomic
+        *b += dm;
+    }
+    // faces crossed on the straight path from x in cell sc to cell te, in the
+    // order of their crossing times (ties: the lower axis first)
+    void trackInternal(const double* x, const double* U, const int* sc, const int* te, int m) {
+        int cur[3] = {sc[0], sc[1], sc[2]}, left[3], dir[3];
+        double t[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < 3; ++a) {
+            const int d = te[a] - sc[a];
+            left[a] = std::abs(d);
+            dir[a] = d > 0 ? 1 : -1;
+            if (left[a]) t[a] = (lo[a] + (d > 0 ? sc[a] + 1 : sc[a]) * dx[a] - x[a]) / U[a];
+        }
+        while (left[0] + left[1] + left[2] > 0) {
+            int a = -1;
+            for (int b = 0; b < 3; ++b)
+                if (left[b] && (a < 0 || t[b] < t[a])) a = b;
+            faceAdd(faceIndex(a, dir[a] > 0 ? cur[a] + 1 : cur[a], cur), m, dir[a] > 0 ? 1.0 : -1.0);
+            cur[a] += dir[a];
+            if (--left[a]) t[a] = (lo[a] + (dir[a] > 0 ? cur[a] + 1 : cur[a]) * dx[a] - x[a]) / U[a];
+        }
+    }
+
     int patchOfSideFace(int s, long long f) const {
         const int* fp = spec.face_patch[s];
         return fp ? fp[f] : spec.side_patch[s];
@@ -281,6 +325,11 @@ struct Oracle {
                 facePatchStore.emplace_back(s->face_patch[q], s->face_patch[q] + (long long)n[b] * n[c]);
                 spec.face_patch[q] = facePatchStore.back().data();
             }
+        }
+        for (int a = 0; a < 3; ++a) {
+            mid[a] = 0.5 * (lo[a] + hi[a]);
+            const int p = spec.face_patch[2 * a] ? spec.face_patch[2 * a][0] : spec.side_patch[2 * a];
+            emptyAx[a] = spec.patches[p].type == DSMC_PATCH_EMPTY;
         }
         C = (long long)n[0] * n[1] * n[2];
         V = dx[0] * dx[1] * dx[2];
@@ -542,12 +591,17 @@ struct Oracle {
         for (int it = 0;; ++it) {
             if (!(tr > ROOTVSMALL)) break;
             if (it >= MAX_CROSSINGS) { *e = 1; break; }
+            // dsmcParcel.C:73-84: the position is held at the mesh centre and
+            // the tracking velocity is zero along a reduced-D (empty) axis
+            double V[3] = {p.U[0], p.U[1], p.U[2]};
+            for (int a = 0; a < 3; ++a)
+                if (emptyAx[a]) { p.x[a] = mid[a]; V[a] = 0.0; }
             double ex[3];
             long long c2[3];
             int ci[3];
             bool out = false;
             for (int a = 0; a < 3; ++a) {
-                ex[a] = std::fma(p.U[a], tr, p.x[a]);
+                ex[a] = std::fma(V[a], tr, p.x[a]);
                 c2[a] = floor2(ex[a], a);
                 ci[a] = (int)(c2[a] >> 1);
                 if (ci[a] < 0 || ci[a] >= n[a]) out = true;
@@ -564,6 +618,7 @@ struct Oracle {
                 obst = ov;
             }
             if (!out && !obst) {
+                if (!faceFlux.empty()) trackInternal(p.x, V, startCell, ci, p.type);
                 for (int a = 0; a < 3; ++a) p.x[a] = ex[a];
                 int sb = 0;
                 for (int a = 0; a < 3; ++a) sb |= (int)(c2[a] & 1) << a;
@@ -576,12 +631,12 @@ struct Oracle {
             int hitKind = -1, hitSide = -1;   // kind 0: domain side, 1+o: obstacle o
             for (int a = 0; a < 3; ++a) {
                 if (ci[a] < 0) {
-                    double t = (lo[a] - p.x[a]) / p.U[a];
+                    double t = (lo[a] - p.x[a]) / V[a];
                     if (!(t >= 0.0)) t = 0.0;
                     if (t > tr) t = tr;
                     if (t < tHit) { tHit = t; hitKind = 0; hitSide = 2 * a; }
                 } else if (ci[a] >= n[a]) {
-                    double t = (hi[a] - p.x[a]) / p.U[a];
+                    double t = (hi[a] - p.x[a]) / V[a];
                     if (!(t >= 0.0)) t = 0.0;
                     if (t > tr) t = tr;
                     if (t < tHit) { tHit = t; hitKind = 0; hitSide = 2 * a + 1; }
@@ -592,9 +647,9 @@ struct Oracle {
                 int ax = -1;
                 bool miss = false;
                 for (int a = 0; a < 3; ++a) {
-                    if (p.U[a] != 0.0) {
-                        const double t1 = (obLo[o][a] - p.x[a]) / p.U[a];
-                        const double t2 = (obHi[o][a] - p.x[a]) / p.U[a];
+                    if (V[a] != 0.0) {
+                        const double t1 = (obLo[o][a] - p.x[a]) / V[a];
+                        const double t2 = (obHi[o][a] - p.x[a]) / V[a];
                         const double ta = std::min(t1, t2), tb = std::max(t1, t2);
                         if (ta > tin) { tin = ta; ax = a; }
                         if (tb < tout) tout = tb;
@@ -605,11 +660,12 @@ struct Oracle {
                 if (!miss && ax >= 0 && tin >= 0.0 && tin < tout && tin <= tr && tin < tHit) {
                     tHit = tin;
                     hitKind = 1 + o;
-                    hitSide = 2 * ax + (p.U[ax] > 0.0 ? 0 : 1);
+                    hitSide = 2 * ax + (V[ax] > 0.0 ? 0 : 1);
                 }
             }
             if (hitKind < 0) {
                 // obstacle candidate without an actual hit
+                if (!faceFlux.empty()) trackInternal(p.x, V, startCell, ci, p.type);
                 for (int a = 0; a < 3; ++a) p.x[a] = ex[a];
                 int sb = 0;
                 for (int a = 0; a < 3; ++a) sb |= (int)(c2[a] & 1) << a;
@@ -621,7 +677,24 @@ struct Oracle {
             double plane;
             if (hitKind == 0) plane = (hitSide & 1) ? hi[axis] : lo[axis];
             else plane = (hitSide & 1) ? obHi[hitKind - 1][axis] : obLo[hitKind - 1][axis];
-            for (int a = 0; a < 3; ++a) p.x[a] = (a == axis) ? plane : std::fma(p.U[a], tHit, p.x[a]);
+            double x0[3] = {p.x[0], p.x[1], p.x[2]};
+            for (int a = 0; a < 3; ++a) p.x[a] = (a == axis) ? plane : std::fma(V[a], tHit, p.x[a]);
+            // the fluid cell at the hit point and the plane index of the face hit
+            int hitCell[3];
+            long long facePlane;
+            for (int a = 0; a < 3; ++a) {
+                const long long cc = floor2(p.x[a], a) >> 1;
+                hitCell[a] = (int)std::min<long long>(std::max<long long>(cc, 0), n[a] - 1);
+            }
+            if (hitKind == 0) {
+                facePlane = (hitSide & 1) ? n[axis] : 0;
+                hitCell[axis] = (hitSide & 1) ? n[axis] - 1 : 0;
+            } else {
+                const dsmc_obstacle& ob = spec.obstacles[hitKind - 1];
+                facePlane = (hitSide & 1) ? ob.hi[axis] : ob.lo[axis];
+                hitCell[axis] = (int)((hitSide & 1) ? facePlane : facePlane - 1);
+            }
+            if (!faceFlux.empty()) trackInternal(x0, V, startCell, hitCell, p.type);
             tr = tr - tHit;
             long long bf;
             int patch;
@@ -636,7 +709,16 @@ struct Oracle {
                 patch = bfPatch[bf];
                 sgn = (hitSide & 1) ? -1.0 : 1.0;       // normal pointing into the solid
             }
-            if (!applyPatch(p, r, patch, bf, axis, sgn, e, hits)) {
+            const bool kept = applyPatch(p, r, patch, bf, axis, sgn, e, hits);
+            if (!faceFlux.empty()) {
+                // after the interaction (deletion: the unchanged velocity); a
+                // cyclic crossing counts +1 on the face it leaves through
+                const bool cyc = spec.patches[patch].type == DSMC_PATCH_CYCLIC;
+                if (!cyc || hitKind == 0)
+                    faceAdd(faceIndex(axis, facePlane, hitCell), p.type,
+                            cyc ? 1.0 : (p.U[axis] * sgn > 0.0 ? 1.0 : -1.0));
+            }
+            if (!kept) {
                 p.cell = -1;
                 return;
             }
@@ -727,6 +809,11 @@ struct Oracle {
                         p.type = m;
                         p.cell = cell;
                         p.fresh = 1;
+                        if (!faceFlux.empty()) {
+                            // dsmcCloud::addNewParcel (dsmcCloud.C:425-437)
+                            const int c3[3] = {(int)cc[0], (int)cc[1], (int)cc[2]};
+                            faceAdd(faceIndex(a, (side & 1) ? n[a] : 0, c3), m, -1.0);
+                        }
                         added.push_back(p);
                     }
                 }
@@ -1306,6 +1393,26 @@ int oracle_get_wall(oracle_handle* h, double* out) {
 }
 
 long long oracle_n_boundary_faces(oracle_handle* h) { return h->o.nBFaces; }
+
+int oracle_set_face_tracking(oracle_handle* h, int on) {
+    Oracle& o = h->o;
+    const long long nx = o.n[0], ny = o.n[1], nz = o.n[2];
+    o.faceOff[0] = 0;
+    o.faceOff[1] = (nx + 1) * ny * nz;
+    o.faceOff[2] = o.faceOff[1] + nx * (ny + 1) * nz;
+    o.nFacesAll = o.faceOff[2] + nx * ny * (nz + 1);
+    if (on) o.faceFlux.assign(2 * (size_t)o.spec.n_species * o.nFacesAll, 0.0);
+    else o.faceFlux.clear();
+    return DSMC_OK;
+}
+
+// [2][nSpecies][nFaces]: parcelIdFlux then massIdFlux
+int oracle_get_face_flux(oracle_handle* h, double* out) {
+    const Oracle& o = h->o;
+    if (o.faceFlux.empty()) return DSMC_ERR_INVALID;
+    std::memcpy(out, o.faceFlux.data(), sizeof(double) * o.faceFlux.size());
+    return DSMC_OK;
+}
 
 int oracle_info(oracle_handle* h, dsmc_info_t* out) {
     const Oracle& o = h->o;

@@ -48,6 +48,8 @@ def lib() -> C.CDLL:
         L.oracle_n_boundary_faces.restype = C.c_longlong
         L.oracle_n_boundary_faces.argtypes = [vp]
         L.oracle_n_accumulators.argtypes = [vp]
+        L.oracle_set_face_tracking.argtypes = [vp, C.c_int]
+        L.oracle_get_face_flux.argtypes = [vp, vp]
         L.oracle_info.argtypes = [vp, C.POINTER(S.Info)]
         L.oracle_philox.argtypes = [C.POINTER(C.c_uint), C.POINTER(C.c_uint), C.POINTER(C.c_uint)]
         L.oracle_u01_from.restype = C.c_double
@@ -142,6 +144,16 @@ class OracleCloud:
         a = np.empty((nf, 14))
         self._chk(lib().oracle_get_wall(self.h, _p(a)))
         return a
+
+    def set_face_tracking(self, on: bool = True):
+        self._chk(lib().oracle_set_face_tracking(self.h, 1 if on else 0))
+
+    def face_flux(self, name: str = "parcelIdFlux", species: int = 0):
+        n = list(self.spec.n_cells)
+        nf = (n[0] + 1) * n[1] * n[2] + n[0] * (n[1] + 1) * n[2] + n[0] * n[1] * (n[2] + 1)
+        a = np.empty((2, self.spec.n_species, nf))
+        self._chk(lib().oracle_get_face_flux(self.h, _p(a)))
+        return a[{"parcelIdFlux": 0, "massIdFlux": 1}[name], species].copy()
 
     def info(self) -> S.Info:
         i = S.Info()
