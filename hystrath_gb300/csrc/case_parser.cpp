@@ -20,6 +20,7 @@
 // Unknown model names are rejected with the list of valid names, as the
 // reference's runtime-selection tables do.
 
+#include <algorithm>
 #include <array>
 #include <cctype>
 #include <cmath>
@@ -316,10 +317,154 @@ std::string fileIn(const std::string& dir, const char* a, const char* b = nullpt
 }
 
 // ------------------------------------------------------------------ mesh
+// A hex block of blockMesh on the axis-aligned grid: its bounds, its cells
+// along each global axis, the global axis and direction of each of its local
+// directions (v0->v1, v0->v3, v0->v4) and its node coordinates along each
+// global axis, ascending.
 struct Block {
     double lo[3], hi[3];
     int n[3];
+    int ax[3], dir[3];
+    int cnt[3];                   // cells along the local directions
+    std::vector<double> nodes[3];
 };
+
+// blockMesh's division of an edge of expansion ratio r into n cells
+// (lineDivide): the widths grow geometrically, last / first = r.
+std::vector<double> edge_division(int n, double r) {
+    std::vector<double> lam((size_t)n + 1);
+    if (n == 1 || std::fabs(r - 1.0) < 1e-12) {
+        for (int i = 0; i <= n; ++i) lam[i] = (double)i / n;
+    } else {
+        const double q = std::pow(r, 1.0 / (n - 1));
+        for (int i = 0; i <= n; ++i) lam[i] = (1.0 - std::pow(q, i)) / (1.0 - std::pow(q, n));
+    }
+    lam[0] = 0.0;
+    lam[n] = 1.0;
+    return lam;
+}
+
+std::vector<Block> parse_blocks(const Node& bn, const std::vector<std::array<double, 3>>& V) {
+    std::vector<Block> blocks;
+    for (size_t i = 0; i < bn.items.size(); ++i) {
+        const Node& it = *bn.items[i];
+        if (!(it.kind == Node::VALUE && !it.words.empty() && it.words[0] == "hex")) continue;
+        // hex (v0..v7) [zoneName] (n1 n2 n3) simpleGrading (g1 g2 g3) | edgeGrading (12)
+        if (i + 3 >= bn.items.size()) throw ParseError(DSMC_ERR_PARSE, "incomplete hex block");
+        auto ids = numList(*bn.items[i + 1], "hex vertices");
+        size_t ci = i + 2;
+        if (bn.items[ci]->kind == Node::VALUE) ++ci;   // cell zone name
+        if (ci + 1 >= bn.items.size()) throw ParseError(DSMC_ERR_PARSE, "incomplete hex block");
+        auto cnt = numList(*bn.items[ci], "hex cell counts");
+        if (ids.size() != 8 || cnt.size() != 3) throw ParseError(DSMC_ERR_PARSE, "malformed hex block");
+        const Node& gw = *bn.items[ci + 1];
+        size_t gi = ci;
+        double g[3] = {1.0, 1.0, 1.0};
+        if (gw.kind == Node::VALUE && !gw.words.empty() &&
+            (gw.words[0] == "simpleGrading" || gw.words[0] == "edgeGrading")) {
+            if (ci + 2 >= bn.items.size()) throw ParseError(DSMC_ERR_PARSE, "grading without values");
+            const Node& gl = *bn.items[ci + 2];
+            for (auto& e : gl.items)
+                if (e->kind != Node::VALUE)
+                    throw ParseError(DSMC_ERR_INVALID, "multi-section grading is not supported on this path");
+            auto gv = numList(gl, "grading");
+            if (gw.words[0] == "simpleGrading") {
+                if (gv.size() != 3) throw ParseError(DSMC_ERR_PARSE, "simpleGrading needs 3 ratios");
+                for (int l = 0; l < 3; ++l) g[l] = gv[l];
+            } else {
+                if (gv.size() != 12) throw ParseError(DSMC_ERR_PARSE, "edgeGrading needs 12 ratios");
+                for (int l = 0; l < 3; ++l) {
+                    for (int e = 1; e < 4; ++e)
+                        if (std::fabs(gv[4 * l + e] - gv[4 * l]) > 1e-12 * std::fabs(gv[4 * l]))
+                            throw ParseError(DSMC_ERR_INVALID, "edgeGrading with unequal parallel edges is not rectilinear");
+                    g[l] = gv[4 * l];
+                }
+            }
+            gi = ci + 2;
+        }
+        Block b{};
+        for (int a = 0; a < 3; ++a) { b.lo[a] = 1e300; b.hi[a] = -1e300; }
+        for (double id : ids) {
+            const auto& p = V.at((size_t)id);
+            for (int a = 0; a < 3; ++a) {
+                b.lo[a] = std::min(b.lo[a], p[a]);
+                b.hi[a] = std::max(b.hi[a], p[a]);
+            }
+        }
+        for (double id : ids) {
+            const auto& p = V.at((size_t)id);
+            for (int a = 0; a < 3; ++a) {
+                const double tol = 1e-9 * (b.hi[a] - b.lo[a] + 1e-300);
+                if (std::fabs(p[a] - b.lo[a]) > tol && std::fabs(p[a] - b.hi[a]) > tol)
+                    throw ParseError(DSMC_ERR_INVALID, "hex block is not an axis-aligned box");
+            }
+        }
+        // local directions: v0 -> v1, v0 -> v3, v0 -> v4
+        const auto& v0 = V.at((size_t)ids[0]);
+        const int other[3] = {1, 3, 4};
+        int used = 0;
+        for (int l = 0; l < 3; ++l) {
+            const auto& v = V.at((size_t)ids[other[l]]);
+            int axis = -1;
+            for (int a = 0; a < 3; ++a) {
+                const double tol = 1e-9 * (b.hi[a] - b.lo[a] + 1e-300);
+                if (std::fabs(v[a] - v0[a]) > tol) {
+                    if (axis >= 0) throw ParseError(DSMC_ERR_INVALID, "hex block edge is not axis-aligned");
+                    axis = a;
+                }
+            }
+            if (axis < 0 || (used >> axis) & 1) throw ParseError(DSMC_ERR_INVALID, "degenerate hex block");
+            used |= 1 << axis;
+            b.ax[l] = axis;
+            b.dir[l] = v[axis] > v0[axis] ? 1 : -1;
+            b.cnt[l] = (int)cnt[l];
+            if (b.cnt[l] < 1) throw ParseError(DSMC_ERR_INVALID, "hex block with no cells");
+            b.n[axis] = b.cnt[l];
+            const double L = b.hi[axis] - b.lo[axis];
+            const std::vector<double> lam = edge_division(b.cnt[l], g[l]);
+            std::vector<double>& nd = b.nodes[axis];
+            nd.resize(lam.size());
+            for (size_t k = 0; k < lam.size(); ++k)
+                nd[b.dir[l] > 0 ? k : lam.size() - 1 - k] = b.dir[l] > 0 ? b.lo[axis] + L * lam[k]
+                                                                       : b.hi[axis] - L * lam[k];
+            nd.front() = b.lo[axis];
+            nd.back() = b.hi[axis];
+        }
+        blocks.push_back(b);
+        i = gi;
+    }
+    return blocks;
+}
+
+// The global nodes of every axis from the blocks' nodes; blocks must meet
+// node to node (a rectilinear grid).  Returns true when the axis is uniform.
+bool merge_axis_nodes(const std::vector<Block>& blocks, int a, std::vector<double>& out) {
+    double lo = 1e300, hi = -1e300;
+    for (auto& b : blocks) { lo = std::min(lo, b.lo[a]); hi = std::max(hi, b.hi[a]); }
+    const double tol = 1e-9 * (hi - lo);
+    std::vector<double> all;
+    for (auto& b : blocks) all.insert(all.end(), b.nodes[a].begin(), b.nodes[a].end());
+    std::sort(all.begin(), all.end());
+    out.clear();
+    for (double x : all)
+        if (out.empty() || x - out.back() > tol) out.push_back(x);
+    for (auto& b : blocks) {
+        size_t k = 0;
+        while (k < out.size() && out[k] < b.lo[a] - tol) ++k;
+        for (double x : b.nodes[a]) {
+            if (k >= out.size() || std::fabs(out[k] - x) > tol)
+                throw ParseError(DSMC_ERR_INVALID, "blocks whose cells do not meet face to face are not supported");
+            ++k;
+        }
+    }
+    const double w0 = (out.back() - out.front()) / (double)(out.size() - 1);
+    bool uniform = true;
+    for (size_t k = 1; k < out.size(); ++k)
+        if (std::fabs((out[k] - out[k - 1]) - w0) > 1e-9 * w0) uniform = false;
+    return uniform;
+}
+
+thread_local std::vector<double> g_nodes[3];
 
 void readMesh(const std::string& dir, dsmc_case_spec* s, std::map<std::string, int>& patchIds,
               std::vector<std::string>& patchTypes) {
@@ -334,68 +479,30 @@ void readMesh(const std::string& dir, dsmc_case_spec* s, std::map<std::string, i
         V.push_back({c[0] * scale, c[1] * scale, c[2] * scale});
     }
     const Node& bn = need(bm.get(), "blocks", path);
-    std::vector<Block> blocks;
-    for (size_t i = 0; i < bn.items.size(); ++i) {
-        const Node& it = *bn.items[i];
-        if (it.kind == Node::VALUE && !it.words.empty() && it.words[0] == "hex") {
-            // hex (v0..v7) (nx ny nz) simpleGrading (gx gy gz)
-            if (i + 3 >= bn.items.size()) throw ParseError(DSMC_ERR_PARSE, "incomplete hex block");
-            auto ids = numList(*bn.items[i + 1], "hex vertices");
-            auto cnt = numList(*bn.items[i + 2], "hex cell counts");
-            const Node& gw = *bn.items[i + 3];
-            if (ids.size() != 8 || cnt.size() != 3) throw ParseError(DSMC_ERR_PARSE, "malformed hex block");
-            size_t gi = i + 3;
-            std::vector<double> grading;
-            if (gw.kind == Node::VALUE && !gw.words.empty() &&
-                (gw.words[0] == "simpleGrading" || gw.words[0] == "edgeGrading")) {
-                if (gi + 1 >= bn.items.size()) throw ParseError(DSMC_ERR_PARSE, "grading without values");
-                grading = numList(*bn.items[gi + 1], "grading");
-                gi += 1;
-            }
-            for (double g : grading)
-                if (std::fabs(g - 1.0) > 1e-12)
-                    throw ParseError(DSMC_ERR_INVALID, "graded blocks are not supported on this path (uniform Cartesian cells only)");
-            Block b{};
-            for (int a = 0; a < 3; ++a) { b.lo[a] = 1e300; b.hi[a] = -1e300; }
-            for (double id : ids) {
-                const auto& p = V.at((size_t)id);
-                for (int a = 0; a < 3; ++a) {
-                    b.lo[a] = std::min(b.lo[a], p[a]);
-                    b.hi[a] = std::max(b.hi[a], p[a]);
-                }
-            }
-            for (double id : ids) {
-                const auto& p = V.at((size_t)id);
-                for (int a = 0; a < 3; ++a) {
-                    const double tol = 1e-9 * (b.hi[a] - b.lo[a] + 1e-300);
-                    if (std::fabs(p[a] - b.lo[a]) > tol && std::fabs(p[a] - b.hi[a]) > tol)
-                        throw ParseError(DSMC_ERR_INVALID, "hex block is not an axis-aligned box");
-                }
-            }
-            for (int a = 0; a < 3; ++a) b.n[a] = (int)cnt[a];
-            blocks.push_back(b);
-            i = gi;
-        }
-    }
+    std::vector<Block> blocks = parse_blocks(bn, V);
     if (blocks.empty()) throw ParseError(DSMC_ERR_PARSE, path + ": no hex blocks");
     double dx[3], lo[3], hi[3];
     for (int a = 0; a < 3; ++a) {
-        dx[a] = (blocks[0].hi[a] - blocks[0].lo[a]) / blocks[0].n[a];
-        lo[a] = 1e300;
-        hi[a] = -1e300;
-        for (auto& b : blocks) {
-            const double d = (b.hi[a] - b.lo[a]) / b.n[a];
-            if (std::fabs(d - dx[a]) > 1e-9 * dx[a])
-                throw ParseError(DSMC_ERR_INVALID, "blocks with different cell sizes are not supported");
-            lo[a] = std::min(lo[a], b.lo[a]);
-            hi[a] = std::max(hi[a], b.hi[a]);
-        }
+        std::vector<double>& nd = g_nodes[a];
+        const bool uniform = merge_axis_nodes(blocks, a, nd);
+        lo[a] = nd.front();
+        hi[a] = nd.back();
+        s->n_cells[a] = (int)nd.size() - 1;
         s->origin[a] = lo[a];
-        s->cell_size[a] = dx[a];
-        s->n_cells[a] = (int)std::lround((hi[a] - lo[a]) / dx[a]);
+        s->cell_size[a] = (hi[a] - lo[a]) / s->n_cells[a];
+        s->node_coords[a] = uniform ? nullptr : nd.data();
+        dx[a] = s->cell_size[a];
+        for (size_t k = 1; k < nd.size(); ++k) dx[a] = std::min(dx[a], nd[k] - nd[k - 1]);
     }
     const int nx = s->n_cells[0], ny = s->n_cells[1], nz = s->n_cells[2];
-    auto idx = [&](double x, int a) { return (int)std::lround((x - lo[a]) / dx[a]); };
+    // index of the global node at coordinate x
+    auto idx = [&](double x, int a) {
+        const std::vector<double>& nd = g_nodes[a];
+        const size_t k = (size_t)(std::lower_bound(nd.begin(), nd.end(), x - 1e-9 * (hi[a] - lo[a])) - nd.begin());
+        if (k >= nd.size() || std::fabs(nd[k] - x) > 1e-9 * (hi[a] - lo[a]))
+            throw ParseError(DSMC_ERR_INVALID, "a block or face corner is not on a mesh node");
+        return (int)k;
+    };
     std::vector<unsigned char> covered((size_t)nx * ny * nz, 0);
     for (auto& b : blocks) {
         int l[3], h[3];
@@ -521,6 +628,7 @@ void readMesh(const std::string& dir, dsmc_case_spec* s, std::map<std::string, i
         }
     }
     static const char* sideName[6] = {"-x", "+x", "-y", "+y", "-z", "+z"};
+    int defaultPatch = -1;
     for (int q = 0; q < 6; ++q) {
         const int a = q / 2, b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
         for (size_t f = 0; f < g_facePatch[q].size(); ++f) {
@@ -534,10 +642,29 @@ void readMesh(const std::string& dir, dsmc_case_spec* s, std::map<std::string, i
                 g_facePatch[q][f] = 0;
                 continue;
             }
-            if (g_facePatch[q][f] < 0)
-                throw ParseError(DSMC_ERR_INVALID, std::string("boundary face ") + std::to_string(f) + " of side " +
-                                                       sideName[q] + " has no patch (blockMesh defaultFaces are "
-                                                       "empty, which is not supported on this path)");
+            // blockMesh puts faces listed in no patch into its default patch
+            // (defaultPatch { name defaultFaces; type empty; })
+            if (defaultPatch < 0) {
+                if (s->n_patches >= DSMC_MAX_PATCHES) throw ParseError(DSMC_ERR_INVALID, "more than 16 patches");
+                defaultPatch = s->n_patches++;
+                std::string dn = "defaultFaces", dt = "empty";
+                if (const Node* dp = bm->find("defaultPatch")) {
+                    dn = wordOr(dp, "name", dn);
+                    dt = wordOr(dp, "type", dt);
+                }
+                int type;
+                if (dt == "empty") type = DSMC_PATCH_EMPTY;
+                else if (dt == "wall") type = DSMC_PATCH_WALL;
+                else if (dt == "patch") type = DSMC_PATCH_PATCH;
+                else if (dt == "symmetry" || dt == "symmetryPlane") type = DSMC_PATCH_SYMMETRY;
+                else throw ParseError(DSMC_ERR_INVALID, "defaultPatch " + dn + ": unsupported patch type " + dt);
+                copyName(s->patches[defaultPatch].name, dn);
+                s->patches[defaultPatch].type = type;
+                patchIds[dn] = defaultPatch;
+                patchTypes.push_back(dt);
+            }
+            (void)sideName;
+            g_facePatch[q][f] = defaultPatch;
         }
         s->face_patch[q] = g_facePatch[q].data();
         s->side_patch[q] = g_facePatch[q].empty() ? 0 : g_facePatch[q][0];
@@ -750,24 +877,29 @@ bool dsmc::foam_cell_order(const std::string& dir, std::vector<long long>& order
             auto c = numList(*it, "vertex");
             V.push_back({c[0] * scale, c[1] * scale, c[2] * scale});
         }
-        const Node& bn = need(bm.get(), "blocks", path);
+        const std::vector<Block> blocks = parse_blocks(need(bm.get(), "blocks", path), V);
         order.clear();
-        for (size_t i = 0; i < bn.items.size(); ++i) {
-            const Node& it = *bn.items[i];
-            if (!(it.kind == Node::VALUE && !it.words.empty() && it.words[0] == "hex")) continue;
-            auto ids = numList(*bn.items[i + 1], "hex vertices");
-            auto cnt = numList(*bn.items[i + 2], "hex cell counts");
-            double lo[3] = {1e300, 1e300, 1e300};
-            for (double id : ids)
-                for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], V.at((size_t)id)[a]);
+        for (const Block& b : blocks) {
+            // first global cell of the block along each axis
             int o[3];
-            for (int a = 0; a < 3; ++a) o[a] = (int)std::lround((lo[a] - s.origin[a]) / s.cell_size[a]);
-            for (int k = 0; k < (int)cnt[2]; ++k)
-                for (int j = 0; j < (int)cnt[1]; ++j)
-                    for (int ii = 0; ii < (int)cnt[0]; ++ii)
-                        order.push_back((o[0] + ii) +
-                                        (long long)s.n_cells[0] * ((o[1] + j) + (long long)s.n_cells[1] * (o[2] + k)));
-            i += 2;
+            for (int a = 0; a < 3; ++a) {
+                const std::vector<double>& nd = g_nodes[a];
+                const double tol = 1e-9 * (nd.back() - nd.front());
+                o[a] = (int)(std::lower_bound(nd.begin(), nd.end(), b.lo[a] - tol) - nd.begin());
+            }
+            // blockMesh numbers a block's cells along its local directions,
+            // the first fastest, each from the block's vertex 0
+            int l3[3];
+            for (l3[2] = 0; l3[2] < b.cnt[2]; ++l3[2])
+                for (l3[1] = 0; l3[1] < b.cnt[1]; ++l3[1])
+                    for (l3[0] = 0; l3[0] < b.cnt[0]; ++l3[0]) {
+                        int g[3];
+                        for (int l = 0; l < 3; ++l) {
+                            const int a = b.ax[l];
+                            g[a] = o[a] + (b.dir[l] > 0 ? l3[l] : b.cnt[l] - 1 - l3[l]);
+                        }
+                        order.push_back(g[0] + (long long)s.n_cells[0] * (g[1] + (long long)s.n_cells[1] * g[2]));
+                    }
         }
         return true;
     } catch (const std::exception& e) {

@@ -30,6 +30,9 @@ using namespace dsmc;
 struct dsmc_handle {
     dsmc_case_spec spec{};
     std::vector<std::vector<int>> facePatch;
+    std::vector<double> node[3];       // node coordinates along each axis (n + 1)
+    std::vector<double> width[3];      // cell widths (cell_size on a uniform axis)
+    std::vector<double> bfAreaHost;    // area of every boundary face
     CaseDev cs{};
     InflowDev inflow{};
     StepBuffers B{};
@@ -102,6 +105,12 @@ int validate(dsmc_handle* h, const dsmc_case_spec& s) {
     }
     const long long C = (long long)s.n_cells[0] * s.n_cells[1] * s.n_cells[2];
     if (C > (1LL << 28)) return fail(h, DSMC_ERR_INVALID, "more than 2^28 cells");
+    for (int a = 0; a < 3; ++a) {
+        if (!s.node_coords[a]) continue;
+        for (int i = 0; i <= s.n_cells[a]; ++i)
+            if (!std::isfinite(s.node_coords[a][i]) || (i > 0 && !(s.node_coords[a][i] > s.node_coords[a][i - 1])))
+                return fail(h, DSMC_ERR_INVALID, "node_coords must be finite and strictly increasing");
+    }
     if (s.n_species < 1 || s.n_species > DSMC_MAX_SPECIES)
         return fail(h, DSMC_ERR_INVALID, "n_species must be 1.." + std::to_string(DSMC_MAX_SPECIES));
     for (int i = 0; i < s.n_species; ++i) {
@@ -211,6 +220,10 @@ void build_faces(dsmc_handle* h, std::vector<int>& bfPatch, std::vector<long lon
         for (long long f = 0; f < nf; ++f) {
             const int p = s.face_patch[q] ? s.face_patch[q][f] : s.side_patch[q];
             bfPatch.push_back(p);
+            {
+                const long long ib = f % s.n_cells[b], ic = f / s.n_cells[b];
+                h->bfAreaHost.push_back(h->width[b][ib] * h->width[c][ic]);
+            }
             if (p < 0 || p >= s.n_patches || s.patches[p].type == DSMC_PATCH_SYMMETRY ||
                 s.patches[p].type == DSMC_PATCH_CYCLIC || s.patches[p].model == DSMC_BC_SPECULAR ||
                 s.patches[p].model == DSMC_BC_DIFFUSE)
@@ -235,7 +248,12 @@ void build_faces(dsmc_handle* h, std::vector<int>& bfPatch, std::vector<long lon
             const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
             cs.obstOff[o][q] = off;
             const long long nf = (long long)(ob.hi[b] - ob.lo[b]) * (ob.hi[c] - ob.lo[c]);
-            for (long long f = 0; f < nf; ++f) bfPatch.push_back(ob.patch[q]);
+            const int nb = ob.hi[b] - ob.lo[b];
+            for (long long f = 0; f < nf; ++f) {
+                bfPatch.push_back(ob.patch[q]);
+                const long long ib = ob.lo[b] + f % nb, ic = ob.lo[c] + f / nb;
+                h->bfAreaHost.push_back(h->width[b][ib] * h->width[c][ic]);
+            }
             off += nf;
         }
     }
@@ -247,13 +265,23 @@ void fill_case_dev(dsmc_handle* h) {
     CaseDev& cs = h->cs;
     for (int a = 0; a < 3; ++a) {
         cs.n[a] = s.n_cells[a];
-        cs.dx[a] = s.cell_size[a];
-        cs.inv[a] = 1.0 / s.cell_size[a];
-        cs.negOinv[a] = -(s.origin[a] * cs.inv[a]);
+        if (s.node_coords[a]) {
+            // graded: cells are found in the half-node table; dx and inv
+            // describe the mean cell only
+            cs.lo[a] = h->node[a].front();
+            cs.hi[a] = h->node[a].back();
+            cs.dx[a] = (cs.hi[a] - cs.lo[a]) / s.n_cells[a];
+            cs.inv[a] = 1.0 / cs.dx[a];
+            cs.negOinv[a] = -(cs.lo[a] * cs.inv[a]);
+        } else {
+            cs.dx[a] = s.cell_size[a];
+            cs.inv[a] = 1.0 / s.cell_size[a];
+            cs.negOinv[a] = -(s.origin[a] * cs.inv[a]);
+            cs.lo[a] = s.origin[a];
+            cs.hi[a] = s.origin[a] + s.n_cells[a] * s.cell_size[a];
+        }
         cs.invF[a] = (float)cs.inv[a];
         cs.negOinvF[a] = (float)cs.negOinv[a];
-        cs.lo[a] = s.origin[a];
-        cs.hi[a] = s.origin[a] + s.n_cells[a] * s.cell_size[a];
         cs.mid[a] = 0.5 * (cs.lo[a] + cs.hi[a]);
         const int p = s.face_patch[2 * a] ? s.face_patch[2 * a][0] : s.side_patch[2 * a];
         cs.emptyAx[a] = s.patches[p].type == DSMC_PATCH_EMPTY;
@@ -325,8 +353,8 @@ void fill_case_dev(dsmc_handle* h) {
         for (int a = 0; a < 3; ++a) {
             cs.obLoI[o][a] = s.obstacles[o].lo[a];
             cs.obHiI[o][a] = s.obstacles[o].hi[a];
-            cs.obLo[o][a] = s.origin[a] + s.obstacles[o].lo[a] * s.cell_size[a];
-            cs.obHi[o][a] = s.origin[a] + s.obstacles[o].hi[a] * s.cell_size[a];
+            cs.obLo[o][a] = h->node[a][s.obstacles[o].lo[a]];
+            cs.obHi[o][a] = h->node[a][s.obstacles[o].hi[a]];
         }
     }
     cs.nAcc = s.n_species * SACC + CACC;
@@ -489,6 +517,16 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
             h->spec.face_patch[q] = h->facePatch.back().data();
         }
     }
+    for (int a = 0; a < 3; ++a) {
+        h->node[a].resize((size_t)spec->n_cells[a] + 1);
+        for (int i = 0; i <= spec->n_cells[a]; ++i)
+            h->node[a][i] = spec->node_coords[a] ? spec->node_coords[a][i]
+                                                 : spec->origin[a] + i * spec->cell_size[a];
+        h->spec.node_coords[a] = spec->node_coords[a] ? h->node[a].data() : nullptr;
+        h->width[a].resize((size_t)spec->n_cells[a]);
+        for (int i = 0; i < spec->n_cells[a]; ++i)
+            h->width[a][i] = spec->node_coords[a] ? h->node[a][i + 1] - h->node[a][i] : spec->cell_size[a];
+    }
     fill_case_dev(h);
     CaseDev& cs = h->cs;
     std::vector<int> bfPatch;
@@ -511,9 +549,14 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
                     if (!sv) { sv = 1; --fluid; }
                 }
     }
-    double perCell = 0;
-    for (int m = 0; m < spec->n_species; ++m) perCell += spec->init_number_density[m] * cs.V / cs.FN;
-    h->expectedN = (long long)(perCell * fluid);
+    double ndSum = 0, fluidV = 0;
+    for (int m = 0; m < spec->n_species; ++m) ndSum += spec->init_number_density[m];
+    for (long long c = 0; c < cs.C; ++c)
+        if (!solid[c])
+            fluidV += h->width[0][c % cs.n[0]] * h->width[1][(c / cs.n[0]) % cs.n[1]] *
+                      h->width[2][c / ((long long)cs.n[0] * cs.n[1])];
+    (void)fluid;
+    h->expectedN = (long long)(ndSum * fluidV / cs.FN);
     long long cap = spec->max_particles;
     if (cap <= 0) cap = (long long)((h->hasInflow ? 2.0 : 1.3) * h->expectedN) + 65536;
     h->B.capacity = cap;
@@ -558,6 +601,33 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.inflowCount, ni))) return rc;
     if ((rc = dalloc(h, &B.inflowOff, ni + 1))) return rc;
     if ((rc = dalloc(h, &B.inflowTerm, ni))) return rc;
+    // graded mesh: half-node tables, cell volumes and boundary-face areas
+    if (spec->node_coords[0] || spec->node_coords[1] || spec->node_coords[2]) {
+        for (int a = 0; a < 3; ++a) {
+            if (!spec->node_coords[a]) continue;
+            const int na = cs.n[a];
+            std::vector<double> hv((size_t)2 * na + 1);
+            for (int i = 0; i <= na; ++i) hv[2 * (size_t)i] = h->node[a][i];
+            for (int i = 0; i < na; ++i) hv[2 * (size_t)i + 1] = 0.5 * (h->node[a][i] + h->node[a][i + 1]);
+            double* d = nullptr;
+            if ((rc = dalloc(h, &d, (long long)hv.size()))) return rc;
+            CUDA_TRY(h, cudaMemcpy(d, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice));
+            cs.half[a] = d;
+        }
+        std::vector<double> vol((size_t)cs.C);
+        for (long long c = 0; c < cs.C; ++c) {
+            const long long i = c % cs.n[0], j = (c / cs.n[0]) % cs.n[1], k = c / ((long long)cs.n[0] * cs.n[1]);
+            vol[(size_t)c] = h->width[0][i] * h->width[1][j] * h->width[2][k];
+        }
+        double* dv = nullptr;
+        double* da = nullptr;
+        if ((rc = dalloc(h, &dv, cs.C))) return rc;
+        if ((rc = dalloc(h, &da, cs.nBFaces))) return rc;
+        CUDA_TRY(h, cudaMemcpy(dv, vol.data(), sizeof(double) * vol.size(), cudaMemcpyHostToDevice));
+        CUDA_TRY(h, cudaMemcpy(da, h->bfAreaHost.data(), sizeof(double) * cs.nBFaces, cudaMemcpyHostToDevice));
+        cs.cellV = dv;
+        cs.bfArea = da;
+    }
     // 1/Zv by quantised level (postCollisionVibrationalEnergyLevel, dsmcCloud.C:1420-1490)
     {
         std::vector<double> tab((size_t)DSMC_MAX_SPECIES * DSMC_MAX_SPECIES * ZV_TAB, 0.0);
@@ -602,7 +672,8 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
             const int a = sd / 2;
             const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
             const double sgnOut = (sd & 1) ? 1.0 : -1.0;
-            const double fA = spec->cell_size[b] * spec->cell_size[c];
+            (void)b; (void)c;
+            const double fA = h->bfAreaHost[(size_t)inflowFace[f]];
             const int pi = bfPatch[(size_t)inflowFace[f]];
             const dsmc_patch& pt = spec->patches[pi];
             for (int m = 0; m < spec->n_species; ++m) {
@@ -911,6 +982,8 @@ int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n) {
 
 long long dsmc_n_boundary_faces(const dsmc_handle* h) { return h->cs.nBFaces; }
 
+long long dsmc_case_spec_size(void) { return (long long)sizeof(dsmc_case_spec); }
+
 int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long n) {
     const long long nf = h->cs.nBFaces;
     const std::string nm(name);
@@ -921,18 +994,38 @@ int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long
         return DSMC_OK;
     }
     if (n != nf) return fail(h, DSMC_ERR_INVALID, "n must equal the number of boundary faces");
+    // dsmcVolFields divides the boundary sums by its sample count
+    // (dsmcVolFields.C:2111-2126), the steps since the last reset
+    flush_sample(h);
     std::vector<double> w(nf * W_N);
     CUDA_TRY(h, cudaMemcpy(w.data(), h->B.wall, sizeof(double) * nf * W_N, cudaMemcpyDeviceToHost));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
-    const double nT = h->ctrHost->step > 0 ? (double)h->ctrHost->step : 1.0;
+    const double nT = h->ctrHost->sampleSteps > 0 ? (double)h->ctrHost->sampleSteps : 1.0;
+    const CaseDev& cs = h->cs;
     for (long long f = 0; f < nf; ++f) {
         const double* W = &w[f * W_N];
+        // normal axis and outward sign of the face (obstacle faces point into the solid)
+        int side = -1;
+        double sgn = 1.0;
+        for (int q = 0; q < 6 && side < 0; ++q)
+            if (f >= cs.sideOff[q] && f < cs.sideOff[q + 1]) { side = q; sgn = (q & 1) ? 1.0 : -1.0; }
+        for (int o = 0; o < cs.nObst && side < 0; ++o)
+            for (int q = 0; q < 6 && side < 0; ++q) {
+                const long long end = (q < 5) ? cs.obstOff[o][q + 1]
+                                              : (o + 1 < cs.nObst ? cs.obstOff[o + 1][0] : cs.nBFaces);
+                if (f >= cs.obstOff[o][q] && f < end) { side = q; sgn = (q & 1) ? -1.0 : 1.0; }
+            }
+        const int a = side / 2;
+        const double fD[3] = {W[W_FDX] / nT, W[W_FDY] / nT, W[W_FDZ] / nT};
         double v;
         if (nm == "wallHeatFlux") v = W[W_Q] / nT;
-        else if (nm == "wallShearStress_x") v = W[W_FDX] / nT;
-        else if (nm == "wallShearStress_y") v = W[W_FDY] / nT;
-        else if (nm == "wallShearStress_z") v = W[W_FDZ] / nT;
-        else if (nm == "rhoN_wall") v = W[W_RHON] * h->cs.FN / nT;
+        else if (nm == "wallShearStress_x") v = fD[0];
+        else if (nm == "wallShearStress_y") v = fD[1];
+        else if (nm == "wallShearStress_z") v = fD[2];
+        else if (nm == "wallShearStress")   // |fD . t1, fD . t2|
+            v = std::sqrt(fD[(a + 1) % 3] * fD[(a + 1) % 3] + fD[(a + 2) % 3] * fD[(a + 2) % 3]);
+        else if (nm == "p_wall") v = fD[a] * sgn;   // fD . n
+        else if (nm == "rhoN_wall") v = W[W_RHON] * cs.FN / nT;
         else return fail(h, DSMC_ERR_INVALID, "unknown wall field " + nm);
         out[f] = v;
     }

@@ -134,7 +134,7 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cs.C) return;
     const double nT = (double)ctr->sampleSteps;
-    const double FN = cs.FN, V = cs.V;
+    const double FN = cs.FN, V = cell_volume(cs, c);
     const long long C = cs.C;
     // accumulator k of cell c lives at acc[k * C + c]
     auto A = [&](int k) { return acc[(long long)k * C + c]; };
@@ -279,9 +279,10 @@ __global__ void k_cell_features(CaseDev cs, Parcels s, const int* __restrict__ s
                                 int every, float4* feat, unsigned char* useR) {
     if (every > 0 && (ctr->step % every) != 0) return;
     const float kOverM0 = (float)(kB / cs.sp[0].m);
-    const float ndScale = (float)(cs.FN / cs.V);
+    const float ndScaleU = (float)(cs.FN / cs.V);
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cs.C;
          c += (long long)gridDim.x * blockDim.x) {
+        const float ndScale = cs.cellV ? (float)(cs.FN / cs.cellV[c]) : ndScaleU;
         const long long off = start[c];
         const int n = start[c + 1] - (int)off;
         float4 f = make_float4(0.f, 0.f, 0.f, 0.f);

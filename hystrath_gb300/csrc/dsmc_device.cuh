@@ -87,6 +87,12 @@ struct CaseDev {
     int emptyAx[3];
     int anyEmpty;
     double mid[3];                // mesh bounding-box midpoint
+    // rectilinear grading: per graded axis the 2n+1 half-node coordinates
+    // (nodes at even, cell midpoints at odd indices), null for a uniform
+    // axis; per-cell volumes and per-boundary-face areas, null when uniform
+    const double* half[3];
+    const double* cellV;
+    const double* bfArea;
     // dsmcFaceTracker: per face and species the signed parcel count and mass
     // through every cell face (x faces, then y faces, then z faces), or null
     double* faceFlux;             // [2][nSpecies][nFacesAll]
@@ -281,8 +287,27 @@ __device__ __forceinline__ float d2f_bits(double v) {
     return __uint_as_float(sign | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7FFFFFu));
 }
 
+// Doubled cell coordinate on a graded axis: k with h[k] <= x < h[k+1] for the
+// half-node coordinates h[0..m], -1 below h[0] and m from h[m] on.
+__device__ __forceinline__ int floor2_graded(const double* __restrict__ h, int m, double x) {
+    if (!(x >= h[0])) return -1;
+    if (x >= h[m]) return m;
+    int lo = 0, hi = m;
+    while (hi - lo > 1) {
+        const int md = (lo + hi) >> 1;
+        if (h[md] <= x) lo = md; else hi = md;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ int floor2_coord(const CaseDev& cs, double x, int a) {
+    if (cs.half[a]) return floor2_graded(cs.half[a], 2 * cs.n[a], x);
     return floor2_bits(fma(x, cs.inv[a], cs.negOinv[a]));
+}
+
+// cell volume and the nodes and widths of the cells along an axis
+__device__ __forceinline__ double cell_volume(const CaseDev& cs, long long c) {
+    return cs.cellV ? cs.cellV[c] : cs.V;
 }
 
 // floor2_coord with the FP64 multiply-add replaced, where it cannot change
@@ -294,6 +319,7 @@ __device__ __forceinline__ int floor2_coord(const CaseDev& cs, double x, int a) 
 // every exact integer) the FP64 path decides.  The result is bit for bit that
 // of floor2_coord.
 __device__ __forceinline__ int floor2_coord_fast(const CaseDev& cs, double x, int a) {
+    if (cs.half[a]) return floor2_graded(cs.half[a], 2 * cs.n[a], x);
     const float xf = d2f_bits(x);
     const float p = xf * cs.invF[a];
     const float t = fmaf(xf, cs.invF[a], cs.negOinvF[a]);

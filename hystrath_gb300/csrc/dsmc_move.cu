@@ -47,8 +47,9 @@ __device__ void wall_measure(const CaseDev& cs, double* wall, long long bf, int 
                              bool after, double* preE, double preMom[3]) {
     const int ax1 = (axis == 0) ? 1 : 0;
     const int ax2 = (axis == 2) ? 1 : 2;
-    const double fA = cs.dx[ax1] * cs.dx[ax2];
-    const double invDtFa = cs.invDtFa[axis];      // 1 / (dt fA), one division per case
+    const double fA = cs.bfArea ? cs.bfArea[bf] : cs.dx[ax1] * cs.dx[ax2];
+    // 1 / (dt fA): one division per case on a uniform mesh
+    const double invDtFa = cs.bfArea ? 1.0 / (cs.dt * fA) : cs.invDtFa[axis];
     const double Un = U[axis] * sgn;
     double Ut[3] = {U[0], U[1], U[2]};
     Ut[axis] = U[axis] - Un * sgn;
@@ -128,6 +129,14 @@ __device__ void diffuse_reflect(const CaseDev& cs, Rng& r, int axis, double sgn,
 // area vector (+axis for a face between two cells, outward for a boundary
 // face), and a cyclic crossing gets +1 on the face it leaves through.
 
+// node p along axis a, and the width of cell i along it
+__device__ __forceinline__ double node_x(const CaseDev& cs, int a, int p) {
+    return cs.half[a] ? cs.half[a][2 * p] : cs.lo[a] + p * cs.dx[a];
+}
+__device__ __forceinline__ double cell_w(const CaseDev& cs, int a, int i) {
+    return cs.half[a] ? cs.half[a][2 * i + 2] - cs.half[a][2 * i] : cs.dx[a];
+}
+
 // face on axis a at plane index p, the other two cell indices from cell[]
 __device__ __forceinline__ long long face_index(const CaseDev& cs, int a, int p, const int* cell) {
     const long long nx = cs.n[0], ny = cs.n[1];
@@ -154,7 +163,7 @@ __device__ void track_internal(const CaseDev& cs, const double* x, const double*
         dir[a] = d > 0 ? 1 : -1;
         if (left[a]) {
             const int p = d > 0 ? sc[a] + 1 : sc[a];
-            t[a] = (cs.lo[a] + p * cs.dx[a] - x[a]) / U[a];
+            t[a] = (node_x(cs, a, p) - x[a]) / U[a];
         }
     }
     while (left[0] + left[1] + left[2] > 0) {
@@ -166,7 +175,7 @@ __device__ void track_internal(const CaseDev& cs, const double* x, const double*
         cur[a] += dir[a];
         if (--left[a]) {
             const int pn = dir[a] > 0 ? cur[a] + 1 : cur[a];
-            t[a] = (cs.lo[a] + pn * cs.dx[a] - x[a]) / U[a];
+            t[a] = (node_x(cs, a, pn) - x[a]) / U[a];
         }
     }
 }
@@ -910,15 +919,15 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
         if (sCos < -3) scaling = fabs(sCos) + 1;
         const long long fl = bf - cs.sideOff[sd];
         const long long ib = fl % cs.n[b], ic = fl / cs.n[b];
-        const double lob = cs.lo[b] + (double)ib * cs.dx[b];
-        const double loc = cs.lo[c] + (double)ic * cs.dx[c];
+        const double lob = node_x(cs, b, ib);
+        const double loc = node_x(cs, c, ic);
         const double scT = sqrt(kB * pt.Ttra / sp.m);
         Rng r(cs, (uint32_t)bf, (uint32_t)ctr->step,
               TAG_INFLOW | ((uint32_t)m << 8) | ((uint32_t)(q + 1) << 11));
         double x[3], U[3];
         x[a] = (sd & 1) ? cs.hi[a] : cs.lo[a];
-        x[b] = fma(r.u01(), cs.dx[b], lob);
-        x[c] = fma(r.u01(), cs.dx[c], loc);
+        x[b] = fma(r.u01(), cell_w(cs, b, ib), lob);
+        x[c] = fma(r.u01(), cell_w(cs, c, ic), loc);
         double uNormal = 0;
         if (fabs(pt.U[a]) > VSMALL) {
             int it = 0;
@@ -981,7 +990,7 @@ __global__ void k_init_count(CaseDev cs, const double* __restrict__ nd, const un
         for (int tet = 0; tet < 12; ++tet) {
             for (int m = 0; m < cs.nSpecies; ++m) {
                 if (!(nd[m] > 0)) continue;
-                const double req = nd[m] * (cs.V / 12.0) / cs.FN;
+                const double req = nd[m] * (cell_volume(cs, c) / 12.0) / cs.FN;
                 int k = (int)req;
                 if ((req - k) > r.u01()) k++;
                 total += k;
@@ -1005,7 +1014,7 @@ __global__ void k_init_fill(CaseDev cs, const double* __restrict__ nd, const uns
         for (int tet = 0; tet < 12; ++tet) {
             for (int m = 0; m < cs.nSpecies; ++m) {
                 if (!(nd[m] > 0)) continue;
-                const double req = nd[m] * (cs.V / 12.0) / cs.FN;
+                const double req = nd[m] * (cell_volume(cs, c) / 12.0) / cs.FN;
                 int k = (int)req;
                 if ((req - k) > r.u01()) k++;
                 per[m] += k;
@@ -1015,7 +1024,8 @@ __global__ void k_init_fill(CaseDev cs, const double* __restrict__ nd, const uns
     const int i0 = (int)(c % cs.n[0]);
     const int j0 = (int)((c / cs.n[0]) % cs.n[1]);
     const int k0 = (int)(c / ((long long)cs.n[0] * cs.n[1]));
-    const double cl[3] = {cs.lo[0] + i0 * cs.dx[0], cs.lo[1] + j0 * cs.dx[1], cs.lo[2] + k0 * cs.dx[2]};
+    const double cl[3] = {node_x(cs, 0, i0), node_x(cs, 1, j0), node_x(cs, 2, k0)};
+    const double cw[3] = {cell_w(cs, 0, i0), cell_w(cs, 1, j0), cell_w(cs, 2, k0)};
     const double Ta[3] = {Tx > 0 ? Tx : Ttra, Ty > 0 ? Ty : Ttra, Tz > 0 ? Tz : Ttra};
     const double Ub[3] = {U0, U1, U2};
     long long slot = cellOff[c];
@@ -1026,7 +1036,7 @@ __global__ void k_init_fill(CaseDev cs, const double* __restrict__ nd, const uns
             const uint32_t pid = (uint32_t)slot;
             Rng r(cs, pid, 0, TAG_INIT_PARTICLE);
             double x[3];
-            for (int a = 0; a < 3; ++a) x[a] = fma(r.u01(), cs.dx[a], cl[a]);
+            for (int a = 0; a < 3; ++a) x[a] = fma(r.u01(), cw[a], cl[a]);
             double g[4];
             r.gauss2(&g[0], &g[1]);
             r.gauss2(&g[2], &g[3]);

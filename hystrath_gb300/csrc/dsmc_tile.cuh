@@ -97,7 +97,7 @@ __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const do
                 if (!useR[c] && pv > 0.f && pv < 3.0e38f) sm = (double)pv;
                 smaxSel[c] = sm;
             }
-            const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cs.V;
+            const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cell_volume(cs, c);
             const double whole = floor(sel);
             rem[c] = sel - whole;
             if (n > ORDER_MAX_N || whole >= (double)MAX_CAND) err |= ERRB_DENSE;
@@ -609,7 +609,7 @@ k_sbt_collide(CaseDev cs, Parcels s, const int* __restrict__ start, double* acc,
     const uint32_t step = (uint32_t)ctr->step;
     const long long nWork = (long long)ctr->nWork;
     const long long C = cs.C;
-    const double prob1 = cs.FN * cs.dt / cs.V;
+    const double prob1u = cs.FN * cs.dt / cs.V;
     unsigned err = 0;
     unsigned long long nColl = 0, nTrials = 0;
     for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nWork;
@@ -617,6 +617,7 @@ k_sbt_collide(CaseDev cs, Parcels s, const int* __restrict__ start, double* acc,
         const int c = work[q].x;
         const long long off = start[c];
         const int n = start[c + 1] - (int)off;
+        const double prob1 = cs.cellV ? cs.FN * cs.dt / cs.cellV[c] : prob1u;
         double stepMax = 0.0, collSep = 0.0;
         unsigned coll = 0;
         for (int p = 0; p < n - 1; ++p) {

@@ -105,6 +105,7 @@ class CaseSpec(C.Structure):
         ("init_velocity", C.c_double * 3),
         ("init_t_tra_xyz", C.c_double * 3),
         ("max_particles", C.c_longlong),
+        ("node_coords", C.POINTER(C.c_double) * 3),
     ]
 
 

@@ -173,6 +173,11 @@ typedef struct {
     double init_t_tra_xyz[3];        /* >0: per-axis translational temperatures
                                         (anisotropic start; not a reference key) */
     long long max_particles;         /* capacity; 0 = 2x the initial fill + inflow margin */
+
+    /* Rectilinear grading (blockMesh simpleGrading): for a graded axis the
+     * n_cells[a] + 1 node coordinates, strictly increasing (origin[a] and
+     * cell_size[a] are then ignored); NULL for a uniform axis. */
+    const double* node_coords[3];
 } dsmc_case_spec;
 
 /* Cloud totals, as printed by dsmcCloud::info (dsmcCloud.C:935-985). */
@@ -197,6 +202,9 @@ typedef struct dsmc_handle dsmc_handle;
 
 /* Fill *spec with the reference's defaults (Tref 273, Zrot 5, ...). */
 void dsmc_spec_defaults(dsmc_case_spec* spec);
+
+/* sizeof(dsmc_case_spec), for bindings that mirror the struct. */
+long long dsmc_case_spec_size(void);
 
 /* Build a cloud from a resolved spec (replaces dsmcCloud ctor). */
 int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out);
@@ -255,8 +263,11 @@ int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n);
  * (dsmcVolFields.C:841), e.g. Ttra_N2 of the N2/O2 Couette case. */
 int dsmc_get_species_field(dsmc_handle* h, const char* name, unsigned species_mask, double* out, long long n);
 
-/* Per-boundary-face wall fields: "wallHeatFlux", "wallShearStress_x|y|z",
- * "rhoN_wall"; n = number of boundary faces (dsmc_info boundary face count). */
+/* Per-boundary-face wall fields averaged over the steps since the last
+ * dsmc_reset_sampling (dsmcVolFields.C:2110-2126): "wallHeatFlux", the force
+ * density "wallShearStress_x|y|z" (fD), its tangential magnitude
+ * "wallShearStress", the surface pressure "p_wall" (fD . n, n the outward
+ * normal of the gas) and "rhoN_wall"; n = number of boundary faces. */
 int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long n);
 long long dsmc_n_boundary_faces(const dsmc_handle* h);
 

@@ -191,6 +191,10 @@ struct Oracle {
     long long C;
     double lo[3], hi[3], dx[3], inv[3], negOinv[3];
     double mid[3];          // mesh bounding-box midpoint
+    // rectilinear grading: nodes and widths of every axis (a uniform axis has
+    // origin + i dx and dx), the 2n+1 half-node coordinates of a graded axis
+    // (empty when uniform) and the cell volumes of a graded mesh
+    std::vector<double> node[3], width[3], half[3], cellVol;
     int emptyAx[3];         // reduced-D: both sides of the axis are empty patches
     double V;
     std::vector<Species> sp;
@@ -223,9 +227,25 @@ struct Oracle {
     // ------------------------------------------------------------ geometry
     // Index of the doubled cell coordinate: floor(2 t), t = x/dx - x0/dx.
     long long floor2(double x, int a) const {
+        if (!half[a].empty()) {
+            // graded: k with h[k] <= x < h[k+1], -1 below and 2n from h[2n] on
+            const std::vector<double>& h = half[a];
+            const int m = 2 * n[a];
+            if (!(x >= h[0])) return -1;
+            if (x >= h[m]) return m;
+            int l = 0, u = m;
+            while (u - l > 1) {
+                const int md = (l + u) >> 1;
+                if (h[md] <= x) l = md; else u = md;
+            }
+            return l;
+        }
         const double t = std::fma(x, inv[a], negOinv[a]);
         return (long long)std::floor(2.0 * t);
     }
+    double nodeX(int a, long long p) const { return half[a].empty() ? lo[a] + p * dx[a] : half[a][2 * p]; }
+    double cellW(int a, long long i) const { return half[a].empty() ? dx[a] : half[a][2 * i + 2] - half[a][2 * i]; }
+    double cellVolume(long long c) const { return cellVol.empty() ? V : cellVol[c]; }
     void cellOf(const double x[3], int* cell, int* sub) const {
         int ci[3];
         int sb = 0;
@@ -267,7 +287,7 @@ struct Oracle {
             const int d = te[a] - sc[a];
             left[a] = std::abs(d);
             dir[a] = d > 0 ? 1 : -1;
-            if (left[a]) t[a] = (lo[a] + (d > 0 ? sc[a] + 1 : sc[a]) * dx[a] - x[a]) / U[a];
+            if (left[a]) t[a] = (nodeX(a, d > 0 ? sc[a] + 1 : sc[a]) - x[a]) / U[a];
         }
         while (left[0] + left[1] + left[2] > 0) {
             int a = -1;
@@ -275,7 +295,7 @@ struct Oracle {
                 if (left[b] && (a < 0 || t[b] < t[a])) a = b;
             faceAdd(faceIndex(a, dir[a] > 0 ? cur[a] + 1 : cur[a], cur), m, dir[a] > 0 ? 1.0 : -1.0);
             cur[a] += dir[a];
-            if (--left[a]) t[a] = (lo[a] + (dir[a] > 0 ? cur[a] + 1 : cur[a]) * dx[a] - x[a]) / U[a];
+            if (--left[a]) t[a] = (nodeX(a, dir[a] > 0 ? cur[a] + 1 : cur[a]) - x[a]) / U[a];
         }
     }
 
@@ -311,12 +331,31 @@ struct Oracle {
         spec = *s;
         for (int a = 0; a < 3; ++a) {
             n[a] = s->n_cells[a];
-            dx[a] = s->cell_size[a];
-            if (n[a] <= 0 || !(dx[a] > 0)) { msg = "invalid mesh"; return false; }
-            inv[a] = 1.0 / dx[a];
-            negOinv[a] = -(s->origin[a] * inv[a]);
-            lo[a] = s->origin[a];
-            hi[a] = s->origin[a] + n[a] * dx[a];
+            if (n[a] <= 0) { msg = "invalid mesh"; return false; }
+            node[a].resize((size_t)n[a] + 1);
+            width[a].resize((size_t)n[a]);
+            if (s->node_coords[a]) {
+                for (int i = 0; i <= n[a]; ++i) node[a][i] = s->node_coords[a][i];
+                for (int i = 0; i < n[a]; ++i) width[a][i] = node[a][i + 1] - node[a][i];
+                half[a].resize(2 * (size_t)n[a] + 1);
+                for (int i = 0; i <= n[a]; ++i) half[a][2 * (size_t)i] = node[a][i];
+                for (int i = 0; i < n[a]; ++i) half[a][2 * (size_t)i + 1] = 0.5 * (node[a][i] + node[a][i + 1]);
+                lo[a] = node[a].front();
+                hi[a] = node[a].back();
+                dx[a] = (hi[a] - lo[a]) / n[a];
+                inv[a] = 1.0 / dx[a];
+                negOinv[a] = -(lo[a] * inv[a]);
+            } else {
+                dx[a] = s->cell_size[a];
+                if (!(dx[a] > 0)) { msg = "invalid mesh"; return false; }
+                inv[a] = 1.0 / dx[a];
+                negOinv[a] = -(s->origin[a] * inv[a]);
+                lo[a] = s->origin[a];
+                hi[a] = s->origin[a] + n[a] * dx[a];
+                for (int i = 0; i <= n[a]; ++i) node[a][i] = s->origin[a] + i * s->cell_size[a];
+                for (int i = 0; i < n[a]; ++i) width[a][i] = dx[a];
+            }
+            spec.node_coords[a] = nullptr;   // the copies above are used
         }
         for (int q = 0; q < 6; ++q) {
             if (s->face_patch[q]) {
@@ -333,6 +372,11 @@ struct Oracle {
         }
         C = (long long)n[0] * n[1] * n[2];
         V = dx[0] * dx[1] * dx[2];
+        if (!half[0].empty() || !half[1].empty() || !half[2].empty()) {
+            cellVol.resize((size_t)C);
+            for (long long c = 0; c < C; ++c)
+                cellVol[c] = width[0][c % n[0]] * width[1][(c / n[0]) % n[1]] * width[2][c / ((long long)n[0] * n[1])];
+        }
         sp.resize(s->n_species);
         for (int i = 0; i < s->n_species; ++i) {
             const dsmc_species& q = s->species[i];
@@ -347,8 +391,8 @@ struct Oracle {
                     for (int i = ob.lo[0]; i < ob.hi[0]; ++i)
                         solid[i + (long long)n[0] * (j + (long long)n[1] * k)] = 1;
             for (int a = 0; a < 3; ++a) {
-                obLo[o][a] = s->origin[a] + ob.lo[a] * dx[a];
-                obHi[o][a] = s->origin[a] + ob.hi[a] * dx[a];
+                obLo[o][a] = node[a][ob.lo[a]];
+                obHi[o][a] = node[a][ob.hi[a]];
             }
         }
         long long off = 0;
@@ -358,7 +402,7 @@ struct Oracle {
             sideOff[q] = off;
             for (long long f = 0; f < (long long)n[b] * n[c]; ++f) {
                 bfPatch.push_back(patchOfSideFace(q, f));
-                bfArea.push_back(dx[b] * dx[c]);
+                bfArea.push_back(width[b][f % n[b]] * width[c][f / n[b]]);
             }
             off += (long long)n[b] * n[c];
         }
@@ -371,9 +415,10 @@ struct Oracle {
                 const int b = (a == 0) ? 1 : 0, c = (a == 2) ? 1 : 2;
                 obstOff[o * 6 + q] = off;
                 const long long nf = (long long)(ob.hi[b] - ob.lo[b]) * (ob.hi[c] - ob.lo[c]);
+                const int nb = ob.hi[b] - ob.lo[b];
                 for (long long f = 0; f < nf; ++f) {
                     bfPatch.push_back(ob.patch[q]);
-                    bfArea.push_back(dx[b] * dx[c]);
+                    bfArea.push_back(width[b][ob.lo[b] + f % nb] * width[c][ob.lo[c] + f / nb]);
                 }
                 off += nf;
             }
@@ -781,8 +826,8 @@ struct Oracle {
                               TAG_INFLOW | ((uint32_t)m << 8) | ((uint32_t)(i + 1) << 11));
                         Parcel p{};
                         p.x[a] = (side & 1) ? hi[a] : lo[a];
-                        p.x[b] = std::fma(r.u01(), dx[b], lo[b] + ib * dx[b]);
-                        p.x[c] = std::fma(r.u01(), dx[c], lo[c] + ic * dx[c]);
+                        p.x[b] = std::fma(r.u01(), cellW(b, ib), nodeX(b, ib));
+                        p.x[c] = std::fma(r.u01(), cellW(c, ic), nodeX(c, ic));
                         double uNormal = 0;
                         if (std::fabs(pt.inflow_velocity[a]) > VSMALL) {
                             int it = 0;
@@ -960,7 +1005,7 @@ struct Oracle {
         for (int i = 0; i < nC; ++i) subs[cp[i].sub].push_back(i);
         const double smax0 = sigmaTcRMax[c];
         const double sel = remainder[c] + 0.5 * nC * (nC - 1) * spec.n_equivalent_particles * smax0 *
-                                              spec.delta_t / V;
+                                              spec.delta_t / cellVolume(c);
         const long long nCandidates = (long long)sel;
         remainder[c] = sel - nCandidates;
         *nCand += nCandidates;
@@ -1017,7 +1062,7 @@ struct Oracle {
         if (nC <= 1) return;
         Parcel* cp = &P[cellStart[c]];
         Rng r(spec.seed, (uint32_t)c, (uint32_t)step, TAG_COLLIDE);
-        const double prob1 = spec.n_equivalent_particles * spec.delta_t / V;
+        const double prob1 = spec.n_equivalent_particles * spec.delta_t / cellVolume(c);
         double* A = &acc[c * nAcc];
         for (int ip = 0; ip < nC - 1; ++ip) {
             const int k = nC - 1 - ip;
@@ -1122,7 +1167,7 @@ struct Oracle {
                 for (int m = 0; m < ns; ++m) {
                     const double nd = spec.init_number_density[m];
                     if (!(nd > 0)) continue;
-                    const double req = nd * (V / 12.0) / spec.n_equivalent_particles;
+                    const double req = nd * (cellVolume(c) / 12.0) / spec.n_equivalent_particles;
                     int k = (int)req;
                     if ((req - k) > r.u01()) k++;
                     counts[c * ns + m] += k;
@@ -1132,14 +1177,15 @@ struct Oracle {
         uint32_t id = 0;
         for (long long c = 0; c < C; ++c) {
             const long long i0 = c % n[0], j0 = (c / n[0]) % n[1], k0 = c / ((long long)n[0] * n[1]);
-            const double cl[3] = {lo[0] + i0 * dx[0], lo[1] + j0 * dx[1], lo[2] + k0 * dx[2]};
+            const double cl[3] = {nodeX(0, i0), nodeX(1, j0), nodeX(2, k0)};
+            const double cw[3] = {cellW(0, i0), cellW(1, j0), cellW(2, k0)};
             for (int m = 0; m < ns; ++m) {
                 const Species& s = sp[m];
                 for (int q = 0; q < counts[c * ns + m]; ++q) {
                     Parcel p{};
                     p.id = id++;
                     Rng r(spec.seed, p.id, 0, TAG_INIT_PARTICLE);
-                    for (int a = 0; a < 3; ++a) p.x[a] = std::fma(r.u01(), dx[a], cl[a]);
+                    for (int a = 0; a < 3; ++a) p.x[a] = std::fma(r.u01(), cw[a], cl[a]);
                     double g[4];
                     r.gauss2(&g[0], &g[1]);
                     r.gauss2(&g[2], &g[3]);
@@ -1176,6 +1222,7 @@ struct Oracle {
         const double FN = spec.n_equivalent_particles;
         for (long long c = 0; c < C; ++c) {
             const double* A = &acc[c * nAcc];
+            const double V = cellVolume(c);
             double v = 0.0;
             const double N = A[ACC_N];
             double rhoN = 0, rhoM = 0, Ux = 0, Uy = 0, Uz = 0, Ttra = 0;

@@ -41,6 +41,9 @@ def test_struct_layout_matches_header(gpu_lib):
     s = S.CaseSpec()
     gpu_lib.dsmc_spec_defaults(ctypes.byref(s))
     assert s.tref == 273.0 and s.zrot == 5.0 and s.inv_zv_formulation == 2 and s.mfp_tref == 273.0
+    gpu_lib.dsmc_case_spec_size.restype = ctypes.c_longlong
+    assert gpu_lib.dsmc_case_spec_size() == ctypes.sizeof(S.CaseSpec)
+    assert not any(bool(s.node_coords[a]) for a in range(3))
 
 
 def test_no_cpu_fallback_without_gpu(gpu_lib):

@@ -133,10 +133,50 @@ def test_missing_patch_in_boundaries(gpu_lib, tmp_path):
     _expect(d, S.ERR_INVALID, "Cannot find patch: wallz")
 
 
-def test_graded_mesh_rejected(gpu_lib, tmp_path):
+def test_graded_block_gives_node_coordinates(gpu_lib, tmp_path):
+    """simpleGrading ratio r over n cells: widths grow geometrically with
+    last / first = r (blockMesh lineDivide); the other block stays uniform,
+    so x becomes a graded axis and y, z stay uniform."""
     d = _copy_case(tmp_path)
     _edit(d / "system/blockMeshDict", "(5 18 18) simpleGrading (1 1 1)", "(5 18 18) simpleGrading (2 1 1)")
-    _expect(d, S.ERR_INVALID, "graded")
+    s = parse(str(d))
+    assert list(s.n_cells) == [30, 18, 18]
+    assert bool(s.node_coords[0]) and not s.node_coords[1] and not s.node_coords[2]
+    x = np.ctypeslib.as_array(s.node_coords[0], shape=(31,))
+    w = np.diff(x)
+    assert w[4] / w[0] == pytest.approx(2.0) and np.allclose(w[1:5] / w[:4], 2.0 ** 0.25)
+    assert x[5] == pytest.approx(0.05) and np.allclose(w[5:], 0.01)
+
+
+def test_reversed_block_grading(gpu_lib, tmp_path):
+    """A block whose vertex 0 sits at its +x corner grades from that corner."""
+    d = _copy_case(tmp_path)
+    _edit(d / "system/blockMeshDict", "hex (0 1 2 3 4 5 6 7) (5 18 18) simpleGrading (1 1 1)",
+          "hex (1 0 4 5 2 3 7 6) (5 18 18) simpleGrading (2 1 1)")
+    s = parse(str(d))
+    w = np.diff(np.ctypeslib.as_array(s.node_coords[0], shape=(31,)))
+    assert w[0] / w[4] == pytest.approx(2.0)
+
+
+def test_blocks_that_do_not_meet_node_to_node(gpu_lib, tmp_path):
+    d = _copy_case(tmp_path)
+    _edit(d / "system/blockMeshDict", "(5 18 18) simpleGrading (1 1 1)", "(5 18 18) simpleGrading (1 2 1)")
+    _expect(d, S.ERR_INVALID, "face to face")
+
+
+def test_unlisted_faces_go_to_an_empty_default_patch(gpu_lib, tmp_path):
+    """blockMesh's defaultFaces: here the z sides, one cell thick."""
+    d = _copy_case(tmp_path)
+    t = open(d / "system/blockMeshDict").read()
+    t = t.replace("(5 18 18) simpleGrading", "(5 18 1) simpleGrading")
+    t = t.replace("(25 18 18) simpleGrading", "(25 18 1) simpleGrading")
+    t = t.replace("(4 5 6 7) (5 10 11 6)", "").replace("(0 3 2 1)", "")
+    t = t.replace("(1 2 9 8)", "")
+    open(d / "system/blockMeshDict", "w").write(t)
+    s = parse(str(d))
+    names = [s.patches[p].name for p in range(s.n_patches)]
+    assert names[-1] == b"defaultFaces" and s.patches[s.n_patches - 1].type == S.PATCH_EMPTY
+    assert s.side_patch[4] == s.side_patch[5] == s.n_patches - 1
 
 
 def test_missing_file(gpu_lib, tmp_path):

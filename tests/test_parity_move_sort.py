@@ -143,3 +143,20 @@ def test_sampling_matches_oracle(gpu_lib, oracle_mod):
     o.run_phases(S.PHASE_SAMPLE)
     for f in ("rhoN", "rhoM", "Ux", "Uy", "Uz", "Ttra", "Trot", "Tvib", "Tov", "p", "dsmcNMean"):
         np.testing.assert_allclose(g.field(f), o.field(f), rtol=1e-10, atol=1e-9, err_msg=f)
+
+
+def test_move_sort_reduced_d_couette(gpu_lib, oracle_mod):
+    """The two-species Couette channel: one cell thick in z with empty front
+    and back (tracked at the mesh centre with no z velocity), cyclic in x,
+    diffuse walls moving at 300 m/s."""
+    import os
+    from hystrath_gb300.dsmc import parse_case
+    s = parse_case(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cases", "couette_N2-O2"))
+    g, o, st = _pair(s, gpu_lib, oracle_mod)
+    before = _canonical(st)
+    tainted = set()
+    for _ in range(3):
+        a, b, exact = _check_step(g, o, before, S.PHASE_MOVE | S.PHASE_SORT, tainted=tainted)
+        before = b
+    assert np.all(a["pos"][:, 2] == 0.005) and np.abs(a["U"][:, 2]).max() > 100.0
+    assert g.info().wall_hits_last_step == o.info().wall_hits_last_step > 0
