@@ -160,3 +160,26 @@ def test_move_sort_reduced_d_couette(gpu_lib, oracle_mod):
         before = b
     assert np.all(a["pos"][:, 2] == 0.005) and np.abs(a["U"][:, 2]).max() > 100.0
     assert g.info().wall_hits_last_step == o.info().wall_hits_last_step > 0
+
+
+def test_move_sort_graded_flat_plate(gpu_lib, oracle_mod):
+    """The supersonic flat plate: graded cells in x and y (blockMesh
+    simpleGrading), an empty z, free-stream inflow and deletion on four sides
+    and a diffuse plate; cells are found in the half-node tables on both
+    sides."""
+    import os
+    from hystrath_gb300.dsmc import parse_case
+    s = parse_case(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cases",
+                                "supersonic_flat_plate"))
+    g, o, st = _pair(s, gpu_lib, oracle_mod, threads=8)
+    before = _canonical(st)
+    tainted = set()
+    for _ in range(3):
+        a, b, exact = _check_step(g, o, before, S.PHASE_INFLOW | S.PHASE_MOVE | S.PHASE_SORT, tainted=tainted)
+        before = b
+    assert exact.sum() > 0.9 * len(exact)
+    gi, oi = g.info(), o.info()
+    assert gi.inserted_last_step == oi.inserted_last_step > 0
+    assert gi.deleted_last_step == oi.deleted_last_step > 0
+    assert gi.wall_hits_last_step == oi.wall_hits_last_step > 0
+    np.testing.assert_allclose(g.wall_accumulators(), o.wall(), rtol=1e-9, atol=1e-30)
