@@ -39,6 +39,7 @@
 namespace dsmc {
 void set_global_error(const std::string& msg);   // dsmc_api.cu
 bool foam_cell_order(const std::string& dir, std::vector<long long>& order, std::string& err);
+bool foam_read_scalar_field(const std::string& path, std::vector<double>& out, std::string& err);
 }
 
 namespace {
@@ -924,6 +925,227 @@ extern "C" int dsmc_parse_case(const char* case_dir, dsmc_case_spec* spec) {
 }
 
 extern "C" const char* dsmc_parse_last_error(void) { return g_perr.c_str(); }
+
+// ------------------------------------------------------------------ lagrangian
+// The parcel files of a dsmcFoam+ time directory, as dsmcParcelIO writes
+// them (dsmcParcelIO.C:133-450): one IOField per file, "N (items)" or
+// "N{uniform item}" after the FoamFile header.
+namespace {
+
+struct ListTokens {
+    std::string text;
+    std::vector<Tok> t;
+    size_t i = 0;
+    const Tok& peek() const { static const Tok end{Tok::END, ""}; return i < t.size() ? t[i] : end; }
+    Tok take() { Tok k = peek(); ++i; return k; }
+    void expect(const char* p, const std::string& where) {
+        const Tok k = take();
+        if (k.kind != Tok::PUNCT || k.s != p) throw ParseError(DSMC_ERR_PARSE, where + ": expected '" + p + "'");
+    }
+};
+
+// Tokens of a field file after its FoamFile header; false when the file is absent.
+bool field_tokens(const std::string& path, ListTokens& L) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    std::stringstream ss;
+    ss << f.rdbuf();
+    L.text = ss.str();
+    Lexer lx(L.text);
+    for (Tok k = lx.next(); k.kind != Tok::END; k = lx.next()) L.t.push_back(k);
+    if (L.peek().kind == Tok::WORD && L.peek().s == "FoamFile") {
+        L.take();
+        L.expect("{", path);
+        int depth = 1;
+        while (depth > 0 && L.peek().kind != Tok::END) {
+            const Tok k = L.take();
+            if (k.kind == Tok::PUNCT && k.s == "{") ++depth;
+            if (k.kind == Tok::PUNCT && k.s == "}") --depth;
+        }
+    }
+    return true;
+}
+
+double tok_num(const Tok& k, const std::string& where) {
+    char* e = nullptr;
+    const double v = std::strtod(k.s.c_str(), &e);
+    if (k.kind != Tok::WORD || e == k.s.c_str() || *e) throw ParseError(DSMC_ERR_PARSE, where + ": expected a number");
+    return v;
+}
+
+// Reads "N" then the items; item(L) parses one item at index k.  A uniform
+// list "N{item}" repeats its item.
+template <class F>
+long long read_list(ListTokens& L, const std::string& where, F item) {
+    const long long n = (long long)tok_num(L.take(), where);
+    if (n < 0) throw ParseError(DSMC_ERR_PARSE, where + ": negative size");
+    if (L.peek().kind == Tok::PUNCT && L.peek().s == "{") {
+        L.take();
+        const size_t at = L.i;
+        for (long long k = 0; k < n; ++k) { L.i = at; item(k); }
+        if (n == 0) item(-1);
+        L.expect("}", where);
+        return n;
+    }
+    L.expect("(", where);
+    for (long long k = 0; k < n; ++k) item(k);
+    L.expect(")", where);
+    return n;
+}
+
+void read_vector(ListTokens& L, const std::string& where, double* v) {
+    L.expect("(", where);
+    for (int a = 0; a < 3; ++a) v[a] = tok_num(L.take(), where);
+    if (!(L.peek().kind == Tok::PUNCT && L.peek().s == ")"))
+        throw ParseError(DSMC_ERR_INVALID, where + ": barycentric positions (OpenFOAM 5 and later) are not supported; "
+                                               "positions must be Cartesian (x y z) celli");
+    L.expect(")", where);
+}
+
+struct ParcelArrays {
+    long long n = -1;
+    std::vector<double> pos, U, erot;
+    std::vector<int> vib, species;
+    std::vector<unsigned> id;
+};
+
+void read_parcel_files(const std::string& dir, ParcelArrays& P) {
+    ListTokens L;
+    const std::string pp = dir + "/positions";
+    if (!field_tokens(pp, L)) throw ParseError(DSMC_ERR_IO, "cannot open " + pp);
+    // (x y z) celli [tetFacei tetPti]: the cell labels are not needed, the
+    // positions decide the cells
+    const long long n = read_list(L, pp, [&](long long k) {
+        double v[3];
+        read_vector(L, pp, v);
+        while (L.peek().kind == Tok::WORD) L.take();
+        if (k < 0) return;
+        if ((long long)P.pos.size() < 3 * (k + 1)) P.pos.resize(3 * (size_t)(k + 1));
+        for (int a = 0; a < 3; ++a) P.pos[3 * (size_t)k + a] = v[a];
+    });
+    P.n = n;
+    P.pos.resize(3 * (size_t)n);
+    auto need_n = [&](long long m, const std::string& f) {
+        if (m != n) throw ParseError(DSMC_ERR_PARSE, f + ": " + std::to_string(m) + " entries, positions has " +
+                                                        std::to_string(n));
+    };
+    {
+        ListTokens T;
+        const std::string f = dir + "/U";
+        if (!field_tokens(f, T)) throw ParseError(DSMC_ERR_IO, "cannot open " + f);
+        P.U.assign(3 * (size_t)n, 0.0);
+        need_n(read_list(T, f, [&](long long k) { double v[3]; read_vector(T, f, v);
+                                                  if (k >= 0) for (int a = 0; a < 3; ++a) P.U[3 * k + a] = v[a]; }), f);
+    }
+    {
+        ListTokens T;
+        const std::string f = dir + "/typeId";
+        if (!field_tokens(f, T)) throw ParseError(DSMC_ERR_IO, "cannot open " + f);
+        P.species.assign((size_t)n, 0);
+        need_n(read_list(T, f, [&](long long k) { const int v = (int)tok_num(T.take(), f); if (k >= 0) P.species[k] = v; }), f);
+    }
+    P.erot.assign((size_t)n, 0.0);
+    {
+        ListTokens T;
+        const std::string f = dir + "/ERot";
+        if (field_tokens(f, T))
+            need_n(read_list(T, f, [&](long long k) { const double v = tok_num(T.take(), f); if (k >= 0) P.erot[k] = v; }), f);
+    }
+    P.vib.assign((size_t)n, 0);
+    {
+        ListTokens T;
+        const std::string f = dir + "/vibLevel";
+        if (field_tokens(f, T))
+            need_n(read_list(T, f, [&](long long k) {
+                       // a labelList per parcel: "m(l0 ...)" or "m{l}"; the first mode is kept
+                       const long long m = (long long)tok_num(T.take(), f);
+                       int first = 0;
+                       if (T.peek().kind == Tok::PUNCT && T.peek().s == "{") {
+                           T.take();
+                           first = (int)tok_num(T.take(), f);
+                           T.expect("}", f);
+                       } else {
+                           T.expect("(", f);
+                           for (long long q = 0; q < m; ++q) {
+                               const int v = (int)tok_num(T.take(), f);
+                               if (q == 0) first = v;
+                           }
+                           T.expect(")", f);
+                       }
+                       if (m > 1) throw ParseError(DSMC_ERR_INVALID, f + ": more than one vibrational mode");
+                       if (k >= 0) P.vib[k] = (m > 0) ? first : 0;
+                   }), f);
+    }
+    P.id.resize((size_t)n);
+    for (long long k = 0; k < n; ++k) P.id[k] = (unsigned)k;
+    {
+        ListTokens T;
+        const std::string f = dir + "/origId";
+        if (field_tokens(f, T))
+            need_n(read_list(T, f, [&](long long k) { const long long v = (long long)tok_num(T.take(), f);
+                                                      if (k >= 0) P.id[k] = (unsigned)v; }), f);
+    }
+}
+
+}  // namespace
+
+// internalField of a volScalarField: "uniform v" (one value) or
+// "nonuniform List<scalar> N (...)".  False with err empty when the file
+// does not exist.
+bool dsmc::foam_read_scalar_field(const std::string& path, std::vector<double>& out, std::string& err) {
+    err.clear();
+    out.clear();
+    try {
+        ListTokens L;
+        if (!field_tokens(path, L)) return false;
+        while (L.peek().kind != Tok::END && !(L.peek().kind == Tok::WORD && L.peek().s == "internalField")) L.take();
+        if (L.peek().kind == Tok::END) throw ParseError(DSMC_ERR_PARSE, path + ": no internalField");
+        L.take();
+        const Tok k = L.take();
+        if (k.s == "uniform") {
+            out.push_back(tok_num(L.take(), path));
+            return true;
+        }
+        if (k.s != "nonuniform") throw ParseError(DSMC_ERR_PARSE, path + ": internalField is neither uniform nor nonuniform");
+        L.take();   // List<scalar>
+        out.resize(0);
+        read_list(L, path, [&](long long i) {
+            const double v = tok_num(L.take(), path);
+            if (i >= 0) { if ((long long)out.size() <= i) out.resize((size_t)i + 1); out[(size_t)i] = v; }
+        });
+        return true;
+    } catch (const std::exception& e) {
+        err = e.what();
+        return false;
+    }
+}
+
+extern "C" int dsmc_parse_parcels(const char* case_dir, const char* time_name, const char* cloud_name, long long* n,
+                                  double* pos, double* U, double* erot, int* vib, int* species, unsigned* id) {
+    try {
+        ParcelArrays P;
+        read_parcel_files(std::string(case_dir) + "/" + time_name + "/lagrangian/" + cloud_name, P);
+        const long long cap = *n;
+        *n = P.n;
+        if (!pos) return DSMC_OK;
+        if (cap < P.n) throw ParseError(DSMC_ERR_CAPACITY, "arrays hold fewer entries than the cloud");
+        std::memcpy(pos, P.pos.data(), sizeof(double) * P.pos.size());
+        if (U) std::memcpy(U, P.U.data(), sizeof(double) * P.U.size());
+        if (erot) std::memcpy(erot, P.erot.data(), sizeof(double) * P.erot.size());
+        if (vib) std::memcpy(vib, P.vib.data(), sizeof(int) * P.vib.size());
+        if (species) std::memcpy(species, P.species.data(), sizeof(int) * P.species.size());
+        if (id) std::memcpy(id, P.id.data(), sizeof(unsigned) * P.id.size());
+        return DSMC_OK;
+    } catch (const ParseError& e) {
+        g_perr = e.what();
+        dsmc::set_global_error(g_perr);
+        return e.code;
+    } catch (const std::exception& e) {
+        g_perr = e.what();
+        dsmc::set_global_error(g_perr);
+        return DSMC_ERR_PARSE;
+    }
+}
 
 extern "C" int dsmc_create(const char* case_dir, dsmc_handle** out) {
     *out = nullptr;

@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -23,6 +24,9 @@
 
 namespace dsmc {
 bool foam_cell_order(const std::string& dir, std::vector<long long>& order, std::string& err);   // case_parser.cpp
+// internalField of a volScalarField file (one value when uniform); false with
+// err empty when the file is absent
+bool foam_read_scalar_field(const std::string& path, std::vector<double>& out, std::string& err);
 }
 
 using namespace dsmc;
@@ -38,6 +42,8 @@ struct dsmc_handle {
     StepBuffers B{};
     Parcels buf[2]{};
     double* faceBuf = nullptr;   // face tracker sums, kept while tracking is off
+    long long nFluid = 0;        // cells outside the solid boxes
+    bool smaxSet = false;        // sigmaTcRMax initialised, restored or read
     int cur = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -555,7 +561,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
         if (!solid[c])
             fluidV += h->width[0][c % cs.n[0]] * h->width[1][(c / cs.n[0]) % cs.n[1]] *
                       h->width[2][c / ((long long)cs.n[0] * cs.n[1])];
-    (void)fluid;
+    h->nFluid = fluid;
     h->expectedN = (long long)(ndSum * fluidV / cs.FN);
     long long cap = spec->max_particles;
     if (cap <= 0) cap = (long long)((h->hasInflow ? 2.0 : 1.3) * h->expectedN) + 65536;
@@ -709,6 +715,22 @@ void dsmc_destroy(dsmc_handle* h) {
     delete h;
 }
 
+// sigmaTcRMax = sigmaT * most probable speed of the most abundant species at
+// the initial temperature (dsmcMeshFill's starting value)
+int init_smax(dsmc_handle* h) {
+    const dsmc_case_spec& s = h->spec;
+    int most = 0;
+    for (int m = 1; m < s.n_species; ++m)
+        if (s.init_number_density[m] > s.init_number_density[most]) most = m;
+    const dsmc_species& sp = s.species[most];
+    const double T = s.init_t_tra > 0 ? s.init_t_tra : 273.0;
+    const double smax = PI * sp.diameter * sp.diameter * std::sqrt(2.0 * kB * T / sp.mass);
+    std::vector<double> sm(h->cs.C, smax);
+    CUDA_TRY(h, cudaMemcpy(h->B.smax, sm.data(), sizeof(double) * h->cs.C, cudaMemcpyHostToDevice));
+    h->smaxSet = true;
+    return DSMC_OK;
+}
+
 int dsmc_initialise(dsmc_handle* h) {
     const CaseDev& cs = h->cs;
     StepBuffers& B = h->B;
@@ -738,14 +760,8 @@ int dsmc_initialise(dsmc_handle* h) {
     CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaStreamSynchronize(st));
     cudaFree(dnd);
-    // sigmaTcRMax = sigmaT * most probable speed of the most abundant species
-    int most = 0;
-    for (int m = 1; m < s.n_species; ++m)
-        if (s.init_number_density[m] > s.init_number_density[most]) most = m;
-    const dsmc_species& sp = s.species[most];
-    const double smax = PI * sp.diameter * sp.diameter * std::sqrt(2.0 * kB * s.init_t_tra / sp.mass);
-    std::vector<double> sm(cs.C, smax);
-    CUDA_TRY(h, cudaMemcpy(B.smax, sm.data(), sizeof(double) * cs.C, cudaMemcpyHostToDevice));
+    int rc0 = init_smax(h);
+    if (rc0) return rc0;
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
     h->ctrHost->nextId = total;
     CUDA_TRY(h, cudaMemcpy(B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
@@ -944,6 +960,7 @@ int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long l
     if (n != C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     if (nm == "sigmaTcRMax" || nm == "collisionSelectionRemainder") {
+        if (nm == "sigmaTcRMax") h->smaxSet = true;
         CUDA_TRY(h, cudaMemcpy(nm == "sigmaTcRMax" ? h->B.smax : h->B.rem, in, sizeof(double) * C,
                                cudaMemcpyHostToDevice));
         return DSMC_OK;
@@ -981,6 +998,7 @@ int dsmc_get_field(dsmc_handle* h, const char* name, double* out, long long n) {
 }
 
 long long dsmc_n_boundary_faces(const dsmc_handle* h) { return h->cs.nBFaces; }
+
 
 long long dsmc_case_spec_size(void) { return (long long)sizeof(dsmc_case_spec); }
 
@@ -1147,6 +1165,7 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
     CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemset(h->B.count, 0, sizeof(int) * h->cs.C));
     CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
+    h->smaxSet = true;
     return DSMC_OK;
 }
 
@@ -1372,7 +1391,7 @@ const char* FOAM_BANNER =
 
 void foam_write(const std::string& path, const std::string& cls, const std::string& object,
                 const std::string& location, const char* dims, const std::vector<const double*>& comps,
-                const std::vector<long long>& order, const dsmc_case_spec& spec, bool* ok) {
+                const std::vector<long long>& order, const dsmc_case_spec& spec, bool* ok, int digits = 10) {
     FILE* f = std::fopen(path.c_str(), "w");
     if (!f) { *ok = false; return; }
     const bool vec = comps.size() == 3;
@@ -1382,8 +1401,8 @@ void foam_write(const std::string& path, const std::string& cls, const std::stri
                  FOAM_BANNER, cls.c_str(), location.c_str(), object.c_str(), dims, vec ? "vector" : "scalar",
                  (long long)order.size());
     for (long long c : order) {
-        if (vec) std::fprintf(f, "(%.10g %.10g %.10g)\n", comps[0][c], comps[1][c], comps[2][c]);
-        else std::fprintf(f, "%.10g\n", comps[0][c]);
+        if (vec) std::fprintf(f, "(%.*g %.*g %.*g)\n", digits, comps[0][c], digits, comps[1][c], digits, comps[2][c]);
+        else std::fprintf(f, "%.*g\n", digits, comps[0][c]);
     }
     std::fprintf(f, ")\n;\n\nboundaryField\n{\n");
     for (int p = 0; p < spec.n_patches; ++p) {
@@ -1402,21 +1421,34 @@ void foam_write(const std::string& path, const std::string& cls, const std::stri
 
 }  // namespace
 
-int dsmc_write_fields(dsmc_handle* h, const char* case_dir, const char* time_name, const char* field_name) {
+// OpenFOAM's cell order of the case (blockMesh: block by block), as the
+// Cartesian cell of each OpenFOAM cell; the Cartesian order itself when the
+// case has no blockMeshDict.
+int case_cell_order(dsmc_handle* h, const char* case_dir, std::vector<long long>& order) {
     const long long C = h->cs.C;
-    std::vector<long long> order;
     std::string err;
     std::string bm = std::string(case_dir) + "/system/blockMeshDict";
     std::ifstream probe(bm);
     if (!probe) probe.open(std::string(case_dir) + "/constant/polyMesh/blockMeshDict");
+    order.clear();
     if (probe) {
         if (!foam_cell_order(case_dir, order, err)) return fail(h, DSMC_ERR_PARSE, "cell order: " + err);
+        if ((long long)order.size() != h->nFluid)
+            return fail(h, DSMC_ERR_INVALID, "the case's blockMeshDict does not match this cloud");
         for (long long c : order)
             if (c < 0 || c >= C) return fail(h, DSMC_ERR_INVALID, "the case's blockMeshDict does not match this cloud");
     } else {
         for (long long c = 0; c < C; ++c)
             order.push_back(c);
     }
+    return DSMC_OK;
+}
+
+int dsmc_write_fields(dsmc_handle* h, const char* case_dir, const char* time_name, const char* field_name) {
+    const long long C = h->cs.C;
+    std::vector<long long> order;
+    int orc = case_cell_order(h, case_dir, order);
+    if (orc) return orc;
     const std::string dir = std::string(case_dir) + "/" + time_name;
     mkdir(dir.c_str(), 0755);
     struct FieldOut {
@@ -1497,6 +1529,123 @@ int dsmc_get_face_flux(dsmc_handle* h, const char* name, int species, double* ou
     CUDA_TRY(h, cudaMemcpy(out, cs.faceFlux + ((long long)k * cs.nSpecies + species) * cs.nFacesAll,
                            sizeof(double) * n, cudaMemcpyDeviceToHost));
     return DSMC_OK;
+}
+
+// ------------------------------------------------------- lagrangian files
+namespace {
+
+// one IOField file of a lagrangian cloud directory
+bool write_ioField(const std::string& path, const char* cls, const std::string& location, const char* object,
+                   long long n, const std::function<void(FILE*, long long)>& item, const char* uniform) {
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) return false;
+    std::fprintf(f, "%sFoamFile\n{\n    version     2.0;\n    format      ascii;\n    class       %s;\n"
+                    "    location    \"%s\";\n    object      %s;\n}\n\n",
+                 FOAM_BANNER, cls, location.c_str(), object);
+    if (uniform) {
+        std::fprintf(f, "%lld{%s}\n", n, uniform);
+    } else {
+        std::fprintf(f, "\n%lld\n(\n", n);
+        for (long long k = 0; k < n; ++k) item(f, k);
+        std::fprintf(f, ")\n");
+    }
+    std::fprintf(f, "\n\n// ************************************************************************* //\n");
+    return std::fclose(f) == 0;
+}
+
+}  // namespace
+
+int dsmc_write_parcels(dsmc_handle* h, const char* case_dir, const char* time_name, const char* cloud_name) {
+    std::vector<long long> order;
+    int rc = case_cell_order(h, case_dir, order);
+    if (rc) return rc;
+    std::vector<long long> label((size_t)h->cs.C, -1);
+    for (size_t k = 0; k < order.size(); ++k) label[(size_t)order[k]] = (long long)k;
+    long long n = 0;
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    const long long cap = h->ctrHost->n;
+    std::vector<double> pos(3 * (size_t)cap), U(3 * (size_t)cap), erot((size_t)cap);
+    std::vector<int> vib((size_t)cap), sp((size_t)cap), cell((size_t)cap);
+    std::vector<unsigned> id((size_t)cap);
+    if ((rc = dsmc_get_particles(h, cap, &n, pos.data(), U.data(), erot.data(), vib.data(), sp.data(), id.data(),
+                                 cell.data())))
+        return rc;
+    std::string dir = std::string(case_dir) + "/" + time_name;
+    mkdir(dir.c_str(), 0755);
+    dir += "/lagrangian";
+    mkdir(dir.c_str(), 0755);
+    dir += std::string("/") + cloud_name;
+    mkdir(dir.c_str(), 0755);
+    const std::string loc = std::string(time_name) + "/lagrangian/" + cloud_name;
+    const dsmc_case_spec& s = h->spec;
+    bool ok = true;
+    // 17 significant digits: a written cloud reads back bit for bit
+    ok &= write_ioField(dir + "/positions", "Cloud<dsmcParcel>", loc, "positions", n, [&](FILE* f, long long k) {
+        std::fprintf(f, "(%.17g %.17g %.17g) %lld\n", pos[3 * k], pos[3 * k + 1], pos[3 * k + 2],
+                     label[(size_t)cell[k]]);
+    }, nullptr);
+    ok &= write_ioField(dir + "/U", "vectorField", loc, "U", n, [&](FILE* f, long long k) {
+        std::fprintf(f, "(%.17g %.17g %.17g)\n", U[3 * k], U[3 * k + 1], U[3 * k + 2]);
+    }, nullptr);
+    ok &= write_ioField(dir + "/ERot", "scalarField", loc, "ERot", n,
+                        [&](FILE* f, long long k) { std::fprintf(f, "%.17g\n", erot[k]); }, nullptr);
+    ok &= write_ioField(dir + "/typeId", "labelField", loc, "typeId", n,
+                        [&](FILE* f, long long k) { std::fprintf(f, "%d\n", sp[k]); }, nullptr);
+    ok &= write_ioField(dir + "/vibLevel", "labelFieldField", loc, "vibLevel", n, [&](FILE* f, long long k) {
+        if (s.species[sp[k]].n_vib_modes > 0) std::fprintf(f, "1(%d)\n", vib[k]);
+        else std::fprintf(f, "0()\n");
+    }, nullptr);
+    ok &= write_ioField(dir + "/origId", "labelField", loc, "origId", n,
+                        [&](FILE* f, long long k) { std::fprintf(f, "%u\n", id[k]); }, nullptr);
+    ok &= write_ioField(dir + "/newParcel", "labelField", loc, "newParcel", n, nullptr, "-1");
+    ok &= write_ioField(dir + "/origProcId", "labelField", loc, "origProcId", n, nullptr, "0");
+    ok &= write_ioField(dir + "/classification", "labelField", loc, "classification", n, nullptr, "0");
+    std::vector<double> sm((size_t)h->cs.C);
+    if ((rc = dsmc_get_cell_array(h, "sigmaTcRMax", sm.data(), h->cs.C))) return rc;
+    const std::string sname = std::string(cloud_name) + "SigmaTcRMax";
+    foam_write(std::string(case_dir) + "/" + time_name + "/" + sname, "volScalarField", sname, time_name,
+               "[0 3 -1 0 0 0 0]", {sm.data()}, order, h->spec, &ok, 17);
+    if (!ok) return fail(h, DSMC_ERR_IO, "cannot write the parcel files in " + dir);
+    return DSMC_OK;
+}
+
+int dsmc_read_parcels(dsmc_handle* h, const char* case_dir, const char* time_name, const char* cloud_name) {
+    long long n = 0;
+    int rc = dsmc_parse_parcels(case_dir, time_name, cloud_name, &n, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                nullptr);
+    if (rc) return fail(h, rc, dsmc_parse_last_error());
+    std::vector<double> pos(3 * (size_t)n), U(3 * (size_t)n), erot((size_t)n);
+    std::vector<int> vib((size_t)n), sp((size_t)n);
+    std::vector<unsigned> id((size_t)n);
+    rc = dsmc_parse_parcels(case_dir, time_name, cloud_name, &n, pos.data(), U.data(), erot.data(), vib.data(),
+                            sp.data(), id.data());
+    if (rc) return fail(h, rc, dsmc_parse_last_error());
+    const CaseDev& cs = h->cs;
+    for (long long k = 0; k < n; ++k)
+        for (int a = 0; a < 3; ++a)
+            if (!(pos[3 * k + a] >= cs.lo[a] && pos[3 * k + a] <= cs.hi[a]))
+                return fail(h, DSMC_ERR_INVALID, "parcel " + std::to_string(k) + " lies outside the mesh");
+    // the cloud's <name>SigmaTcRMax field of the same time (MUST_READ in
+    // dsmcCloud.C:625-636); without it, the starting value of the mesh fill
+    const std::string sfile = std::string(case_dir) + "/" + time_name + "/" + cloud_name + "SigmaTcRMax";
+    std::vector<double> sf;
+    std::string err;
+    if (foam_read_scalar_field(sfile, sf, err)) {
+        std::vector<long long> order;
+        if ((rc = case_cell_order(h, case_dir, order))) return rc;
+        if (sf.size() == 1) sf.assign(order.size(), sf[0]);
+        if (sf.size() != order.size()) return fail(h, DSMC_ERR_INVALID, sfile + ": wrong number of cells");
+        std::vector<double> sm((size_t)cs.C, 0.0);
+        for (size_t k = 0; k < order.size(); ++k) sm[(size_t)order[k]] = sf[k];
+        CUDA_TRY(h, cudaMemcpy(h->B.smax, sm.data(), sizeof(double) * cs.C, cudaMemcpyHostToDevice));
+        h->smaxSet = true;
+    } else if (!err.empty()) {
+        return fail(h, DSMC_ERR_PARSE, err);
+    } else if (!h->smaxSet) {
+        if ((rc = init_smax(h))) return rc;
+    }
+    return dsmc_set_particles(h, n, pos.data(), U.data(), erot.data(), vib.data(), sp.data(), id.data());
 }
 
 }  // extern "C"

@@ -49,6 +49,11 @@ def _load() -> C.CDLL:
     L.dsmc_n_boundary_faces.restype = C.c_longlong
     L.dsmc_reset_sampling.argtypes = [vp]
     L.dsmc_write_fields.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p]
+    L.dsmc_write_parcels.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p]
+    L.dsmc_read_parcels.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p]
+    L.dsmc_parse_parcels.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_longlong),
+                                     vp, vp, vp, vp, vp, vp]
+    L.dsmc_parse_last_error.restype = C.c_char_p
     L.dsmc_set_face_tracking.argtypes = [vp, C.c_int]
     L.dsmc_n_faces.argtypes = [vp]
     L.dsmc_n_faces.restype = C.c_longlong
@@ -91,6 +96,23 @@ class DsmcError(RuntimeError):
 
 def _p(a):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def parse_parcels(case_dir: str, time_name: str, cloud_name: str = "dsmc"):
+    """The parcels of an OpenFOAM lagrangian cloud directory (no GPU needed)."""
+    n = C.c_longlong(0)
+    args = (case_dir.encode(), time_name.encode(), cloud_name.encode())
+    rc = lib().dsmc_parse_parcels(*args, C.byref(n), None, None, None, None, None, None)
+    if rc != 0:
+        raise DsmcError(rc, lib().dsmc_parse_last_error().decode())
+    out = {"pos": np.empty((n.value, 3)), "U": np.empty((n.value, 3)), "erot": np.empty(n.value),
+           "vib": np.empty(n.value, np.int32), "species": np.empty(n.value, np.int32),
+           "id": np.empty(n.value, np.uint32)}
+    rc = lib().dsmc_parse_parcels(*args, C.byref(n), _p(out["pos"]), _p(out["U"]), _p(out["erot"]),
+                                  _p(out["vib"]), _p(out["species"]), _p(out["id"]))
+    if rc != 0:
+        raise DsmcError(rc, lib().dsmc_parse_last_error().decode())
+    return out
 
 
 def parse_case(case_dir: str) -> S.CaseSpec:
@@ -228,6 +250,13 @@ class DsmcCloud:
 
     def reset_sampling(self):
         self._chk(lib().dsmc_reset_sampling(self.h))
+
+    def write_parcels(self, case_dir: str, time_name: str, cloud_name: str = "dsmc"):
+        """The cloud as <case_dir>/<time_name>/lagrangian/<cloud_name>/ files."""
+        self._chk(lib().dsmc_write_parcels(self.h, case_dir.encode(), time_name.encode(), cloud_name.encode()))
+
+    def read_parcels(self, case_dir: str, time_name: str, cloud_name: str = "dsmc"):
+        self._chk(lib().dsmc_read_parcels(self.h, case_dir.encode(), time_name.encode(), cloud_name.encode()))
 
     def set_face_tracking(self, on: bool = True):
         self._chk(lib().dsmc_set_face_tracking(self.h, 1 if on else 0))

@@ -16,7 +16,8 @@
  *                   src/lagrangian/dsmc/macroscopicProperties/derived/
  *                   combined/dsmcVolFields/dsmcVolFields.C:1365-1876 dsmc_get_field
  *   lagrangian/dsmc parcel IO    src/lagrangian/dsmc/parcels/
- *                   dsmcParcelIO.C:133-450                          dsmc_get_particles / dsmc_set_particles
+ *                   dsmcParcelIO.C:133-450                          dsmc_get_particles / dsmc_set_particles,
+ *                                                                   dsmc_read_parcels / dsmc_write_parcels
  *   sigmaTcRMax field (MUST_READ/AUTO_WRITE) dsmcCloud.C:625-636     dsmc_get_cell_array / dsmc_set_cell_array
  *   runtime selection New() of BinaryCollisionModel
  *                   (collisions/BinaryCollisionModel/.../BinaryCollisionModel.C:59-90),
@@ -281,6 +282,22 @@ int dsmc_reset_sampling(dsmc_handle* h);
  * in the order of the case's blockMeshDict when case_dir has one (block by
  * block, i fastest), else in the Cartesian order i + nx (j + ny k). */
 int dsmc_write_fields(dsmc_handle* h, const char* case_dir, const char* time_name, const char* field_name);
+
+/* dsmcParcelIO (dsmcParcelIO.C:133-450): the cloud as the lagrangian files of
+ * an OpenFOAM time directory, <case_dir>/<time_name>/lagrangian/<cloud_name>/
+ * (positions "(x y z) celli" with OpenFOAM's cell labels, U, ERot, typeId,
+ * vibLevel, origId, newParcel, origProcId, classification), 17 significant
+ * digits.  Reading takes positions, U and typeId, and ERot, vibLevel and
+ * origId when present; cells follow from the positions.  Cartesian positions
+ * only (the OpenFOAM v1706 format of dsmcFoam+; not the barycentric one of
+ * OpenFOAM 5 and later).  dsmc_parse_parcels reads without a cloud or a GPU:
+ * call it with pos == NULL for *n, then with arrays of *n entries (*n on
+ * input is their capacity). */
+int dsmc_write_parcels(dsmc_handle* h, const char* case_dir, const char* time_name, const char* cloud_name);
+int dsmc_read_parcels(dsmc_handle* h, const char* case_dir, const char* time_name, const char* cloud_name);
+int dsmc_parse_parcels(const char* case_dir, const char* time_name, const char* cloud_name, long long* n,
+                       double* pos, double* U, double* erot, int* vib, int* species, unsigned* id);
+const char* dsmc_parse_last_error(void);
 
 /* dsmcFaceTracker (faceTracker/dsmcFaceTracker.C:124-190, dsmcCloud.C:425-437):
  * with tracking on, every cell face a parcel crosses in the move gets

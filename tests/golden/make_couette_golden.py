@@ -7,13 +7,17 @@ t = 0.5 s on (resetAtOutputUntilTime 0.5).  The mesh is one 5 x 100 x 1 block,
 so OpenFOAM's cell order is already i + 5 j.  The fixture keeps each field as
 a profile across the channel: the mean over the 5 cells of every row, and
 the standard deviation of those 5 cells (their noise); and the mixture's
-wall heat flux, shear stress and pressure on the 5 faces of each wall.
+wall heat flux, shear stress and pressure on the 5 faces of each wall.  The
+first 2000 parcels of its lagrangian cloud are kept as files of the same
+format (cases/couette_N2-O2/5/lagrangian/dsmc) with their values, beside the
+cloud's dsmcSigmaTcRMax field of that time.
 
 Run in a checkout next to the reference:
     python tests/golden/make_couette_golden.py /path/to/hystrath/hyStrath
 """
 import os
 import re
+import shutil
 import sys
 
 import numpy as np
@@ -43,6 +47,44 @@ def read_patch(path, patch):
     return np.array(m.group(2).split(), dtype=np.float64)
 
 
+N_LAGRANGIAN = 2000
+
+
+def write_lagrangian_sample(src):
+    """The first N_LAGRANGIAN parcels of the reference's cloud files, in the
+    same file format (header, count, one entry per line), as the case's
+    time directory 5/lagrangian/dsmc, with their parsed values beside them."""
+    here = os.path.dirname(os.path.abspath(__file__))
+    dst = os.path.join(here, "cases", "couette_N2-O2", "5", "lagrangian", "dsmc")
+    os.makedirs(dst, exist_ok=True)
+    parsed = {}
+    for name in ("positions", "U", "ERot", "typeId", "vibLevel", "origId", "newParcel", "origProcId",
+                 "classification"):
+        text = open(os.path.join(src, name)).read()
+        head_end = text.index("}", text.index("FoamFile")) + 1
+        head = text[:head_end]
+        rest = text[head_end:]
+        m = re.search(r"\n(\d+)\s*(\(|\{)", rest)
+        n = int(m.group(1))
+        if m.group(2) == "{":
+            val = re.search(r"\{([^}]*)\}", rest[m.start():]).group(1)
+            body = f"\n{N_LAGRANGIAN}{{{val}}}\n"
+        else:
+            lines = rest[m.end():].lstrip("\n").split("\n")[:N_LAGRANGIAN]
+            body = f"\n{N_LAGRANGIAN}\n(\n" + "\n".join(lines) + "\n)\n"
+            parsed[name] = lines
+        assert n >= N_LAGRANGIAN
+        with open(os.path.join(dst, name), "w") as f:
+            f.write(head + "\n" + body)
+    pos = np.array([[float(v) for v in l[l.index("(") + 1:l.index(")")].split()] for l in parsed["positions"]])
+    U = np.array([[float(v) for v in l.strip()[1:-1].split()] for l in parsed["U"]])
+    vib = np.array([int(l[l.index("(") + 1:l.index(")")] or 0) for l in parsed["vibLevel"]])
+    np.savez_compressed(os.path.join(here, "couette_N2-O2_5_parcels.npz"), pos=pos, U=U,
+                        erot=np.array(parsed["ERot"], dtype=float), species=np.array(parsed["typeId"], dtype=int),
+                        vib=vib, id=np.array(parsed["origId"], dtype=np.int64),
+                        cell=np.array([int(l[l.index(")") + 1:].split()[0]) for l in parsed["positions"]]))
+
+
 def main():
     ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
     d = os.path.join(ref, "run/hyStrath/dsmcFoam+/couette_N2-O2/backup-5")
@@ -59,6 +101,11 @@ def main():
     for f in ("wallHeatFlux", "wallShearStress", "p"):
         for w in ("upperWall", "lowerWall"):
             out[f"{f}_{w}"] = read_patch(os.path.join(d, f"{f}_mixture"), w)
+    write_lagrangian_sample(os.path.join(d, "lagrangian", "dsmc"))
+    # the cloud's sigmaTcRMax field of the same time, read with the parcels
+    here = os.path.dirname(os.path.abspath(__file__))
+    shutil.copyfile(os.path.join(d, "dsmcSigmaTcRMax"),
+                    os.path.join(here, "cases", "couette_N2-O2", "5", "dsmcSigmaTcRMax"))
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "couette_N2-O2_5.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, len(out), "profiles")
