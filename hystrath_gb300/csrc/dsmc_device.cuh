@@ -318,8 +318,7 @@ __device__ __forceinline__ double cell_volume(const CaseDev& cs, long long c) {
 // integer both floors agree; otherwise (about one coordinate in 10^4, and
 // every exact integer) the FP64 path decides.  The result is bit for bit that
 // of floor2_coord.
-__device__ __forceinline__ int floor2_coord_fast(const CaseDev& cs, double x, int a) {
-    if (cs.half[a]) return floor2_graded(cs.half[a], 2 * cs.n[a], x);
+__device__ __forceinline__ int floor2_coord_fast_uniform(const CaseDev& cs, double x, int a) {
     const float xf = d2f_bits(x);
     const float p = xf * cs.invF[a];
     const float t = fmaf(xf, cs.invF[a], cs.negOinvF[a]);
@@ -327,7 +326,12 @@ __device__ __forceinline__ int floor2_coord_fast(const CaseDev& cs, double x, in
     const float f = floorf(u);
     const float margin = 1.9073486e-6f * (fabsf(p) + fabsf(cs.negOinvF[a]) + fabsf(t));   // 2 x 2^-20 x (...)
     if (fabsf(u) < 4194304.0f && u - f > margin && (f + 1.0f) - u > margin) return (int)f;
-    return floor2_coord(cs, x, a);
+    return floor2_bits(fma(x, cs.inv[a], cs.negOinv[a]));
+}
+
+__device__ __forceinline__ int floor2_coord_fast(const CaseDev& cs, double x, int a) {
+    if (cs.half[a]) return floor2_graded(cs.half[a], 2 * cs.n[a], x);
+    return floor2_coord_fast_uniform(cs, x, a);
 }
 
 // ------------------------------------------------------- sampling sums

@@ -42,9 +42,14 @@ __device__ __forceinline__ int eq_vib(Rng& r, double T, const SpeciesDev& s) {
     return (int)(-log(r.u01()) * T / s.thetaV);
 }
 
+// dsmcPatchBoundary::measurePropertiesBeforeControl / AfterControl
+// (dsmcPatchBoundary.C:263-482).  The before call keeps its flux terms in
+// pre[] (10 sums, then energy and momentum); the after call adds before and
+// after together, one atomic per sum.
+constexpr int WPRE = W_EVIB + 1 + 4;
 __device__ void wall_measure(const CaseDev& cs, double* wall, long long bf, int axis, double sgn,
                              const double U[3], double erot, int vib, const SpeciesDev& s,
-                             bool after, double* preE, double preMom[3]) {
+                             bool after, double* pre) {
     const int ax1 = (axis == 0) ? 1 : 0;
     const int ax2 = (axis == 2) ? 1 : 2;
     const double fA = cs.bfArea ? cs.bfArea[bf] : cs.dx[ax1] * cs.dx[ax2];
@@ -57,27 +62,22 @@ __device__ void wall_measure(const CaseDev& cs, double* wall, long long bf, int 
     w = 1.0 / (w < SMALL ? SMALL : w);
     const double UU = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
     const double evib = s.nVib ? vib * s.kThetaV : 0.0;
-    double* W = wall + bf * W_N;
-    atomicAdd(W + W_RHON, w);
-    atomicAdd(W + W_RHOM, s.m * w);
-    atomicAdd(W + W_LINKE, 0.5 * s.m * UU * w);
-    atomicAdd(W + W_MCC, s.m * UU * w);
-    atomicAdd(W + W_MOMX, s.m * Ut[0] * w);
-    atomicAdd(W + W_MOMY, s.m * Ut[1] * w);
-    atomicAdd(W + W_MOMZ, s.m * Ut[2] * w);
-    atomicAdd(W + W_EROT, erot * w);
-    atomicAdd(W + W_ZETAROT, s.rotDof * w);
-    atomicAdd(W + W_EVIB, evib * w);
+    const double t[W_EVIB + 1] = {w, s.m * w, 0.5 * s.m * UU * w, s.m * UU * w, s.m * Ut[0] * w,
+                                  s.m * Ut[1] * w, s.m * Ut[2] * w, erot * w, s.rotDof * w, evib * w};
     const double E = 0.5 * s.m * UU + erot + evib;
     if (!after) {
-        *preE = E;
-        for (int a = 0; a < 3; ++a) preMom[a] = s.m * U[a];
-    } else {
-        atomicAdd(W + W_Q, cs.FN * (*preE - E) * invDtFa);
-        atomicAdd(W + W_FDX, cs.FN * (preMom[0] - s.m * U[0]) * invDtFa);
-        atomicAdd(W + W_FDY, cs.FN * (preMom[1] - s.m * U[1]) * invDtFa);
-        atomicAdd(W + W_FDZ, cs.FN * (preMom[2] - s.m * U[2]) * invDtFa);
+        for (int k = 0; k <= W_EVIB; ++k) pre[k] = t[k];
+        pre[W_EVIB + 1] = E;
+        for (int a = 0; a < 3; ++a) pre[W_EVIB + 2 + a] = s.m * U[a];
+        return;
     }
+    double* W = wall + bf * W_N;
+#pragma unroll
+    for (int k = 0; k <= W_EVIB; ++k) atomicAdd(W + k, pre[k] + t[k]);
+    atomicAdd(W + W_Q, cs.FN * (pre[W_EVIB + 1] - E) * invDtFa);
+    atomicAdd(W + W_FDX, cs.FN * (pre[W_EVIB + 2] - s.m * U[0]) * invDtFa);
+    atomicAdd(W + W_FDY, cs.FN * (pre[W_EVIB + 3] - s.m * U[1]) * invDtFa);
+    atomicAdd(W + W_FDZ, cs.FN * (pre[W_EVIB + 4] - s.m * U[2]) * invDtFa);
 }
 
 // dsmcDiffuseWallPatch::performDiffuseReflection for a face of outward normal
@@ -342,16 +342,16 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             // the tracker adds +1 to that face's coupled face: the exit face
             if (cs.faceFlux && hitKind == 0) face_add(cs, face_index(cs, axis, facePlane, hitCell), type, 1.0);
         } else if (pt.model == DSMC_BC_SPECULAR || pt.model == DSMC_BC_DIFFUSE) {
-            double preE, preM[3];
+            double pre[WPRE];
             if (cs.hasWallMeasure)
-                wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, false, &preE, preM);
+                wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, false, pre);
             if (pt.model == DSMC_BC_SPECULAR) {
                 if (U[axis] * sgn > 0.0) U[axis] = -U[axis];
             } else {
                 diffuse_reflect(cs, r, axis, sgn, pt, sp, U, &erot, &vib, err);
             }
             if (cs.hasWallMeasure)
-                wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, true, &preE, preM);
+                wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, true, pre);
             atomicAdd(hits, 1ull);
         } else {
             // deletion (and any patch without a model) removes the parcel
@@ -402,7 +402,7 @@ __device__ __forceinline__ void agg_count(int* count, int key) {
 // not depend on the order of parcels, warps or atomics.
 __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int skey, double ux, double uy,
                                                double uz, double er, int vb, unsigned* err) {
-    long long f[SACC] = {0, 0, 0, 0, 0, 0, 0};
+    long long f[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // SACC values, then a zero pad
     if (skey >= 0) {
         f[SACC_N] = 1;
         f[SACC_UX] = fixp(ux, F_U, err);
@@ -425,6 +425,75 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
     const unsigned lane = lane_id();
     const int prev = __shfl_up_sync(0xFFFFFFFFu, skey, 1);
     const unsigned hm = __ballot_sync(0xFFFFFFFFu, lane == 0 || prev != skey);
+    const int nSeg = __popc(hm);
+    if (nSeg <= 2) {
+        // One or two runs of equal keys (most warps: cells hold tens of
+        // parcels): a transposing butterfly leaves every lane with one total.
+        // With one run lane l ends with value (l >> 2) & 7; with two, lane l
+        // holds value (l >> 1) & 7 of run (l >> 4) & 1.  Run 1 starts at
+        // lane b; its values ride in the upper half of a 16-value vector.
+        const int b = nSeg == 2 ? 31 - __clz(hm) : 32;
+        const bool inB = (int)lane >= b;
+        long long v[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            v[k] = inB ? 0 : f[k];
+            v[8 + k] = inB ? f[k] : 0;
+        }
+        int width = 16;
+        if (nSeg == 1) {
+            width = 8;
+        } else {
+            // 16 -> 8 values across lanes 16 apart
+            const bool up = (lane & 16u) != 0;
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                const long long send = up ? v[k] : v[8 + k];
+                const long long keep = up ? v[8 + k] : v[k];
+                v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 16);
+            }
+        }
+        // 8 -> 4 -> 2 -> 1 values across lanes d apart
+        const int d0 = width == 16 ? 8 : 16;
+        {
+            const bool up = (lane & (unsigned)d0) != 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const long long send = up ? v[k] : v[4 + k];
+                const long long keep = up ? v[4 + k] : v[k];
+                v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, d0);
+            }
+        }
+        {
+            const int d = d0 >> 1;
+            const bool up = (lane & (unsigned)d) != 0;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                const long long send = up ? v[k] : v[2 + k];
+                const long long keep = up ? v[2 + k] : v[k];
+                v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, d);
+            }
+        }
+        {
+            const int d = d0 >> 2;
+            const bool up = (lane & (unsigned)d) != 0;
+            const long long send = up ? v[0] : v[1];
+            const long long keep = up ? v[1] : v[0];
+            v[0] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, d);
+        }
+        for (int d = d0 >> 3; d >= 1; d >>= 1) v[0] += __shfl_xor_sync(0xFFFFFFFFu, v[0], d);
+        // the lane holding (run, value) adds it
+        const int shiftV = nSeg == 1 ? 2 : 1;
+        const int val = (int)(lane >> shiftV) & 7;
+        const int run = nSeg == 1 ? 0 : (int)(lane >> 4) & 1;
+        const bool first = (lane & ((1u << shiftV) - 1u)) == 0;
+        const int rkey = __shfl_sync(0xFFFFFFFFu, skey, run == 0 ? 0 : (b & 31));
+        if (first && val < SACC && rkey >= 0 && v[0])
+            atomicAdd(reinterpret_cast<unsigned long long*>(
+                          sfix + (long long)((rkey & 7) * SACC + val) * C + (rkey >> 3)),
+                      (unsigned long long)v[0]);
+        return;
+    }
     const int segStart = 31 - __clz(hm & (0xFFFFFFFFu >> (31 - (int)lane)));
     // the count is the run's length; vibrational levels sum in 32 bits
     f[SACC_N] = (long long)((int)lane - segStart + 1);
@@ -451,6 +520,9 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
 // state after the previous step's collisions, which the reference samples at
 // the end of that step) into the per-cell sample sums: it streams the
 // velocities anyway, in cell order.
+// GEN = false is the instantiation for uniform meshes without reduced-D axes,
+// solid boxes or face tracking: their branches are compiled out.
+template <bool GEN>
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix) {
     const long long n = ctr->nMoved;
@@ -477,7 +549,7 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                 // tracking velocity (zero along an empty axis, whose coordinate
                 // is held at the mesh centre: dsmcParcel.C:73-84)
                 double tux = ux, tuy = uy, tuz = uz;
-                if (cs.anyEmpty) {
+                if (GEN && cs.anyEmpty) {
                     if (cs.emptyAx[0]) { x = cs.mid[0]; tux = 0.0; }
                     if (cs.emptyAx[1]) { y = cs.mid[1]; tuy = 0.0; }
                     if (cs.emptyAx[2]) { z = cs.mid[2]; tuz = 0.0; }
@@ -500,9 +572,9 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                 const double ex = fma(tux, tr, x);
                 const double ey = fma(tuy, tr, y);
                 const double ez = fma(tuz, tr, z);
-                const int c2x = floor2_coord_fast(cs, ex, 0);
-                const int c2y = floor2_coord_fast(cs, ey, 1);
-                const int c2z = floor2_coord_fast(cs, ez, 2);
+                const int c2x = GEN ? floor2_coord_fast(cs, ex, 0) : floor2_coord_fast_uniform(cs, ex, 0);
+                const int c2y = GEN ? floor2_coord_fast(cs, ey, 1) : floor2_coord_fast_uniform(cs, ey, 1);
+                const int c2z = GEN ? floor2_coord_fast(cs, ez, 2) : floor2_coord_fast_uniform(cs, ez, 2);
                 const int cx = c2x >> 1, cy = c2y >> 1, cz = c2z >> 1;
                 const bool inX = (unsigned)cx < (unsigned)cs.n[0], inY = (unsigned)cy < (unsigned)cs.n[1],
                            inZ = (unsigned)cz < (unsigned)cs.n[2];
@@ -515,9 +587,9 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     const int a = !inX ? 0 : !inY ? 1 : 2;
                     const int c2a = a == 0 ? c2x : a == 1 ? c2y : c2z;
                     const int side = 2 * a + (c2a < 0 ? 0 : 1);
-                    if (cs.sideDeletes[side] && !cs.faceFlux) delSide = side;
+                    if (cs.sideDeletes[side] && !(GEN && cs.faceFlux)) delSide = side;
                 }
-                if ((inside || delSide >= 0) && cs.nObst) {
+                if (GEN && (inside || delSide >= 0) && cs.nObst) {
                     const uint32_t c = cellw_cell(w);
                     const int sx = (int)(c % (uint32_t)cs.n[0]);
                     const int sy = (int)((c / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]);
@@ -535,7 +607,7 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     s.cellw[i] = CELLW_DELETED;
                     fast = true;
                 } else if (inside) {
-                    if (cs.faceFlux) {
+                    if (GEN && cs.faceFlux) {
                         const uint32_t c0 = cellw_cell(w);
                         const int sc[3] = {(int)(c0 % (uint32_t)cs.n[0]),
                                            (int)((c0 / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]),
@@ -763,9 +835,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
 // the warp) and writes only the parcel's source index there.  k_gather then
 // walks the destination slots in order and pulls each parcel's state from its
 // source: every store is coalesced, and the loads of one warp come from a few
-// runs of neighbouring source cells.  Storing the payload from the source side
-// instead leaves most sectors partly written (parcels that changed cell land
-// in short runs all over the destination).
+// runs of neighbouring source cells.  Storing the 64-byte records from the
+// source side instead (each parcel to start[cell] + a rank taken in the move)
+// measured 16% slower on the sort and 4% on the move that keeps the ranks.
 __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_scatter_index(const uint32_t* __restrict__ cellw, Counters* ctr,
                                                        const int* __restrict__ start, int* count,
                                                        int2* __restrict__ sortSrc) {
@@ -1104,7 +1176,9 @@ int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TIL
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
     const int T = B.cfg.streamThreads;
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
-    k_move<<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
+    const bool general = cs.anyEmpty || cs.nObst || cs.faceFlux || cs.half[0] || cs.half[1] || cs.half[2];
+    if (general) k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
+    else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
     k_move_slow<<<grid_for(B.capacity, T, 2), T, 0, st>>>(cs, s, B.ctr, B.slowList,
                                                                                B.bfPatch, B.wall, B.count);
 }
