@@ -120,7 +120,9 @@ KERNELS_PER_STEP = 21
 def bytes_model(N, C, coll, cand, n_acc):
     """Algorithmic bytes per step, per phase.
 
-    move:    read pos,U (48) + cell word (4); write pos (24) + cell word (4)
+    move:    read pos, U, ERot and species word (64: the step's sample of the
+             post-collision state is folded into the move) + cell word (4);
+             write pos (24) + cell word (4)
     sort:    stable counting sort of the state, read + write (2 x 68), plus
              the per-cell count and offset (8 B per cell)
     collide: per cell the candidate count (start, sigmaTcRMax, remainder,
@@ -130,7 +132,7 @@ def bytes_model(N, C, coll, cand, n_acc):
              draw (8 B); per candidate the two velocities and species words
              (2 x 32 B); per collision the energies written back (2 x 64 B)
     """
-    move = 80.0 * N
+    move = 96.0 * N
     sort = 2.0 * STATE_BYTES * N + 8.0 * C
     collide = (36.0 + 0.5 * n_acc) * C + 8.0 * N + 64.0 * cand + 128.0 * coll
     return move, sort, collide

@@ -80,6 +80,18 @@ __device__ void wall_measure(const CaseDev& cs, double* wall, long long bf, int 
     atomicAdd(W + W_FDZ, cs.FN * (pre[W_EVIB + 4] - s.m * U[2]) * invDtFa);
 }
 
+// The after call of a specular reflection: |U.n|, the tangential velocity and
+// the energies are unchanged, so every flux term equals its before term, the
+// heat flux is zero and the force is along the normal only.
+__device__ void wall_measure_specular(const CaseDev& cs, double* wall, long long bf, int axis, const double U[3],
+                                      const SpeciesDev& s, const double* pre) {
+    double* W = wall + bf * W_N;
+#pragma unroll
+    for (int k = 0; k <= W_EVIB; ++k) atomicAdd(W + k, pre[k] + pre[k]);
+    const double invDtFa = cs.bfArea ? 1.0 / (cs.dt * cs.bfArea[bf]) : cs.invDtFa[axis];
+    atomicAdd(W + W_FDX + axis, cs.FN * (pre[W_EVIB + 2 + axis] - s.m * U[axis]) * invDtFa);
+}
+
 // dsmcDiffuseWallPatch::performDiffuseReflection for a face of outward normal
 // sgn * e_axis, with dsmcPatchBoundary::calculateWallUnitVectors.
 __device__ void diffuse_reflect(const CaseDev& cs, Rng& r, int axis, double sgn, const PatchDev& pt,
@@ -222,7 +234,7 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
         bool out = false;
         for (int a = 0; a < 3; ++a) {
             ex[a] = fma(V[a], tr, x[a]);
-            c2[a] = floor2_coord(cs, ex[a], a);
+            c2[a] = floor2_coord_fast(cs, ex[a], a);
             ci[a] = c2[a] >> 1;
             if (ci[a] < 0 || ci[a] >= cs.n[a]) out = true;
         }
@@ -297,7 +309,7 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
         // the fluid cell at the hit point and the plane index of the face hit
         int hitCell[3], facePlane;
         for (int a = 0; a < 3; ++a) {
-            const int cc = floor2_coord(cs, x[a], a) >> 1;
+            const int cc = floor2_coord_fast(cs, x[a], a) >> 1;
             hitCell[a] = min(max(cc, 0), cs.n[a] - 1);
         }
         if (hitKind == 0) {
@@ -314,8 +326,8 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
         long long bf;
         double sgn;
         if (hitKind == 0) {
-            int ib = floor2_coord(cs, x[b], b) >> 1;
-            int ic = floor2_coord(cs, x[c], c) >> 1;
+            int ib = floor2_coord_fast(cs, x[b], b) >> 1;
+            int ic = floor2_coord_fast(cs, x[c], c) >> 1;
             ib = min(max(ib, 0), cs.n[b] - 1);
             ic = min(max(ic, 0), cs.n[c] - 1);
             bf = cs.sideOff[hitSide] + ib + (long long)cs.n[b] * ic;
@@ -324,8 +336,8 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             const int o = hitKind - 1;
             const int nb = cs.obHiI[o][b] - cs.obLoI[o][b];
             const int nc = cs.obHiI[o][c] - cs.obLoI[o][c];
-            int ib = (floor2_coord(cs, x[b], b) >> 1) - cs.obLoI[o][b];
-            int ic = (floor2_coord(cs, x[c], c) >> 1) - cs.obLoI[o][c];
+            int ib = (floor2_coord_fast(cs, x[b], b) >> 1) - cs.obLoI[o][b];
+            int ic = (floor2_coord_fast(cs, x[c], c) >> 1) - cs.obLoI[o][c];
             ib = min(max(ib, 0), nb - 1);
             ic = min(max(ic, 0), nc - 1);
             bf = cs.obstOff[o][hitSide] + ib + (long long)nb * ic;
@@ -350,8 +362,10 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
             } else {
                 diffuse_reflect(cs, r, axis, sgn, pt, sp, U, &erot, &vib, err);
             }
-            if (cs.hasWallMeasure)
-                wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, true, pre);
+            if (cs.hasWallMeasure) {
+                if (pt.model == DSMC_BC_SPECULAR) wall_measure_specular(cs, wall, bf, axis, U, sp, pre);
+                else wall_measure(cs, wall, bf, axis, sgn, U, erot, vib, sp, true, pre);
+            }
             atomicAdd(hits, 1ull);
         } else {
             // deletion (and any patch without a model) removes the parcel
@@ -365,14 +379,14 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
         if (cs.faceFlux && pt.type != DSMC_PATCH_CYCLIC)
             face_add(cs, face_index(cs, axis, facePlane, hitCell), type, U[axis] * sgn > 0.0 ? 1.0 : -1.0);
         for (int a = 0; a < 3; ++a) {
-            int cc = floor2_coord(cs, x[a], a) >> 1;
+            int cc = floor2_coord_fast(cs, x[a], a) >> 1;
             sc[a] = min(max(cc, 0), cs.n[a] - 1);
         }
     }
     if (!done) {
         int ci[3], sb = 0;
         for (int a = 0; a < 3; ++a) {
-            int c2 = floor2_coord(cs, x[a], a);
+            int c2 = floor2_coord_fast(cs, x[a], a);
             c2 = min(max(c2, 0), 2 * cs.n[a] - 1);
             ci[a] = c2 >> 1;
             sb |= (c2 & 1) << a;
