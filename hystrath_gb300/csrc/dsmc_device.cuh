@@ -345,23 +345,15 @@ constexpr int F_E = 100;       // rotational energy: resolution 7.9e-31 J
 
 // round(v 2^F), halves away from zero, from the bits on the integer pipe;
 // |v 2^F| must stay below 2^62 (saturates and flags otherwise)
+// round(v 2^F) as a 64-bit integer: the exponent field takes the scaling
+// (exact) and one round-to-nearest conversion the rest; zero and subnormal
+// inputs give 0, magnitudes of 2^(62-F) and more set the bounds flag.
 __device__ __forceinline__ long long fixp(double v, int F, unsigned* err) {
     const long long b = __double_as_longlong(v);
     const int e = (int)((b >> 52) & 0x7FF);
-    if (e == 0) return 0;
-    const long long m = (b & 0x000FFFFFFFFFFFFFll) | 0x0010000000000000ll;
-    const int sh = e - 1075 + F;
-    long long r;
-    if (sh >= 0) {
-        if (sh > 9) { *err |= ERRB_BOUNDS; r = (1ll << 62); }
-        else r = m << sh;
-    } else if (sh > -63) {
-        const int rs = -sh;
-        r = (m >> rs) + ((m >> (rs - 1)) & 1);
-    } else {
-        r = 0;
-    }
-    return b < 0 ? -r : r;
+    if (e - 1075 + F > 9) *err |= ERRB_BOUNDS;
+    const long long r = __double2ll_rn(__longlong_as_double(b + ((long long)F << 52)));
+    return e == 0 ? 0 : r;
 }
 
 __device__ __forceinline__ double unfix(long long s, int F) { return ldexp((double)s, -F); }

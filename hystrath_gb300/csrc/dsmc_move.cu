@@ -409,6 +409,38 @@ __device__ __forceinline__ void agg_count(int* count, int key) {
     if (key >= 0 && (int)lane_id() == leader) atomicAdd(&count[key], __popc(peers));
 }
 
+// Three transposing rounds over lanes d, d/2, d/4 apart: 8 values per lane
+// become 1, lane l keeping value 4 b(d) + 2 b(d/2) + b(d/4) of its partners'
+// sums (b(x): whether bit x of the lane is set).
+__device__ __forceinline__ void butterfly8(long long* v, unsigned lane, int d) {
+    {
+        const bool up = (lane & (unsigned)d) != 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const long long send = up ? v[k] : v[4 + k];
+            const long long keep = up ? v[4 + k] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, d);
+        }
+    }
+    {
+        const int e = d >> 1;
+        const bool up = (lane & (unsigned)e) != 0;
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const long long send = up ? v[k] : v[2 + k];
+            const long long keep = up ? v[2 + k] : v[k];
+            v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, e);
+        }
+    }
+    {
+        const int e = d >> 2;
+        const bool up = (lane & (unsigned)e) != 0;
+        const long long send = up ? v[0] : v[1];
+        const long long keep = up ? v[1] : v[0];
+        v[0] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, e);
+    }
+}
+
 // One parcel's contribution to the dsmcVolFields sample sums
 // (dsmcVolFields.C:1115-1239) per lane, valid when skey = cell * 8 + species
 // is not negative: summed over the warp's runs of equal keys and added to the
@@ -440,71 +472,45 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
     const int prev = __shfl_up_sync(0xFFFFFFFFu, skey, 1);
     const unsigned hm = __ballot_sync(0xFFFFFFFFu, lane == 0 || prev != skey);
     const int nSeg = __popc(hm);
-    if (nSeg <= 2) {
-        // One or two runs of equal keys (most warps: cells hold tens of
-        // parcels): a transposing butterfly leaves every lane with one total.
-        // With one run lane l ends with value (l >> 2) & 7; with two, lane l
-        // holds value (l >> 1) & 7 of run (l >> 4) & 1.  Run 1 starts at
-        // lane b; its values ride in the upper half of a 16-value vector.
-        const int b = nSeg == 2 ? 31 - __clz(hm) : 32;
+    if (nSeg == 1) {
+        // One run (most warps: cells hold tens of parcels): a transposing
+        // butterfly, each round sending half of a lane's vector to its
+        // partner, leaves lane l with the total of value (l >> 2) & 7.
+        long long v[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = f[k];
+        butterfly8(v, lane, 16);
+        v[0] += __shfl_xor_sync(0xFFFFFFFFu, v[0], 2);
+        v[0] += __shfl_xor_sync(0xFFFFFFFFu, v[0], 1);
+        const int val = (int)(lane >> 2) & 7;
+        if ((lane & 3u) == 0 && val < SACC && skey >= 0 && v[0])
+            atomicAdd(reinterpret_cast<unsigned long long*>(sfix + (long long)((skey & 7) * SACC + val) * C +
+                                                            (skey >> 3)),
+                      (unsigned long long)v[0]);
+        return;
+    }
+    if (nSeg == 2) {
+        // Two runs, the second from lane b: the first round splits a
+        // 16-value vector (run 0's values, then run 1's) across lanes 16
+        // apart; lane l ends with value (l >> 1) & 7 of run (l >> 4) & 1.
+        const int b = 31 - __clz(hm);
         const bool inB = (int)lane >= b;
-        long long v[16];
+        const bool up = (lane & 16u) != 0;
+        long long v[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            v[k] = inB ? 0 : f[k];
-            v[8 + k] = inB ? f[k] : 0;
+            // keep my half's run, send the other run's values
+            const long long mine = (up == inB) ? f[k] : 0;
+            const long long other = (up == inB) ? 0 : f[k];
+            v[k] = mine + __shfl_xor_sync(0xFFFFFFFFu, other, 16);
         }
-        int width = 16;
-        if (nSeg == 1) {
-            width = 8;
-        } else {
-            // 16 -> 8 values across lanes 16 apart
-            const bool up = (lane & 16u) != 0;
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const long long send = up ? v[k] : v[8 + k];
-                const long long keep = up ? v[8 + k] : v[k];
-                v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, 16);
-            }
-        }
-        // 8 -> 4 -> 2 -> 1 values across lanes d apart
-        const int d0 = width == 16 ? 8 : 16;
-        {
-            const bool up = (lane & (unsigned)d0) != 0;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const long long send = up ? v[k] : v[4 + k];
-                const long long keep = up ? v[4 + k] : v[k];
-                v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, d0);
-            }
-        }
-        {
-            const int d = d0 >> 1;
-            const bool up = (lane & (unsigned)d) != 0;
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const long long send = up ? v[k] : v[2 + k];
-                const long long keep = up ? v[2 + k] : v[k];
-                v[k] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, d);
-            }
-        }
-        {
-            const int d = d0 >> 2;
-            const bool up = (lane & (unsigned)d) != 0;
-            const long long send = up ? v[0] : v[1];
-            const long long keep = up ? v[1] : v[0];
-            v[0] = keep + __shfl_xor_sync(0xFFFFFFFFu, send, d);
-        }
-        for (int d = d0 >> 3; d >= 1; d >>= 1) v[0] += __shfl_xor_sync(0xFFFFFFFFu, v[0], d);
-        // the lane holding (run, value) adds it
-        const int shiftV = nSeg == 1 ? 2 : 1;
-        const int val = (int)(lane >> shiftV) & 7;
-        const int run = nSeg == 1 ? 0 : (int)(lane >> 4) & 1;
-        const bool first = (lane & ((1u << shiftV) - 1u)) == 0;
-        const int rkey = __shfl_sync(0xFFFFFFFFu, skey, run == 0 ? 0 : (b & 31));
-        if (first && val < SACC && rkey >= 0 && v[0])
-            atomicAdd(reinterpret_cast<unsigned long long*>(
-                          sfix + (long long)((rkey & 7) * SACC + val) * C + (rkey >> 3)),
+        butterfly8(v, lane, 8);
+        v[0] += __shfl_xor_sync(0xFFFFFFFFu, v[0], 1);
+        const int val = (int)(lane >> 1) & 7;
+        const int rkey = __shfl_sync(0xFFFFFFFFu, skey, up ? b : 0);
+        if ((lane & 1u) == 0 && val < SACC && rkey >= 0 && v[0])
+            atomicAdd(reinterpret_cast<unsigned long long*>(sfix + (long long)((rkey & 7) * SACC + val) * C +
+                                                            (rkey >> 3)),
                       (unsigned long long)v[0]);
         return;
     }
