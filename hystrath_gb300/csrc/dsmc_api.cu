@@ -99,6 +99,7 @@ int alloc_soa(dsmc_handle* h, Parcels* s, long long cap) {
     int rc;
     if ((rc = dalloc(h, &s->r, cap))) return rc;
     if ((rc = dalloc(h, &s->cellw, cap))) return rc;
+    if ((rc = dalloc(h, &s->id, cap))) return rc;
     return DSMC_OK;
 }
 
@@ -1154,6 +1155,7 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
     int rc;
     if ((rc = load(s.r, sizeof(Rec) * n))) return rc;
     if ((rc = load(s.cellw, sizeof(uint32_t) * n))) return rc;
+    launch_ids_from_records(s, n, h->stream);
     if ((rc = load(h->B.start, sizeof(int) * (h->cs.C + 1)))) return rc;
     if ((rc = load(h->B.smax, sizeof(double) * h->cs.C))) return rc;
     if ((rc = load(h->B.rem, sizeof(double) * h->cs.C))) return rc;

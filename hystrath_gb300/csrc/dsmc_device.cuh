@@ -155,6 +155,8 @@ __host__ __device__ inline uint32_t make_sv(int species, int vib) { return (uint
 struct Parcels {
     Rec* r;            // [capacity]
     uint32_t* cellw;   // [capacity]
+    uint32_t* id;      // [capacity] copy of r[i].id, written wherever records take new slots: the
+                       // collision kernels stage a cell's ids from here (8 per sector)
 };
 
 // Whole-record access with four 16-byte loads or stores.

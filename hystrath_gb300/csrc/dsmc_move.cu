@@ -907,9 +907,16 @@ __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_gather(Parcels src, Parc
             atomicOr(&ctr->err, ERRB_BOUNDS);
             continue;
         }
-        st_rec(dst.r + j, ldg_rec(src.r + i));
+        const Rec p = ldg_rec(src.r + i);
+        st_rec(dst.r + j, p);
         __stcs(dst.cellw + j, (uint32_t)sk.y);
+        dst.id[j] = p.id;
     }
+}
+
+__global__ void k_ids_from_records(Parcels s, long long n) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s.id[i] = s.r[i].id;
 }
 
 __global__ void k_finish_sort(Counters* ctr) {
@@ -1048,6 +1055,7 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
         p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
         p.erot = erot;
         p.id = (uint32_t)(ctr->nextId + g);
+        s.id[slot] = p.id;
         p.sv = make_sv(m, vib);
         st_rec(s.r + slot, p);
         s.cellw[slot] = ((uint32_t)cellOf[f] << 3) | CELLW_FRESH;
@@ -1148,6 +1156,7 @@ __global__ void k_init_fill(CaseDev cs, const double* __restrict__ nd, const uns
             p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
             p.erot = erot;
             p.id = pid;
+            s.id[slot] = pid;
             p.sv = make_sv(m, vib);
             st_rec(s.r + slot, p);
             s.cellw[slot] = ((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) | (uint32_t)sb;
@@ -1223,6 +1232,10 @@ void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src,
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
     k_scatter_index<<<grid, T, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortSrc);
     k_gather<<<grid, T, 0, st>>>(src, dst, B.ctr, B.sortSrc);
+}
+
+void launch_ids_from_records(const Parcels& s, long long n, cudaStream_t st) {
+    if (n > 0) k_ids_from_records<<<grid_for(n, 256, 8), 256, 0, st>>>(s, n);
 }
 
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st) {

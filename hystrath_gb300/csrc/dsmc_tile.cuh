@@ -220,7 +220,7 @@ k_cell_order(Parcels s, const int* __restrict__ start, const Counters* ctr, cons
             if (j < n) {
                 const uint32_t w = s.cellw[off + j];
                 sb = (int)(w & 7u);
-                key = order_key(w, s.r[off + j].id, j);
+                key = order_key(w, __ldg(s.id + off + j), j);
             }
             keys[j] = key;
 #pragma unroll
@@ -256,7 +256,7 @@ k_cell_order_big(Parcels s, const int* __restrict__ start, const Counters* ctr, 
             if (j < n) {
                 const uint32_t w = s.cellw[off + j];
                 atomicAdd(&cnt[w & 7u], 1);
-                key = order_key(w, s.r[off + j].id, j);
+                key = order_key(w, __ldg(s.id + off + j), j);
             }
             keysBig[j] = key;
         }
@@ -546,7 +546,7 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
         for (int j = 0; j < n; ++j) {
             const uint32_t sb = __ldg(s.cellw + off + j) & 7u;
             st.sub[j][lane] = (uint8_t)sb;
-            st.id[j][lane] = s.r[off + j].id;
+            st.id[j][lane] = __ldg(s.id + off + j);
             subCnt += 1ull << (8u * sb);
         }
         const double R = smax[c];
