@@ -69,6 +69,7 @@ def _bind():
         return L
     vp = C.c_void_p
     L.dsmc_batch_create.argtypes = [C.c_int, vp, C.POINTER(vp)]
+    L.dsmc_batch_create_from_dirs.argtypes = [C.c_int, C.POINTER(C.c_char_p), C.POINTER(vp)]
     L.dsmc_batch_destroy.argtypes = [vp]
     L.dsmc_batch_destroy.restype = None
     L.dsmc_batch_last_error.argtypes = [vp]
@@ -90,10 +91,15 @@ class BatchCloud:
     """Independent clouds stepped together by one graph launch per step."""
 
     def __init__(self, specs):
+        """specs: CaseSpec objects, or OpenFOAM case directories (str)."""
         L = _bind()
-        arr = (S.CaseSpec * len(specs))(*specs)
         h = C.c_void_p()
-        rc = L.dsmc_batch_create(len(specs), C.cast(arr, C.c_void_p), C.byref(h))
+        if specs and all(isinstance(x, str) for x in specs):
+            arr = (C.c_char_p * len(specs))(*[x.encode() for x in specs])
+            rc = L.dsmc_batch_create_from_dirs(len(specs), arr, C.byref(h))
+        else:
+            arr = (S.CaseSpec * len(specs))(*specs)
+            rc = L.dsmc_batch_create(len(specs), C.cast(arr, C.c_void_p), C.byref(h))
         if rc != 0:
             raise DsmcError(rc, L.dsmc_batch_last_error(None).decode())
         self.h = h

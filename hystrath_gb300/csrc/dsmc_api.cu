@@ -1302,6 +1302,30 @@ int dsmc_batch_create(int n, const dsmc_case_spec* specs, dsmc_batch** out) {
     return DSMC_OK;
 }
 
+int dsmc_batch_create_from_dirs(int n, const char* const* case_dirs, dsmc_batch** out) {
+    *out = nullptr;
+    if (n < 1) return bfail(nullptr, DSMC_ERR_INVALID, "a batch needs at least one case");
+    auto b = std::make_unique<dsmc_batch>();
+    for (int i = 0; i < n; ++i) {
+        // each case is parsed and created before the next is parsed: the
+        // parser's per-face and node tables live until the next parse
+        dsmc_handle* h = nullptr;
+        int rc = dsmc_create(case_dirs[i], &h);
+        if (rc) {
+            const std::string m = std::string("case ") + case_dirs[i] + ": " + dsmc_last_global_error();
+            for (dsmc_handle* q : b->cases) dsmc_destroy(q);
+            return bfail(nullptr, rc, m);
+        }
+        b->cases.push_back(h);
+    }
+    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        for (dsmc_handle* q : b->cases) dsmc_destroy(q);
+        return bfail(nullptr, DSMC_ERR_CUDA, "cannot create the batch stream");
+    }
+    *out = b.release();
+    return DSMC_OK;
+}
+
 void dsmc_batch_destroy(dsmc_batch* b) {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);

@@ -412,6 +412,8 @@ int dsmc_get_launch(dsmc_handle* h, int* cta_threads, int* cells_per_cta);
  */
 typedef struct dsmc_batch dsmc_batch;
 int dsmc_batch_create(int n, const dsmc_case_spec* specs, dsmc_batch** out);
+/* The same from n OpenFOAM case directories (each as dsmc_create). */
+int dsmc_batch_create_from_dirs(int n, const char* const* case_dirs, dsmc_batch** out);
 void dsmc_batch_destroy(dsmc_batch* b);
 const char* dsmc_batch_last_error(const dsmc_batch* b);
 int dsmc_batch_size(const dsmc_batch* b);

@@ -90,3 +90,25 @@ def test_launch_shape_does_not_change_results(shape):
     for k in a:
         assert np.array_equal(a[k], b[k]), k
     np.testing.assert_array_equal(ref.field("Ttra"), g.field("Ttra"))
+
+
+@pytest.mark.gpu
+def test_batch_from_case_directories():
+    """Cases given as OpenFOAM directories (each parsed and created before the
+    next is parsed) step together as they step alone."""
+    import os
+    from hystrath_gb300.batch import BatchCloud
+    from hystrath_gb300.dsmc import DsmcCloud
+    here = os.path.dirname(os.path.abspath(__file__))
+    dirs = [os.path.join(here, "golden", "cases", c) for c in ("couette_N2-O2", "hypersonic_corner")]
+    b = BatchCloud(dirs)
+    b.initialise()
+    b.evolve(5)
+    for i, d in enumerate(dirs):
+        g = DsmcCloud(d)
+        g.initialise()
+        g.evolve(5)
+        a, c = b.info(i), g.info()
+        assert a.n_particles == c.n_particles and a.collisions_total == c.collisions_total
+        assert a.linear_ke == c.linear_ke
+    b.close()

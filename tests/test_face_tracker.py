@@ -17,6 +17,7 @@ from hystrath_gb300 import spec as S
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CORNER = os.path.join(HERE, "golden", "cases", "hypersonic_corner")
+PLATE = os.path.join(HERE, "golden", "cases", "supersonic_flat_plate")
 
 
 def _split(F, n):
@@ -156,16 +157,17 @@ def _gpu_oracle_pair(spec, oracle_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("case", ["specular", "cyclic", "channel_cube", "corner"])
+@pytest.mark.parametrize("case", ["specular", "cyclic", "channel_cube", "corner", "graded_plate"])
 def test_gpu_face_flux_matches_oracle(gpu_lib, oracle_mod, case):
     """Same parcels, same random streams: every face gets the same count on
     the GPU and in the oracle (walls, symmetry, cyclic, obstacle, inflow,
-    deletion)."""
+    deletion, graded cells with an empty axis)."""
     from hystrath_gb300.dsmc import parse_case
     spec = {"specular": lambda: S.config0(seed=31),
             "cyclic": lambda: S.config0(seed=32, cyclic=True),
             "channel_cube": lambda: S.config2(seed=33, scale=8),
-            "corner": lambda: parse_case(CORNER)}[case]()
+            "corner": lambda: parse_case(CORNER),
+            "graded_plate": lambda: parse_case(PLATE)}[case]()
     g, o = _gpu_oracle_pair(spec, oracle_mod)
     for _ in range(3):
         g.run_phases(S.PHASE_INFLOW | S.PHASE_MOVE | S.PHASE_SORT)
