@@ -306,6 +306,7 @@ void fill_case_dev(dsmc_handle* h) {
     cs.collModel = s.binary_collision_model;
     cs.selModel = s.partner_selection_model;
     cs.zrot = s.zrot;
+    cs.invZrot = 1.0 / s.zrot;
     cs.fixedZv = s.fixed_zv;
     cs.invZvForm = s.inv_zv_formulation;
     cs.nPatches = s.n_patches;
@@ -335,6 +336,9 @@ void fill_case_dev(dsmc_handle* h) {
             p.mPfrac = a.mass / (a.mass + b.mass);
             p.mQfrac = b.mass / (a.mass + b.mass);
             p.invAlphaPQ = 1.0 / (0.5 * (a.alpha + b.alpha));
+            p.invAlphaF = (float)p.invAlphaPQ;
+            p.chiBF = (float)(2.5 - om);
+            p.invChiBF = (float)(1.0 / (2.5 - om));
             p.sigmaPrefactorF = (float)p.sigmaPrefactor;
             p.expoF = (float)p.expo;
         }

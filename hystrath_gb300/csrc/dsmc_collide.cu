@@ -25,18 +25,24 @@ namespace {
 
 
 
-__device__ __forceinline__ double post_rot(Rng& r, double dof, double ChiB, unsigned* err) {
-    if (dof == 2.0) return 1.0 - pow(r.u01(), 1.0 / ChiB);
-    const double ChiA = 0.5 * dof;
-    const double A1 = ChiA - 1., B1 = ChiB - 1.;
-    if (A1 < SMALL && B1 < SMALL) return r.u01();
+// postCollisionRotationalEnergy (dsmcCloud.C:1327-1387): the fraction of
+// the collision energy that goes to rotation.  Energy is conserved by the
+// caller (the translational part is the remainder), so the fraction only
+// needs its distribution: it is drawn in FP32 (an FP64 pow costs tens of
+// FP64 instructions, which on this part issue over the whole warp).
+__device__ __forceinline__ double post_rot(Rng& r, double dof, const PairDev& pr, unsigned* err) {
+    if (dof == 2.0) return 1.0 - (double)powf((float)r.u01(), pr.invChiBF);
+    const float ChiA = (float)(0.5 * dof);
+    const float A1 = ChiA - 1.f, B1 = pr.chiBF - 1.f;
+    if (A1 < (float)SMALL && B1 < (float)SMALL) return r.u01();
     for (int it = 0; it < MAX_REJECTION; ++it) {
         const double ratio = r.u01();
-        double Pr;
-        if (A1 < SMALL) Pr = pow(1.0 - ratio, B1);
-        else if (B1 < SMALL) Pr = pow(1.0 - ratio, A1);
-        else Pr = pow((A1 + B1) * ratio / A1, A1) * pow((A1 + B1) * (1 - ratio) / B1, B1);
-        if (!(Pr < r.u01())) return ratio;
+        const float rf = (float)ratio;
+        float Pr;
+        if (A1 < (float)SMALL) Pr = powf(1.f - rf, B1);
+        else if (B1 < (float)SMALL) Pr = powf(1.f - rf, A1);
+        else Pr = powf((A1 + B1) * rf / A1, A1) * powf((A1 + B1) * (1.f - rf) / B1, B1);
+        if (!((double)Pr < r.u01())) return ratio;
     }
     *err |= ERRB_REJECTION;
     return 0.0;
@@ -78,8 +84,9 @@ __device__ __forceinline__ int post_vib(const CaseDev& cs, Rng& r, int vib, int 
 }
 
 __device__ __forceinline__ void redistribute(const CaseDev& cs, const SpeciesDev& s, double* erot, int* vib,
-                                             double& Et, double omegaPQ, Rng& r, const double* tab,
+                                             double& Et, const PairDev& pr, Rng& r, const double* tab,
                                              unsigned* err) {
+    const double omegaPQ = pr.omegaPQ;
     if (s.nVib > 0) {
         const double EcP = Et + *vib * s.kThetaV;
         const int iMax = (int)(EcP / s.kThetaV);
@@ -90,10 +97,9 @@ __device__ __forceinline__ void redistribute(const CaseDev& cs, const SpeciesDev
     }
     if (s.rotDof > 0) {
         const double pre = *erot;
-        if (1.0 / cs.zrot > r.u01()) {
+        if (cs.invZrot > r.u01()) {
             const double EcP = Et + pre;
-            const double ChiB = 2.5 - omegaPQ;
-            const double ratio = post_rot(r, s.rotDof, ChiB, err);
+            const double ratio = post_rot(r, s.rotDof, pr, err);
             *erot = ratio * EcP;
             Et = EcP - *erot;
         }

@@ -65,6 +65,9 @@ struct PairDev {
     double mPfrac;          // mP / (mP + mQ)
     double mQfrac;          // mQ / (mP + mQ)
     double invAlphaPQ;      // 1 / alphaPQ, alphaPQ = (alphaP + alphaQ) / 2 (VariableSoftSphere)
+    float invAlphaF;        // FP32 copies for the energy-ratio and deflection draws
+    float invChiBF;         // 1 / (5/2 - omegaPQ)
+    float chiBF;            // 5/2 - omegaPQ
 };
 
 struct PatchDev {
@@ -106,6 +109,7 @@ struct CaseDev {
     int collModel;
     int selModel;       // DSMC_SEL_*
     double zrot, fixedZv;
+    double invZrot;     // 1 / Zrot
     int invZvForm;
     int nPatches;
     SpeciesDev sp[DSMC_MAX_SPECIES];

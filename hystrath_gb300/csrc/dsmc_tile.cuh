@@ -281,13 +281,25 @@ struct Post {
     int vP, vQ;
 };
 
+// A uniform azimuth phi = 2 pi U as (sin, cos): the angle in FP32
+// (sincospif), the pair then scaled to unit length in FP64 so that the
+// scattered relative speed, and with it the energy, stays exact to FP64.
+__device__ __forceinline__ void azimuth(Rng& r, double* s, double* c) {
+    float sf, cf;
+    sincospif(2.0f * (float)r.u01(), &sf, &cf);
+    const double sd = sf, cd = cf;
+    const double inv = rsqrt(sd * sd + cd * cd);
+    *s = sd * inv;
+    *c = cd * inv;
+}
+
 __device__ __forceinline__ void collide_pair(const CaseDev& cs, Rng& r, const PairDev& pr, int tP, int tQ,
                                              double cr2, Post& o, unsigned* err) {
     double cR;
     if (cs.collModel == DSMC_COLL_LB_VHS || cs.collModel == DSMC_COLL_LB_VSS) {
         double Et = 0.5 * pr.mR * cr2;
-        redistribute(cs, cs.sp[tP], &o.eP, &o.vP, Et, pr.omegaPQ, r, zv_row(cs, tP, tQ), err);
-        redistribute(cs, cs.sp[tQ], &o.eQ, &o.vQ, Et, pr.omegaPQ, r, zv_row(cs, tQ, tP), err);
+        redistribute(cs, cs.sp[tP], &o.eP, &o.vP, Et, pr, r, zv_row(cs, tP, tQ), err);
+        redistribute(cs, cs.sp[tQ], &o.eQ, &o.vQ, Et, pr, r, zv_row(cs, tQ, tP), err);
         cR = sqrt(2.0 * Et / pr.mR);
     } else {
         cR = sqrt(cr2);
@@ -301,11 +313,10 @@ __device__ __forceinline__ void collide_pair(const CaseDev& cs, Rng& r, const Pa
         // relative velocity, Bird eq. 2.22.  Its components are first scaled
         // to the post-exchange speed cR (equal for plain VSS), so the
         // Larsen-Borgnakke variant keeps the energy it computed.
-        const double cosT = 2.0 * pow(r.u01(), pr.invAlphaPQ) - 1.0;
+        const double cosT = 2.0 * (double)powf((float)r.u01(), pr.invAlphaF) - 1.0;
         const double sinT = sqrt(1.0 - cosT * cosT);
-        const double phi = 2.0 * PI * r.u01();
         double sph, cph;
-        sincos(phi, &sph, &cph);
+        azimuth(r, &sph, &cph);
         const double cpre = sqrt(cr2);
         const double k = cpre > 0.0 ? cR / cpre : 0.0;
         const double c0 = k * (o.UP[0] - o.UQ[0]), c1 = k * (o.UP[1] - o.UQ[1]), c2 = k * (o.UP[2] - o.UQ[2]);
@@ -322,9 +333,8 @@ __device__ __forceinline__ void collide_pair(const CaseDev& cs, Rng& r, const Pa
     } else {
         const double cosT = 2.0 * r.u01() - 1.0;
         const double sinT = sqrt(1.0 - cosT * cosT);
-        const double phi = 2.0 * PI * r.u01();
         double sph, cph;
-        sincos(phi, &sph, &cph);
+        azimuth(r, &sph, &cph);
         prel[0] = cR * cosT;
         prel[1] = cR * sinT * cph;
         prel[2] = cR * sinT * sph;
