@@ -318,6 +318,7 @@ void fill_case_dev(dsmc_handle* h) {
         d.thetaV = q.theta_v; d.thetaD = q.theta_d; d.zref = q.zref; d.trefZv = q.tref_zv;
         d.nVib = q.n_vib_modes;
         d.kThetaV = kB * q.theta_v;
+        d.invKThetaV = q.theta_v > 0 ? 1.0 / d.kThetaV : 0.0;
         d.sqrtKoverM = std::sqrt(kB / q.mass);
     }
     for (int i = 0; i < s.n_species; ++i) {
@@ -339,6 +340,7 @@ void fill_case_dev(dsmc_handle* h) {
             p.invAlphaF = (float)p.invAlphaPQ;
             p.chiBF = (float)(2.5 - om);
             p.invChiBF = (float)(1.0 / (2.5 - om));
+            p.twoOverMR = 2.0 / mR;
             p.sigmaPrefactorF = (float)p.sigmaPrefactor;
             p.expoF = (float)p.expo;
         }

@@ -89,7 +89,7 @@ __device__ __forceinline__ void redistribute(const CaseDev& cs, const SpeciesDev
     const double omegaPQ = pr.omegaPQ;
     if (s.nVib > 0) {
         const double EcP = Et + *vib * s.kThetaV;
-        const int iMax = (int)(EcP / s.kThetaV);
+        const int iMax = (int)(EcP * s.invKThetaV);
         if (iMax > 0) {
             *vib = post_vib(cs, r, *vib, iMax, s, omegaPQ, EcP, tab, err);
             Et = EcP - *vib * s.kThetaV;

@@ -50,6 +50,7 @@ __host__ __device__ inline uint32_t cellw_sub(uint32_t w) { return w & 7u; }
 struct SpeciesDev {
     double m, d, omega, rotDof, thetaV, thetaD, zref, trefZv;
     double kThetaV;     // kB * thetaV
+    double invKThetaV;  // 1 / (kB * thetaV), 0 without vibration
     double sqrtKoverM;  // sqrt(kB / m)
     int nVib;
     int pad;
@@ -68,6 +69,7 @@ struct PairDev {
     float invAlphaF;        // FP32 copies for the energy-ratio and deflection draws
     float invChiBF;         // 1 / (5/2 - omegaPQ)
     float chiBF;            // 5/2 - omegaPQ
+    double twoOverMR;       // 2 / mR
 };
 
 struct PatchDev {

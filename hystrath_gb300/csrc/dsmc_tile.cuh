@@ -300,7 +300,7 @@ __device__ __forceinline__ void collide_pair(const CaseDev& cs, Rng& r, const Pa
         double Et = 0.5 * pr.mR * cr2;
         redistribute(cs, cs.sp[tP], &o.eP, &o.vP, Et, pr, r, zv_row(cs, tP, tQ), err);
         redistribute(cs, cs.sp[tQ], &o.eQ, &o.vQ, Et, pr, r, zv_row(cs, tQ, tP), err);
-        cR = sqrt(2.0 * Et / pr.mR);
+        cR = sqrt(Et * pr.twoOverMR);
     } else {
         cR = sqrt(cr2);
     }
@@ -371,6 +371,48 @@ __device__ __forceinline__ void draw_pair(Rng& r, int n, const uint4& so, int* p
 
 // Candidate (gP, gQ): sigma_T c_R, the running maximum, the acceptance test
 // against the maximum the candidate count was based on, and the collision.
+// run_candidate in two parts: the acceptance test (loads the pair, keeps
+// the step's largest product) and the collision of an accepted pair.
+__device__ __forceinline__ bool test_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
+                                               long long gQ, double smax0, double* stepMax, Rec* P, Rec* Q,
+                                               double* cr2) {
+    *P = ld_rec(s.r + gP);
+    *Q = ld_rec(s.r + gQ);
+    const int tP = sv_species(P->sv), tQ = sv_species(Q->sv);
+    const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
+    const double d0 = P->ux - Q->ux, d1 = P->uy - Q->uy, d2 = P->uz - Q->uz;
+    *cr2 = d0 * d0 + d1 * d1 + d2 * d2;
+    const double sigma = sigma_cr(pr, *cr2);
+    if (sigma > *stepMax) *stepMax = sigma;
+    return sigma > r.u01() * smax0;
+}
+
+__device__ __forceinline__ void collide_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
+                                                  long long gQ, Rec P, Rec Q, double cr2, double* collSep,
+                                                  unsigned* err) {
+    const int tP = sv_species(P.sv), tQ = sv_species(Q.sv);
+    const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
+    Post o;
+    o.UP[0] = P.ux; o.UP[1] = P.uy; o.UP[2] = P.uz;
+    o.UQ[0] = Q.ux; o.UQ[1] = Q.uy; o.UQ[2] = Q.uz;
+    o.eP = P.erot; o.eQ = Q.erot;
+    o.vP = sv_vib(P.sv); o.vQ = sv_vib(Q.sv);
+    collide_pair(cs, r, pr, tP, tQ, cr2, o, err);
+    if (o.vP > SV_MAX_VIB || o.vQ > SV_MAX_VIB) *err |= ERRB_BOUNDS;
+    P.ux = o.UP[0]; P.uy = o.UP[1]; P.uz = o.UP[2];
+    Q.ux = o.UQ[0]; Q.uy = o.UQ[1]; Q.uz = o.UQ[2];
+    P.erot = o.eP; Q.erot = o.eQ;
+    P.sv = make_sv(tP, o.vP); Q.sv = make_sv(tQ, o.vQ);
+    st_rec(s.r + gP, P);
+    st_rec(s.r + gQ, Q);
+    // the separation only feeds the mean collision separation field: FP32
+    // after the FP64 differences
+    const float dx = (float)(P.x - Q.x);
+    const float dy = (float)(P.y - Q.y);
+    const float dz = (float)(P.z - Q.z);
+    *collSep += (double)sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
 __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
                                               long long gQ, double smax0, double* stepMax, double* collSep,
                                               unsigned* err) {
@@ -395,10 +437,12 @@ __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& 
     P.sv = make_sv(tP, o.vP); Q.sv = make_sv(tQ, o.vQ);
     st_rec(s.r + gP, P);
     st_rec(s.r + gQ, Q);
-    const double dx = P.x - Q.x;
-    const double dy = P.y - Q.y;
-    const double dz = P.z - Q.z;
-    *collSep += sqrt(dx * dx + dy * dy + dz * dz);
+    // the separation only feeds the mean collision separation field: FP32
+    // after the FP64 differences
+    const float dx = (float)(P.x - Q.x);
+    const float dy = (float)(P.y - Q.y);
+    const float dz = (float)(P.z - Q.z);
+    *collSep += (double)sqrtf(dx * dx + dy * dy + dz * dz);
     return true;
 }
 
@@ -563,13 +607,35 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
         const double smax0 = learned ? smaxSel[c] : R;
         double stepMax = 0.0, collSep = 0.0;
         unsigned coll = 0;
-        for (int k = 0; k < nCand; ++k) {
-            const int jP = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k), -1, -1);
-            const int sub = (int)st.sub[jP][lane];
-            const bool inSub = ((subCnt >> (8 * sub)) & 0xFFu) > 1;
-            const int jQ = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k + 1u), inSub ? sub : -1, jP);
+        // The lane tests candidates until one is accepted, then collides it:
+        // lanes that reach an accepted candidate in the same pass run the
+        // FP64 exchange together, whatever the rejections before it.
+        int k = 0;
+        while (k < nCand) {
+            bool accepted = false;
+            long long gP = 0, gQ = 0;
             Rng r(cs, (uint32_t)c, step, cand_tag(k));
-            if (run_candidate(cs, s, r, off + jP, off + jQ, smax0, &stepMax, &collSep, &err)) ++coll;
+            double cr2 = 0.0;
+            Rec P, Q;
+            while (k < nCand) {
+                const int jP = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k), -1, -1);
+                const int sub = (int)st.sub[jP][lane];
+                const bool inSub = ((subCnt >> (8 * sub)) & 0xFFu) > 1;
+                const int jQ =
+                    hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k + 1u), inSub ? sub : -1, jP);
+                r = Rng(cs, (uint32_t)c, step, cand_tag(k));
+                gP = off + jP;
+                gQ = off + jQ;
+                ++k;
+                if (test_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &P, &Q, &cr2)) {
+                    accepted = true;
+                    break;
+                }
+            }
+            if (accepted) {
+                collide_candidate(cs, s, r, gP, gQ, P, Q, cr2, &collSep, &err);
+                ++coll;
+            }
         }
         cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax);
         if (coll) {
