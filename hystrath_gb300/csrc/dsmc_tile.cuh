@@ -47,7 +47,7 @@ namespace tile {
 
 constexpr int WARPS = 4;             // warps per block
 constexpr int LIGHT_N = 64;          // light cells: at most this many parcels
-constexpr int LIGHT_CAND = 8;        //   and fewer candidates than this
+constexpr int LIGHT_CAND = 16;       //   and fewer candidates than this
 constexpr int ORDER_WARP_N = 1024;   // cells up to this size are ordered by one warp
 constexpr int ORDER_MAX_N = 16384;   // cells up to this size are ordered by one block
 constexpr int ORDER_BLOCK = 512;     // threads of the block that orders a large cell
