@@ -44,6 +44,7 @@ struct dsmc_handle {
     double* faceBuf = nullptr;   // face tracker sums, kept while tracking is off
     long long nFluid = 0;        // cells outside the solid boxes
     bool smaxSet = false;        // sigmaTcRMax initialised, restored or read
+    unsigned* packFlags = nullptr;   // dsmc_set_particles: range flags and largest id + 1
     int cur = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -605,6 +606,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &h->solid, cs.C))) return rc;
     if ((rc = dalloc(h, &h->info6, 8))) return rc;
     if ((rc = dalloc(h, &h->fieldTmp, cs.C))) return rc;
+    if ((rc = dalloc(h, &h->packFlags, 2))) return rc;
     B.nInflowFaces = (int)inflowFace.size();
     const long long ni = (long long)B.nInflowFaces * spec->n_species;
     if ((rc = dalloc(h, &B.inflowFace, B.nInflowFaces))) return rc;
@@ -861,44 +863,49 @@ int dsmc_phase_times(dsmc_handle* h, double* a, double* b, double* c, double* d,
     return DSMC_OK;
 }
 
-// Host <-> device parcel transfers go through pinned-free chunks of packed
-// records (PACK_CHUNK parcels at a time).
+// Device -> host parcel reads go through chunks of packed records
+// (PACK_CHUNK parcels at a time); writes are packed on the device.
 constexpr long long PACK_CHUNK = 1 << 20;
 
 int dsmc_set_particles(dsmc_handle* h, long long n, const double* pos, const double* U, const double* erot,
                        const int* vib, const int* species, const unsigned* id) {
     if (n < 0 || n > h->B.capacity) return fail(h, DSMC_ERR_CAPACITY, "particle count exceeds capacity");
-    for (long long i = 0; i < n; ++i) {
-        if (species && (species[i] < 0 || species[i] >= h->spec.n_species))
-            return fail(h, DSMC_ERR_INVALID, "species index out of range");
-        if (vib && (vib[i] < 0 || vib[i] > SV_MAX_VIB))
-            return fail(h, DSMC_ERR_INVALID, "vibrational level out of range");
-    }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    // the arrays are copied as they are into the spare buffer (68 B per parcel
+    // of room: 56 B of doubles and two int arrays in its records, the ids in
+    // its cell words) and packed into records on the device
     Parcels& s = cur_soa(h);
-    std::vector<Rec> rec((size_t)std::min(n, PACK_CHUNK));
-    uint32_t maxId = 0;
-    for (long long c0 = 0; c0 < n; c0 += PACK_CHUNK) {
-        const long long m = std::min(PACK_CHUNK, n - c0);
-        for (long long k = 0; k < m; ++k) {
-            const long long i = c0 + k;
-            Rec& r = rec[k];
-            r.x = pos ? pos[3 * i] : 0.0;
-            r.y = pos ? pos[3 * i + 1] : 0.0;
-            r.z = pos ? pos[3 * i + 2] : 0.0;
-            r.ux = U ? U[3 * i] : 0.0;
-            r.uy = U ? U[3 * i + 1] : 0.0;
-            r.uz = U ? U[3 * i + 2] : 0.0;
-            r.erot = erot ? erot[i] : 0.0;
-            r.id = id ? id[i] : (uint32_t)i;
-            r.sv = make_sv(species ? species[i] : 0, vib ? vib[i] : 0);
-            if (r.id + 1 > maxId) maxId = r.id + 1;
-        }
-        CUDA_TRY(h, cudaMemcpy(s.r + c0, rec.data(), sizeof(Rec) * m, cudaMemcpyHostToDevice));
+    Parcels& spare = h->buf[h->cur ^ 1];
+    char* base = reinterpret_cast<char*>(spare.r);
+    const size_t N = (size_t)n;
+    double* dPos = pos ? reinterpret_cast<double*>(base) : nullptr;
+    double* dU = U ? reinterpret_cast<double*>(base + 24 * N) : nullptr;
+    double* dE = erot ? reinterpret_cast<double*>(base + 48 * N) : nullptr;
+    int* dVib = vib ? reinterpret_cast<int*>(base + 56 * N) : nullptr;
+    int* dSp = species ? reinterpret_cast<int*>(base + 60 * N) : nullptr;
+    unsigned* dId = id ? spare.cellw : nullptr;
+    cudaStream_t st = h->stream;
+    if (n > 0) {
+        if (pos) CUDA_TRY(h, cudaMemcpyAsync(dPos, pos, 24 * N, cudaMemcpyHostToDevice, st));
+        if (U) CUDA_TRY(h, cudaMemcpyAsync(dU, U, 24 * N, cudaMemcpyHostToDevice, st));
+        if (erot) CUDA_TRY(h, cudaMemcpyAsync(dE, erot, 8 * N, cudaMemcpyHostToDevice, st));
+        if (vib) CUDA_TRY(h, cudaMemcpyAsync(dVib, vib, 4 * N, cudaMemcpyHostToDevice, st));
+        if (species) CUDA_TRY(h, cudaMemcpyAsync(dSp, species, 4 * N, cudaMemcpyHostToDevice, st));
+        if (id) CUDA_TRY(h, cudaMemcpyAsync(dId, id, 4 * N, cudaMemcpyHostToDevice, st));
     }
-    CUDA_TRY(h, cudaMemset(s.cellw, 0, sizeof(uint32_t) * n));
+    // check first: a rejected call leaves the cloud as it was
+    CUDA_TRY(h, cudaMemsetAsync(h->packFlags, 0, 2 * sizeof(unsigned), st));
+    launch_pack(s, n, dPos, dU, dE, dVib, dSp, dId, h->spec.n_species, h->packFlags, 0, st);
+    CUDA_TRY(h, cudaGetLastError());
+    unsigned flags[2] = {0, 0};
+    CUDA_TRY(h, cudaMemcpyAsync(flags, h->packFlags, sizeof(flags), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(h, cudaStreamSynchronize(st));
+    if (flags[0] & 1u) return fail(h, DSMC_ERR_INVALID, "species index out of range");
+    if (flags[0] & 2u) return fail(h, DSMC_ERR_INVALID, "vibrational level out of range");
+    launch_pack(s, n, dPos, dU, dE, dVib, dSp, dId, h->spec.n_species, h->packFlags, 1, st);
+    CUDA_TRY(h, cudaGetLastError());
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
-    h->ctrHost->nextId = maxId;
+    h->ctrHost->nextId = flags[1];
     CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
     return sort_current(h, n);
 }
@@ -1070,6 +1077,21 @@ int dsmc_reset_sampling(dsmc_handle* h) {
     h->ctrHost->pendingSample = 0;
     h->ctrHost->unflushed = 0;
     CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
+    return DSMC_OK;
+}
+
+int dsmc_counts(dsmc_handle* h, dsmc_counts_t* o) {
+    // the step counters only: one small read, no pass over the parcels
+    CUDA_TRY(h, cudaMemcpyAsync(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const Counters& c = *h->ctrHost;
+    o->n_particles = c.n;
+    o->step = c.step;
+    o->collisions_last_step = (long long)c.coll;
+    o->candidates_last_step = (long long)c.cand;
+    o->collisions_total = (long long)c.collTot;
+    o->candidates_total = (long long)c.candTot;
+    if (c.err) return check_device_error(h);
     return DSMC_OK;
 }
 

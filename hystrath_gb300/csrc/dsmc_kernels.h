@@ -137,6 +137,9 @@ void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Parcels& s,
                       double Trot, double Tvib, const double* U, cudaStream_t st);
 void launch_count_n(const Parcels& s, long long n, int* count, cudaStream_t st);
 void launch_ids_from_records(const Parcels& s, long long n, cudaStream_t st);
+void launch_pack(const Parcels& dst, long long n, const double* pos, const double* U, const double* erot,
+                 const int* vib, const int* species, const unsigned* id, int nSpecies, unsigned* flags,
+                 int write, cudaStream_t st);
 void launch_zero_step(const StepBuffers& B, cudaStream_t st);
 void launch_cellw(const CaseDev& cs, const Parcels& s, long long n, cudaStream_t st);
 void launch_remainder_init(const CaseDev& cs, double* rem, cudaStream_t st);

@@ -914,6 +914,42 @@ __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_gather(Parcels src, Parc
     }
 }
 
+// Parcels handed over as arrays (positions and velocities n x 3, ERot,
+// vibrational level, species, id; a null array gives zeros, and ids 0..n-1)
+// packed into records.  flags[0] gets bit 0 for a species and bit 1 for a
+// vibrational level out of range; flags[1] the largest id + 1.  With write
+// false the arrays are only checked (the caller fails before any state
+// changes).
+__global__ void k_pack(Parcels dst, long long n, const double* __restrict__ pos, const double* __restrict__ U,
+                       const double* __restrict__ erot, const int* __restrict__ vib,
+                       const int* __restrict__ species, const unsigned* __restrict__ id, int nSpecies,
+                       unsigned* flags, int write) {
+    unsigned bad = 0, maxId = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        Rec r;
+        r.x = pos ? pos[3 * i] : 0.0;
+        r.y = pos ? pos[3 * i + 1] : 0.0;
+        r.z = pos ? pos[3 * i + 2] : 0.0;
+        r.ux = U ? U[3 * i] : 0.0;
+        r.uy = U ? U[3 * i + 1] : 0.0;
+        r.uz = U ? U[3 * i + 2] : 0.0;
+        r.erot = erot ? erot[i] : 0.0;
+        r.id = id ? id[i] : (uint32_t)i;
+        int sp = species ? species[i] : 0;
+        int vb = vib ? vib[i] : 0;
+        if (sp < 0 || sp >= nSpecies) { bad |= 1u; sp = 0; }
+        if (vb < 0 || vb > SV_MAX_VIB) { bad |= 2u; vb = 0; }
+        r.sv = make_sv(sp, vb);
+        if (r.id + 1u > maxId) maxId = r.id + 1u;
+        if (!write) continue;
+        st_rec(dst.r + i, r);
+        dst.cellw[i] = 0;
+        dst.id[i] = r.id;
+    }
+    if (bad) atomicOr(flags, bad);
+    if (maxId) atomicMax(flags + 1, maxId);
+}
+
 __global__ void k_ids_from_records(Parcels s, long long n) {
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         s.id[i] = s.r[i].id;
@@ -1232,6 +1268,13 @@ void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src,
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
     k_scatter_index<<<grid, T, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortSrc);
     k_gather<<<grid, T, 0, st>>>(src, dst, B.ctr, B.sortSrc);
+}
+
+void launch_pack(const Parcels& dst, long long n, const double* pos, const double* U, const double* erot,
+                 const int* vib, const int* species, const unsigned* id, int nSpecies, unsigned* flags,
+                 int write, cudaStream_t st) {
+    if (n > 0)
+        k_pack<<<grid_for(n, 256, 8), 256, 0, st>>>(dst, n, pos, U, erot, vib, species, id, nSpecies, flags, write);
 }
 
 void launch_ids_from_records(const Parcels& s, long long n, cudaStream_t st) {

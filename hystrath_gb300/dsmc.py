@@ -54,6 +54,7 @@ def _load() -> C.CDLL:
     L.dsmc_parse_parcels.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_longlong),
                                      vp, vp, vp, vp, vp, vp]
     L.dsmc_parse_last_error.restype = C.c_char_p
+    L.dsmc_counts.argtypes = [vp, C.POINTER(S.Counts)]
     L.dsmc_set_face_tracking.argtypes = [vp, C.c_int]
     L.dsmc_n_faces.argtypes = [vp]
     L.dsmc_n_faces.restype = C.c_longlong
@@ -275,6 +276,12 @@ class DsmcCloud:
         i = S.Info()
         self._chk(lib().dsmc_info(self.h, C.byref(i)))
         return i
+
+    def counts(self) -> S.Counts:
+        """Particle count and collision counters (no pass over the parcels)."""
+        c = S.Counts()
+        self._chk(lib().dsmc_counts(self.h, C.byref(c)))
+        return c
 
     def checkpoint(self, path: str):
         self._chk(lib().dsmc_checkpoint(self.h, path.encode()))

@@ -109,6 +109,17 @@ class CaseSpec(C.Structure):
     ]
 
 
+class Counts(C.Structure):
+    _fields_ = [
+        ("n_particles", C.c_longlong),
+        ("step", C.c_longlong),
+        ("collisions_last_step", C.c_longlong),
+        ("candidates_last_step", C.c_longlong),
+        ("collisions_total", C.c_longlong),
+        ("candidates_total", C.c_longlong),
+    ]
+
+
 class Info(C.Structure):
     _fields_ = [
         ("n_particles", C.c_longlong),

@@ -199,6 +199,16 @@ typedef struct {
     long long sample_steps;
 } dsmc_info_t;
 
+/* The step counters alone (no pass over the parcels). */
+typedef struct {
+    long long n_particles;
+    long long step;
+    long long collisions_last_step;
+    long long candidates_last_step;
+    long long collisions_total;
+    long long candidates_total;
+} dsmc_counts_t;
+
 typedef struct dsmc_handle dsmc_handle;
 
 /* Fill *spec with the reference's defaults (Tref 273, Zrot 5, ...). */
@@ -315,6 +325,10 @@ long long dsmc_n_faces(const dsmc_handle* h);
 int dsmc_get_face_flux(dsmc_handle* h, const char* name, int species, double* out, long long n);
 
 int dsmc_info(dsmc_handle* h, dsmc_info_t* out);
+/* Particle count and collision counters after the last step, read without
+ * the energy sums of dsmc_info (a few bytes instead of a pass over the
+ * parcels). */
+int dsmc_counts(dsmc_handle* h, dsmc_counts_t* out);
 
 /* Binary checkpoint: particles, per-cell state, step and seed.  Together with
  * the counter-based random stream this resumes bit for bit. */

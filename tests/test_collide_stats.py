@@ -111,3 +111,17 @@ def test_gpu_checkpoint_resume_is_bit_exact(gpu_lib, tmp_path):
     for k in ("pos", "U", "erot", "vib", "id", "cell"):
         np.testing.assert_array_equal(pa[k][oa], pb[k][ob])
     np.testing.assert_array_equal(a.field("Ttra"), b.field("Ttra"))
+
+
+@pytest.mark.gpu
+def test_counts_agree_with_info(gpu_lib):
+    """dsmc_counts reads the step counters without the energy pass."""
+    from hystrath_gb300 import spec as S
+    from hystrath_gb300.dsmc import DsmcCloud
+    g = DsmcCloud(S.config0(seed=9))
+    g.initialise()
+    g.evolve(3)
+    c, i = g.counts(), g.info()
+    assert (c.n_particles, c.step, c.collisions_total, c.candidates_total) == \
+        (i.n_particles, i.step, i.collisions_total, i.candidates_total)
+    assert c.collisions_last_step == i.collisions_last_step > 0
