@@ -597,6 +597,8 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
         const int n = start[c + 1] - (int)off;
         // sub-cell occupancy, 8 bits per sub-cell (n <= LIGHT_N < 256)
         unsigned long long subCnt = 0;
+        // unrolled so that eight loads per lane are in flight at once
+#pragma unroll 8
         for (int j = 0; j < n; ++j) {
             const uint32_t sb = __ldg(s.cellw + off + j) & 7u;
             st.sub[j][lane] = (uint8_t)sb;
