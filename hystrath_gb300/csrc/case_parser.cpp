@@ -104,6 +104,7 @@ struct Node {
     std::vector<std::string> words;                          // VALUE
     std::vector<std::shared_ptr<Node>> items;                // LIST
     std::vector<std::string> itemNames;                      // LIST: name of a named dict item or ""
+    std::vector<std::shared_ptr<Node>> more;                 // LIST: the value's later lists ("box (a) (b)")
     std::vector<std::pair<std::string, std::shared_ptr<Node>>> entries;  // DICT
 
     const Node* find(const std::string& k) const {
@@ -161,6 +162,7 @@ class Parser {
                 advance();
                 auto l = parseList();
                 if (!list) list = l;
+                else list->more.push_back(l);
                 continue;
             }
             if (list && cur_.kind == Tok::WORD) {   // words after the first list
@@ -1147,10 +1149,139 @@ extern "C" int dsmc_parse_parcels(const char* case_dir, const char* time_name, c
     }
 }
 
+// ------------------------------------------------------------------ flux surfaces
+// dsmcFluxSurface entries of system/fieldPropertiesDict (dsmcFluxSurface.C:
+// 203-309: fieldName, faceZoneName, typeIds, fluxDirection) and the faceZone
+// each names, from system/topoSetDict.
+namespace {
+
+const Node* topo_source(const Node* action) {
+    const Node* si = action->find("sourceInfo");
+    return si ? si : action;   // later OpenFOAM versions put the source keys in the action
+}
+
+// the box of faceSet `set`: exactly one action on it, "new" from boxToFace
+void face_set_box(const Node& actions, const std::string& set, const std::string& where, double* lo, double* hi) {
+    int found = 0;
+    for (auto& a : actions.items) {
+        if (a->kind != Node::DICT || wordOr(a.get(), "name", "") != set) continue;
+        if (wordOr(a.get(), "type", "") != "faceSet") continue;
+        ++found;
+        const std::string act = wordOr(a.get(), "action", "");
+        const std::string src = wordOr(a.get(), "source", "");
+        if (act != "new" || src != "boxToFace")
+            throw ParseError(DSMC_ERR_INVALID, "faceSet " + set + " in " + where +
+                                                   ": only one 'action new; source boxToFace;' is supported");
+        const Node& box = need(topo_source(a.get()), "box", "boxToFace of " + set);
+        if (box.kind != Node::LIST || box.more.size() != 1)
+            throw ParseError(DSMC_ERR_PARSE, "box of faceSet " + set + " is not '(min) (max)'");
+        const auto a0 = numList(box, "box"), a1 = numList(*box.more[0], "box");
+        if (a0.size() != 3 || a1.size() != 3) throw ParseError(DSMC_ERR_PARSE, "box of faceSet " + set + " is not two points");
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = a0[k];
+            hi[k] = a1[k];
+        }
+    }
+    if (found != 1)
+        throw ParseError(DSMC_ERR_INVALID, "Cannot find region: " + set + " in " + where +
+                                               (found ? " (more than one action on the set)" : ""));
+}
+
+// faceZone `zone`: a faceZoneSet made by setToFaceZone from a faceSet, or a
+// faceSet of that name (setsToZones makes a zone of every set)
+void face_zone_box(const Node& actions, const std::string& zone, const std::string& where, double* lo, double* hi) {
+    for (auto& a : actions.items) {
+        if (a->kind != Node::DICT || wordOr(a.get(), "name", "") != zone) continue;
+        if (wordOr(a.get(), "type", "") != "faceZoneSet") continue;
+        if (wordOr(a.get(), "source", "") != "setToFaceZone")
+            throw ParseError(DSMC_ERR_INVALID, "faceZoneSet " + zone + " in " + where +
+                                                   ": only source setToFaceZone is supported");
+        face_set_box(actions, word(topo_source(a.get()), "faceSet", "setToFaceZone of " + zone), where, lo, hi);
+        return;
+    }
+    face_set_box(actions, zone, where, lo, hi);
+}
+
+void read_flux_surfaces(const std::string& dir, std::vector<dsmc_flux_surface>* out) {
+    const std::string fpPath = dir + "/system/fieldPropertiesDict";
+    {
+        std::ifstream probe(fpPath);
+        if (!probe) return;
+    }
+    auto fp = readDict(fpPath);
+    const Node* fl = fp->find("dsmcFields");
+    if (!fl) return;
+    std::shared_ptr<Node> topo, dp;
+    std::vector<std::string> types;
+    for (auto& it : fl->items) {
+        if (it->kind != Node::DICT || wordOr(it.get(), "fieldModel", "") != "dsmcFluxSurface") continue;
+        if (!dp) {
+            const std::string dpPath = fileIn(dir, "constant/dsmcProperties");
+            dp = readDict(dpPath);
+            types = wordList(need(dp.get(), "typeIdList", dpPath));
+        }
+        const Node& pr = need(it.get(), "dsmcFluxSurfaceProperties", fpPath);
+        dsmc_flux_surface s;
+        std::memset(&s, 0, sizeof(s));
+        const std::string zone = word(&pr, "faceZoneName", "dsmcFluxSurfaceProperties");
+        copyName(s.field_name, word(&pr, "fieldName", "dsmcFluxSurfaceProperties"));
+        copyName(s.zone_name, zone);
+        for (const std::string& t : wordList(need(&pr, "typeIds", "dsmcFluxSurfaceProperties"))) {
+            const auto k = std::find(types.begin(), types.end(), t);
+            if (k == types.end())
+                throw ParseError(DSMC_ERR_INVALID, "Cannot find typeId: " + t + " in: " + fpPath);
+            s.species_mask |= 1u << (unsigned)(k - types.begin());
+        }
+        const auto d = numList(need(&pr, "fluxDirection", "dsmcFluxSurfaceProperties"), "fluxDirection");
+        if (d.size() != 3) throw ParseError(DSMC_ERR_PARSE, "fluxDirection is not a vector");
+        for (int k = 0; k < 3; ++k) s.direction[k] = d[k];
+        const std::string tsPath = dir + "/system/topoSetDict";
+        if (!topo) topo = readDict(tsPath);
+        face_zone_box(need(topo.get(), "actions", tsPath), zone, tsPath, s.box_min, s.box_max);
+        out->push_back(s);
+    }
+}
+
+}  // namespace
+
+extern "C" int dsmc_parse_flux_surfaces(const char* case_dir, dsmc_flux_surface* out, int* n) {
+    try {
+        std::vector<dsmc_flux_surface> v;
+        read_flux_surfaces(case_dir, &v);
+        if (out) {
+            if (*n < (int)v.size()) throw ParseError(DSMC_ERR_INVALID, "flux surface capacity too small");
+            std::copy(v.begin(), v.end(), out);
+        }
+        *n = (int)v.size();
+        return DSMC_OK;
+    } catch (const ParseError& e) {
+        g_perr = e.what();
+        dsmc::set_global_error(g_perr);
+        return e.code;
+    } catch (const std::exception& e) {
+        g_perr = e.what();
+        dsmc::set_global_error(g_perr);
+        return (g_perr.find("cannot open") != std::string::npos) ? DSMC_ERR_IO : DSMC_ERR_PARSE;
+    }
+}
+
 extern "C" int dsmc_create(const char* case_dir, dsmc_handle** out) {
     *out = nullptr;
     dsmc_case_spec s;
-    const int rc = dsmc_parse_case(case_dir, &s);
+    int rc = dsmc_parse_case(case_dir, &s);
     if (rc != DSMC_OK) return rc;
-    return dsmc_create_from_spec(&s, out);
+    int nS = 0;
+    if ((rc = dsmc_parse_flux_surfaces(case_dir, nullptr, &nS)) != DSMC_OK) return rc;
+    std::vector<dsmc_flux_surface> surf(nS);
+    if (nS && (rc = dsmc_parse_flux_surfaces(case_dir, surf.data(), &nS)) != DSMC_OK) return rc;
+    if ((rc = dsmc_create_from_spec(&s, out)) != DSMC_OK) return rc;
+    for (const auto& f : surf) {
+        if ((rc = dsmc_add_flux_surface(*out, &f)) != DSMC_OK) {
+            dsmc::set_global_error(dsmc_last_error(*out));
+            dsmc_destroy(*out);
+            *out = nullptr;
+            return rc;
+        }
+    }
+    return DSMC_OK;
 }

@@ -42,6 +42,17 @@ struct dsmc_handle {
     StepBuffers B{};
     Parcels buf[2]{};
     double* faceBuf = nullptr;   // face tracker sums, kept while tracking is off
+    long long faceStep0 = 0;     // step count when the face sums were last cleared
+    struct FluxSurface {
+        dsmc_flux_surface d;
+        int* faces;       // device: the zone's faces
+        double* w;        // device: FN (S/|S| . fluxDirection) of each face
+        int nF;
+        double area;
+    };
+    std::vector<FluxSurface> surfaces;
+    double* surfOut = nullptr;   // device: the two sums of k_flux_surface
+    std::vector<unsigned char> solidHost;   // 1 for cells inside a solid box
     long long nFluid = 0;        // cells outside the solid boxes
     bool smaxSet = false;        // sigmaTcRMax initialised, restored or read
     unsigned* packFlags = nullptr;   // dsmc_set_particles: range flags and largest id + 1
@@ -570,6 +581,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
             fluidV += h->width[0][c % cs.n[0]] * h->width[1][(c / cs.n[0]) % cs.n[1]] *
                       h->width[2][c / ((long long)cs.n[0] * cs.n[1])];
     h->nFluid = fluid;
+    h->solidHost = solid;
     h->expectedN = (long long)(ndSum * fluidV / cs.FN);
     long long cap = spec->max_particles;
     if (cap <= 0) cap = (long long)((h->hasInflow ? 2.0 : 1.3) * h->expectedN) + 65536;
@@ -1073,6 +1085,7 @@ int dsmc_reset_sampling(dsmc_handle* h) {
     if (h->cs.faceFlux)
         CUDA_TRY(h, cudaMemset(h->cs.faceFlux, 0, sizeof(double) * 2 * h->cs.nSpecies * h->cs.nFacesAll));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    h->faceStep0 = h->ctrHost->step;
     h->ctrHost->sampleSteps = 0;
     h->ctrHost->pendingSample = 0;
     h->ctrHost->unflushed = 0;
@@ -1195,6 +1208,10 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
     CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemset(h->B.count, 0, sizeof(int) * h->cs.C));
     CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
+    // the face sums start again from the restored step
+    if (h->cs.faceFlux)
+        CUDA_TRY(h, cudaMemset(h->cs.faceFlux, 0, sizeof(double) * 2 * h->cs.nSpecies * h->cs.nFacesAll));
+    h->faceStep0 = c.step;
     h->smaxSet = true;
     return DSMC_OK;
 }
@@ -1558,7 +1575,11 @@ int dsmc_set_face_tracking(dsmc_handle* h, int on) {
         int rc;
         if ((rc = dalloc(h, &h->faceBuf, n))) return rc;
     }
-    if (on && !cs.faceFlux) CUDA_TRY(h, cudaMemset(h->faceBuf, 0, sizeof(double) * n));
+    if (on && !cs.faceFlux) {
+        CUDA_TRY(h, cudaMemset(h->faceBuf, 0, sizeof(double) * n));
+        CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+        h->faceStep0 = h->ctrHost->step;
+    }
     cs.faceFlux = on ? h->faceBuf : nullptr;
     drop_graphs(h);
     return DSMC_OK;
@@ -1582,6 +1603,153 @@ int dsmc_get_face_flux(dsmc_handle* h, const char* name, int species, double* ou
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     CUDA_TRY(h, cudaMemcpy(out, cs.faceFlux + ((long long)k * cs.nSpecies + species) * cs.nFacesAll,
                            sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return DSMC_OK;
+}
+
+// ------------------------------------------------------- flux surfaces
+namespace {
+
+// The mesh face f of the tracker numbering: its axis, centre, area and the
+// sign of its area vector along the axis (+ between two fluid cells and on
+// the high side of a fluid cell, - on the low side).  False when no fluid
+// cell touches it (inside a solid box): then it is not a mesh face.
+bool face_geometry(const dsmc_handle* h, long long f, int* axis, double* centre, double* area, double* sgn) {
+    const CaseDev& cs = h->cs;
+    const long long nx = cs.n[0], ny = cs.n[1];
+    int a, p, c[3];
+    if (f < cs.faceOff[1]) {
+        a = 0;
+        p = (int)(f % (nx + 1));
+        c[1] = (int)((f / (nx + 1)) % ny);
+        c[2] = (int)(f / ((nx + 1) * ny));
+    } else if (f < cs.faceOff[2]) {
+        const long long l = f - cs.faceOff[1];
+        a = 1;
+        c[0] = (int)(l % nx);
+        p = (int)((l / nx) % (ny + 1));
+        c[2] = (int)(l / (nx * (ny + 1)));
+    } else {
+        const long long l = f - cs.faceOff[2];
+        a = 2;
+        c[0] = (int)(l % nx);
+        c[1] = (int)((l / nx) % ny);
+        p = (int)(l / (nx * ny));
+    }
+    auto fluid = [&](int i) {
+        if (i < 0 || i >= cs.n[a]) return false;
+        int q[3] = {c[0], c[1], c[2]};
+        q[a] = i;
+        return !h->solidHost[q[0] + (long long)cs.n[0] * (q[1] + (long long)cs.n[1] * q[2])];
+    };
+    const bool lo = fluid(p - 1), hi = fluid(p);
+    if (!lo && !hi) return false;
+    *axis = a;
+    *sgn = lo ? 1.0 : -1.0;
+    *area = 1.0;
+    for (int b = 0; b < 3; ++b) {
+        if (b == a) {
+            centre[b] = h->node[b][p];
+        } else {
+            centre[b] = 0.5 * (h->node[b][c[b]] + h->node[b][c[b] + 1]);
+            *area *= h->width[b][c[b]];
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+int dsmc_add_flux_surface(dsmc_handle* h, const dsmc_flux_surface* sf) {
+    const CaseDev& cs = h->cs;
+    dsmc_handle::FluxSurface fs{};
+    fs.d = *sf;
+    fs.d.field_name[DSMC_NAME_LEN - 1] = 0;
+    fs.d.zone_name[DSMC_NAME_LEN - 1] = 0;
+    const double* d = sf->direction;
+    const double mag = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (!(mag > 0.0) || !std::isfinite(mag))
+        return fail(h, DSMC_ERR_INVALID, std::string("flux surface ") + fs.d.zone_name + ": fluxDirection is zero");
+    for (int a = 0; a < 3; ++a) fs.d.direction[a] = d[a] / mag;
+    if (sf->species_mask == 0 || (sf->species_mask >> cs.nSpecies) != 0)
+        return fail(h, DSMC_ERR_INVALID, std::string("flux surface ") + fs.d.zone_name +
+                                             ": typeIds must name species of the cloud");
+    for (const auto& o : h->surfaces)
+        if (!std::strcmp(o.d.zone_name, fs.d.zone_name) && !std::strcmp(o.d.field_name, fs.d.field_name))
+            return fail(h, DSMC_ERR_INVALID, std::string("flux surface ") + fs.d.zone_name + " (" +
+                                                 fs.d.field_name + ") exists already");
+    int rc = dsmc_set_face_tracking(h, 1);
+    if (rc) return rc;
+    std::vector<int> faces;
+    std::vector<double> w;
+    const long long nAll = cs.nFacesAll;
+    for (long long f = 0; f < nAll; ++f) {
+        int a;
+        double x[3], area, sgn;
+        if (!face_geometry(h, f, &a, x, &area, &sgn)) continue;
+        bool in = true;
+        for (int b = 0; b < 3; ++b) in = in && x[b] >= sf->box_min[b] && x[b] <= sf->box_max[b];
+        if (!in) continue;
+        faces.push_back((int)f);
+        w.push_back(cs.FN * sgn * fs.d.direction[a]);
+        fs.area += area;
+    }
+    if (faces.empty())
+        return fail(h, DSMC_ERR_INVALID, std::string("Cannot find region: ") + fs.d.zone_name +
+                                             " (no mesh face centre in its box)");
+    fs.nF = (int)faces.size();
+    if ((rc = dalloc(h, &fs.faces, fs.nF))) return rc;
+    if ((rc = dalloc(h, &fs.w, fs.nF))) return rc;
+    if (!h->surfOut && (rc = dalloc(h, &h->surfOut, 2))) return rc;
+    CUDA_TRY(h, cudaMemcpy(fs.faces, faces.data(), sizeof(int) * fs.nF, cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(fs.w, w.data(), sizeof(double) * fs.nF, cudaMemcpyHostToDevice));
+    h->surfaces.push_back(fs);
+    return DSMC_OK;
+}
+
+int dsmc_n_flux_surfaces(const dsmc_handle* h) { return (int)h->surfaces.size(); }
+
+int dsmc_get_flux_surface(dsmc_handle* h, int i, dsmc_flux_surface* surface, double* out) {
+    if (i < 0 || i >= (int)h->surfaces.size()) return fail(h, DSMC_ERR_INVALID, "flux surface index out of range");
+    const auto& fs = h->surfaces[i];
+    if (surface) *surface = fs.d;
+    if (!h->cs.faceFlux) return fail(h, DSMC_ERR_INVALID, "face tracking is off (dsmc_set_face_tracking)");
+    launch_flux_surface(h->cs, fs.faces, fs.w, fs.nF, fs.d.species_mask, h->surfOut, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    double sums[2];
+    CUDA_TRY(h, cudaMemcpyAsync(sums, h->surfOut, sizeof(sums), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    const long long steps = h->ctrHost->step - h->faceStep0;
+    if (steps <= 0) return fail(h, DSMC_ERR_INVALID, "no step since the face sums were reset");
+    // dsmcFluxSurface.C:364-386
+    const double T = (double)steps * h->spec.delta_t;
+    out[1] = sums[0] / T;
+    out[0] = out[1] / fs.area;
+    out[3] = sums[1] / T;
+    out[2] = out[3] / fs.area;
+    out[4] = fs.area;
+    out[5] = T;
+    return DSMC_OK;
+}
+
+int dsmc_write_flux_surfaces(dsmc_handle* h, const char* case_dir, double time_value) {
+    const std::string dir = std::string(case_dir) + "/fieldMeasurements";
+    mkdir(dir.c_str(), 0755);
+    static const char* names[4] = {"faceParticleFlux_", "faceParticleFlowRate_", "faceMassFlux_",
+                                   "faceMassFlowRate_"};
+    for (int i = 0; i < (int)h->surfaces.size(); ++i) {
+        double v[6];
+        int rc = dsmc_get_flux_surface(h, i, nullptr, v);
+        if (rc) return rc;
+        const auto& d = h->surfaces[i].d;
+        for (int k = 0; k < 4; ++k) {
+            const std::string path = dir + "/" + names[k] + d.zone_name + "_" + d.field_name + ".xy";
+            FILE* f = std::fopen(path.c_str(), "a");
+            if (!f) return fail(h, DSMC_ERR_IO, "cannot open " + path);
+            std::fprintf(f, "%.11g\t%.11g\n", time_value, v[k]);
+            if (std::fclose(f)) return fail(h, DSMC_ERR_IO, "cannot write " + path);
+        }
+    }
     return DSMC_OK;
 }
 

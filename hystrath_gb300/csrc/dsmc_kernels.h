@@ -137,6 +137,10 @@ void launch_init_fill(const CaseDev& cs, const StepBuffers& B, const Parcels& s,
                       double Trot, double Tvib, const double* U, cudaStream_t st);
 void launch_count_n(const Parcels& s, long long n, int* count, cudaStream_t st);
 void launch_ids_from_records(const Parcels& s, long long n, cudaStream_t st);
+// dsmcFluxSurface: out2 = {sum of parcel sums x w, sum of mass sums x w} over
+// the nF faces (device arrays) and the species of mask
+void launch_flux_surface(const CaseDev& cs, const int* faces, const double* w, int nF, unsigned mask,
+                         double* out2, cudaStream_t st);
 void launch_pack(const Parcels& dst, long long n, const double* pos, const double* U, const double* erot,
                  const int* vib, const int* species, const unsigned* id, int nSpecies, unsigned* flags,
                  int write, cudaStream_t st);

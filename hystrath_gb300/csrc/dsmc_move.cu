@@ -1277,6 +1277,48 @@ void launch_pack(const Parcels& dst, long long n, const double* pos, const doubl
         k_pack<<<grid_for(n, 256, 8), 256, 0, st>>>(dst, n, pos, U, erot, vib, species, id, nSpecies, flags, write);
 }
 
+// dsmcFluxSurface::calculateField (dsmcFluxSurface.C:316-343): the sum over
+// the zone's faces and the selected species of the face sums times w, where
+// w = FN (S/|S| . fluxDirection) of the face; out[0] parcels, out[1] mass.
+// One block with a fixed reduction order, so equal sums give equal results.
+__global__ void __launch_bounds__(256) k_flux_surface(const double* __restrict__ flux, int nSpecies,
+                                                      long long nFacesAll, const int* __restrict__ faces,
+                                                      const double* __restrict__ w, int nF, unsigned mask,
+                                                      double* out) {
+    __shared__ double sh[2][256];
+    double p = 0.0, m = 0.0;
+    for (int i = threadIdx.x; i < nF; i += 256) {
+        const long long f = faces[i];
+        double fp = 0.0, fm = 0.0;
+        for (int q = 0; q < nSpecies; ++q)
+            if ((mask >> q) & 1u) {
+                fp += flux[(long long)q * nFacesAll + f];
+                fm += flux[((long long)nSpecies + q) * nFacesAll + f];
+            }
+        p = fma(fp, w[i], p);
+        m = fma(fm, w[i], m);
+    }
+    sh[0][threadIdx.x] = p;
+    sh[1][threadIdx.x] = m;
+    __syncthreads();
+    for (int k = 128; k > 0; k >>= 1) {
+        if ((int)threadIdx.x < k) {
+            sh[0][threadIdx.x] += sh[0][threadIdx.x + k];
+            sh[1][threadIdx.x] += sh[1][threadIdx.x + k];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sh[0][0];
+        out[1] = sh[1][0];
+    }
+}
+
+void launch_flux_surface(const CaseDev& cs, const int* faces, const double* w, int nF, unsigned mask,
+                         double* out2, cudaStream_t st) {
+    k_flux_surface<<<1, 256, 0, st>>>(cs.faceFlux, cs.nSpecies, cs.nFacesAll, faces, w, nF, mask, out2);
+}
+
 void launch_ids_from_records(const Parcels& s, long long n, cudaStream_t st) {
     if (n > 0) k_ids_from_records<<<grid_for(n, 256, 8), 256, 0, st>>>(s, n);
 }

@@ -59,6 +59,11 @@ def _load() -> C.CDLL:
     L.dsmc_n_faces.argtypes = [vp]
     L.dsmc_n_faces.restype = C.c_longlong
     L.dsmc_get_face_flux.argtypes = [vp, C.c_char_p, C.c_int, vp, C.c_longlong]
+    L.dsmc_add_flux_surface.argtypes = [vp, C.POINTER(S.FluxSurface)]
+    L.dsmc_n_flux_surfaces.argtypes = [vp]
+    L.dsmc_get_flux_surface.argtypes = [vp, C.c_int, C.POINTER(S.FluxSurface), vp]
+    L.dsmc_write_flux_surfaces.argtypes = [vp, C.c_char_p, C.c_double]
+    L.dsmc_parse_flux_surfaces.argtypes = [C.c_char_p, C.POINTER(S.FluxSurface), C.POINTER(C.c_int)]
     L.dsmc_info.argtypes = [vp, C.POINTER(S.Info)]
     L.dsmc_checkpoint.argtypes = [vp, C.c_char_p]
     L.dsmc_restore.argtypes = [vp, C.c_char_p]
@@ -114,6 +119,20 @@ def parse_parcels(case_dir: str, time_name: str, cloud_name: str = "dsmc"):
     if rc != 0:
         raise DsmcError(rc, lib().dsmc_parse_last_error().decode())
     return out
+
+
+def parse_flux_surfaces(case_dir: str) -> list:
+    """The dsmcFluxSurface entries of a case (fieldPropertiesDict with their
+    zones from topoSetDict), as FluxSurface structs (no GPU needed)."""
+    n = C.c_int(0)
+    rc = lib().dsmc_parse_flux_surfaces(case_dir.encode(), None, C.byref(n))
+    if rc != 0:
+        raise DsmcError(rc, lib().dsmc_parse_last_error().decode())
+    arr = (S.FluxSurface * max(n.value, 1))()
+    rc = lib().dsmc_parse_flux_surfaces(case_dir.encode(), arr, C.byref(n))
+    if rc != 0:
+        raise DsmcError(rc, lib().dsmc_parse_last_error().decode())
+    return [arr[i] for i in range(n.value)]
 
 
 def parse_case(case_dir: str) -> S.CaseSpec:
@@ -267,6 +286,39 @@ class DsmcCloud:
         out = np.empty(n)
         self._chk(lib().dsmc_get_face_flux(self.h, name.encode(), int(species), _p(out), n))
         return out
+
+    def add_flux_surface(self, zone_name: str, box_min, box_max, direction, species=None,
+                         field_name: str = "dsmc") -> int:
+        """A dsmcFluxSurface over the faces whose centres lie in the box, for
+        the species indices given (all by default); returns its index."""
+        f = S.FluxSurface()
+        f.zone_name = zone_name.encode()
+        f.field_name = field_name.encode()
+        for a in range(3):
+            f.box_min[a], f.box_max[a], f.direction[a] = box_min[a], box_max[a], direction[a]
+        ns = self.spec.n_species
+        f.species_mask = sum(1 << m for m in (range(ns) if species is None else species))
+        self._chk(lib().dsmc_add_flux_surface(self.h, C.byref(f)))
+        return lib().dsmc_n_flux_surfaces(self.h) - 1
+
+    def n_flux_surfaces(self) -> int:
+        return lib().dsmc_n_flux_surfaces(self.h)
+
+    def flux_surface(self, i: int = 0) -> dict:
+        """faceParticleFlux, faceParticleFlowRate, faceMassFlux,
+        faceMassFlowRate, area and averaging_time of surface i, with its
+        zone_name and field_name."""
+        f = S.FluxSurface()
+        out = np.empty(6)
+        self._chk(lib().dsmc_get_flux_surface(self.h, int(i), C.byref(f), _p(out)))
+        d = dict(zip(S.FLUX_SURFACE_VALUES, out.tolist()))
+        d["zone_name"] = f.zone_name.decode()
+        d["field_name"] = f.field_name.decode()
+        return d
+
+    def write_flux_surfaces(self, case_dir: str, time_value: float):
+        """Append this output time to case_dir/fieldMeasurements/*.xy."""
+        self._chk(lib().dsmc_write_flux_surfaces(self.h, case_dir.encode(), float(time_value)))
 
     def write_fields(self, case_dir: str, time_name: str, field_name: str = ""):
         """The averaged fields as OpenFOAM files in case_dir/time_name."""

@@ -120,6 +120,23 @@ class Counts(C.Structure):
     ]
 
 
+class FluxSurface(C.Structure):
+    """dsmc_flux_surface: a dsmcFluxSurface over the faces whose centres lie
+    in [box_min, box_max] (topoSet boxToFace)."""
+    _fields_ = [
+        ("field_name", C.c_char * NAME_LEN),
+        ("zone_name", C.c_char * NAME_LEN),
+        ("box_min", C.c_double * 3),
+        ("box_max", C.c_double * 3),
+        ("direction", C.c_double * 3),
+        ("species_mask", C.c_uint),
+    ]
+
+
+FLUX_SURFACE_VALUES = ("faceParticleFlux", "faceParticleFlowRate", "faceMassFlux", "faceMassFlowRate",
+                       "area", "averaging_time")
+
+
 class Info(C.Structure):
     _fields_ = [
         ("n_particles", C.c_longlong),

@@ -132,7 +132,8 @@ typedef struct {
 } dsmc_obstacle;
 
 /*
- * Fully resolved case: a uniform Cartesian hexahedral mesh, its patches, the
+ * Fully resolved case: a Cartesian hexahedral mesh (uniform unless node_coords
+ * gives an axis its nodes), its patches, the
  * species, the dsmcProperties models and the dsmcMeshFill initial state.
  * Side order everywhere is -x, +x, -y, +y, -z, +z.  The face grid of a side
  * is indexed (a + na*b) with (a, b) = (y, z) for x sides, (x, z) for y sides
@@ -323,6 +324,45 @@ const char* dsmc_parse_last_error(void);
 int dsmc_set_face_tracking(dsmc_handle* h, int on);
 long long dsmc_n_faces(const dsmc_handle* h);
 int dsmc_get_face_flux(dsmc_handle* h, const char* name, int species, double* out, long long n);
+
+/* dsmcFluxSurface (macroscopicProperties/derived/flux/dsmcFluxSurface/
+ * dsmcFluxSurface.C:203-400), the fieldModel that reads the face tracker:
+ * over the faces of a face zone and the species of typeIds it sums
+ * parcelIdFlux FN (S/|S| . d) and massIdFlux FN (S/|S| . d), d the
+ * normalised fluxDirection, and divides by the averaging time (steps since
+ * the face sums were reset x deltaT) and by the zone's area (the sum of |S|).
+ * The zone is the set of mesh faces whose centres lie in a box, bounds
+ * included: topoSet's boxToFace, which is how a faceZone of a blockMesh case
+ * is made.  A face between two solid cells is not a mesh face.
+ * dsmc_add_flux_surface switches face tracking on; a surface added to a cloud
+ * that already tracks faces reads the sums since their last reset. */
+typedef struct {
+    char field_name[DSMC_NAME_LEN];   /* fieldName */
+    char zone_name[DSMC_NAME_LEN];    /* faceZoneName */
+    double box_min[3];
+    double box_max[3];
+    double direction[3];              /* fluxDirection (any length > 0) */
+    unsigned species_mask;            /* typeIds: bit m for species m */
+} dsmc_flux_surface;
+
+int dsmc_add_flux_surface(dsmc_handle* h, const dsmc_flux_surface* surface);
+int dsmc_n_flux_surfaces(const dsmc_handle* h);
+/* out[6]: faceParticleFlux (1/(m^2 s)), faceParticleFlowRate (1/s),
+ * faceMassFlux (kg/(m^2 s)), faceMassFlowRate (kg/s), the zone's area (m^2)
+ * and the averaging time (s); surface may be NULL.  DSMC_ERR_INVALID before
+ * the first step after a reset (the averaging time is zero). */
+int dsmc_get_flux_surface(dsmc_handle* h, int i, dsmc_flux_surface* surface, double* out);
+/* dsmcFluxSurface::writeField (dsmcFluxSurface.C:455-509): appends
+ * "time<TAB>value" (11 significant digits) to
+ * case_dir/fieldMeasurements/face{ParticleFlux,ParticleFlowRate,MassFlux,
+ * MassFlowRate}_<zone>_<field>.xy for every surface. */
+int dsmc_write_flux_surfaces(dsmc_handle* h, const char* case_dir, double time_value);
+/* The dsmcFluxSurface entries of system/fieldPropertiesDict with their
+ * zones from system/topoSetDict (a faceSet made by one boxToFace, turned
+ * into a zone by setsToZones or a faceZoneSet's setToFaceZone).  Call with
+ * out == NULL for *n; then *n on input is the capacity of out.  dsmc_create
+ * adds them to the cloud it makes. */
+int dsmc_parse_flux_surfaces(const char* case_dir, dsmc_flux_surface* out, int* n);
 
 int dsmc_info(dsmc_handle* h, dsmc_info_t* out);
 /* Particle count and collision counters after the last step, read without
