@@ -379,7 +379,7 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
                                                                 B.perm, B.subs, learned, B.smaxSel, B.useR,
                                                                 B.obsMax);
     const int L = B.cfg.lightCells;
-    tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * sizeof(tile::LightStage), st>>>(
+    tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * sizeof(tile::LightPicks), st>>>(
         cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.obsMax);
 }
 

@@ -35,7 +35,10 @@
 // with the smallest hash under a second key.  For a given key the hash is a
 // bijection of the id, so every member is equally likely and picks under
 // different keys are independent: the same distribution as the list draws,
-// for a few passes over the cell instead of a sort.
+// without a sort.  The picks do not depend on earlier candidates' outcomes,
+// so a warp makes all picks of its 32 light cells first, cell by cell (one
+// coalesced load of the cell's ids, a warp minimum per pick), and each lane
+// then tests and collides its own cell's candidates.
 //
 // Both paths give results that do not depend on the parcels' order in
 // memory, so a run is reproducible.  Serial work is spread across lanes
@@ -542,45 +545,46 @@ __device__ __forceinline__ uint32_t fmix32(uint32_t h) {
     return h;
 }
 
-__device__ __forceinline__ uint32_t pick_key(const CaseDev& cs, uint32_t cell, uint32_t step, uint32_t draw) {
+// pick_key in two parts: the cell's and step's base, then one draw of it
+__device__ __forceinline__ uint32_t pick_base(const CaseDev& cs, uint32_t cell, uint32_t step) {
     uint32_t h = fmix32(cs.seedHi ^ 0x51ED270Bu);
     h = fmix32(h ^ cell);
-    h = fmix32(h ^ step);
-    h = fmix32(h ^ draw);
-    return h ^ cs.seedLo;
+    return fmix32(h ^ step);
+}
+__device__ __forceinline__ uint32_t pick_draw(const CaseDev& cs, uint32_t base, uint32_t draw) {
+    return fmix32(base ^ draw) ^ cs.seedLo;
+}
+__device__ __forceinline__ uint32_t pick_key(const CaseDev& cs, uint32_t cell, uint32_t step, uint32_t draw) {
+    return pick_draw(cs, pick_base(cs, cell, step), draw);
 }
 
-// Light cells stage their members' ids and sub-cells in shared memory, one
-// column per lane (member j of lane l at [j][l]: the lanes of a warp read
-// consecutive words).
-struct LightStage {
-    uint32_t id[LIGHT_N][32];
-    uint8_t sub[LIGHT_N][32];
+// The picks of a light cell's candidates, made by the whole warp: member j
+// hashes to fmix32(key ^ id_j); P is the member with the smallest hash, Q the
+// smallest among the others of P's sub-cell when it holds two or more
+// parcels, else among all others (no two members share a hash: ids are
+// distinct and fmix32 is a bijection).
+struct LightPicks {
+    uint8_t pq[LIGHT_CAND][2][32];   // [candidate][P, Q][lane of the cell]
 };
 
-// member of the staged cell of n members with the smallest hash under key;
-// sub < 0: any sub-cell; skip: excluded member
-__device__ __forceinline__ int hash_pick(const LightStage& st, int lane, int n, uint32_t key, int sub, int skip) {
-    uint32_t best = 0xFFFFFFFFu;
-    int arg = -1;
-    for (int j = 0; j < n; ++j) {
-        if (j == skip) continue;
-        if (sub >= 0 && (int)st.sub[j][lane] != sub) continue;
-        const uint32_t h = fmix32(key ^ st.id[j][lane]);
-        if (arg < 0 || h < best) { best = h; arg = j; }
-    }
-    return arg;
+// index j (lane, or lane + 32) of the valid member with the smallest hash
+__device__ __forceinline__ int warp_argmin(uint32_t hA, bool vA, uint32_t hB, bool vB) {
+    const uint32_t m = min(vA ? hA : 0xFFFFFFFFu, vB ? hB : 0xFFFFFFFFu);
+    const uint32_t w = __reduce_min_sync(0xFFFFFFFFu, m);
+    const unsigned a = __ballot_sync(0xFFFFFFFFu, vA && hA == w);
+    const unsigned b = __ballot_sync(0xFFFFFFFFu, vB && hB == w);
+    return a ? __ffs(a) - 1 : (b ? 31 + __ffs(b) : -1);
 }
 
 // one lane per light cell, its candidates one after the other; blockDim.x
-// (the cells per CTA) is 32, 64 or 128, with one LightStage per warp in
+// (the cells per CTA) is 32, 64 or 128, with one LightPicks per warp in
 // dynamic shared memory
 __global__ void __launch_bounds__(128, 4)
 k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, int learned, const double* __restrict__ smaxSel, unsigned char* useR,
                 float* obsMax) {
     extern __shared__ __align__(16) unsigned char lightSmem[];
-    LightStage& st = reinterpret_cast<LightStage*>(lightSmem)[threadIdx.x >> 5];
+    LightPicks& pk = reinterpret_cast<LightPicks*>(lightSmem)[threadIdx.x >> 5];
     const int lane = (int)(threadIdx.x & 31u);
     const uint32_t step = (uint32_t)ctr->step;
     const long long nWork = (long long)ctr->nWork;
@@ -588,64 +592,131 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
     const long long C = cs.C;
     unsigned err = 0;
     unsigned long long nColl = 0, nCandTot = 0;
-    for (long long q = nHeavy + (long long)blockIdx.x * blockDim.x + threadIdx.x; q < nWork;
-         q += (long long)gridDim.x * blockDim.x) {
-        const int2 it = work[q];
-        const long long c = it.x;
-        const int nCand = it.y;
-        const long long off = start[c];
-        const int n = start[c + 1] - (int)off;
-        // sub-cell occupancy, 8 bits per sub-cell (n <= LIGHT_N < 256)
-        unsigned long long subCnt = 0;
-        // unrolled so that eight loads per lane are in flight at once
-#pragma unroll 8
-        for (int j = 0; j < n; ++j) {
-            const uint32_t sb = __ldg(s.cellw + off + j) & 7u;
-            st.sub[j][lane] = (uint8_t)sb;
-            st.id[j][lane] = __ldg(s.id + off + j);
-            subCnt += 1ull << (8u * sb);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long qb = nHeavy + (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); qb < nWork;
+         qb += stride) {
+        const long long q = qb + lane;
+        int2 it = make_int2(0, 0);
+        long long off = 0;
+        int n = 0;
+        if (q < nWork) {
+            it = work[q];
+            off = start[it.x];
+            n = start[it.x + 1] - (int)off;
         }
-        const double R = smax[c];
-        const double smax0 = learned ? smaxSel[c] : R;
-        double stepMax = 0.0, collSep = 0.0;
-        unsigned coll = 0;
-        // The lane tests candidates until one is accepted, then collides it:
-        // lanes that reach an accepted candidate in the same pass run the
-        // FP64 exchange together, whatever the rejections before it.
-        int k = 0;
-        while (k < nCand) {
-            bool accepted = false;
-            long long gP = 0, gQ = 0;
-            Rng r(cs, (uint32_t)c, step, cand_tag(k));
-            double cr2 = 0.0;
-            Rec P, Q;
-            while (k < nCand) {
-                const int jP = hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k), -1, -1);
-                const int sub = (int)st.sub[jP][lane];
-                const bool inSub = ((subCnt >> (8 * sub)) & 0xFFu) > 1;
-                const int jQ =
-                    hash_pick(st, lane, n, pick_key(cs, (uint32_t)c, step, 2u * k + 1u), inSub ? sub : -1, jP);
-                r = Rng(cs, (uint32_t)c, step, cand_tag(k));
-                gP = off + jP;
-                gQ = off + jQ;
-                ++k;
-                if (test_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &P, &Q, &cr2)) {
-                    accepted = true;
-                    break;
+        const long long c = it.x;
+        int nCand = it.y;   // 0 past the end of the list
+        if (nCand >= LIGHT_CAND || n > LIGHT_N) {
+            // the list put a heavy cell here: record, never index past the picks
+            err |= ERRB_BOUNDS;
+            nCand = 0;
+        }
+        // every lane's picks, one cell at a time: coalesced loads of the
+        // cell's ids and cell words (the next cell's issued before this
+        // cell's picks), a warp minimum per pick
+        const uint32_t myBase = pick_base(cs, (uint32_t)c, step);
+        int ncN = __shfl_sync(0xFFFFFFFFu, nCand, 0);
+        int nN = __shfl_sync(0xFFFFFFFFu, n, 0);
+        long long offN = __shfl_sync(0xFFFFFFFFu, off, 0);
+        uint32_t idAN = 0, idBN = 0, sAN = 0, sBN = 0;
+        if (ncN) {
+            if (lane < nN) {
+                idAN = __ldg(s.id + offN + lane);
+                sAN = __ldg(s.cellw + offN + lane);
+            }
+            if (lane + 32 < nN) {
+                idBN = __ldg(s.id + offN + lane + 32);
+                sBN = __ldg(s.cellw + offN + lane + 32);
+            }
+        }
+        for (int L = 0; L < 32; ++L) {
+            const int nc = min(ncN, LIGHT_CAND - 1), nL = nN;
+            const uint32_t idA = idAN, idB = idBN, sA = sAN & 7u, sB = sBN & 7u;
+            const uint32_t baseL = __shfl_sync(0xFFFFFFFFu, myBase, L);
+            if (L + 1 < 32) {
+                ncN = __shfl_sync(0xFFFFFFFFu, nCand, L + 1);
+                nN = __shfl_sync(0xFFFFFFFFu, n, L + 1);
+                offN = __shfl_sync(0xFFFFFFFFu, off, L + 1);
+                idAN = idBN = sAN = sBN = 0;
+                if (ncN) {
+                    if (lane < nN) {
+                        idAN = __ldg(s.id + offN + lane);
+                        sAN = __ldg(s.cellw + offN + lane);
+                    }
+                    if (lane + 32 < nN) {
+                        idBN = __ldg(s.id + offN + lane + 32);
+                        sBN = __ldg(s.cellw + offN + lane + 32);
+                    }
                 }
             }
-            if (accepted) {
-                collide_candidate(cs, s, r, gP, gQ, P, Q, cr2, &collSep, &err);
-                ++coll;
+            if (nc == 0) continue;
+            const bool vA = lane < nL, vB = lane + 32 < nL;
+            // sub-cell occupancy, 8 bits per sub-cell (nL <= LIGHT_N < 256)
+            uint32_t cnt0 = 0, cnt1 = 0;
+            if (vA) (sA < 4 ? cnt0 : cnt1) += 1u << (8u * (sA & 3u));
+            if (vB) (sB < 4 ? cnt0 : cnt1) += 1u << (8u * (sB & 3u));
+            cnt0 = __reduce_add_sync(0xFFFFFFFFu, cnt0);
+            cnt1 = __reduce_add_sync(0xFFFFFFFFu, cnt1);
+            for (int k = 0; k < nc; ++k) {
+                const uint32_t kP = pick_draw(cs, baseL, 2u * k);
+                const int jP = warp_argmin(fmix32(kP ^ idA), vA, fmix32(kP ^ idB), vB);
+                const uint32_t sub = __shfl_sync(0xFFFFFFFFu, jP < 32 ? sA : sB, jP & 31);
+                const bool inSub = (((sub < 4 ? cnt0 : cnt1) >> (8u * (sub & 3u))) & 0xFFu) > 1;
+                const uint32_t kQ = pick_draw(cs, baseL, 2u * k + 1u);
+                const bool qA = vA && lane != jP && (!inSub || sA == sub);
+                const bool qB = vB && lane + 32 != jP && (!inSub || sB == sub);
+                const int jQ = warp_argmin(fmix32(kQ ^ idA), qA, fmix32(kQ ^ idB), qB);
+                if (lane == L) {
+                    pk.pq[k][0][L] = (uint8_t)(jP < 0 ? 255 : jP);
+                    pk.pq[k][1][L] = (uint8_t)(jQ < 0 ? 255 : jQ);
+                }
             }
         }
-        cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax);
-        if (coll) {
-            acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
-            acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
+        __syncwarp();
+        if (q < nWork) {
+            const double R = smax[c];
+            const double smax0 = learned ? smaxSel[c] : R;
+            double stepMax = 0.0, collSep = 0.0;
+            unsigned coll = 0;
+            // The lane tests candidates until one is accepted, then collides
+            // it: lanes that reach an accepted candidate in the same pass run
+            // the FP64 exchange together, whatever the rejections before it.
+            int k = 0;
+            while (k < nCand) {
+                bool accepted = false;
+                long long gP = 0, gQ = 0;
+                Rng r(cs, (uint32_t)c, step, cand_tag(k));
+                double cr2 = 0.0;
+                Rec P, Q;
+                while (k < nCand) {
+                    const int jP = pk.pq[k][0][lane], jQ = pk.pq[k][1][lane];
+                    r = Rng(cs, (uint32_t)c, step, cand_tag(k));
+                    ++k;
+                    if (jP >= n || jQ >= n) {
+                        err |= ERRB_BOUNDS;
+                        continue;
+                    }
+                    gP = off + jP;
+                    gQ = off + jQ;
+                    if (test_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &P, &Q, &cr2)) {
+                        accepted = true;
+                        break;
+                    }
+                }
+                if (accepted) {
+                    collide_candidate(cs, s, r, gP, gQ, P, Q, cr2, &collSep, &err);
+                    ++coll;
+                }
+            }
+            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax);
+            if (coll) {
+                acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
+                acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
+            }
+            nColl += coll;
+            nCandTot += (unsigned long long)nCand;
         }
-        nColl += coll;
-        nCandTot += (unsigned long long)nCand;
+        __syncwarp();   // the picks are read before the next cells overwrite them
     }
     if (nColl) atomicAdd(&ctr->coll, nColl);
     if (nCandTot) atomicAdd(&ctr->cand, nCandTot);
