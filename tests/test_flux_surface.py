@@ -289,3 +289,17 @@ def test_gpu_case_directory_flux_surface(gpu_lib, tmp_path):
         assert rows.shape == (2, 2)
         assert rows[0, 1] == pytest.approx(v1[k], rel=1e-10)
         assert rows[1, 0] == pytest.approx(10 * spec.delta_t, rel=1e-10)
+
+
+@pytest.mark.gpu
+def test_gpu_case_with_an_empty_zone_is_rejected(gpu_lib, tmp_path):
+    """A zone whose box holds no face centre fails dsmc_create with the
+    reference's message, and the half-made cloud is released."""
+    from hystrath_gb300.dsmc import DsmcCloud, DsmcError
+    d = _flux_case(tmp_path, box="(0.1003 -1 -1) (0.1004 1 1)")
+    with pytest.raises(DsmcError) as e:
+        DsmcCloud(d)
+    assert "Cannot find region: plane" in str(e.value) and e.value.code == 4
+    g = DsmcCloud(CORNER)   # the library stays usable
+    assert g.n_flux_surfaces() == 0
+    g.close()
