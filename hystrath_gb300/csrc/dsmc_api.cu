@@ -65,6 +65,8 @@ struct dsmc_handle {
     double* info6 = nullptr;
     double* fieldTmp = nullptr;
     Counters* ctrHost = nullptr;   // pinned mirror
+    Counters* ctrRing = nullptr;   // pinned, one per step of dsmc_evolve_counts
+    long long ctrRingN = 0;
     std::vector<void*> allocs;
     std::string err;
     double phaseMs[5] = {0, 0, 0, 0, 0};
@@ -732,6 +734,7 @@ void dsmc_destroy(dsmc_handle* h) {
     drop_graphs(h);
     for (void* q : h->allocs) cudaFree(q);
     if (h->ctrHost) cudaFreeHost(h->ctrHost);
+    if (h->ctrRing) cudaFreeHost(h->ctrRing);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -1106,6 +1109,40 @@ int dsmc_counts(dsmc_handle* h, dsmc_counts_t* o) {
     o->candidates_total = (long long)c.candTot;
     if (c.err) return check_device_error(h);
     return DSMC_OK;
+}
+
+int dsmc_evolve_counts(dsmc_handle* h, long long n, dsmc_counts_t* out) {
+    if (n < 0) return fail(h, DSMC_ERR_INVALID, "n must not be negative");
+    int rc = build_graphs(h);
+    if (rc) return rc;
+    if (n > h->ctrRingN) {
+        if (h->ctrRing) cudaFreeHost(h->ctrRing);
+        h->ctrRing = nullptr;
+        h->ctrRingN = 0;
+        void* p = nullptr;
+        CUDA_TRY(h, cudaMallocHost(&p, sizeof(Counters) * (size_t)n));
+        h->ctrRing = static_cast<Counters*>(p);
+        h->ctrRingN = n;
+    }
+    // each step's counters follow it to the host on the same stream: no
+    // host round trip between steps
+    for (long long i = 0; i < n; ++i) {
+        CUDA_TRY(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
+        h->cur ^= 1;
+        CUDA_TRY(h, cudaMemcpyAsync(h->ctrRing + i, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, h->stream));
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    for (long long i = 0; i < n; ++i) {
+        const Counters& c = h->ctrRing[i];
+        dsmc_counts_t& o = out[i];
+        o.n_particles = c.n;
+        o.step = c.step;
+        o.collisions_last_step = (long long)c.coll;
+        o.candidates_last_step = (long long)c.cand;
+        o.collisions_total = (long long)c.collTot;
+        o.candidates_total = (long long)c.candTot;
+    }
+    return check_device_error(h);
 }
 
 int dsmc_info(dsmc_handle* h, dsmc_info_t* o) {

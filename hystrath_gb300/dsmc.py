@@ -55,6 +55,7 @@ def _load() -> C.CDLL:
                                      vp, vp, vp, vp, vp, vp]
     L.dsmc_parse_last_error.restype = C.c_char_p
     L.dsmc_counts.argtypes = [vp, C.POINTER(S.Counts)]
+    L.dsmc_evolve_counts.argtypes = [vp, C.c_longlong, vp]
     L.dsmc_set_face_tracking.argtypes = [vp, C.c_int]
     L.dsmc_n_faces.argtypes = [vp]
     L.dsmc_n_faces.restype = C.c_longlong
@@ -334,6 +335,13 @@ class DsmcCloud:
         c = S.Counts()
         self._chk(lib().dsmc_counts(self.h, C.byref(c)))
         return c
+
+    def evolve_counts(self, n: int):
+        """n steps, each followed by its counters (copied to the host without a
+        wait between steps); returns the n Counts."""
+        arr = (S.Counts * max(int(n), 1))()
+        self._chk(lib().dsmc_evolve_counts(self.h, int(n), arr))
+        return [arr[i] for i in range(int(n))]
 
     def checkpoint(self, path: str):
         self._chk(lib().dsmc_checkpoint(self.h, path.encode()))

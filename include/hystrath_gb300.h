@@ -369,6 +369,10 @@ int dsmc_info(dsmc_handle* h, dsmc_info_t* out);
  * the energy sums of dsmc_info (a few bytes instead of a pass over the
  * parcels). */
 int dsmc_counts(dsmc_handle* h, dsmc_counts_t* out);
+/* n steps of dsmc_evolve with each step's counters (dsmc_counts) in out[0..n):
+ * every step's counters are copied to pinned host memory on the cloud's
+ * stream right after the step, and the host waits once, at the end. */
+int dsmc_evolve_counts(dsmc_handle* h, long long n, dsmc_counts_t* out);
 
 /* Binary checkpoint: particles, per-cell state, step and seed.  Together with
  * the counter-based random stream this resumes bit for bit. */

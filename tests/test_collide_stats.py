@@ -125,3 +125,24 @@ def test_counts_agree_with_info(gpu_lib):
     assert (c.n_particles, c.step, c.collisions_total, c.candidates_total) == \
         (i.n_particles, i.step, i.collisions_total, i.candidates_total)
     assert c.collisions_last_step == i.collisions_last_step > 0
+
+
+@pytest.mark.gpu
+def test_evolve_counts_equal_step_by_step_counts(gpu_lib):
+    """dsmc_evolve_counts returns, for every step, the counters that
+    dsmc_evolve(1) followed by dsmc_counts gives on the same case."""
+    from hystrath_gb300 import spec as S
+    from hystrath_gb300.dsmc import DsmcCloud
+    a, b = DsmcCloud(S.config0(seed=10)), DsmcCloud(S.config0(seed=10))
+    a.initialise()
+    b.initialise()
+    got = a.evolve_counts(7)
+    want = []
+    for _ in range(7):
+        b.evolve(1)
+        want.append(b.counts())
+    key = lambda c: (c.n_particles, c.step, c.collisions_last_step, c.candidates_last_step,
+                     c.collisions_total, c.candidates_total)
+    assert [key(c) for c in got] == [key(c) for c in want]
+    assert [c.step for c in got] == list(range(got[0].step, got[0].step + 7))
+    assert a.evolve_counts(0) == []
