@@ -61,6 +61,7 @@ struct dsmc_handle {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraph_t graphT[2] = {nullptr, nullptr};   // the captured steps (child graphs of a batch)
+    unsigned long long graphGen = 0;   // bumped whenever the step graphs are dropped
     unsigned char* solid = nullptr;
     double* info6 = nullptr;
     double* fieldTmp = nullptr;
@@ -401,6 +402,7 @@ int check_device_error(dsmc_handle* h) {
         if (e & ERRB_BOUNDS) m += " index out of bounds;";
         if (e & ERRB_PATCH) m += " boundary face without a patch;";
         if (e & ERRB_DENSE) m += " a cell above 16384 parcels or 2^24 candidates (its collisions were skipped);";
+        if (e & ERRB_IDS) m += " parcel id space exhausted (more than 2^32 parcels inserted since the start);";
         return fail(h, e & ERRB_CAPACITY ? DSMC_ERR_CAPACITY : DSMC_ERR_DEVICE, m);
     }
     return DSMC_OK;
@@ -470,6 +472,7 @@ int build_graphs(dsmc_handle* h) {
 // The step graphs hold the launch shape and the selection mode: drop them
 // when either changes (they are captured again on the next step).
 void drop_graphs(dsmc_handle* h) {
+    ++h->graphGen;
     for (int p = 0; p < 2; ++p) {
         if (h->graph[p]) cudaGraphExecDestroy(h->graph[p]);
         if (h->graphT[p]) cudaGraphDestroy(h->graphT[p]);
@@ -1113,6 +1116,7 @@ int dsmc_counts(dsmc_handle* h, dsmc_counts_t* o) {
 
 int dsmc_evolve_counts(dsmc_handle* h, long long n, dsmc_counts_t* out) {
     if (n < 0) return fail(h, DSMC_ERR_INVALID, "n must not be negative");
+    if (n > 0 && !out) return fail(h, DSMC_ERR_INVALID, "dsmc_evolve_counts: out is NULL");
     int rc = build_graphs(h);
     if (rc) return rc;
     if (n > h->ctrRingN) {
@@ -1320,6 +1324,10 @@ struct dsmc_batch {
     std::vector<dsmc_handle*> cases;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // each case's graph generation when the batch graphs were built: a case
+    // whose step graphs were dropped since (learned model, face tracking,
+    // launch shape, ...) makes the batch graphs stale
+    std::vector<unsigned long long> gen;
     std::string err;
 };
 
@@ -1342,6 +1350,9 @@ static void drop_batch_graphs(dsmc_batch* b) {
 // child: a batched step is one launch, and the cases' kernels run side by
 // side as the GPU has room.
 static int build_batch_graphs(dsmc_batch* b) {
+    bool stale = b->gen.size() != b->cases.size();
+    for (size_t i = 0; !stale && i < b->cases.size(); ++i) stale = b->gen[i] != b->cases[i]->graphGen;
+    if (stale) drop_batch_graphs(b);
     for (int p = 0; p < 2; ++p) {
         if (b->graph[p]) continue;
         for (dsmc_handle* h : b->cases) {
@@ -1358,6 +1369,8 @@ static int build_batch_graphs(dsmc_batch* b) {
         cudaGraphDestroy(pg);
         if (e != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
     }
+    b->gen.resize(b->cases.size());
+    for (size_t i = 0; i < b->cases.size(); ++i) b->gen[i] = b->cases[i]->graphGen;
     return DSMC_OK;
 }
 

@@ -31,7 +31,7 @@ constexpr int ZV_TAB = 512;     // iMax values tabulated for 1/Zv
 // Error bits of the device error word.
 enum : unsigned {
     ERRB_CROSSINGS = 1u, ERRB_REJECTION = 2u, ERRB_CAPACITY = 4u, ERRB_BOUNDS = 8u,
-    ERRB_PATCH = 16u, ERRB_DENSE = 32u
+    ERRB_PATCH = 16u, ERRB_DENSE = 32u, ERRB_IDS = 64u
 };
 
 // Random-stream tags (counter word 3) shared with the CPU replay.

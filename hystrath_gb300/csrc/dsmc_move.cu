@@ -455,7 +455,7 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
         f[SACC_UY] = fixp(uy, F_U, err);
         f[SACC_UZ] = fixp(uz, F_U, err);
         // |U|^2 in fixed point from the fixed-point components, on the
-        // integer pipe: (u 2^32)^2 >> 48 = u^2 2^16
+        // integer pipe: (u 2^28)^2 >> 42 = u^2 2^14
         unsigned long long uu = 0;
 #pragma unroll
         for (int a = SACC_UX; a <= SACC_UZ; ++a) {
@@ -1112,6 +1112,10 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
 __global__ void k_inflow_commit(Counters* ctr) {
     const long long add = ctr->inflowTotal;
     ctr->inserted = (unsigned long long)add;
+    // parcel ids are 32-bit and must stay unique (the light-cell picks and
+    // the canonical (sub-cell, id) order rely on it): flag the step whose
+    // insertions run past 2^32 ids
+    if ((unsigned long long)ctr->nextId + (unsigned long long)add > 0x100000000ull) ctr->err |= ERRB_IDS;
     ctr->nextId += add;
     ctr->nMoved = ctr->n + add;
 }

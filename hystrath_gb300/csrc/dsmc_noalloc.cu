@@ -10,9 +10,10 @@
 //
 // That array is a file-scope __device__ variable of NA_MAX_BLOCKS (4096)
 // ints (16 KiB): every GPU that loads the library holds it until the process
-// exits.  Host code cannot use its name as an address, so the first call on a
-// device looks the address up with cudaGetSymbolAddress (with that device
-// current) and keeps it; make that first call before any stream capture.
+// exits.  Host code cannot use its name as an address, so every call made
+// outside stream capture looks the address up with cudaGetSymbolAddress (with
+// the calling device current) and keeps it for captured calls; make the first
+// call on a device, and the first one after a device reset, outside capture.
 // All calls share the one array and it keeps what the last call left there;
 // each call writes every entry it reads before reading it.  Calls whose
 // kernels overlap on the GPU race on the array: serialise them (one stream,
@@ -130,10 +131,18 @@ int dsmc_cell_starts_noalloc(const int* d_counts, long long n_cells, int* d_star
     if (e != cudaSuccess) return na_fail(DSMC_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= NA_MAX_DEVICES)
         return na_fail(DSMC_ERR_INVALID, "dsmc_cell_starts_noalloc: device index beyond 63");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // The array's address is looked up again on every call made outside
+    // stream capture, so a device reset (which reloads the module and may
+    // move the array) never leaves a stale address behind; a captured call
+    // uses the address of the last uncaptured one.
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(st, &cap);
+    if (e != cudaSuccess) return na_fail(DSMC_ERR_CUDA, cudaGetErrorString(e));
     int* sums = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_na_mutex);
-        if (!g_na_ptr[dev]) {
+        if (!g_na_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
             void* p = nullptr;
             e = cudaGetSymbolAddress(&p, g_noalloc_block_sums);
             if (e != cudaSuccess) return na_fail(DSMC_ERR_CUDA, cudaGetErrorString(e));
@@ -141,7 +150,6 @@ int dsmc_cell_starts_noalloc(const int* d_counts, long long n_cells, int* d_star
         }
         sums = g_na_ptr[dev];
     }
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int nb = (int)((n_cells + NA_TILE - 1) / NA_TILE);
     k_na_reduce<<<nb, NA_THREADS, 0, st>>>(d_counts, n_cells, sums);
     k_na_top<<<1, NA_THREADS, 0, st>>>(sums, nb, d_start, n_cells);

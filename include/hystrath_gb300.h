@@ -397,8 +397,10 @@ void dsmc_destroy(dsmc_handle* h);
  * entry is the total), on the given cudaStream_t (NULL = legacy stream).
  * No cudaMalloc/cudaFree: the block sums live in a 16 KiB static device array
  * that every GPU loading the library holds until exit, which limits n_cells to
- * 2^24.  The first call on a device resolves that array's address (call it
- * before any stream capture).  Calls share the array: calls that overlap on
+ * 2^24.  Every call made outside stream capture resolves that array's
+ * address on the current device (the first call on a device, and the first
+ * after a device reset, must come before any stream capture; captured calls
+ * use the last address resolved).  Calls share the array: calls that overlap on
  * the GPU race.  Errors: DSMC_ERR_INVALID beyond 2^24 cells or for null
  * buffers, message in dsmc_noalloc_last_error().
  */

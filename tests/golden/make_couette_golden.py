@@ -86,7 +86,10 @@ def write_lagrangian_sample(src):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # root of the reference tree: first argument, else $HYSTRATH_REFERENCE
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HYSTRATH_REFERENCE", "")
+    if not ref:
+        sys.exit(f"usage: python {sys.argv[0]} <reference tree root> (or set HYSTRATH_REFERENCE)")
     d = os.path.join(ref, "run/hyStrath/dsmcFoam+/couette_N2-O2/backup-5")
     out = {}
     for sp in ("N2", "O2", "mixture"):

@@ -55,7 +55,10 @@ def to_cartesian(vals):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # root of the reference tree: first argument, else $HYSTRATH_REFERENCE
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HYSTRATH_REFERENCE", "")
+    if not ref:
+        sys.exit(f"usage: python {sys.argv[0]} <reference tree root> (or set HYSTRATH_REFERENCE)")
     d = os.path.join(ref, "run/hyStrath/dsmcFoam+/supersonicFlatPlate/backup-0.04")
     out = {}
     for name in ("rhoN", "Ttra", "Trot", "p", "dsmcNMean"):

@@ -48,7 +48,10 @@ def to_cartesian(vals):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    # root of the reference tree: first argument, else $HYSTRATH_REFERENCE
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HYSTRATH_REFERENCE", "")
+    if not ref:
+        sys.exit(f"usage: python {sys.argv[0]} <reference tree root> (or set HYSTRATH_REFERENCE)")
     d = os.path.join(ref, "run/hyStrath/dsmcFoam+/hypersonicCorner/backup-0.003")
     fields = {}
     for name in ("rhoN_Ar", "rhoM_Ar", "Ttra_Ar", "p_Ar", "U_Ar", "dsmcSigmaTcRMax", "dsmcNMean_Ar", "mfp_Ar"):

@@ -113,3 +113,66 @@ def test_batch_from_case_directories():
         # the totals are sums of FP64 atomics: equal to the last bits
         assert abs(a.linear_ke / c.linear_ke - 1.0) < 1e-12
     b.close()
+
+
+def _case_view(b, i):
+    import ctypes as C
+    from hystrath_gb300.dsmc import DsmcCloud, lib
+    view = DsmcCloud.__new__(DsmcCloud)
+    view.h = C.c_void_p(lib().dsmc_batch_case(b.h, i))
+    view.spec = b.specs[i]
+    s = view.spec
+    view.n_cells = s.n_cells[0] * s.n_cells[1] * s.n_cells[2]
+    return view
+
+
+@pytest.mark.gpu
+def test_batch_follows_settings_changed_on_a_case():
+    """Switching face tracking or the learned maximum on a batched case (which
+    drops that case's step graphs) rebuilds the batch graph: the batch keeps
+    giving each case the state it reaches alone with the same switches, and a
+    model detached and destroyed is no longer read."""
+    from hystrath_gb300.batch import BatchCloud
+    from hystrath_gb300.dsmc import DsmcCloud, Mlp
+    from hystrath_gb300.learn import init_params
+    specs = [S.config1(seed=21, n=10), S.config1(seed=22, n=12)]
+    b = BatchCloud(specs)
+    b.initialise()
+    b.evolve(2)
+    alone = [DsmcCloud(s) for s in specs]
+    for g in alone:
+        g.initialise()
+        g.evolve(2)
+    model = Mlp()
+    norm = np.array([45.0, 8.0, 0.5, 1.0, 1.0, 0.5, -13.0, 1.0], dtype=np.float32)
+    model.set_params(init_params(3), norm)
+    views = [_case_view(b, i) for i in range(2)]
+    try:
+        views[0].set_face_tracking(True)
+        alone[0].set_face_tracking(True)
+        views[1].set_learned(model, 2, 0.5)
+        alone[1].set_learned(model, 2, 0.5)
+        b.evolve(3)
+        for g in alone:
+            g.evolve(3)
+        flux_b = views[0].face_flux("parcelIdFlux")
+        assert np.abs(flux_b).sum() > 0
+        np.testing.assert_array_equal(flux_b, alone[0].face_flux("parcelIdFlux"))
+        assert b.info(1).candidates_total == alone[1].info().candidates_total
+        views[1].set_learned(None)
+        alone[1].set_learned(None)
+        model.close()
+        b.evolve(2)
+        for g in alone:
+            g.evolve(2)
+        for i in range(2):
+            assert b.info(i).collisions_total == alone[i].info().collisions_total
+            sb, sg = _state(views[i]), _state(alone[i])
+            for k in sb:
+                assert np.array_equal(sb[k], sg[k]), k
+    finally:
+        for v in views:
+            v.h = None      # owned by the batch
+        for g in alone:
+            g.close()
+        b.close()

@@ -13,7 +13,9 @@ from hystrath_gb300 import spec as S
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CASE = os.path.join(HERE, "golden", "cases", "hypersonic_corner")
-REF_CASE = "/root/reference/run/hyStrath/dsmcFoam+/hypersonicCorner"
+# the reference tree, when present, via HYSTRATH_REFERENCE (its root directory)
+REF_ROOT = os.environ.get("HYSTRATH_REFERENCE", "")
+REF_CASE = os.path.join(REF_ROOT, "run/hyStrath/dsmcFoam+/hypersonicCorner") if REF_ROOT else ""
 
 
 def parse(path):
@@ -55,7 +57,8 @@ def test_parse_corner_case(gpu_lib):
     assert s.measure_mean_free_path == 1 and s.n_obstacles == 0
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="reference tree not present")
+@pytest.mark.skipif(not REF_CASE or not os.path.isdir(REF_CASE),
+                    reason="HYSTRATH_REFERENCE does not name a reference tree")
 def test_reference_tutorial_parses_to_the_same_case(gpu_lib):
     """The reference's own hypersonicCorner dictionaries (old 'patches'
     syntax, no ';' after the list) resolve to the same case."""
