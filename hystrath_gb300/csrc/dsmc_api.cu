@@ -408,49 +408,90 @@ int check_device_error(dsmc_handle* h) {
     return DSMC_OK;
 }
 
+// Event marks of a step (enqueue_step with events): the intervals between
+// consecutive marks are the kernel groups of dsmc_evolve_kernel_profile, and
+// the coarse phases of dsmc_evolve_profiled are unions of them.
+enum {
+    MK_START = 0,
+    MK_ZERO,          // k_zero_step (and the sample flush of a step without a move)
+    MK_INFLOW,        // k_inflow_count/scan/fill/commit
+    MK_MOVE,          // k_move, k_move_slow
+    MK_SAMPLE,        // k_sample_done/finalize/flushed
+    MK_SCAN,          // k_scan_reduce/top/down (k_count_dev before them without a move)
+    MK_SCATTER,       // k_scatter_index
+    MK_GATHER,        // k_gather
+    MK_FINISH,        // k_finish_sort
+    MK_LEARNED,       // k_cell_features, k_mlp_infer
+    MK_SELECT,        // k_ntc_select/buckets/list, k_cell_order(_big)
+    MK_HEAVY,         // k_collide_heavy (k_sbt_collide)
+    MK_LIGHT,         // k_collide_light
+    MK_PENDING,       // k_set_pending
+    MK_END,           // k_end_step
+    MK_COUNT
+};
+
 // Enqueue one step on the handle's stream (graph capture or direct launch).
+// ev: NULL, or MK_COUNT events recorded at the marks above.
 void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) {
     const CaseDev& cs = h->cs;
     StepBuffers& B = h->B;
     cudaStream_t st = h->stream;
     Parcels& a = h->buf[parity];
     Parcels& b = h->buf[parity ^ 1];
-    if (ev) cudaEventRecord(ev[0], st);
+    auto mark = [&](int k) {
+        if (ev) cudaEventRecord(ev[k], st);
+    };
+    mark(MK_START);
     launch_zero_step(B, st);
     // a sample pending from the previous step is taken by the move kernel,
     // or here when this step does not move
     if (!(phases & DSMC_PHASE_MOVE)) launch_sample_flush(cs, B, a, 0, st);
+    mark(MK_ZERO);
     if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
-    if (ev) cudaEventRecord(ev[1], st);
-    if (phases & DSMC_PHASE_MOVE) {
-        launch_move(cs, B, a, st);
-        launch_sample_commit(cs, B, 0, st);
-    }
-    if (ev) cudaEventRecord(ev[2], st);
+    mark(MK_INFLOW);
+    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st);
+    mark(MK_MOVE);
+    if (phases & DSMC_PHASE_MOVE) launch_sample_commit(cs, B, 0, st);
+    mark(MK_SAMPLE);
     if (phases & DSMC_PHASE_SORT) {
         if (!(phases & DSMC_PHASE_MOVE)) launch_count(cs, B, a, st);
         launch_scan(cs, B, st);
-        launch_scatter(cs, B, a, b, st);
+        mark(MK_SCAN);
+        launch_scatter(cs, B, a, b, st, ev ? ev[MK_SCATTER] : nullptr);
+        mark(MK_GATHER);
         launch_finish_sort(B, st);
-    } else if (phases & DSMC_PHASE_MOVE) {
-        cudaMemsetAsync(B.count, 0, sizeof(int) * cs.C, st);
+    } else {
+        if (phases & DSMC_PHASE_MOVE) cudaMemsetAsync(B.count, 0, sizeof(int) * cs.C, st);
+        mark(MK_SCAN);
+        mark(MK_SCATTER);
+        mark(MK_GATHER);
     }
-    if (ev) cudaEventRecord(ev[3], st);
+    mark(MK_FINISH);
     if (phases & DSMC_PHASE_COLLIDE) {
         const Parcels& cur = (phases & DSMC_PHASE_SORT) ? b : a;
         if (h->model) {
             launch_cell_features(cs, B, cur, h->learnEvery, 1, st);
             mlp_launch_infer(h->model, B.feat, cs.C, B.pred, h->learnMargin, &B.ctr->step, h->learnEvery, st);
         }
-        launch_collide(cs, B, cur, h->model ? 1 : 0, st);
+        mark(MK_LEARNED);
+        launch_collide(cs, B, cur, h->model ? 1 : 0, st, ev ? ev + MK_SELECT : nullptr);
+    } else {
+        mark(MK_LEARNED);
+        mark(MK_SELECT);
+        mark(MK_HEAVY);
     }
+    mark(MK_LIGHT);
     // dsmcVolFields samples the state after the collisions; the sums are
     // taken when that state is next streamed (the next move, or a flush)
     if (phases & DSMC_PHASE_SAMPLE) launch_set_pending(B, st);
-    if (ev) cudaEventRecord(ev[4], st);
+    mark(MK_PENDING);
     launch_end_step(B, st);
-    if (ev) cudaEventRecord(ev[5], st);
+    mark(MK_END);
 }
+
+// The coarse phases (inflow, move, sort, collide+sample, bookkeeping) as
+// mark intervals [PHASE_MARKS[k], PHASE_MARKS[k + 1]).
+const int PHASE_MARKS[6] = {MK_START, MK_INFLOW, MK_SAMPLE, MK_FINISH, MK_PENDING, MK_END};
 
 // Takes a pending sample of the current state (before fields are read,
 // checkpointed or reset).
@@ -805,32 +846,52 @@ int dsmc_evolve(dsmc_handle* h, long long n) {
     return check_device_error(h);
 }
 
-int dsmc_evolve_profiled(dsmc_handle* h, long long n, double* phase_ms, double* total_ms) {
+// n steps enqueued with the events of every mark; per_mark[k] receives the
+// summed time of interval k (mark k to mark k + 1), total the first-to-last
+// event time.
+int profile_steps(dsmc_handle* h, long long n, double* per_mark, double* total_ms) {
     if (n <= 0) return fail(h, DSMC_ERR_INVALID, "n must be positive");
-    std::vector<cudaEvent_t> ev((size_t)n * 6);
+    std::vector<cudaEvent_t> ev((size_t)n * MK_COUNT);
     for (auto& e : ev) CUDA_TRY(h, cudaEventCreate(&e));
     for (long long i = 0; i < n; ++i) {
-        enqueue_step(h, h->cur, DSMC_PHASE_ALL, &ev[(size_t)i * 6]);
+        enqueue_step(h, h->cur, DSMC_PHASE_ALL, &ev[(size_t)i * MK_COUNT]);
         h->cur ^= 1;
     }
     CUDA_TRY(h, cudaGetLastError());
     int rc = check_device_error(h);
-    double sums[5] = {0, 0, 0, 0, 0};
+    for (int k = 0; k + 1 < MK_COUNT; ++k) per_mark[k] = 0.0;
     for (long long i = 0; i < n; ++i) {
-        for (int k = 0; k < 5; ++k) {
+        for (int k = 0; k + 1 < MK_COUNT; ++k) {
             float ms = 0;
-            cudaEventElapsedTime(&ms, ev[(size_t)i * 6 + k], ev[(size_t)i * 6 + k + 1]);
-            sums[k] += ms;
+            cudaEventElapsedTime(&ms, ev[(size_t)i * MK_COUNT + k], ev[(size_t)i * MK_COUNT + k + 1]);
+            per_mark[k] += ms;
         }
     }
     float tot = 0;
-    cudaEventElapsedTime(&tot, ev[0], ev[(size_t)(n - 1) * 6 + 5]);
+    cudaEventElapsedTime(&tot, ev[0], ev[(size_t)(n - 1) * MK_COUNT + MK_END]);
     for (auto& e : ev) cudaEventDestroy(e);
-    for (int k = 0; k < 5; ++k) {
-        if (phase_ms) phase_ms[k] = sums[k];
-        h->phaseMs[k] = sums[k] / (double)n;
-    }
     if (total_ms) *total_ms = tot;
+    return rc;
+}
+
+int dsmc_evolve_profiled(dsmc_handle* h, long long n, double* phase_ms, double* total_ms) {
+    double per[MK_COUNT] = {0};
+    const int rc = profile_steps(h, n, per, total_ms);
+    if (n <= 0) return rc;
+    for (int k = 0; k < 5; ++k) {
+        double sum = 0;
+        for (int m = PHASE_MARKS[k]; m < PHASE_MARKS[k + 1]; ++m) sum += per[m];
+        if (phase_ms) phase_ms[k] = sum;
+        h->phaseMs[k] = sum / (double)n;
+    }
+    return rc;
+}
+
+int dsmc_evolve_kernel_profile(dsmc_handle* h, long long n, double* group_ms, int n_groups, double* total_ms) {
+    if (n_groups < 0) return fail(h, DSMC_ERR_INVALID, "n_groups must not be negative");
+    double per[MK_COUNT] = {0};
+    const int rc = profile_steps(h, n, per, total_ms);
+    for (int k = 0; k < n_groups && k + 1 < MK_COUNT; ++k) group_ms[k] = per[k];
     return rc;
 }
 
@@ -856,18 +917,18 @@ int dsmc_evolve_timed(dsmc_handle* h, long long n, double* total_ms) {
 }
 
 int dsmc_run_phases(dsmc_handle* h, unsigned phases) {
-    cudaEvent_t ev[6];
-    for (int k = 0; k < 6; ++k) cudaEventCreate(&ev[k]);
+    cudaEvent_t ev[MK_COUNT];
+    for (int k = 0; k < MK_COUNT; ++k) cudaEventCreate(&ev[k]);
     enqueue_step(h, h->cur, phases, ev);
     CUDA_TRY(h, cudaGetLastError());
     if (phases & DSMC_PHASE_SORT) h->cur ^= 1;
     int rc = check_device_error(h);
-    float ms;
     for (int k = 0; k < 5; ++k) {
-        cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev[PHASE_MARKS[k]], ev[PHASE_MARKS[k + 1]]);
         h->phaseMs[k] = ms;
     }
-    for (int k = 0; k < 6; ++k) cudaEventDestroy(ev[k]);
+    for (int k = 0; k < MK_COUNT; ++k) cudaEventDestroy(ev[k]);
     return rc;
 }
 

@@ -353,7 +353,8 @@ int collide_init() {
     return e == cudaSuccess ? 0 : (int)e;
 }
 
-void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st) {
+void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st,
+                    cudaEvent_t* marks) {
     const int sms = sm_count();
     long long selBlocks = (cs.C + 255) / 256;
     if (selBlocks > (long long)sms * 8) selBlocks = (long long)sms * 8;
@@ -371,13 +372,16 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
     tile::k_cell_order<<<sms * 8, tile::WARPS * 32, 0, st>>>(s, B.start, B.ctr, B.work, B.perm, B.subs);
     tile::k_cell_order_big<<<sms, tile::ORDER_BLOCK, tile::ORDER_MAX_N * sizeof(unsigned long long), st>>>(
         s, B.start, B.ctr, B.work, B.bigList, B.perm, B.subs);
+    if (marks) cudaEventRecord(marks[0], st);
     if (sbt) {
         tile::k_sbt_collide<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.acc, B.ctr, B.work, B.perm);
+        if (marks) cudaEventRecord(marks[1], st);
         return;
     }
     tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
                                                                 B.perm, B.subs, learned, B.smaxSel, B.useR,
                                                                 B.obsMax);
+    if (marks) cudaEventRecord(marks[1], st);
     const int L = B.cfg.lightCells;
     tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * sizeof(tile::LightPicks), st>>>(
         cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.obsMax);

@@ -94,12 +94,16 @@ int scan_scratch_ints(long long C);
 void launch_count(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
 void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
+// mid (optional): an event recorded between the index scatter and the gather
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
-                    cudaStream_t st);
+                    cudaStream_t st, cudaEvent_t mid = nullptr);
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
 // learned != 0: the selection uses the prediction (or the running maximum of
 // cells that fell back to it) instead of the running maximum alone
-void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st);
+// marks (optional): two events, recorded after the selection, list and
+// ordering kernels and after the heavy-cell kernel
+void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st,
+                    cudaEvent_t* marks = nullptr);
 // per-cell features of the learned maximum; every > 0: only on steps that are
 // multiples of every, every == 0: always; resetFallback: the cells go back to
 // the prediction

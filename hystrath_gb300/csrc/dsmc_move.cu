@@ -1269,11 +1269,12 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st) {
 }
 
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
-                    cudaStream_t st) {
+                    cudaStream_t st, cudaEvent_t mid) {
     (void)cs;
     const int T = B.cfg.streamThreads;
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
     k_scatter_index<<<grid, T, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortSrc);
+    if (mid) cudaEventRecord(mid, st);
     k_gather<<<grid, T, 0, st>>>(src, dst, B.ctr, B.sortSrc);
 }
 

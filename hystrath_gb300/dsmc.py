@@ -38,6 +38,8 @@ def _load() -> C.CDLL:
     L.dsmc_run_phases.argtypes = [vp, C.c_uint]
     L.dsmc_evolve_timed.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double)]
     L.dsmc_evolve_profiled.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.dsmc_evolve_kernel_profile.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double), C.c_int,
+                                             C.POINTER(C.c_double)]
     L.dsmc_set_particles.argtypes = [vp, C.c_longlong, vp, vp, vp, vp, vp, vp]
     L.dsmc_get_particles.argtypes = [vp, C.c_longlong, C.POINTER(C.c_longlong), vp, vp, vp, vp, vp, vp, vp]
     L.dsmc_get_cell_array.argtypes = [vp, C.c_char_p, vp, C.c_longlong]
@@ -196,6 +198,18 @@ class DsmcCloud:
         tot = C.c_double()
         self._chk(lib().dsmc_evolve_profiled(self.h, n, ph, C.byref(tot)))
         return tot.value, dict(zip(("inflow", "move", "sort", "collide_sample", "end"), list(ph)))
+
+    KERNEL_GROUPS = ("zero", "inflow", "move", "sample", "scan", "scatter_index", "gather", "finish",
+                     "learned", "select", "collide_heavy", "collide_light", "pending", "end")
+
+    def evolve_kernel_profile(self, n: int):
+        """n steps with CUDA events between the kernel groups; returns (total
+        ms, dict of summed group ms in the order of KERNEL_GROUPS)."""
+        k = len(self.KERNEL_GROUPS)
+        g = (C.c_double * k)()
+        tot = C.c_double()
+        self._chk(lib().dsmc_evolve_kernel_profile(self.h, n, g, k, C.byref(tot)))
+        return tot.value, dict(zip(self.KERNEL_GROUPS, list(g)))
 
     def run_phases(self, phases: int):
         self._chk(lib().dsmc_run_phases(self.h, phases))

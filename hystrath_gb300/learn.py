@@ -9,9 +9,12 @@ The pipeline of the learned selection, all on the GPU through the C ABI:
    library's own forward/backward and Adam kernels (``dsmc_mlp_train``).
 3. ``calibrate``: the margin added to the log prediction so that a given
    fraction of the recorded maxima lie below the prediction.
-4. ``compare``: run the plain and the learned selection from the same state
-   and report candidates per accepted collision, collision throughput, the
-   collision-count error and field differences.
+4. ``run_window`` / ``compare_windows``: run the plain and the learned
+   selection from the same developed state (the speed comparison) and from
+   independently seeded runs of the same development (the per-cell
+   collision-count test and the field differences in standard errors), and
+   report candidates per accepted collision, collision throughput, the
+   collision-count error and the field differences.
 
 ``python -m hystrath_gb300.learn`` runs the learned form of the benchmark
 workloads (heat bath and Mach-10 channel) and prints one JSON line.
@@ -19,6 +22,7 @@ workloads (heat bath and Mach-10 channel) and prints one JSON line.
 from __future__ import annotations
 
 import json
+import math
 import sys
 import time
 
@@ -105,84 +109,220 @@ def calibrate(model: Mlp, X, Y, coverage=0.99):
     return float(np.quantile(r, coverage))
 
 
-def _run(spec, develop, steps, model=None, every=1, margin=0.0):
-    # the step is deterministic: two clouds from the same spec reach the same
-    # state after the same number of steps
+FIELDS = ("rhoN", "Ttra", "Ux", "Trot", "Tvib")
+
+
+def develop(spec, steps):
+    """A cloud of spec after the mesh fill and `steps` plain steps (the step is
+    deterministic: two clouds of the same spec reach the same state)."""
     g = DsmcCloud(spec)
     g.initialise()
-    g.evolve(develop)
-    if model is not None:
-        g.set_learned(model, every, margin)
-    g.reset_sampling()
-    i0 = g.info()
-    total_ms, phases = g.evolve_profiled(steps)
-    i1 = g.info()
-    out = {
-        "ms_per_step": total_ms / steps,
-        "collide_ms_per_step": phases["collide_sample"] / steps,
-        "collisions": int(i1.collisions_total - i0.collisions_total),
-        "candidates": int(i1.candidates_total - i0.candidates_total),
-        "nColls": g.field("nColls"),
-        "fields": {k: g.field(k) for k in ("rhoN", "Ttra", "Ux", "Trot", "Tvib")},
-        "count": g.cell_array("count"),
-    }
-    g.close()
+    if steps:
+        g.evolve(steps)
+    return g
+
+
+def run_window(g, steps, batches=8, fields=FIELDS, blk=8):
+    """`steps` graph-launched steps in `batches` equal batches (sampling reset
+    at the start of each): device time, collision and candidate counts, the
+    parcel counts at both ends, the per-cell collision counts summed over the
+    batches, the per-cell mean of Ttra over the batches, and every batch's
+    time-averaged fields as means over blocks of blk^3 cells (batch means)."""
+    n = list(g.spec.n_cells)
+    per = max(1, steps // batches)
+    c0 = g.counts()
+    out = {"steps": per * batches, "ms": 0.0, "n_start": int(c0.n_particles), "nColls": None, "Ttra": None,
+           "blk": blk, "batches": {k: [] for k in fields}}
+    for _ in range(batches):
+        g.reset_sampling()
+        out["ms"] += g.evolve_timed(per)
+        nc = g.field("nColls")
+        out["nColls"] = nc if out["nColls"] is None else out["nColls"] + nc
+        for k in fields:
+            f = g.field(k)
+            if k == "Ttra":
+                out["Ttra"] = f / batches if out["Ttra"] is None else out["Ttra"] + f / batches
+            out["batches"][k].append(_block_means(f, n, blk))
+    c1 = g.counts()
+    out["n_end"] = int(c1.n_particles)
+    out["collisions"] = int(c1.collisions_total - c0.collisions_total)
+    out["candidates"] = int(c1.candidates_total - c0.candidates_total)
     return out
 
 
-def _block_sums(a, n, b):
+def arm_rates(w):
+    """Throughput of a run_window result."""
+    t = w["ms"] * 1e-3
+    n_avg = 0.5 * (w["n_start"] + w["n_end"])
+    return {"ms_per_step": w["ms"] / w["steps"], "particle_steps_per_s": n_avg * w["steps"] / t,
+            "collisions_per_s": w["collisions"] / t,
+            "candidates_per_collision": w["candidates"] / max(w["collisions"], 1),
+            "collisions": w["collisions"], "candidates": w["candidates"]}
+
+
+def per_cell_count_test(a, b, groups=None, group_names=None):
+    """Per-cell collision counts of two independent runs of the same flow.
+
+    Given a cell's total s = a + b, a equal mean in both runs makes a
+    Binomial(s, 1/2): (a - b)^2 / s then has mean 1 and variance 2 - 2/s
+    exactly.  X = sum over cells of (a - b)^2 / s tests for any per-cell
+    difference (z = (X - n) / sd).  A relative bias r_c of cell c adds about
+    r_c^2 mu_c / 2 to X, so the rms per-cell bias weighted by counts is
+    sqrt(2 (X - n) / sum(a)), with a one-sided 95% upper bound from
+    X - n + 1.645 sd.  groups: an integer label per cell; each group's total
+    relative difference and its standard error are reported as well."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    s = a + b
+    m = s > 0
+    d = b[m] - a[m]
+    X = float(np.sum(d * d / s[m]))
+    n = int(m.sum())
+    var = float(np.sum(2.0 - 2.0 / s[m]))
+    sd = math.sqrt(max(var, 1e-300))
+    z = (X - n) / sd
+    tot_a = float(a.sum())
+    rms2 = 2.0 * (X - n) / max(tot_a, 1.0)
+    rms2_hi = 2.0 * (X - n + 1.645 * sd) / max(tot_a, 1.0)
+    res = {"cells": n, "statistic": X, "expected": float(n), "sd": sd, "z": z,
+           "p_value_two_sided": math.erfc(abs(z) / math.sqrt(2.0)),
+           "mean_count_per_cell": tot_a / max(n, 1),
+           "rms_rel_bias_estimate": math.sqrt(max(rms2, 0.0)),
+           "rms_rel_bias_upper95": math.sqrt(max(rms2_hi, 0.0)),
+           "total_rel_diff": float(b.sum() / max(tot_a, 1.0) - 1.0),
+           "total_rel_diff_se": math.sqrt(float(s.sum())) / max(tot_a, 1.0)}
+    if groups is not None:
+        gl = []
+        for gi in np.unique(groups):
+            if gi < 0:
+                continue   # cells without a label (no temperature: solid or empty)
+            sel = groups == gi
+            ta, tb = float(a[sel].sum()), float(b[sel].sum())
+            if ta <= 0:
+                continue
+            gl.append({"group": group_names[int(gi)] if group_names else int(gi), "cells": int(sel.sum()),
+                       "rel_diff": tb / ta - 1.0, "se": math.sqrt(ta + tb) / ta})
+        res["groups"] = gl
+    return res
+
+
+def _block_means(a, n, blk):
     nx, ny, nz = n
     a = a.reshape(nz, ny, nx)
-    return a[:nz - nz % b, :ny - ny % b, :nx - nx % b].reshape(
-        nz // b, b, ny // b, b, nx // b, b).sum(axis=(1, 3, 5))
+    a = a[:nz - nz % blk, :ny - ny % blk, :nx - nx % blk]
+    return a.reshape(nz // blk, blk, ny // blk, blk, nx // blk, blk).mean(axis=(1, 3, 5)).ravel()
 
 
-def compare(spec, develop, steps, model, every=1, margin=0.0, block=8, plain=None):
-    """Plain and learned selection from the same state (develop plain steps
-    after the mesh fill).  plain: a previous plain _run of the same arguments."""
-    if plain is None:
-        plain = _run(spec, develop, steps)
-    learned = _run(spec, develop, steps, model, every, margin)
-    n = list(spec.n_cells)
-    res = {}
-    for name, r in (("plain", plain), ("learned", learned)):
-        res[name] = {
-            "ms_per_step": round(r["ms_per_step"], 4),
-            "collide_ms_per_step": round(r["collide_ms_per_step"], 4),
-            "collisions_per_s": r["collisions"] / (r["ms_per_step"] * steps * 1e-3),
-            "collide_phase_collisions_per_s": r["collisions"] / (r["collide_ms_per_step"] * steps * 1e-3),
-            "candidates_per_collision": r["candidates"] / max(r["collisions"], 1),
-            "collisions": r["collisions"],
-        }
-    res["speedup_collisions_per_s"] = res["learned"]["collisions_per_s"] / res["plain"]["collisions_per_s"]
-    res["speedup_collide_phase"] = (res["learned"]["collide_phase_collisions_per_s"]
-                                    / res["plain"]["collide_phase_collisions_per_s"])
-    res["total_collision_error"] = learned["collisions"] / plain["collisions"] - 1
-    # per-cell counts (nColls: collisions of the cell over the sampled steps);
-    # the per-cell error is judged on blocks of block^3 cells (a single cell
-    # sees too few collisions for a 1% statement) and on the total
-    cp = _block_sums(plain["nColls"], n, block)
-    cl = _block_sums(learned["nColls"], n, block)
-    ok = cp > 0
-    rel = (cl[ok] - cp[ok]) / cp[ok]
-    se = np.sqrt(cl[ok] + cp[ok]) / cp[ok]          # Poisson standard error of the difference
-    res["block_collision_error"] = {
-        "block_cells": block ** 3, "blocks": int(ok.sum()),
-        "mean_abs": float(np.mean(np.abs(rel))), "mean": float(np.mean(rel)),
-        "mean_abs_in_se": float(np.mean(np.abs(rel) / se)),
-        "mean_se": float(np.mean(se)),
-    }
-    # fields: difference in units of its standard error, estimated from the
-    # spread of the two runs' block means
-    fd = {}
-    for k in plain["fields"]:
-        a = _block_sums(plain["fields"][k], n, block) / block ** 3
-        b = _block_sums(learned["fields"][k], n, block) / block ** 3
-        d = b - a
-        fd[k] = {"mean_rel_diff": float(np.mean(d) / max(abs(np.mean(a)), 1e-300)),
-                 "rms_diff_over_rms_field": float(np.sqrt(np.mean(d ** 2)) / max(np.sqrt(np.mean(a ** 2)), 1e-300))}
-    res["fields"] = fd
+def batch_mean_z(batches_a, batches_b):
+    """Differences of time-averaged fields between two independent runs in
+    units of their standard error, per block of cells (the batches hold
+    block means): each run's block value is the mean of its batch means and
+    its standard error the spread of the batch means / sqrt(batches) (batch
+    means absorb the autocorrelation).  Blocks where a field does not vary
+    (solid cells, or a temperature with no excited level) are left out."""
+    A = np.array(batches_a)
+    B = np.array(batches_b)
+    ka, kb = A.shape[0], B.shape[0]
+    ma, mb = A.mean(0), B.mean(0)
+    va, vb = A.var(0, ddof=1) / ka, B.var(0, ddof=1) / kb
+    se = np.sqrt(va + vb)
+    ok = (se > 0) & np.isfinite(se) & (np.abs(ma) > 0)
+    z = (mb[ok] - ma[ok]) / se[ok]
+    # Welch-Satterthwaite degrees of freedom: |z| > 2 is expected in the
+    # fraction 2 P(t_nu > 2), not 4.6%, with this few batches
+    nu = (va[ok] + vb[ok]) ** 2 / (va[ok] ** 2 / (ka - 1) + vb[ok] ** 2 / (kb - 1))
+    return {"blocks": int(ok.sum()), "mean_abs_z": float(np.mean(np.abs(z))) if z.size else 0.0,
+            "frac_abs_z_gt_2": float(np.mean(np.abs(z) > 2.0)) if z.size else 0.0,
+            "expected_frac_abs_z_gt_2": float(np.mean(_t_two_sided_tail(2.0, nu))) if z.size else 0.0,
+            "mean_z": float(np.mean(z)) if z.size else 0.0,
+            "rel_diff_of_means": float(np.sum(mb[ok] - ma[ok]) / max(abs(np.sum(ma[ok])), 1e-300))}
+
+
+def _t_two_sided_tail(t, nu):
+    """P(|T| > t) for Student's t with nu degrees of freedom (array)."""
+    from scipy.stats import t as student_t
+    return 2.0 * student_t.sf(t, np.asarray(nu, dtype=np.float64))
+
+
+def temperature_groups(ttra, k=5):
+    """Cells grouped by quantiles of a temperature field (k groups; cells with
+    no temperature, e.g. solid ones, in group -1)."""
+    t = np.asarray(ttra)
+    g = np.full(t.shape, -1, dtype=np.int64)
+    ok = t > 0
+    if ok.any():
+        edges = np.quantile(t[ok], np.linspace(0, 1, k + 1)[1:-1])
+        g[ok] = np.searchsorted(edges, t[ok], side="right")
+    names = [f"Ttra quantile {i + 1}/{k}" for i in range(k)]
+    return g, names
+
+
+def compare_windows(spec, plain, learned, replicate=None):
+    """The learned_vs_plain report.  plain and learned: run_window results
+    from the same developed state (the speed comparison); replicate: a
+    run_window of the learned selection from an independently seeded run of
+    the same development, the per-cell count and field comparisons (which
+    need independent runs) use it when given."""
+    del spec
+    rp, rl = arm_rates(plain), arm_rates(learned)
+    res = {"window_steps": plain["steps"], "plain": rp, "learned": rl,
+           "ratio_collisions_per_s": rl["collisions_per_s"] / rp["collisions_per_s"],
+           "ratio_particle_steps_per_s": rl["particle_steps_per_s"] / rp["particle_steps_per_s"],
+           "candidate_reduction": 1.0 - rl["candidates_per_collision"] / rp["candidates_per_collision"],
+           "total_collision_error_same_state": learned["collisions"] / plain["collisions"] - 1.0}
+    other = replicate if replicate is not None else learned
+    tp = plain.get("Ttra")
+    groups, names = temperature_groups(tp) if tp is not None else (None, None)
+    res["per_cell_counts"] = per_cell_count_test(plain["nColls"], other["nColls"], groups, names)
+    res["per_cell_counts"]["runs"] = "independent seeds" if replicate is not None else "same state"
+    res["fields_in_se"] = {k: batch_mean_z(plain["batches"][k], other["batches"][k])
+                           for k in plain["batches"] if k in other["batches"]}
+    res["fields_in_se"]["block_cells"] = plain["blk"] ** 3
     return res
+
+
+def train_default(scale=1, seeds=range(5), rows=5_000_000, train_steps=20000, batch=65536, tau=0.95,
+                  coverage=0.99, log=None):
+    """The learned maximum of the benchmark: rows recorded from plain runs of
+    the heat bath (the relaxation from 10^4 K) and the Mach-10 channel
+    (developing and developed flow) at the given seeds, then Adam on the GPU.
+    Returns (model, margin, description)."""
+    t0 = time.time()
+    half = rows // 2
+    Xa, Ya = collect(lambda sd: S.config1(seed=sd), seeds, [10, 30, 60, 100, 200, 400],
+                     keep_per_record=half // (6 * len(seeds)) + 1, rng_seed=1, log=log)
+    Xb, Yb = collect(lambda sd: S.config2(seed=sd, scale=scale), seeds, [200, 400, 600],
+                     keep_per_record=half // (3 * len(seeds)) + 1, rng_seed=2, log=log)
+    X = np.concatenate([Xa, Xb])
+    Y = np.concatenate([Ya, Yb])
+    t1 = time.time()
+    model, loss = train(X, Y, train_steps, batch, 1e-3, seed=0, tau=tau)
+    t2 = time.time()
+    margin = calibrate(model, X, Y, coverage) if tau == 0 else 0.0
+    desc = {"rows": int(len(Y)), "seeds": list(seeds), "loss": "squared error" if tau == 0 else f"pinball {tau}",
+            "train_steps": train_steps, "batch": batch, "lr": 1e-3, "loss_first": float(loss[0]),
+            "loss_last": float(np.mean(loss[-100:])), "margin": margin,
+            "seconds": {"collect": round(t1 - t0, 2), "train": round(t2 - t1, 2)}}
+    return model, margin, desc
+
+
+def evaluate(spec, spec_replicate, model, margin, every, develop_steps, window, batches=8, log=None):
+    """Plain and learned from the same developed state, and the learned run
+    of an independently seeded development, over `window` steps each."""
+    p = develop(spec, develop_steps)
+    lr = develop(spec, develop_steps)
+    lr.set_learned(model, every, margin)
+    wp = run_window(p, window, batches)
+    wl = run_window(lr, window, batches)
+    p.close()
+    lr.close()
+    rep = None
+    if spec_replicate is not None:
+        l2 = develop(spec_replicate, develop_steps)
+        l2.set_learned(model, every, margin)
+        rep = run_window(l2, window, batches)
+        l2.close()
+    return compare_windows(spec, wp, wl, rep)
 
 
 def main():
@@ -195,7 +335,7 @@ def main():
     ap.add_argument("--develop", type=int, default=600)
     ap.add_argument("--every", type=int, default=50)
     ap.add_argument("--coverage", type=float, default=0.99)
-    ap.add_argument("--taus", default="0", help="comma-separated loss settings: 0 = squared error + "
+    ap.add_argument("--taus", default="0.95", help="comma-separated loss settings: 0 = squared error + "
                     "calibrated margin, (0,1) = pinball loss at that quantile")
     ap.add_argument("--scale", type=int, default=1, help="Mach-10 channel cells divided by scale per axis")
     args = ap.parse_args()
@@ -203,38 +343,18 @@ def main():
     def log(msg):
         print(msg, file=sys.stderr, flush=True)
 
-    t0 = time.time()
-    half = args.rows // 2
-    # heat bath (config 1): the relaxation from 10^4 K
-    Xa, Ya = collect(lambda sd: S.config1(seed=sd), range(5), [10, 30, 60, 100, 200, 400],
-                     keep_per_record=half // 30 + 1, rng_seed=1, log=log)
-    # Mach-10 channel (config 2): developing and developed flow
-    Xb, Yb = collect(lambda sd: S.config2(seed=sd, scale=args.scale), range(5), [200, 400, 600],
-                     keep_per_record=half // 15 + 1, rng_seed=2, log=log)
-    X = np.concatenate([Xa, Xb])
-    Y = np.concatenate([Ya, Yb])
-    t1 = time.time()
-    t_collect = t1 - t0
-    log(f"collected {len(Y)} rows in {t_collect:.1f} s")
     spec = S.config2(seed=11, scale=args.scale)
-    plain = _run(spec, args.develop, args.eval_steps)
+    rep = S.config2(seed=12, scale=args.scale)
     for tau in [float(v) for v in args.taus.split(",")]:
-        t1 = time.time()
-        model, loss = train(X, Y, args.train_steps, args.batch, 1e-3, seed=0, tau=tau)
-        t2 = time.time()
-        log(f"tau {tau}: trained {args.train_steps} steps in {t2 - t1:.1f} s: loss {loss[0]:.4f} -> {loss[-1]:.4f}")
-        margin = calibrate(model, X, Y, args.coverage) if tau == 0 else 0.0
-        res = compare(spec, args.develop, args.eval_steps, model, args.every, margin, plain=plain)
-        t3 = time.time()
-        line = {"workload": "learned (sigma_T c_R)max, Mach-10 N2 channel", "rows": int(len(Y)),
-                "loss": "squared error" if tau == 0 else f"pinball {tau}",
-                "train_steps": args.train_steps, "batch": args.batch, "loss_first": float(loss[0]),
-                "loss_last": float(np.mean(loss[-100:])), "margin": margin,
-                "coverage": args.coverage if tau == 0 else tau,
-                "every": args.every, "eval_steps": args.eval_steps, "develop_steps": args.develop,
-                "scale": args.scale,
-                "seconds": {"collect": t_collect, "train": t2 - t1, "evaluate": t3 - t2}, **res}
+        t0 = time.time()
+        model, margin, desc = train_default(args.scale, range(5), args.rows, args.train_steps, args.batch, tau,
+                                            args.coverage, log)
+        res = evaluate(spec, rep, model, margin, args.every, args.develop, args.eval_steps)
+        line = {"workload": "learned (sigma_T c_R)max, Mach-10 N2 channel", "model": desc, "every": args.every,
+                "develop_steps": args.develop, "scale": args.scale, "seconds": round(time.time() - t0, 1),
+                **res}
         print(json.dumps(line), flush=True)
+        model.close()
 
 
 if __name__ == "__main__":

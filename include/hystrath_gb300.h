@@ -248,6 +248,29 @@ int dsmc_run_phases(dsmc_handle* h, unsigned phases);
 int dsmc_evolve_timed(dsmc_handle* h, long long n_steps, double* total_ms);
 int dsmc_evolve_profiled(dsmc_handle* h, long long n_steps, double* phase_ms, double* total_ms);
 
+/* The same with events between the step's kernel groups: group_ms[k] (k <
+ * n_groups <= DSMC_KGROUP_COUNT) receives the summed time of group k over the
+ * n steps.  No counterpart in the reference (a profiling aid). */
+enum {
+    DSMC_KGROUP_ZERO = 0,      /* step counters reset */
+    DSMC_KGROUP_INFLOW,        /* freestream inflow (count, scan, fill, commit) */
+    DSMC_KGROUP_MOVE,          /* k_move (fast path) + k_move_slow (boundary path) */
+    DSMC_KGROUP_SAMPLE,        /* sample commit of the fixed-point sums */
+    DSMC_KGROUP_SCAN,          /* occupancy scan */
+    DSMC_KGROUP_SCATTER,       /* k_scatter_index: a slot per parcel */
+    DSMC_KGROUP_GATHER,        /* k_gather: the records into cell order */
+    DSMC_KGROUP_FINISH,        /* sort bookkeeping */
+    DSMC_KGROUP_LEARNED,       /* learned maximum: features and inference */
+    DSMC_KGROUP_SELECT,        /* candidate counts, work list, heavy-cell ordering */
+    DSMC_KGROUP_HEAVY,         /* collisions of heavy cells */
+    DSMC_KGROUP_LIGHT,         /* collisions of light cells */
+    DSMC_KGROUP_PENDING,       /* marks the post-collision state for sampling */
+    DSMC_KGROUP_END,           /* step bookkeeping */
+    DSMC_KGROUP_COUNT
+};
+int dsmc_evolve_kernel_profile(dsmc_handle* h, long long n_steps, double* group_ms, int n_groups,
+                               double* total_ms);
+
 /* Replace the particle set.  pos and U are n x 3 interleaved; vib may be NULL;
  * ids must be unique.  Particles are placed in their cells and sorted. */
 int dsmc_set_particles(dsmc_handle* h, long long n, const double* pos, const double* U,

@@ -208,6 +208,7 @@ struct Oracle {
     double obLo[DSMC_MAX_OBSTACLES][3], obHi[DSMC_MAX_OBSTACLES][3];
 
     std::vector<Parcel> P;
+    std::vector<Parcel> Pbuf;                   // the sort's destination, swapped with P
     std::vector<int> cellStart, cellCount;      // occupancy after the last sort
     std::vector<double> sigmaTcRMax, remainder;
     std::vector<double> acc;                    // [C][nAcc]
@@ -887,21 +888,41 @@ struct Oracle {
     }
 
     // buildCellOccupancy: parcels grouped by cell, ordered by id inside a cell.
+    // Parallel counting sort: cell counts with atomics, a prefix over cells,
+    // slots taken with atomics (in any order), then every cell's parcels
+    // sorted by id, which makes the result independent of the slot order.
     void sort() {
-        std::vector<Parcel> kept;
-        kept.reserve(P.size());
+        const long long N = (long long)P.size();
         long long del = 0;
-        for (const Parcel& p : P) {
-            if (p.cell >= 0) kept.push_back(p); else ++del;
+        std::fill(cellCount.begin(), cellCount.end(), 0);
+        int* cnt = cellCount.data();
+#pragma omp parallel for schedule(static) reduction(+ : del) num_threads(nThreads)
+        for (long long i = 0; i < N; ++i) {
+            const int c = P[i].cell;
+            if (c < 0) { ++del; continue; }
+#pragma omp atomic
+            cnt[c]++;
         }
         deletedLast = del;
-        std::fill(cellCount.begin(), cellCount.end(), 0);
-        for (const Parcel& p : kept) cellCount[p.cell]++;
         long long s = 0;
         for (long long c = 0; c < C; ++c) { cellStart[c] = (int)s; s += cellCount[c]; }
-        std::vector<Parcel> out(kept.size());
+        // the other buffer keeps its capacity from step to step, with room
+        // for the next steps' inflow, so neither the sort nor the inflow's
+        // append reallocates (or zero-fills) the parcel array every step
+        std::vector<Parcel>& out = Pbuf;
+        if (out.capacity() < (size_t)s) out.reserve((size_t)s + (size_t)s / 8 + 65536);
+        out.resize((size_t)s);
         std::vector<int> cur(cellStart.begin(), cellStart.end());
-        for (const Parcel& p : kept) out[cur[p.cell]++] = p;
+        int* cp = cur.data();
+#pragma omp parallel for schedule(static) num_threads(nThreads)
+        for (long long i = 0; i < N; ++i) {
+            const int c = P[i].cell;
+            if (c < 0) continue;
+            int q;
+#pragma omp atomic capture
+            q = cp[c]++;
+            out[q] = P[i];
+        }
 #pragma omp parallel for schedule(dynamic, 4096) num_threads(nThreads)
         for (long long c = 0; c < C; ++c) {
             std::sort(out.begin() + cellStart[c], out.begin() + cellStart[c] + cellCount[c],
@@ -1340,6 +1361,8 @@ oracle_handle* oracle_create(const dsmc_case_spec* spec, int n_threads) {
 }
 
 void oracle_destroy(oracle_handle* h) { delete h; }
+
+void oracle_set_threads(oracle_handle* h, int n_threads) { h->o.nThreads = n_threads > 0 ? n_threads : 1; }
 
 int oracle_initialise(oracle_handle* h) {
     h->o.initialise();

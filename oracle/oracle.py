@@ -33,6 +33,7 @@ def lib() -> C.CDLL:
         L.oracle_create.restype = vp
         L.oracle_create.argtypes = [C.POINTER(S.CaseSpec), C.c_int]
         L.oracle_destroy.argtypes = [vp]
+        L.oracle_set_threads.argtypes = [vp, C.c_int]
         for f in ("oracle_initialise",):
             getattr(L, f).argtypes = [vp]
         L.oracle_run_phases.argtypes = [vp, C.c_uint]
@@ -89,6 +90,9 @@ class OracleCloud:
     def _chk(self, rc):
         if rc != 0:
             raise RuntimeError(f"oracle status {rc}")
+
+    def set_threads(self, threads: int):
+        lib().oracle_set_threads(self.h, int(threads))
 
     def initialise(self):
         self._chk(lib().oracle_initialise(self.h))
