@@ -329,6 +329,8 @@ def gpu_arm(args, rank, world, local):
         lg = learn.develop(s, args.develop)
         lg.set_learned(model, args.learn_every, margin)
         lg.evolve(args.warmup)
+        # the selection audit (per-cell expected collision shortfall) in the
+        # evaluation windows; switched on after the timed steps
     c0 = g.counts()
 
     if dist:
@@ -350,15 +352,20 @@ def gpu_arm(args, rank, world, local):
         ms_l = lg.evolve_timed(args.steps)
         cl1 = lg.counts()
         log("evaluation windows")
+        for x in (g, lg):
+            x.set_selection_audit(True)
         wp = learn.run_window(g, args.eval_steps, args.eval_batches)
         wl = learn.run_window(lg, args.eval_steps, args.eval_batches)
+        for x in (g, lg):
+            x.set_selection_audit(False)
         _, kl = lg.evolve_kernel_profile(args.steps)
         lg.close()
         lg = None
-        # an independently seeded run of the same development, learned
+        # an independently seeded run of the same development, learned, its
+        # window starting at the same step as the other two
         rep = learn.develop(make_spec(args, SEED + 7919 + rank), args.develop)
         rep.set_learned(model, args.learn_every, margin)
-        rep.evolve(args.warmup)
+        rep.evolve(args.warmup + args.steps)
         wr = learn.run_window(rep, args.eval_steps, args.eval_batches)
         rep.close()
         lvp = learn.compare_windows(s, wp, wl, wr)

@@ -42,6 +42,7 @@ struct dsmc_handle {
     StepBuffers B{};
     Parcels buf[2]{};
     double* faceBuf = nullptr;   // face tracker sums, kept while tracking is off
+    double2* auditBuf = nullptr; // selection audit sums, kept while the audit is off
     long long faceStep0 = 0;     // step count when the face sums were last cleared
     struct FluxSurface {
         dsmc_flux_surface d;
@@ -386,6 +387,10 @@ void fill_case_dev(dsmc_handle* h) {
         }
     }
     cs.nAcc = s.n_species * SACC + CACC;
+    cs.maxRejection = MAX_REJECTION;
+    cs.maxCrossings = MAX_CROSSINGS;
+    cs.maxCellParcels = MAX_ORDERED_CELL;
+    cs.capacityLimit = 1LL << 62;
 }
 
 Parcels& cur_soa(dsmc_handle* h) { return h->buf[h->cur]; }
@@ -395,13 +400,19 @@ int check_device_error(dsmc_handle* h) {
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
     const unsigned e = h->ctrHost->err;
     if (e) {
+        // reported once: the bits are cleared, and the handle steps on (the
+        // step that set them is not undone)
+        h->ctrHost->err = 0;
+        CUDA_TRY(h, cudaMemcpy(&h->B.ctr->err, &h->ctrHost->err, sizeof(unsigned), cudaMemcpyHostToDevice));
         std::string m = "device error bits 0x" + std::to_string(e) + ":";
         if (e & ERRB_CROSSINGS) m += " face-crossing cap reached;";
         if (e & ERRB_REJECTION) m += " acceptance-rejection cap reached;";
         if (e & ERRB_CAPACITY) m += " particle capacity exceeded;";
         if (e & ERRB_BOUNDS) m += " index out of bounds;";
         if (e & ERRB_PATCH) m += " boundary face without a patch;";
-        if (e & ERRB_DENSE) m += " a cell above 16384 parcels or 2^24 candidates (its collisions were skipped);";
+        if (e & ERRB_DENSE)
+            m += " a cell above " + std::to_string(h->cs.maxCellParcels) +
+                 " parcels or 2^24 candidates (its collisions were skipped);";
         if (e & ERRB_IDS) m += " parcel id space exhausted (more than 2^32 parcels inserted since the start);";
         return fail(h, e & ERRB_CAPACITY ? DSMC_ERR_CAPACITY : DSMC_ERR_DEVICE, m);
     }
@@ -1043,15 +1054,51 @@ int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n
         CUDA_TRY(h, cudaMemcpy(out, h->B.acc, sizeof(double) * n, cudaMemcpyDeviceToHost));
         return DSMC_OK;
     }
+    if (nm == "selectionAudit") {
+        if (n != 2 * C) return fail(h, DSMC_ERR_INVALID, "n must equal 2 x the number of cells");
+        if (!h->B.audit) return fail(h, DSMC_ERR_INVALID, "the selection audit is off (dsmc_set_selection_audit)");
+        CUDA_TRY(h, cudaMemcpy(out, h->B.audit, sizeof(double2) * C, cudaMemcpyDeviceToHost));
+        return DSMC_OK;
+    }
+    if (nm == "inflowAccumulator") {
+        const int ns = h->spec.n_species;
+        if (n != h->cs.nBFaces * ns) return fail(h, DSMC_ERR_INVALID, "n must equal boundary faces x species");
+        std::vector<double> acc((size_t)h->B.nInflowFaces * ns);
+        std::vector<long long> face((size_t)h->B.nInflowFaces);
+        if (!acc.empty()) {
+            CUDA_TRY(h, cudaMemcpy(acc.data(), h->B.inflowAcc, sizeof(double) * acc.size(), cudaMemcpyDeviceToHost));
+            CUDA_TRY(h, cudaMemcpy(face.data(), h->B.inflowFace, sizeof(long long) * face.size(),
+                                   cudaMemcpyDeviceToHost));
+        }
+        double* o = static_cast<double*>(out);
+        std::fill(o, o + n, 0.0);
+        for (size_t f = 0; f < face.size(); ++f)
+            for (int m = 0; m < ns; ++m) o[face[f] * ns + m] = acc[f * ns + m];
+        return DSMC_OK;
+    }
     return fail(h, DSMC_ERR_INVALID, "unknown cell array " + nm +
-                                         "; valid: count start sigmaTcRMax collisionSelectionRemainder accumulators");
+                                         "; valid: count start sigmaTcRMax collisionSelectionRemainder accumulators "
+                                         "inflowAccumulator selectionAudit");
 }
 
 int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long long n) {
     const std::string nm(name);
     const long long C = h->cs.C;
-    if (n != C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (nm == "inflowAccumulator") {
+        const int ns = h->spec.n_species;
+        if (n != h->cs.nBFaces * ns) return fail(h, DSMC_ERR_INVALID, "n must equal boundary faces x species");
+        std::vector<long long> face((size_t)h->B.nInflowFaces);
+        if (face.empty()) return DSMC_OK;
+        CUDA_TRY(h, cudaMemcpy(face.data(), h->B.inflowFace, sizeof(long long) * face.size(), cudaMemcpyDeviceToHost));
+        const double* v = static_cast<const double*>(in);
+        std::vector<double> acc(face.size() * ns);
+        for (size_t f = 0; f < face.size(); ++f)
+            for (int m = 0; m < ns; ++m) acc[f * ns + m] = v[face[f] * ns + m];
+        CUDA_TRY(h, cudaMemcpy(h->B.inflowAcc, acc.data(), sizeof(double) * acc.size(), cudaMemcpyHostToDevice));
+        return DSMC_OK;
+    }
+    if (n != C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
     if (nm == "sigmaTcRMax" || nm == "collisionSelectionRemainder") {
         if (nm == "sigmaTcRMax") h->smaxSet = true;
         CUDA_TRY(h, cudaMemcpy(nm == "sigmaTcRMax" ? h->B.smax : h->B.rem, in, sizeof(double) * C,
@@ -1149,6 +1196,7 @@ int dsmc_reset_sampling(dsmc_handle* h) {
     CUDA_TRY(h, cudaMemset(h->B.acc, 0, sizeof(double) * h->cs.C * h->cs.nAcc));
     CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
     CUDA_TRY(h, cudaMemset(h->B.wall, 0, sizeof(double) * h->cs.nBFaces * W_N));
+    if (h->B.audit) CUDA_TRY(h, cudaMemset(h->B.audit, 0, sizeof(double2) * h->cs.C));
     if (h->cs.faceFlux)
         CUDA_TRY(h, cudaMemset(h->cs.faceFlux, 0, sizeof(double) * 2 * h->cs.nSpecies * h->cs.nFacesAll));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
@@ -1357,6 +1405,37 @@ int dsmc_learn_record(dsmc_handle* h, long long max_rows, float* X, float* Y, lo
     cudaFree(dn);
     if (e != cudaSuccess) return fail(h, DSMC_ERR_CUDA, std::string("dsmc_learn_record: ") + cudaGetErrorString(e));
     if (n_out) *n_out = m;
+    return DSMC_OK;
+}
+
+// ------------------------------------------------------- selection audit
+int dsmc_set_selection_audit(dsmc_handle* h, int on) {
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    if (on && !h->auditBuf) {
+        int rc = dalloc(h, &h->auditBuf, h->cs.C);
+        if (rc) return rc;
+    }
+    if (on) CUDA_TRY(h, cudaMemset(h->auditBuf, 0, sizeof(double2) * h->cs.C));
+    h->B.audit = on ? h->auditBuf : nullptr;
+    drop_graphs(h);   // the collision kernels take the buffer as a parameter
+    return DSMC_OK;
+}
+
+// ------------------------------------------------------- loop caps
+int dsmc_set_limits(dsmc_handle* h, int max_rejection, int max_crossings, int max_cell_parcels,
+                    long long capacity) {
+    if (max_rejection < 0 || max_crossings < 0 || max_cell_parcels < 0 || capacity < 0)
+        return fail(h, DSMC_ERR_INVALID, "limits must not be negative");
+    if (max_rejection > MAX_REJECTION || max_crossings > MAX_CROSSINGS || max_cell_parcels > MAX_ORDERED_CELL)
+        return fail(h, DSMC_ERR_INVALID, "limits can only be lowered (at most " + std::to_string(MAX_REJECTION) +
+                                             " draws, " + std::to_string(MAX_CROSSINGS) + " crossings, " +
+                                             std::to_string(MAX_ORDERED_CELL) + " parcels per cell)");
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->cs.maxRejection = max_rejection ? max_rejection : MAX_REJECTION;
+    h->cs.maxCrossings = max_crossings ? max_crossings : MAX_CROSSINGS;
+    h->cs.maxCellParcels = max_cell_parcels ? max_cell_parcels : MAX_ORDERED_CELL;
+    h->cs.capacityLimit = capacity ? capacity : (1LL << 62);
+    drop_graphs(h);   // the step graphs hold the case constants
     return DSMC_OK;
 }
 

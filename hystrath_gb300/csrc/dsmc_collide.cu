@@ -72,7 +72,7 @@ __device__ __forceinline__ int post_vib(const CaseDev& cs, Rng& r, int vib, int 
     }
     if (invZv > r.u01()) {
         const float ex = (float)(1.5 - omega);
-        for (int it = 0; it < MAX_REJECTION; ++it) {
+        for (int it = 0; it < cs.maxRejection; ++it) {
             const int iDash = r.label(0, iMax, err);
             const float base = (float)(1.0 - (iDash * s.kThetaV) / Ec);
             const float func = powf(base > 0.0f ? base : 0.0f, ex);
@@ -380,11 +380,11 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
     }
     tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
                                                                 B.perm, B.subs, learned, B.smaxSel, B.useR,
-                                                                B.obsMax);
+                                                                B.obsMax, B.audit);
     if (marks) cudaEventRecord(marks[1], st);
     const int L = B.cfg.lightCells;
     tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * sizeof(tile::LightPicks), st>>>(
-        cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.obsMax);
+        cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.obsMax, B.audit);
 }
 
 void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,

@@ -26,6 +26,7 @@ constexpr double GREAT = 1.0e15;
 // sets an error bit that the host turns into DSMC_ERR_DEVICE.
 constexpr int MAX_CROSSINGS = 64;
 constexpr int MAX_REJECTION = 100000;
+constexpr int MAX_ORDERED_CELL = 16384;   // parcels of the largest cell the collision kernels order
 constexpr int ZV_TAB = 512;     // iMax values tabulated for 1/Zv
 
 // Error bits of the device error word.
@@ -125,6 +126,14 @@ struct CaseDev {
     long long nBFaces;
     int nAcc;           // doubles per cell of sampling accumulators
     int hasWallMeasure;
+    // caps of the loops the reference runs without bound and of the cell size
+    // the collision kernels order (MAX_REJECTION, MAX_CROSSINGS, ORDER_MAX_N
+    // unless lowered by dsmc_set_limits), and the parcel capacity the inflow
+    // may fill (the allocation unless lowered)
+    int maxRejection;
+    int maxCrossings;
+    int maxCellParcels;
+    long long capacityLimit;
     // 1/Zv of the variable-Zv model by quantised collision level iMax
     // (dsmcCloud.C:1420-1490 depends on iMax, species and pair omega only):
     // invZvTab[((p * DSMC_MAX_SPECIES + q) * ZV_TAB) + iMax]

@@ -61,6 +61,11 @@ struct StepBuffers {
     float* pred;              // [C] predicted (sigma_T c_R)max
     unsigned char* useR;      // [C] 1: the cell has fallen back to the running maximum
     double* smaxSel;          // [C] the maximum this step's selection used
+    // selection audit (null when off): per cell, summed over candidates,
+    // x = sigma_T c_R / max (the expected acceptances) and
+    // y = max(0, sigma_T c_R / max - 1) (the expected collisions lost
+    // because the maximum used was below the product)
+    double2* audit;
     int* slowList;            // [capacity] parcels that take the boundary path this step
     int2* sortSrc;            // [capacity] (source index, cell word) of each destination slot of the sort
     // inflow

@@ -222,7 +222,7 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
     bool done = false;
     for (int it = 0; !done; ++it) {
         if (!(tr > ROOTVSMALL)) break;
-        if (it >= MAX_CROSSINGS) { *err |= ERRB_CROSSINGS; break; }
+        if (it >= cs.maxCrossings) { *err |= ERRB_CROSSINGS; break; }
         // tracking velocity: none along an empty (reduced-D) axis, whose
         // coordinate is held at the mesh centre; U keeps all three components
         double V[3] = {U[0], U[1], U[2]};
@@ -1076,7 +1076,7 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
                 if (uNormal < 0.0) Pr = -1;
                 else Pr = 2.0 * uNormal / coeffA * exp(coeffB - uth * uth);
                 if (!(Pr < r.u01())) break;
-                if (++it >= MAX_REJECTION) { err |= ERRB_REJECTION; break; }
+                if (++it >= cs.maxRejection) { err |= ERRB_REJECTION; break; }
             }
         } else {
             uNormal = sqrt(-log(r.u01()));
@@ -1361,7 +1361,8 @@ void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B,
     const int grid = (nt + 255) / 256;
     k_inflow_count<<<grid, 256, 0, st>>>(cs, B.nInflowFaces, B.inflowFace, B.inflowTerm, B.inflowAcc,
                                          B.inflowCount, B.ctr);
-    k_inflow_scan<<<1, 1024, 0, st>>>(B.inflowCount, nt, B.inflowOff, B.ctr, B.capacity);
+    k_inflow_scan<<<1, 1024, 0, st>>>(B.inflowCount, nt, B.inflowOff, B.ctr,
+                                      cs.capacityLimit < B.capacity ? cs.capacityLimit : B.capacity);
     k_inflow_fill<<<grid_for(B.capacity, 256, 8), 256, 0, st>>>(cs, in, B.nInflowFaces, B.inflowFace,
                                                                 B.inflowSide, B.inflowCell, B.bfPatch,
                                                                 B.inflowOff, s, B.ctr);

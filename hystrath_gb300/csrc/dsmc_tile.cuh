@@ -52,7 +52,7 @@ constexpr int WARPS = 4;             // warps per block
 constexpr int LIGHT_N = 64;          // light cells: at most this many parcels
 constexpr int LIGHT_CAND = 16;       //   and fewer candidates than this
 constexpr int ORDER_WARP_N = 1024;   // cells up to this size are ordered by one warp
-constexpr int ORDER_MAX_N = 16384;   // cells up to this size are ordered by one block
+constexpr int ORDER_MAX_N = MAX_ORDERED_CELL;   // cells up to this size are ordered by one block
 constexpr int ORDER_BLOCK = 512;     // threads of the block that orders a large cell
 constexpr int NBUCKET = 8;           // candidate-count buckets per class
 constexpr int MAX_CAND = 1 << 24;    // candidates of one cell in one step
@@ -103,7 +103,7 @@ __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const do
             const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cell_volume(cs, c);
             const double whole = floor(sel);
             rem[c] = sel - whole;
-            if (n > ORDER_MAX_N || whole >= (double)MAX_CAND) err |= ERRB_DENSE;
+            if (n > cs.maxCellParcels || whole >= (double)MAX_CAND) err |= ERRB_DENSE;
             else nc = (int)whole;
         }
         ncCell[c] = nc;
@@ -376,9 +376,17 @@ __device__ __forceinline__ void draw_pair(Rng& r, int n, const uint4& so, int* p
 // against the maximum the candidate count was based on, and the collision.
 // run_candidate in two parts: the acceptance test (loads the pair, keeps
 // the step's largest product) and the collision of an accepted pair.
+// audit (selection audit on): the candidate's expected acceptance
+// sigma/max and the part of it above 1, which the test cannot honour
+__device__ __forceinline__ void audit_add(float2* au, double sigma, double smax0) {
+    const float a = (float)(sigma / smax0);
+    au->x += a;
+    au->y += fmaxf(a - 1.0f, 0.0f);
+}
+
 __device__ __forceinline__ bool test_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
                                                long long gQ, double smax0, double* stepMax, Rec* P, Rec* Q,
-                                               double* cr2) {
+                                               double* cr2, float2* au) {
     *P = ld_rec(s.r + gP);
     *Q = ld_rec(s.r + gQ);
     const int tP = sv_species(P->sv), tQ = sv_species(Q->sv);
@@ -387,6 +395,7 @@ __device__ __forceinline__ bool test_candidate(const CaseDev& cs, const Parcels&
     *cr2 = d0 * d0 + d1 * d1 + d2 * d2;
     const double sigma = sigma_cr(pr, *cr2);
     if (sigma > *stepMax) *stepMax = sigma;
+    if (au) audit_add(au, sigma, smax0);
     return sigma > r.u01() * smax0;
 }
 
@@ -418,7 +427,7 @@ __device__ __forceinline__ void collide_candidate(const CaseDev& cs, const Parce
 
 __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
                                               long long gQ, double smax0, double* stepMax, double* collSep,
-                                              unsigned* err) {
+                                              unsigned* err, float2* au = nullptr) {
     Rec P = ld_rec(s.r + gP), Q = ld_rec(s.r + gQ);
     const int tP = sv_species(P.sv), tQ = sv_species(Q.sv);
     const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
@@ -429,6 +438,7 @@ __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& 
     const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
     const double sigma = sigma_cr(pr, cr2);
     if (sigma > *stepMax) *stepMax = sigma;
+    if (au) audit_add(au, sigma, smax0);
     if (!(sigma > r.u01() * smax0)) return false;      // (sigma/smax0) > U with smax0 > 0
     o.eP = P.erot; o.eQ = Q.erot;
     o.vP = sv_vib(P.sv); o.vQ = sv_vib(Q.sv);
@@ -454,10 +464,17 @@ __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& 
 // training, and a learned cell whose prediction was exceeded falls back to
 // the running maximum until the next prediction.
 __device__ __forceinline__ void cell_epilogue(double* smax, long long c, double R, double smax0, double stepMax,
-                                              int learned, unsigned char* useR, float* obsMax) {
+                                              int learned, unsigned char* useR, float* obsMax, double2* audit,
+                                              float2 au) {
     if (stepMax > R) smax[c] = stepMax;
     obsMax[c] = (float)stepMax;
     if (learned && stepMax > smax0) useR[c] = 1;
+    if (audit) {
+        double2 v = audit[c];
+        v.x += (double)au.x;
+        v.y += (double)au.y;
+        audit[c] = v;
+    }
 }
 
 __device__ __forceinline__ uint32_t cand_tag(int k) { return (uint32_t)TAG_COLLIDE | ((uint32_t)k << 8); }
@@ -466,7 +483,8 @@ __device__ __forceinline__ uint32_t cand_tag(int k) { return (uint32_t)TAG_COLLI
 __global__ void __launch_bounds__(WARPS * 32)
 k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs,
-                int learned, const double* __restrict__ smaxSel, unsigned char* useR, float* obsMax) {
+                int learned, const double* __restrict__ smaxSel, unsigned char* useR, float* obsMax,
+                double2* audit) {
     const unsigned lane = lane_id();
     const uint32_t step = (uint32_t)ctr->step;
     const long long nHeavy = (long long)ctr->nHeavy;
@@ -485,6 +503,7 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
         const double smax0 = learned ? smaxSel[c] : R;
         double stepMax = 0.0, collSep = 0.0;
         unsigned coll = 0;
+        float2 au = make_float2(0.f, 0.f);
         for (int base = 0; base < nCand; base += 32) {
             const int k = base + (int)lane;
             Rng r(cs, (uint32_t)c, step, cand_tag(k));
@@ -507,7 +526,8 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
                     const int b = __shfl_sync(0xFFFFFFFFu, pQ, j);
                     if (j < (int)lane && (a == pP || a == pQ || b == pP || b == pQ)) ready = false;
                 }
-                if (ready && run_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &collSep, &err)) ++coll;
+                if (ready && run_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &collSep, &err,
+                                           audit ? &au : nullptr)) ++coll;
                 __syncwarp();
                 pend &= ~__ballot_sync(0xFFFFFFFFu, ready);
             }
@@ -517,9 +537,13 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
             collSep += __shfl_xor_sync(0xFFFFFFFFu, collSep, o);
             stepMax = fmax(stepMax, __shfl_xor_sync(0xFFFFFFFFu, stepMax, o));
             coll += __shfl_xor_sync(0xFFFFFFFFu, coll, o);
+            if (audit) {
+                au.x += __shfl_xor_sync(0xFFFFFFFFu, au.x, o);
+                au.y += __shfl_xor_sync(0xFFFFFFFFu, au.y, o);
+            }
         }
         if (lane == 0) {
-            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax);
+            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax, audit, au);
             if (coll) {
                 acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
                 acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
@@ -582,7 +606,7 @@ __device__ __forceinline__ int warp_argmin(uint32_t hA, bool vA, uint32_t hB, bo
 __global__ void __launch_bounds__(128, 4)
 k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, int learned, const double* __restrict__ smaxSel, unsigned char* useR,
-                float* obsMax) {
+                float* obsMax, double2* audit) {
     extern __shared__ __align__(16) unsigned char lightSmem[];
     LightPicks& pk = reinterpret_cast<LightPicks*>(lightSmem)[threadIdx.x >> 5];
     const int lane = (int)(threadIdx.x & 31u);
@@ -678,6 +702,7 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
             const double smax0 = learned ? smaxSel[c] : R;
             double stepMax = 0.0, collSep = 0.0;
             unsigned coll = 0;
+            float2 au = make_float2(0.f, 0.f);
             // The lane tests candidates until one is accepted, then collides
             // it: lanes that reach an accepted candidate in the same pass run
             // the FP64 exchange together, whatever the rejections before it.
@@ -698,7 +723,7 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
                     }
                     gP = off + jP;
                     gQ = off + jQ;
-                    if (test_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &P, &Q, &cr2)) {
+                    if (test_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &P, &Q, &cr2, audit ? &au : nullptr)) {
                         accepted = true;
                         break;
                     }
@@ -708,7 +733,7 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
                     ++coll;
                 }
             }
-            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax);
+            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax, audit, au);
             if (coll) {
                 acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
                 acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
@@ -740,7 +765,7 @@ __global__ void k_sbt_select(CaseDev cs, const int* __restrict__ start, Counters
         const int n = start[c + 1] - start[c];
         int nt = 0;
         if (n > 1) {
-            if (n > ORDER_MAX_N) err |= ERRB_DENSE;
+            if (n > cs.maxCellParcels) err |= ERRB_DENSE;
             else nt = n - 1;
         }
         ncCell[c] = nt;

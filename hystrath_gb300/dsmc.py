@@ -38,6 +38,8 @@ def _load() -> C.CDLL:
     L.dsmc_run_phases.argtypes = [vp, C.c_uint]
     L.dsmc_evolve_timed.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double)]
     L.dsmc_evolve_profiled.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.dsmc_set_selection_audit.argtypes = [vp, C.c_int]
+    L.dsmc_set_limits.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_longlong]
     L.dsmc_evolve_kernel_profile.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double), C.c_int,
                                              C.POINTER(C.c_double)]
     L.dsmc_set_particles.argtypes = [vp, C.c_longlong, vp, vp, vp, vp, vp, vp]
@@ -211,6 +213,19 @@ class DsmcCloud:
         self._chk(lib().dsmc_evolve_kernel_profile(self.h, n, g, k, C.byref(tot)))
         return tot.value, dict(zip(self.KERNEL_GROUPS, list(g)))
 
+    def set_selection_audit(self, on: bool = True):
+        """Per-cell sums of sigma c_R / max and of its part above 1 over the
+        candidates (cell_array("selectionAudit")): the expected collision
+        shortfall of a maximum below the product."""
+        self._chk(lib().dsmc_set_selection_audit(self.h, 1 if on else 0))
+
+    def set_limits(self, max_rejection: int = 0, max_crossings: int = 0, max_cell_parcels: int = 0,
+                   capacity: int = 0):
+        """Lower the device loop caps, the ordered cell size and the inflow
+        capacity (0: default); a cap reached is reported as a status."""
+        self._chk(lib().dsmc_set_limits(self.h, int(max_rejection), int(max_crossings), int(max_cell_parcels),
+                                        int(capacity)))
+
     def run_phases(self, phases: int):
         self._chk(lib().dsmc_run_phases(self.h, phases))
 
@@ -249,6 +264,10 @@ class DsmcCloud:
         elif name == "accumulators":
             n_acc = self.spec.n_species * 7 + 2
             a = np.empty(self.n_cells * n_acc)
+        elif name == "inflowAccumulator":
+            a = np.empty(lib().dsmc_n_boundary_faces(self.h) * self.spec.n_species)
+        elif name == "selectionAudit":
+            a = np.empty((self.n_cells, 2))
         else:
             a = np.empty(self.n_cells)
         self._chk(lib().dsmc_get_cell_array(self.h, name.encode(), _p(a), a.size))

@@ -125,24 +125,29 @@ def develop(spec, steps):
 def run_window(g, steps, batches=8, fields=FIELDS, blk=8):
     """`steps` graph-launched steps in `batches` equal batches (sampling reset
     at the start of each): device time, collision and candidate counts, the
-    parcel counts at both ends, the per-cell collision counts summed over the
-    batches, the per-cell mean of Ttra over the batches, and every batch's
-    time-averaged fields as means over blocks of blk^3 cells (batch means)."""
+    parcel counts at both ends, every batch's per-cell collision counts, the
+    per-cell mean of Ttra over the batches, every batch's time-averaged
+    fields as means over blocks of blk^3 cells (batch means), and the
+    selection audit summed over the window when it is on."""
     n = list(g.spec.n_cells)
     per = max(1, steps // batches)
     c0 = g.counts()
-    out = {"steps": per * batches, "ms": 0.0, "n_start": int(c0.n_particles), "nColls": None, "Ttra": None,
-           "blk": blk, "batches": {k: [] for k in fields}}
+    out = {"steps": per * batches, "ms": 0.0, "n_start": int(c0.n_particles), "nColls": [], "Ttra": None,
+           "blk": blk, "batches": {k: [] for k in fields}, "audit": None}
     for _ in range(batches):
         g.reset_sampling()
         out["ms"] += g.evolve_timed(per)
-        nc = g.field("nColls")
-        out["nColls"] = nc if out["nColls"] is None else out["nColls"] + nc
+        out["nColls"].append(g.field("nColls").astype(np.float32))
         for k in fields:
             f = g.field(k)
             if k == "Ttra":
                 out["Ttra"] = f / batches if out["Ttra"] is None else out["Ttra"] + f / batches
             out["batches"][k].append(_block_means(f, n, blk))
+        try:
+            a = g.cell_array("selectionAudit")
+            out["audit"] = a if out["audit"] is None else out["audit"] + a
+        except Exception:
+            pass
     c1 = g.counts()
     out["n_end"] = int(c1.n_particles)
     out["collisions"] = int(c1.collisions_total - c0.collisions_total)
@@ -160,49 +165,78 @@ def arm_rates(w):
             "collisions": w["collisions"], "candidates": w["candidates"]}
 
 
-def per_cell_count_test(a, b, groups=None, group_names=None):
-    """Per-cell collision counts of two independent runs of the same flow.
+def per_cell_count_test(batches_a, batches_b, groups=None, group_names=None):
+    """Per-cell collision counts of two independent runs of the same flow,
+    each given as per-batch counts (batches x cells).
 
-    Given a cell's total s = a + b, a equal mean in both runs makes a
-    Binomial(s, 1/2): (a - b)^2 / s then has mean 1 and variance 2 - 2/s
-    exactly.  X = sum over cells of (a - b)^2 / s tests for any per-cell
-    difference (z = (X - n) / sd).  A relative bias r_c of cell c adds about
-    r_c^2 mu_c / 2 to X, so the rms per-cell bias weighted by counts is
-    sqrt(2 (X - n) / sum(a)), with a one-sided 95% upper bound from
-    X - n + 1.645 sd.  groups: an integer label per cell; each group's total
-    relative difference and its standard error are reported as well."""
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
-    s = a + b
-    m = s > 0
-    d = b[m] - a[m]
-    X = float(np.sum(d * d / s[m]))
+    NTC counts are not Poisson (the candidate remainder is carried from step
+    to step and a candidate is a Bernoulli trial of high probability: their
+    variance is about half their mean), so each cell's variance is taken from
+    its own batch-to-batch spread.  With d_c the difference of the two runs'
+    batch means and v_c its estimated variance, T = sum_c (d_c^2 - v_c) has
+    mean zero when every cell has the same expected count in both runs, and
+    T / sum_c m_c^2 estimates the mean square relative difference of the
+    per-cell counts (weighted by m_c^2, m_c the first run's batch mean); its
+    one-sided 95% upper bound uses the spread of d_c^2 - v_c over cells.
+    groups: an integer label per cell (-1: none); each group's total
+    relative difference with its standard error is reported as well."""
+    A = np.asarray(batches_a, dtype=np.float64)
+    B = np.asarray(batches_b, dtype=np.float64)
+    ka, kb = A.shape[0], B.shape[0]
+    ma, mb = A.mean(0), B.mean(0)
+    va, vb = A.var(0, ddof=1), B.var(0, ddof=1)
+    m = (ma + mb) > 0
+    d = mb[m] - ma[m]
+    v = va[m] / ka + vb[m] / kb
+    t = d * d - v
     n = int(m.sum())
-    var = float(np.sum(2.0 - 2.0 / s[m]))
-    sd = math.sqrt(max(var, 1e-300))
-    z = (X - n) / sd
-    tot_a = float(a.sum())
-    rms2 = 2.0 * (X - n) / max(tot_a, 1.0)
-    rms2_hi = 2.0 * (X - n + 1.645 * sd) / max(tot_a, 1.0)
-    res = {"cells": n, "statistic": X, "expected": float(n), "sd": sd, "z": z,
-           "p_value_two_sided": math.erfc(abs(z) / math.sqrt(2.0)),
-           "mean_count_per_cell": tot_a / max(n, 1),
-           "rms_rel_bias_estimate": math.sqrt(max(rms2, 0.0)),
-           "rms_rel_bias_upper95": math.sqrt(max(rms2_hi, 0.0)),
-           "total_rel_diff": float(b.sum() / max(tot_a, 1.0) - 1.0),
-           "total_rel_diff_se": math.sqrt(float(s.sum())) / max(tot_a, 1.0)}
+    T = float(t.sum())
+    sd = float(np.std(t) * math.sqrt(n)) if n > 1 else 1.0
+    # sum of m_c^2 with the sampling variance of m_c removed
+    w = float(np.sum(ma[m] ** 2 - va[m] / ka))
+    tot_a, tot_b = float(A.sum()), float(B.sum())
+    res = {"cells": n, "batches": [ka, kb], "statistic": T, "sd": sd, "z": T / sd if sd > 0 else 0.0,
+           "mean_count_per_cell_and_batch": float(ma[m].mean()) if n else 0.0,
+           "variance_over_mean": float(np.sum(va[m]) / max(np.sum(ma[m]), 1e-300)),
+           "rms_rel_diff_estimate": math.sqrt(max(T, 0.0) / w) if w > 0 else 0.0,
+           "rms_rel_diff_upper95": math.sqrt(max(T + 1.645 * sd, 0.0) / w) if w > 0 else 0.0,
+           "total_rel_diff": tot_b / max(tot_a, 1e-300) - 1.0}
+    # the totals' standard error from the batch totals
+    sa, sb = A.sum(1), B.sum(1)
+    res["total_rel_diff_se"] = math.sqrt(sa.var(ddof=1) / ka + sb.var(ddof=1) / kb) / max(sa.mean(), 1e-300)
     if groups is not None:
         gl = []
         for gi in np.unique(groups):
             if gi < 0:
                 continue   # cells without a label (no temperature: solid or empty)
             sel = groups == gi
-            ta, tb = float(a[sel].sum()), float(b[sel].sum())
-            if ta <= 0:
+            ga, gb = A[:, sel].sum(1), B[:, sel].sum(1)
+            if ga.sum() <= 0:
                 continue
+            se = math.sqrt(ga.var(ddof=1) / ka + gb.var(ddof=1) / kb) / ga.mean()
             gl.append({"group": group_names[int(gi)] if group_names else int(gi), "cells": int(sel.sum()),
-                       "rel_diff": tb / ta - 1.0, "se": math.sqrt(ta + tb) / ta})
+                       "rel_diff": gb.mean() / ga.mean() - 1.0, "se": se})
         res["groups"] = gl
+    return res
+
+
+def audit_summary(audit, min_expected=10.0):
+    """The selection audit of a run (cells x 2: summed acceptances
+    sigma/max and their part above 1): per cell the expected relative
+    shortfall of the collision count, y/x.  Cells with fewer than
+    min_expected expected collisions are left out of the per-cell figures
+    (the total includes them)."""
+    a = np.asarray(audit, dtype=np.float64)
+    x, y = a[:, 0], a[:, 1]
+    ok = x >= min_expected
+    r = y[ok] / x[ok]
+    res = {"expected_shortfall_total": float(y.sum() / max(x.sum(), 1e-300)), "cells": int(ok.sum()),
+           "min_expected_collisions": min_expected}
+    if r.size:
+        res.update({"cells_above_1pct": float(np.mean(r > 0.01)),
+                    "collisions_in_cells_above_1pct": float(x[ok][r > 0.01].sum() / x[ok].sum()),
+                    "p99": float(np.quantile(r, 0.99)), "p999": float(np.quantile(r, 0.999)),
+                    "max": float(r.max()), "mean": float(r.mean())})
     return res
 
 
@@ -275,6 +309,9 @@ def compare_windows(spec, plain, learned, replicate=None):
     groups, names = temperature_groups(tp) if tp is not None else (None, None)
     res["per_cell_counts"] = per_cell_count_test(plain["nColls"], other["nColls"], groups, names)
     res["per_cell_counts"]["runs"] = "independent seeds" if replicate is not None else "same state"
+    for name, w in (("plain", plain), ("learned", learned)):
+        if w.get("audit") is not None:
+            res.setdefault("selection_audit", {})[name] = audit_summary(w["audit"])
     res["fields_in_se"] = {k: batch_mean_z(plain["batches"][k], other["batches"][k])
                            for k in plain["batches"] if k in other["batches"]}
     res["fields_in_se"]["block_cells"] = plain["blk"] ** 3
@@ -312,12 +349,15 @@ def evaluate(spec, spec_replicate, model, margin, every, develop_steps, window, 
     p = develop(spec, develop_steps)
     lr = develop(spec, develop_steps)
     lr.set_learned(model, every, margin)
+    for g in (p, lr):
+        g.set_selection_audit(True)
     wp = run_window(p, window, batches)
     wl = run_window(lr, window, batches)
     p.close()
     lr.close()
     rep = None
     if spec_replicate is not None:
+        # the same development and window start as the other two
         l2 = develop(spec_replicate, develop_steps)
         l2.set_learned(model, every, margin)
         rep = run_window(l2, window, batches)

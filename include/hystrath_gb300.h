@@ -283,7 +283,13 @@ int dsmc_get_particles(dsmc_handle* h, long long capacity, long long* n, double*
                        double* erot, int* vib, int* species, unsigned* id, int* cell);
 
 /* Per-cell arrays: "count" (int, parcels per cell after the last sort),
- * "start" (int), "sigmaTcRMax", "collisionSelectionRemainder" (double). */
+ * "start" (int), "sigmaTcRMax", "collisionSelectionRemainder" (double); and
+ * per boundary face and species (n = dsmc_n_boundary_faces x species, face
+ * major) "inflowAccumulator" (double): the fraction of a parcel that the
+ * freestream inflow carries to the next step (accumulatedParcelsToInsert_,
+ * dsmcFreeStreamInflowPatch.C:131-141), zero on faces without inflow; and
+ * with the selection audit on, "selectionAudit" (double, n = 2 x cells,
+ * cell major): the audit sums of dsmc_set_selection_audit. */
 int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n);
 int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long long n);
 
@@ -467,12 +473,40 @@ int dsmc_mlp_train(dsmc_mlp* m, int steps, int batch, float lr, unsigned long lo
 int dsmc_mlp_grad(dsmc_mlp* m, const float* X, const float* Y, int n, float* grad_out, float* loss_out);
 /* log-maximum predictions for n rows */
 int dsmc_mlp_predict(dsmc_mlp* m, const float* X, long long n, float* out);
+/* Selection audit (no counterpart in the reference): with it on, every
+   noTimeCounter candidate adds, to its cell, sigma_T c_R / max (its
+   acceptance probability when the maximum bounds the product) and
+   max(0, sigma_T c_R / max - 1) (the part the acceptance test cannot
+   honour).  Per cell, the ratio of the second sum to the first is the
+   expected relative shortfall of its collision count caused by a maximum
+   below the product: zero for an exact NTC, the reference's own snapshot
+   shortfall for the running maximum (noTimeCounter.C:243-248), the learned
+   selection's error with a prediction.  Read with dsmc_get_cell_array
+   "selectionAudit"; cleared by dsmc_reset_sampling and when switched on. */
+int dsmc_set_selection_audit(dsmc_handle* h, int on);
 /* attach a model (NULL: plain running maximum); predictions every `every`
    steps, used as exp(prediction + margin) */
 int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float margin);
 /* after a step: (features, log largest product among the step's candidates)
    of the cells that had candidates, at most max_rows of them */
 int dsmc_learn_record(dsmc_handle* h, long long max_rows, float* X, float* Y, long long* n_out);
+
+/*
+ * Lower the caps of the device loops that the reference runs without bound
+ * (acceptance-rejection draws: the inflow normal speed, the vibrational
+ * level, dsmcFreeStreamInflowPatch.C:288-305, dsmcCloud.C:1516-1526; face
+ * crossings of one move), of the cell size the collision kernels order (a
+ * larger cell skips its collisions), and of the parcel capacity the inflow
+ * may fill.  0 keeps the default (100000 draws, 64 crossings, 16384 parcels,
+ * the allocated capacity); larger values are rejected.  A cap that is
+ * reached sets a bit of the device error word instead of faulting or
+ * hanging: the next call that checks it returns DSMC_ERR_DEVICE (caps) or
+ * DSMC_ERR_CAPACITY with a message, the bits are cleared once reported and
+ * the handle steps on.  For tests of that path; the reference's FatalError
+ * sites (BinaryCollisionModel.C:72-83, dsmcCloud.C:1354-1383) abort instead.
+ */
+int dsmc_set_limits(dsmc_handle* h, int max_rejection, int max_crossings, int max_cell_parcels,
+                    long long capacity);
 
 /*
  * Launch shape of a cloud's step (no counterpart in the reference, which runs

@@ -1364,6 +1364,10 @@ void oracle_destroy(oracle_handle* h) { delete h; }
 
 void oracle_set_threads(oracle_handle* h, int n_threads) { h->o.nThreads = n_threads > 0 ? n_threads : 1; }
 
+// The step counter that keys the random streams (to continue a state that
+// another implementation advanced to that step).
+void oracle_set_step(oracle_handle* h, long long step) { h->o.step = step; }
+
 int oracle_initialise(oracle_handle* h) {
     h->o.initialise();
     return h->o.err ? DSMC_ERR_DEVICE : DSMC_OK;
@@ -1432,6 +1436,7 @@ int oracle_get_cell_array(oracle_handle* h, const char* name, void* out) {
     else if (nm == "sigmaTcRMax") std::memcpy(out, o.sigmaTcRMax.data(), sizeof(double) * o.C);
     else if (nm == "collisionSelectionRemainder") std::memcpy(out, o.remainder.data(), sizeof(double) * o.C);
     else if (nm == "accumulators") std::memcpy(out, o.acc.data(), sizeof(double) * o.C * o.nAcc);
+    else if (nm == "inflowAccumulator") std::memcpy(out, o.inflowAcc.data(), sizeof(double) * o.inflowAcc.size());
     else return DSMC_ERR_INVALID;
     return DSMC_OK;
 }
@@ -1441,6 +1446,7 @@ int oracle_set_cell_array(oracle_handle* h, const char* name, const void* in) {
     const std::string nm(name);
     if (nm == "sigmaTcRMax") std::memcpy(o.sigmaTcRMax.data(), in, sizeof(double) * o.C);
     else if (nm == "collisionSelectionRemainder") std::memcpy(o.remainder.data(), in, sizeof(double) * o.C);
+    else if (nm == "inflowAccumulator") std::memcpy(o.inflowAcc.data(), in, sizeof(double) * o.inflowAcc.size());
     else return DSMC_ERR_INVALID;
     return DSMC_OK;
 }

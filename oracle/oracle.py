@@ -34,6 +34,7 @@ def lib() -> C.CDLL:
         L.oracle_create.argtypes = [C.POINTER(S.CaseSpec), C.c_int]
         L.oracle_destroy.argtypes = [vp]
         L.oracle_set_threads.argtypes = [vp, C.c_int]
+        L.oracle_set_step.argtypes = [vp, C.c_longlong]
         for f in ("oracle_initialise",):
             getattr(L, f).argtypes = [vp]
         L.oracle_run_phases.argtypes = [vp, C.c_uint]
@@ -94,6 +95,10 @@ class OracleCloud:
     def set_threads(self, threads: int):
         lib().oracle_set_threads(self.h, int(threads))
 
+    def set_step(self, step: int):
+        """The step counter that keys the random streams."""
+        lib().oracle_set_step(self.h, int(step))
+
     def initialise(self):
         self._chk(lib().oracle_initialise(self.h))
 
@@ -129,6 +134,8 @@ class OracleCloud:
             a = np.empty(self.n_cells, np.int32)
         elif name == "accumulators":
             a = np.empty(self.n_cells * lib().oracle_n_accumulators(self.h))
+        elif name == "inflowAccumulator":
+            a = np.empty(lib().oracle_n_boundary_faces(self.h) * self.spec.n_species)
         else:
             a = np.empty(self.n_cells)
         self._chk(lib().oracle_get_cell_array(self.h, name.encode(), _p(a)))

@@ -144,7 +144,10 @@ def test_batch_follows_settings_changed_on_a_case():
         g.initialise()
         g.evolve(2)
     model = Mlp()
-    norm = np.array([45.0, 8.0, 0.5, 1.0, 1.0, 0.5, -13.0, 1.0], dtype=np.float32)
+    # inputs about (log n, log T, speed ratio) of the bath; output about the
+    # log of its sigma_T c_R (~1e-15 m^3/s), so the untrained net predicts a
+    # maximum of the right order
+    norm = np.array([45.0, 8.0, 0.5, 1.0, 1.0, 0.5, -34.5, 0.3], dtype=np.float32)
     model.set_params(init_params(3), norm)
     views = [_case_view(b, i) for i in range(2)]
     try:

@@ -138,14 +138,22 @@ def test_learned_selection_draws_fewer_candidates_at_the_same_rate():
         g.evolve(100)
         if learned:
             g.set_learned(model, 10, margin)
+        g.set_selection_audit(True)
         i0 = g.info()
         g.evolve(steps)
         i1 = g.info()
+        audit = learn.audit_summary(g.cell_array("selectionAudit"))
         g.close()
-        return i1.collisions_total - i0.collisions_total, i1.candidates_total - i0.candidates_total
+        return i1.collisions_total - i0.collisions_total, i1.candidates_total - i0.candidates_total, audit
 
-    cp, kp = run(False)
-    cl, kl = run(True)
+    cp, kp, ap = run(False)
+    cl, kl, al = run(True)
     assert kl / cl < 0.95 * (kp / cp), (kp / cp, kl / cl)
-    # both are Poisson-like counts of about 1e6: 1% is several standard errors
+    # both are counts of about 1e6: 1% is several standard errors
     assert abs(cl / cp - 1) < 0.01, (cp, cl)
+    # the audit: the expected per-cell shortfall of the collision count that
+    # a maximum below the product causes -- tiny for the running maximum,
+    # within 1% in total and in almost every cell for the learned one
+    assert ap["expected_shortfall_total"] < 1e-3, ap
+    assert al["expected_shortfall_total"] < 0.01, al
+    assert al["cells_above_1pct"] < 0.05, al

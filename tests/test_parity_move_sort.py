@@ -32,10 +32,16 @@ def _pair(spec, gpu_lib, oracle_mod, threads=4):
     return g, o, st
 
 
+def _taint():
+    """Ids whose state went through a transcendental function (inflow
+    creation, diffuse wall) in some step so far: compared with a tolerance."""
+    return {"ids": np.empty(0, dtype=np.uint32)}
+
+
 def _check_step(g, o, before, phases, allow_resampled=True, tainted=None):
-    """One step on both sides.  ``tainted`` collects ids whose state went
-    through a transcendental function (inflow creation, diffuse wall) in
-    this or an earlier step; they are compared with a tolerance."""
+    """One step on both sides.  ``tainted`` (from _taint) collects ids whose
+    state went through a transcendental function in this or an earlier step;
+    they are compared with a tolerance.  Vectorised: runs at 10^8 parcels."""
     g.run_phases(phases)
     o.run_phases(phases)
     a = _canonical(g.particles())
@@ -46,18 +52,20 @@ def _check_step(g, o, before, phases, allow_resampled=True, tainted=None):
     np.testing.assert_array_equal(g.cell_array("count"), o.cell_array("count"))
     np.testing.assert_array_equal(g.cell_array("start"), o.cell_array("start"))
     # parcels whose velocity only changed by exact sign flips (specular, symmetry)
-    prev = {int(i): k for k, i in enumerate(before["id"])}
-    idx = np.array([prev.get(int(i), -1) for i in b["id"]])
-    old = idx >= 0
+    order = np.argsort(before["id"], kind="stable")
+    ids_sorted = before["id"][order]
+    k = np.minimum(np.searchsorted(ids_sorted, b["id"]), max(len(ids_sorted) - 1, 0))
+    old = ids_sorted[k] == b["id"] if len(ids_sorted) else np.zeros(len(b["id"]), bool)
+    idx = order[k]
     exact = old.copy()
     exact[old] = np.all(np.abs(b["U"][old]) == np.abs(before["U"][idx[old]]), axis=1)
     if tainted is not None:
-        tainted.update(int(i) for i in b["id"][~exact])
-        exact &= ~np.isin(b["id"], np.fromiter(tainted, dtype=np.uint32, count=len(tainted)))
+        tainted["ids"] = np.union1d(tainted["ids"], b["id"][~exact])
+        exact &= ~np.isin(b["id"], tainted["ids"])
     n_exact = int(exact.sum())
     assert n_exact > 0
-    for k in ("pos", "U"):
-        np.testing.assert_array_equal(a[k][exact], b[k][exact])
+    for key in ("pos", "U"):
+        np.testing.assert_array_equal(a[key][exact], b[key][exact])
     np.testing.assert_array_equal(a["erot"][exact], b["erot"][exact])
     np.testing.assert_array_equal(a["vib"][exact], b["vib"][exact])
     if not allow_resampled:
@@ -100,7 +108,7 @@ def test_move_sort_inflow_obstacle_diffuse(gpu_lib, oracle_mod):
     s = S.config2(seed=14, scale=8)
     g, o, st = _pair(s, gpu_lib, oracle_mod)
     before = _canonical(st)
-    tainted = set()
+    tainted = _taint()
     for _ in range(4):
         a, b, exact = _check_step(g, o, before, S.PHASE_INFLOW | S.PHASE_MOVE | S.PHASE_SORT,
                                   tainted=tainted)
@@ -154,7 +162,7 @@ def test_move_sort_reduced_d_couette(gpu_lib, oracle_mod):
     s = parse_case(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "cases", "couette_N2-O2"))
     g, o, st = _pair(s, gpu_lib, oracle_mod)
     before = _canonical(st)
-    tainted = set()
+    tainted = _taint()
     for _ in range(3):
         a, b, exact = _check_step(g, o, before, S.PHASE_MOVE | S.PHASE_SORT, tainted=tainted)
         before = b
@@ -173,7 +181,7 @@ def test_move_sort_graded_flat_plate(gpu_lib, oracle_mod):
                                 "supersonic_flat_plate"))
     g, o, st = _pair(s, gpu_lib, oracle_mod, threads=8)
     before = _canonical(st)
-    tainted = set()
+    tainted = _taint()
     for _ in range(3):
         a, b, exact = _check_step(g, o, before, S.PHASE_INFLOW | S.PHASE_MOVE | S.PHASE_SORT, tainted=tainted)
         before = b
@@ -183,3 +191,72 @@ def test_move_sort_graded_flat_plate(gpu_lib, oracle_mod):
     assert gi.deleted_last_step == oi.deleted_last_step > 0
     assert gi.wall_hits_last_step == oi.wall_hits_last_step > 0
     np.testing.assert_allclose(g.wall_accumulators(), o.wall(), rtol=1e-9, atol=1e-30)
+
+
+# ------------------------------------------------------ benchmarked sizes
+def _oracle_from_gpu(spec, g, oracle_mod):
+    """The oracle continuing the GPU cloud's state: parcels, the per-cell
+    selection state, the inflow remainders and the step that keys the random
+    streams (sampling sums restart on both sides)."""
+    import os
+    st = g.particles()
+    o = oracle_mod.OracleCloud(spec, threads=os.cpu_count() or 4)
+    o.set_particles(st["pos"], st["U"], st["erot"], st["vib"], st["species"], st["id"])
+    for k in ("sigmaTcRMax", "collisionSelectionRemainder", "inflowAccumulator"):
+        o.set_cell_array(k, g.cell_array(k))
+    o.set_step(g.counts().step)
+    g.reset_sampling()
+    return o, st
+
+
+def test_move_sort_heat_bath_bench_size(gpu_lib, oracle_mod):
+    """The 64^3 heat bath of the benchmark (13.1M parcels) after 20 full steps
+    on the GPU: one move and sort, bit for bit."""
+    from hystrath_gb300.dsmc import DsmcCloud
+    s = S.config1(seed=1000, n=64)
+    g = DsmcCloud(s)
+    g.initialise()
+    g.evolve(20)
+    o, st = _oracle_from_gpu(s, g, oracle_mod)
+    assert len(st["id"]) > 13_000_000
+    _check_step(g, o, _canonical(st), S.PHASE_MOVE | S.PHASE_SORT, allow_resampled=False)
+    assert g.info().wall_hits_last_step == o.info().wall_hits_last_step > 0
+
+
+def test_move_sort_channel_full_size_developed(gpu_lib, oracle_mod):
+    """The Mach-10 channel of the benchmark at full size (256x128x128 cells,
+    about 84M parcels) after 600 full steps on the GPU (bow shock and wake
+    formed): one inflow+move+sort step compared parcel by parcel with the
+    wall accumulators of every boundary face, then two more with the face
+    tracker on, compared face by face."""
+    from hystrath_gb300.dsmc import DsmcCloud
+    s = S.config2(seed=1000, scale=1)
+    g = DsmcCloud(s)
+    g.initialise()
+    g.evolve(600)
+    o, st = _oracle_from_gpu(s, g, oracle_mod)
+    assert len(st["id"]) > 80_000_000
+    before = _canonical(st)
+    del st
+    tainted = _taint()
+    phases = S.PHASE_INFLOW | S.PHASE_MOVE | S.PHASE_SORT
+    a, b, exact = _check_step(g, o, before, phases, tainted=tainted)
+    assert exact.sum() > 0.99 * len(exact)
+    gi, oi = g.info(), o.info()
+    assert gi.inserted_last_step == oi.inserted_last_step > 0
+    assert gi.deleted_last_step == oi.deleted_last_step > 0
+    assert gi.wall_hits_last_step == oi.wall_hits_last_step > 0
+    np.testing.assert_allclose(g.wall_accumulators(), o.wall(), rtol=1e-9, atol=1e-30)
+    g.set_face_tracking(True)
+    o.set_face_tracking(True)
+    before = b
+    del a
+    for _ in range(2):
+        _, before, _ = _check_step(g, o, before, phases, tainted=tainted)
+    for key in ("parcelIdFlux", "massIdFlux"):
+        fa, fb = g.face_flux(key, 0), o.face_flux(key, 0)
+        assert np.abs(fb).sum() > 0
+        if key == "parcelIdFlux":
+            np.testing.assert_array_equal(fa, fb)
+        else:
+            np.testing.assert_allclose(fa, fb, rtol=1e-12, atol=1e-40)
