@@ -750,6 +750,17 @@ void readCase(const std::string& dir, dsmc_case_spec* s) {
     const std::string cdPath = dir + "/system/controlDict";
     auto cd = readDict(cdPath);
     s->delta_t = scalar(cd.get(), "deltaT", cdPath);
+    // output times: writeControl timeStep (every writeInterval steps) or
+    // runTime / adjustableRunTime (every writeInterval seconds)
+    {
+        const double wi = scalarOr(cd.get(), "writeInterval", 0.0);
+        const std::string wc = wordOr(cd.get(), "writeControl", "timeStep");
+        if (wi > 0) {
+            const double steps = (wc == "timeStep") ? wi : wi / s->delta_t;
+            s->write_interval_steps = (long long)std::llround(steps);
+            if (s->write_interval_steps < 1) s->write_interval_steps = 1;
+        }
+    }
 
     // system/boundariesDict
     const std::string bdPath = dir + "/system/boundariesDict";
@@ -828,6 +839,12 @@ void readCase(const std::string& dir, dsmc_case_spec* s) {
                     const Node* pr = it->find("dsmcVolFieldsProperties");
                     s->measure_mean_free_path = boolOr(pr, "measureMeanFreePath", false) ? 1 : 0;
                     s->mfp_tref = scalarOr(pr, "mfpReferenceTemperature", 273.0);
+                    s->measure_errors = boolOr(pr, "measureErrors", false) ? 1 : 0;
+                    s->measure_heat_flux_shear_stress = boolOr(pr, "measureHeatFluxShearStress", false) ? 1 : 0;
+                    if (const Node* tp = it->find("timeProperties")) {
+                        s->reset_at_output = boolOr(tp, "resetAtOutput", false) ? 1 : 0;
+                        s->reset_at_output_until_time = scalarOr(tp, "resetAtOutputUntilTime", 0.0);
+                    }
                 }
             }
         }

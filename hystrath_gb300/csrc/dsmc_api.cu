@@ -74,6 +74,12 @@ struct dsmc_handle {
     double phaseMs[5] = {0, 0, 0, 0, 0};
     bool hasInflow = false;
     long long expectedN = 0;
+    // output schedule of the time averages (resetAtOutput): the step count
+    // as of the last read of the counters, whether resets at output are
+    // still on, and a reset due before the next step
+    long long stepHost = 0;
+    bool resetActive = true;
+    bool resetPending = false;
     // learned selection
     const MlpModel* model = nullptr;
     int learnEvery = 0;
@@ -395,9 +401,22 @@ void fill_case_dev(dsmc_handle* h) {
 
 Parcels& cur_soa(dsmc_handle* h) { return h->buf[h->cur]; }
 
+// The output schedule as of step h->stepHost: resets at output stay on
+// until the first output time t with t + deltaT > resetAtOutputUntilTime
+// (dsmcField::updateBasicFieldProperties, dsmcField.C:113-150).
+void schedule_sync(dsmc_handle* h) {
+    const long long wi = h->spec.write_interval_steps;
+    const double until = h->spec.reset_at_output_until_time;
+    h->resetActive = true;
+    if (wi <= 0 || until <= 0) return;
+    const long long last = (h->stepHost / wi) * wi;   // the last output step so far
+    if (last > 0 && (double)last * h->spec.delta_t + h->spec.delta_t > until) h->resetActive = false;
+}
+
 int check_device_error(dsmc_handle* h) {
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    h->stepHost = h->ctrHost->step;
     const unsigned e = h->ctrHost->err;
     if (e) {
         // reported once: the bits are cleared, and the handle steps on (the
@@ -417,6 +436,40 @@ int check_device_error(dsmc_handle* h) {
         return fail(h, e & ERRB_CAPACITY ? DSMC_ERR_CAPACITY : DSMC_ERR_DEVICE, m);
     }
     return DSMC_OK;
+}
+
+// Restart the time averages on stream st (dsmcVolFields' reset at output,
+// dsmcVolFields.C:2269-2300): the sampling sums, wall and face sums and the
+// selection audit; a pending sample belongs to the window being discarded.
+void enqueue_reset(dsmc_handle* h, cudaStream_t st) {
+    const CaseDev& cs = h->cs;
+    cudaMemsetAsync(h->B.acc, 0, sizeof(double) * cs.C * cs.nAcc, st);
+    cudaMemsetAsync(h->B.sfix, 0, sizeof(long long) * cs.C * cs.nSpecies * SACC, st);
+    cudaMemsetAsync(h->B.wall, 0, sizeof(double) * cs.nBFaces * W_N, st);
+    if (h->B.audit) cudaMemsetAsync(h->B.audit, 0, sizeof(double2) * cs.C, st);
+    if (h->B.macc) cudaMemsetAsync(h->B.macc, 0, sizeof(double) * cs.C * cs.nSpecies * MACC, st);
+    if (cs.faceFlux) cudaMemsetAsync(cs.faceFlux, 0, sizeof(double) * 2 * cs.nSpecies * cs.nFacesAll, st);
+    launch_reset_sample_counters(h->B, st);
+}
+
+// Before a step: a reset that an output time left due.
+void schedule_pre(dsmc_handle* h, cudaStream_t st) {
+    if (!h->resetPending) return;
+    enqueue_reset(h, st);
+    h->faceStep0 = h->stepHost;
+    h->resetPending = false;
+}
+
+// After a step: at an output time, a reset is due before the next step (the
+// caller reads or writes the output in between), while resets are on.
+void schedule_post(dsmc_handle* h) {
+    ++h->stepHost;
+    const long long wi = h->spec.write_interval_steps;
+    if (wi <= 0 || h->stepHost % wi) return;
+    if (h->spec.reset_at_output && h->resetActive) h->resetPending = true;
+    const double t = (double)h->stepHost * h->spec.delta_t;
+    const double until = h->spec.reset_at_output_until_time;
+    if (until > 0 && t + h->spec.delta_t > until) h->resetActive = false;
 }
 
 // Event marks of a step (enqueue_step with events): the intervals between
@@ -493,8 +546,12 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
     }
     mark(MK_LIGHT);
     // dsmcVolFields samples the state after the collisions; the sums are
-    // taken when that state is next streamed (the next move, or a flush)
-    if (phases & DSMC_PHASE_SAMPLE) launch_set_pending(B, st);
+    // taken when that state is next streamed (the next move, or a flush);
+    // the velocity moments of measureHeatFluxShearStress are taken here
+    if (phases & DSMC_PHASE_SAMPLE) {
+        if (B.macc) launch_sample_moments(cs, B, (phases & DSMC_PHASE_SORT) ? b : a, st);
+        launch_set_pending(B, st);
+    }
     mark(MK_PENDING);
     launch_end_step(B, st);
     mark(MK_END);
@@ -656,6 +713,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.rem, cs.C))) return rc;
     if ((rc = dalloc(h, &B.acc, cs.C * cs.nAcc))) return rc;
     if ((rc = dalloc(h, &B.sfix, cs.C * cs.nSpecies * SACC))) return rc;
+    if (spec->measure_heat_flux_shear_stress && (rc = dalloc(h, &B.macc, cs.C * cs.nSpecies * MACC))) return rc;
     if ((rc = dalloc(h, &B.wall, cs.nBFaces * W_N))) return rc;
     if ((rc = dalloc(h, &B.bfPatch, cs.nBFaces))) return rc;
     if ((rc = dalloc(h, &B.bigList, cs.C))) return rc;
@@ -851,8 +909,10 @@ int dsmc_evolve(dsmc_handle* h, long long n) {
     int rc = build_graphs(h);
     if (rc) return rc;
     for (long long i = 0; i < n; ++i) {
+        schedule_pre(h, h->stream);
         CUDA_TRY(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
         h->cur ^= 1;
+        schedule_post(h);
     }
     return check_device_error(h);
 }
@@ -865,8 +925,10 @@ int profile_steps(dsmc_handle* h, long long n, double* per_mark, double* total_m
     std::vector<cudaEvent_t> ev((size_t)n * MK_COUNT);
     for (auto& e : ev) CUDA_TRY(h, cudaEventCreate(&e));
     for (long long i = 0; i < n; ++i) {
+        schedule_pre(h, h->stream);
         enqueue_step(h, h->cur, DSMC_PHASE_ALL, &ev[(size_t)i * MK_COUNT]);
         h->cur ^= 1;
+        schedule_post(h);
     }
     CUDA_TRY(h, cudaGetLastError());
     int rc = check_device_error(h);
@@ -914,8 +976,10 @@ int dsmc_evolve_timed(dsmc_handle* h, long long n, double* total_ms) {
     CUDA_TRY(h, cudaEventCreate(&e1));
     CUDA_TRY(h, cudaEventRecord(e0, h->stream));
     for (long long i = 0; i < n; ++i) {
+        schedule_pre(h, h->stream);
         CUDA_TRY(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
         h->cur ^= 1;
+        schedule_post(h);
     }
     CUDA_TRY(h, cudaEventRecord(e1, h->stream));
     rc = check_device_error(h);
@@ -930,7 +994,9 @@ int dsmc_evolve_timed(dsmc_handle* h, long long n, double* total_ms) {
 int dsmc_run_phases(dsmc_handle* h, unsigned phases) {
     cudaEvent_t ev[MK_COUNT];
     for (int k = 0; k < MK_COUNT; ++k) cudaEventCreate(&ev[k]);
+    if (phases == DSMC_PHASE_ALL) schedule_pre(h, h->stream);
     enqueue_step(h, h->cur, phases, ev);
+    if (phases == DSMC_PHASE_ALL) schedule_post(h);
     CUDA_TRY(h, cudaGetLastError());
     if (phases & DSMC_PHASE_SORT) h->cur ^= 1;
     int rc = check_device_error(h);
@@ -1111,7 +1177,13 @@ int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long l
 int dsmc_get_species_field(dsmc_handle* h, const char* name, unsigned species_mask, double* out, long long n) {
     static const char* names[F_COUNT_FIELDS] = {"rhoN", "rhoM", "Ux", "Uy", "Uz", "Ttra", "p", "Trot", "Tvib",
                                                 "Tov", "dsmcNMean", "nColls", "measuredCollisionRate",
-                                                "meanCollisionRate", "mfp"};
+                                                "meanCollisionRate", "mfp", "Ma", "rhoMError", "UError",
+                                                "TError", "pError", "pressureTensor_xx", "pressureTensor_xy",
+                                                "pressureTensor_xz", "pressureTensor_yy", "pressureTensor_yz",
+                                                "pressureTensor_zz", "shearStressTensor_xx", "shearStressTensor_xy",
+                                                "shearStressTensor_xz", "shearStressTensor_yy",
+                                                "shearStressTensor_yz", "shearStressTensor_zz", "heatFluxVector_x",
+                                                "heatFluxVector_y", "heatFluxVector_z"};
     int which = -1;
     for (int k = 0; k < F_COUNT_FIELDS; ++k)
         if (!std::strcmp(name, names[k])) which = k;
@@ -1121,6 +1193,8 @@ int dsmc_get_species_field(dsmc_handle* h, const char* name, unsigned species_ma
         return fail(h, DSMC_ERR_INVALID, std::string("unknown field ") + name + "; valid:" + valid);
     }
     if (n != h->cs.C) return fail(h, DSMC_ERR_INVALID, "n must equal the number of cells");
+    if (which >= F_PXX && which <= F_QZ && !h->B.macc)
+        return fail(h, DSMC_ERR_INVALID, std::string(name) + " needs measureHeatFluxShearStress in the case");
     const unsigned all = (1u << h->cs.nSpecies) - 1u;
     if (!(species_mask & all) || (species_mask & ~all))
         return fail(h, DSMC_ERR_INVALID, "species_mask must select species of the case");
@@ -1191,20 +1265,13 @@ int dsmc_get_wall_field(dsmc_handle* h, const char* name, double* out, long long
 }
 
 int dsmc_reset_sampling(dsmc_handle* h) {
-    // a pending sample belongs to the window being discarded
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-    CUDA_TRY(h, cudaMemset(h->B.acc, 0, sizeof(double) * h->cs.C * h->cs.nAcc));
-    CUDA_TRY(h, cudaMemset(h->B.sfix, 0, sizeof(long long) * h->cs.C * h->cs.nSpecies * SACC));
-    CUDA_TRY(h, cudaMemset(h->B.wall, 0, sizeof(double) * h->cs.nBFaces * W_N));
-    if (h->B.audit) CUDA_TRY(h, cudaMemset(h->B.audit, 0, sizeof(double2) * h->cs.C));
-    if (h->cs.faceFlux)
-        CUDA_TRY(h, cudaMemset(h->cs.faceFlux, 0, sizeof(double) * 2 * h->cs.nSpecies * h->cs.nFacesAll));
+    enqueue_reset(h, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     CUDA_TRY(h, cudaMemcpy(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
     h->faceStep0 = h->ctrHost->step;
-    h->ctrHost->sampleSteps = 0;
-    h->ctrHost->pendingSample = 0;
-    h->ctrHost->unflushed = 0;
-    CUDA_TRY(h, cudaMemcpy(h->B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
+    h->resetPending = false;
     return DSMC_OK;
 }
 
@@ -1240,8 +1307,10 @@ int dsmc_evolve_counts(dsmc_handle* h, long long n, dsmc_counts_t* out) {
     // each step's counters follow it to the host on the same stream: no
     // host round trip between steps
     for (long long i = 0; i < n; ++i) {
+        schedule_pre(h, h->stream);
         CUDA_TRY(h, cudaGraphLaunch(h->graph[h->cur], h->stream));
         h->cur ^= 1;
+        schedule_post(h);
         CUDA_TRY(h, cudaMemcpyAsync(h->ctrRing + i, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, h->stream));
     }
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
@@ -1362,6 +1431,9 @@ int dsmc_restore(dsmc_handle* h, const char* path) {
     if (h->cs.faceFlux)
         CUDA_TRY(h, cudaMemset(h->cs.faceFlux, 0, sizeof(double) * 2 * h->cs.nSpecies * h->cs.nFacesAll));
     h->faceStep0 = c.step;
+    h->stepHost = c.step;
+    h->resetPending = false;
+    schedule_sync(h);
     h->smaxSet = true;
     return DSMC_OK;
 }
@@ -1614,9 +1686,12 @@ int dsmc_batch_evolve_timed(dsmc_batch* b, long long n, double* total_ms) {
     }
     int p = cur;
     for (long long s = 0; s < n; ++s) {
+        // each case's output schedule (resets at output) around the launch
+        for (dsmc_handle* h : b->cases) schedule_pre(h, b->stream);
         const cudaError_t e = cudaGraphLaunch(b->graph[p], b->stream);
         if (e != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
         p ^= 1;
+        for (dsmc_handle* h : b->cases) schedule_post(h);
     }
     if (total_ms) cudaEventRecord(e1, b->stream);
     const cudaError_t e = cudaStreamSynchronize(b->stream);

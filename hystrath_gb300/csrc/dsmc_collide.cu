@@ -132,11 +132,64 @@ __global__ void k_zero_step(Counters* ctr) {
     ctr->nHeavy = 0;
 }
 
+// ---------------------------------------------------------------- moments
+// One thread per cell: the cell's parcels (contiguous after the sort) summed
+// species by species as exact fixed-point integers, so the step's sums do not
+// depend on the parcels' order in the cell, then added to the FP64
+// accumulators in step order (reproducible bit for bit).
+constexpr int F_MUU = 14;   // u_i u_j: resolution 6.1e-5 m^2/s^2
+constexpr int F_MCCU = 4;   // |U|^2 u_i: resolution 0.0625 m^3/s^3
+constexpr int F_MEU = 90;   // E_int u_i: resolution 8.1e-28 J m/s
+
+__global__ void k_sample_moments(CaseDev cs, Parcels s, const int* __restrict__ start, double* macc,
+                                 Counters* ctr) {
+    const long long C = cs.C;
+    unsigned err = 0;
+    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < C;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int j0 = start[c], j1 = start[c + 1];
+        if (j1 <= j0) continue;
+        for (int sp = 0; sp < cs.nSpecies; ++sp) {
+            long long m[MACC];
+#pragma unroll
+            for (int k = 0; k < MACC; ++k) m[k] = 0;
+            int any = 0;
+            for (int j = j0; j < j1; ++j) {
+                const Rec p = ldg_rec(s.r + j);
+                if (sv_species(p.sv) != sp) continue;
+                any = 1;
+                const double u = p.ux, v = p.uy, w = p.uz;
+                const double cc = u * u + v * v + w * w;
+                const double E = p.erot + (double)sv_vib(p.sv) * cs.sp[sp].kThetaV;
+                m[MACC_UU] += fixp(u * u, F_MUU, &err);
+                m[MACC_UV] += fixp(u * v, F_MUU, &err);
+                m[MACC_UW] += fixp(u * w, F_MUU, &err);
+                m[MACC_VV] += fixp(v * v, F_MUU, &err);
+                m[MACC_VW] += fixp(v * w, F_MUU, &err);
+                m[MACC_WW] += fixp(w * w, F_MUU, &err);
+                m[MACC_CCU] += fixp(cc * u, F_MCCU, &err);
+                m[MACC_CCV] += fixp(cc * v, F_MCCU, &err);
+                m[MACC_CCW] += fixp(cc * w, F_MCCU, &err);
+                m[MACC_EU] += fixp(E * u, F_MEU, &err);
+                m[MACC_EV] += fixp(E * v, F_MEU, &err);
+                m[MACC_EW] += fixp(E * w, F_MEU, &err);
+            }
+            if (!any) continue;
+#pragma unroll
+            for (int k = 0; k < MACC; ++k) {
+                const int F = k < MACC_CCU ? F_MUU : k < MACC_EU ? F_MCCU : F_MEU;
+                macc[(long long)(sp * MACC + k) * C + c] += ldexp((double)m[k], -F);
+            }
+        }
+    }
+    if (err) atomicOr(&ctr->err, err);
+}
+
 // ---------------------------------------------------------------- fields
 // Species outside mask are left out of every sum (a dsmcVolFields typeIds
 // subset, dsmcVolFields.C:841).
-__global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counters* ctr, int which, double* out,
-                        int measureMfp, double mfpTref, unsigned mask) {
+__global__ void k_field(CaseDev cs, const double* __restrict__ acc, const double* __restrict__ macc,
+                        const Counters* ctr, int which, double* out, int measureMfp, double mfpTref, unsigned mask) {
     const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= cs.C) return;
     const double nT = (double)ctr->sampleSteps;
@@ -244,7 +297,80 @@ __global__ void k_field(CaseDev cs, const double* __restrict__ acc, const Counte
         v = (which == F_MFP) ? mfp : mcr;
         break;
     }
-    default: v = 0.0;
+    case F_MA:
+    case F_RHOM_ERR:
+    case F_U_ERR:
+    case F_T_ERR:
+    case F_P_ERR: {
+        // dsmcVolFields.C:1625-1661 (Mach number from the trans-rotational
+        // gamma of the mixture) and :1859-1873 (statistical error estimates)
+        double Ma = 0.0, gamma = 0.0, particleCv = 0.0;
+        if (N > SMALL && Ttra > SMALL) {
+            double molarCv = 0.0, molarCp = 0.0, mMol = 0.0;
+            for (int s = 0; s < cs.nSpecies; ++s) {
+                if (!((mask >> s) & 1u)) continue;
+                const double Xs = A(s * SACC + SACC_N) / N;
+                mMol += Xs * cs.sp[s].m;
+                molarCv += Xs * (3.0 + cs.sp[s].rotDof);
+                molarCp += Xs * (5.0 + cs.sp[s].rotDof);
+            }
+            particleCv = molarCv / NAVO;
+            gamma = molarCp / molarCv;
+            Ma = sqrt(Ux * Ux + Uy * Uy + Uz * Uz) / sqrt(gamma * kB / mMol * Ttra);
+        }
+        if (which == F_MA) {
+            v = Ma;
+            break;
+        }
+        const double nMean = (N > 1e-3 && nT > 0) ? N / nT : 0.001;
+        v = 0.0;
+        if (nMean > SMALL && Ma > SMALL && gamma > SMALL && particleCv > SMALL) {
+            const double deno = sqrt(nMean * nT);
+            if (which == F_RHOM_ERR) v = 1.0 / deno;
+            else if (which == F_U_ERR) v = 1.0 / (deno * Ma * sqrt(gamma));
+            else if (which == F_T_ERR) v = sqrt(kB / particleCv) / deno;
+            else v = sqrt(gamma) / deno;
+        }
+        break;
+    }
+    default:
+        if (which >= F_PXX && which <= F_QZ && macc && N > SMALL && nT > 0) {
+            // dsmcVolFields.C:1511-1607: pressure tensor, shear stress tensor
+            // (pressure tensor minus its trace part, negated) and heat flux
+            double Muu[6] = {0, 0, 0, 0, 0, 0}, Mccu[3] = {0, 0, 0}, Eu[3] = {0, 0, 0}, E = Er;
+            for (int s = 0; s < cs.nSpecies; ++s) {
+                if (!((mask >> s) & 1u)) continue;
+                const double m = cs.sp[s].m;
+                auto Q = [&](int k) { return macc[(long long)(s * MACC + k) * C + c]; };
+                for (int k = 0; k < 6; ++k) Muu[k] += m * Q(MACC_UU + k);
+                for (int k = 0; k < 3; ++k) {
+                    Mccu[k] += m * Q(MACC_CCU + k);
+                    Eu[k] += Q(MACC_EU + k);
+                }
+                E += cs.sp[s].kThetaV * A(s * SACC + SACC_VIB);
+            }
+            const double U[3] = {Ux, Uy, Uz};
+            const double f = rhoN / N;
+            // symmetric tensor in xx xy xz yy yz zz order
+            const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+            double P[6];
+            for (int k = 0; k < 6; ++k) P[k] = f * (Muu[k] - M * U[ia[k]] * U[ib[k]]);
+            if (which <= F_PZZ) {
+                v = P[which - F_PXX];
+            } else if (which <= F_SZZ) {
+                const int k = which - F_SXX;
+                const double sp = (P[0] + P[3] + P[5]) / 3.0;
+                v = -P[k] + (ia[k] == ib[k] ? sp : 0.0);
+            } else {
+                const int i = which - F_QX;
+                // row i of the (symmetric) pressure tensor
+                const int row[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+                v = f * (0.5 * Mccu[i] - 0.5 * mcc * U[i] + Eu[i] - E * U[i]) - P[row[i][0]] * U[0] -
+                    P[row[i][1]] * U[1] - P[row[i][2]] * U[2];
+            }
+        } else {
+            v = 0.0;
+        }
     }
     (void)measureMfp;
     out[c] = v;
@@ -407,7 +533,14 @@ void launch_zero_step(const StepBuffers& B, cudaStream_t st) { k_zero_step<<<1, 
 
 void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* out, int measureMfp,
                   double mfpTref, unsigned mask, cudaStream_t st) {
-    k_field<<<(int)((cs.C + 255) / 256), 256, 0, st>>>(cs, B.acc, B.ctr, which, out, measureMfp, mfpTref, mask);
+    k_field<<<(int)((cs.C + 255) / 256), 256, 0, st>>>(cs, B.acc, B.macc, B.ctr, which, out, measureMfp, mfpTref,
+                                                       mask);
+}
+
+void launch_sample_moments(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
+    long long blocks = (cs.C + 255) / 256;
+    if (blocks > (long long)sm_count() * 16) blocks = (long long)sm_count() * 16;
+    k_sample_moments<<<(int)blocks, 256, 0, st>>>(cs, s, B.start, B.macc, B.ctr);
 }
 
 void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, double* out6, cudaStream_t st) {

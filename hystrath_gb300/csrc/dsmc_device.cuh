@@ -16,6 +16,7 @@ namespace dsmc {
 
 // OpenFOAM v1706 constants (physicoChemicalConstants, doubleScalar.H)
 constexpr double kB = 1.3806504e-23;
+constexpr double NAVO = 6.0221417930e+23;   // Avogadro constant of the same (CODATA 2006) set
 constexpr double PI = 3.14159265358979323846;
 constexpr double SMALL = 1.0e-15;
 constexpr double VSMALL = 1.0e-300;
@@ -350,6 +351,14 @@ __device__ __forceinline__ int floor2_coord_fast(const CaseDev& cs, double x, in
     if (cs.half[a]) return floor2_graded(cs.half[a], 2 * cs.n[a], x);
     return floor2_coord_fast_uniform(cs, x, a);
 }
+
+// ------------------------------------------------------- velocity moments
+// Per species and cell (measureHeatFluxShearStress, dsmcVolFields.C:
+// 1186-1206): sums of u_i u_j (6), |U|^2 u_i (3) and E_int u_i (3), E_int the
+// rotational plus vibrational energy; the mass is applied when fields are
+// made.
+enum { MACC_UU = 0, MACC_UV, MACC_UW, MACC_VV, MACC_VW, MACC_WW, MACC_CCU, MACC_CCV, MACC_CCW,
+       MACC_EU, MACC_EV, MACC_EW, MACC };
 
 // ------------------------------------------------------- sampling sums
 // The per-step sums of the dsmcVolFields sample loop are exact integer

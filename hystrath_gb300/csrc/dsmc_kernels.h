@@ -47,6 +47,9 @@ struct StepBuffers {
     double* rem;              // collisionSelectionRemainder [C]
     double* acc;              // sampling accumulators, accumulator-major [nAcc][C]
     long long* sfix;          // one sample's fixed-point sums [nSpecies*SACC][C]
+    // measureHeatFluxShearStress (null when off): per species the velocity
+    // moments of the samples, [nSpecies*MACC][C] (MACC_* order)
+    double* macc;
     double* wall;             // [nBFaces][W_N]
     int* bfPatch;             // [nBFaces]
     int2* work;               // [C] cells with candidates: (cell, candidates)
@@ -103,6 +106,9 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
                     cudaStream_t st, cudaEvent_t mid = nullptr);
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
+// sample count, pending sample and unflushed samples back to zero (a reset
+// of the time averages)
+void launch_reset_sample_counters(const StepBuffers& B, cudaStream_t st);
 // learned != 0: the selection uses the prediction (or the running maximum of
 // cells that fell back to it) instead of the running maximum alone
 // marks (optional): two events, recorded after the selection, list and
@@ -156,6 +162,8 @@ void launch_pack(const Parcels& dst, long long n, const double* pos, const doubl
 void launch_zero_step(const StepBuffers& B, cudaStream_t st);
 void launch_cellw(const CaseDev& cs, const Parcels& s, long long n, cudaStream_t st);
 void launch_remainder_init(const CaseDev& cs, double* rem, cudaStream_t st);
+// velocity moments of the current (cell-sorted) state, added to B.macc
+void launch_sample_moments(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
 void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* out,
                   int measureMfp, double mfpTref, unsigned speciesMask, cudaStream_t st);
 void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, double* out7,
@@ -164,7 +172,11 @@ void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, doubl
 // field selectors of launch_field
 enum {
     F_RHON = 0, F_RHOM, F_UX, F_UY, F_UZ, F_TTRA, F_P, F_TROT, F_TVIB, F_TOV, F_NMEAN, F_NCOLLS,
-    F_MEASCR, F_MEANCR, F_MFP, F_COUNT_FIELDS
+    F_MEASCR, F_MEANCR, F_MFP, F_MA, F_RHOM_ERR, F_U_ERR, F_T_ERR, F_P_ERR,
+    // measureHeatFluxShearStress: pressure tensor xx xy xz yy yz zz, shear
+    // stress tensor in the same order, heat flux vector x y z
+    F_PXX, F_PXY, F_PXZ, F_PYY, F_PYZ, F_PZZ, F_SXX, F_SXY, F_SXZ, F_SYY, F_SYZ, F_SZZ, F_QX, F_QY, F_QZ,
+    F_COUNT_FIELDS
 };
 
 }  // namespace dsmc

@@ -964,6 +964,12 @@ __global__ void k_finish_sort(Counters* ctr) {
     ctr->nMoved = ctr->nKept;
 }
 
+__global__ void k_reset_sample_counters(Counters* ctr) {
+    ctr->sampleSteps = 0;
+    ctr->pendingSample = 0;
+    ctr->unflushed = 0;
+}
+
 __global__ void k_end_step(Counters* ctr) {
     ctr->collTot += ctr->coll;
     ctr->candTot += ctr->cand;
@@ -1349,6 +1355,10 @@ void launch_sample_flush(const CaseDev& cs, const StepBuffers& B, const Parcels&
 }
 
 void launch_set_pending(const StepBuffers& B, cudaStream_t st) { k_set_pending<<<1, 1, 0, st>>>(B.ctr); }
+
+void launch_reset_sample_counters(const StepBuffers& B, cudaStream_t st) {
+    k_reset_sample_counters<<<1, 1, 0, st>>>(B.ctr);
+}
 
 void launch_end_step(const StepBuffers& B, cudaStream_t st) {
     k_end_step<<<1, 1, 0, st>>>(B.ctr);

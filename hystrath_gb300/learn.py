@@ -167,43 +167,48 @@ def arm_rates(w):
 
 def per_cell_count_test(batches_a, batches_b, groups=None, group_names=None):
     """Per-cell collision counts of two independent runs of the same flow,
-    each given as per-batch counts (batches x cells).
+    each given as per-batch counts (batches x cells), batch b of both runs
+    covering the same steps.
 
     NTC counts are not Poisson (the candidate remainder is carried from step
-    to step and a candidate is a Bernoulli trial of high probability: their
-    variance is about half their mean), so each cell's variance is taken from
-    its own batch-to-batch spread.  With d_c the difference of the two runs'
-    batch means and v_c its estimated variance, T = sum_c (d_c^2 - v_c) has
-    mean zero when every cell has the same expected count in both runs, and
+    to step and a candidate is a Bernoulli trial of high probability), and a
+    developing flow changes every cell's expected count from batch to batch
+    in both runs alike.  So each cell's difference is taken batch by batch,
+    d_cb = b_cb - a_cb, and its variance from the spread of d_cb over the
+    batches, which the common trend does not enter.  With d_c the mean of
+    d_cb and v_c its estimated variance, T = sum_c (d_c^2 - v_c) has mean
+    zero when every cell has the same expected count in both runs, and
     T / sum_c m_c^2 estimates the mean square relative difference of the
     per-cell counts (weighted by m_c^2, m_c the first run's batch mean); its
     one-sided 95% upper bound uses the spread of d_c^2 - v_c over cells.
     groups: an integer label per cell (-1: none); each group's total
-    relative difference with its standard error is reported as well."""
+    relative difference with its standard error (from the paired batch
+    totals) is reported as well."""
     A = np.asarray(batches_a, dtype=np.float64)
     B = np.asarray(batches_b, dtype=np.float64)
-    ka, kb = A.shape[0], B.shape[0]
+    if A.shape != B.shape:
+        raise ValueError("both runs need the same batches")
+    k = A.shape[0]
     ma, mb = A.mean(0), B.mean(0)
-    va, vb = A.var(0, ddof=1), B.var(0, ddof=1)
     m = (ma + mb) > 0
-    d = mb[m] - ma[m]
-    v = va[m] / ka + vb[m] / kb
+    D = B[:, m] - A[:, m]
+    d = D.mean(0)
+    v = D.var(0, ddof=1) / k
     t = d * d - v
     n = int(m.sum())
     T = float(t.sum())
     sd = float(np.std(t) * math.sqrt(n)) if n > 1 else 1.0
     # sum of m_c^2 with the sampling variance of m_c removed
-    w = float(np.sum(ma[m] ** 2 - va[m] / ka))
+    w = float(np.sum(ma[m] ** 2 - A[:, m].var(0, ddof=1) / k))
     tot_a, tot_b = float(A.sum()), float(B.sum())
-    res = {"cells": n, "batches": [ka, kb], "statistic": T, "sd": sd, "z": T / sd if sd > 0 else 0.0,
+    res = {"cells": n, "batches": k, "statistic": T, "sd": sd, "z": T / sd if sd > 0 else 0.0,
            "mean_count_per_cell_and_batch": float(ma[m].mean()) if n else 0.0,
-           "variance_over_mean": float(np.sum(va[m]) / max(np.sum(ma[m]), 1e-300)),
+           "paired_variance_over_mean": float(np.sum(D.var(0, ddof=1)) / max(np.sum(ma[m] + mb[m]), 1e-300)),
            "rms_rel_diff_estimate": math.sqrt(max(T, 0.0) / w) if w > 0 else 0.0,
            "rms_rel_diff_upper95": math.sqrt(max(T + 1.645 * sd, 0.0) / w) if w > 0 else 0.0,
            "total_rel_diff": tot_b / max(tot_a, 1e-300) - 1.0}
-    # the totals' standard error from the batch totals
-    sa, sb = A.sum(1), B.sum(1)
-    res["total_rel_diff_se"] = math.sqrt(sa.var(ddof=1) / ka + sb.var(ddof=1) / kb) / max(sa.mean(), 1e-300)
+    dt = B.sum(1) - A.sum(1)
+    res["total_rel_diff_se"] = math.sqrt(dt.var(ddof=1) / k) / max(A.sum(1).mean(), 1e-300)
     if groups is not None:
         gl = []
         for gi in np.unique(groups):
@@ -213,7 +218,7 @@ def per_cell_count_test(batches_a, batches_b, groups=None, group_names=None):
             ga, gb = A[:, sel].sum(1), B[:, sel].sum(1)
             if ga.sum() <= 0:
                 continue
-            se = math.sqrt(ga.var(ddof=1) / ka + gb.var(ddof=1) / kb) / ga.mean()
+            se = math.sqrt((gb - ga).var(ddof=1) / k) / ga.mean()
             gl.append({"group": group_names[int(gi)] if group_names else int(gi), "cells": int(sel.sum()),
                        "rel_diff": gb.mean() / ga.mean() - 1.0, "se": se})
         res["groups"] = gl
@@ -256,18 +261,21 @@ def batch_mean_z(batches_a, batches_b):
     (solid cells, or a temperature with no excited level) are left out."""
     A = np.array(batches_a)
     B = np.array(batches_b)
-    ka, kb = A.shape[0], B.shape[0]
+    if A.shape != B.shape:
+        raise ValueError("both runs need the same batches")
+    # batch b of both runs covers the same steps: the difference is taken
+    # batch by batch, so a trend common to both runs (a developing flow)
+    # stays out of the standard error
+    k = A.shape[0]
     ma, mb = A.mean(0), B.mean(0)
-    va, vb = A.var(0, ddof=1) / ka, B.var(0, ddof=1) / kb
-    se = np.sqrt(va + vb)
+    D = B - A
+    se = np.sqrt(D.var(0, ddof=1) / k)
     ok = (se > 0) & np.isfinite(se) & (np.abs(ma) > 0)
     z = (mb[ok] - ma[ok]) / se[ok]
-    # Welch-Satterthwaite degrees of freedom: |z| > 2 is expected in the
-    # fraction 2 P(t_nu > 2), not 4.6%, with this few batches
-    nu = (va[ok] + vb[ok]) ** 2 / (va[ok] ** 2 / (ka - 1) + vb[ok] ** 2 / (kb - 1))
-    return {"blocks": int(ok.sum()), "mean_abs_z": float(np.mean(np.abs(z))) if z.size else 0.0,
+    # |z| > 2 is expected in the fraction 2 P(t_(k-1) > 2), not 4.6%, with this few batches
+    return {"blocks": int(ok.sum()), "batches": k, "mean_abs_z": float(np.mean(np.abs(z))) if z.size else 0.0,
             "frac_abs_z_gt_2": float(np.mean(np.abs(z) > 2.0)) if z.size else 0.0,
-            "expected_frac_abs_z_gt_2": float(np.mean(_t_two_sided_tail(2.0, nu))) if z.size else 0.0,
+            "expected_frac_abs_z_gt_2": float(np.ravel(_t_two_sided_tail(2.0, k - 1))[0]) if z.size else 0.0,
             "mean_z": float(np.mean(z)) if z.size else 0.0,
             "rel_diff_of_means": float(np.sum(mb[ok] - ma[ok]) / max(abs(np.sum(ma[ok])), 1e-300))}
 

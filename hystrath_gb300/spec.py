@@ -106,6 +106,11 @@ class CaseSpec(C.Structure):
         ("init_t_tra_xyz", C.c_double * 3),
         ("max_particles", C.c_longlong),
         ("node_coords", C.POINTER(C.c_double) * 3),
+        ("write_interval_steps", C.c_longlong),
+        ("reset_at_output", C.c_int),
+        ("reset_at_output_until_time", C.c_double),
+        ("measure_errors", C.c_int),
+        ("measure_heat_flux_shear_stress", C.c_int),
     ]
 
 

@@ -180,6 +180,21 @@ typedef struct {
      * n_cells[a] + 1 node coordinates, strictly increasing (origin[a] and
      * cell_size[a] are then ignored); NULL for a uniform axis. */
     const double* node_coords[3];
+
+    /* Output schedule of the time averages (dsmcField timeProperties,
+     * dsmcField.C:113-150; controlDict writeInterval): every
+     * write_interval_steps steps is an output time (0: none).  With
+     * reset_at_output set, the averages restart after every output time t
+     * whose previous output time t' (or the start) has t' + deltaT <=
+     * reset_at_output_until_time (every output if that is 0). */
+    long long write_interval_steps;
+    int reset_at_output;
+    double reset_at_output_until_time;
+    /* dsmcVolFieldsProperties switches: measureErrors (the rhoMError,
+     * UError, TError, pError fields) and measureHeatFluxShearStress (the
+     * moment sums behind heatFluxVector, pressureTensor, shearStressTensor). */
+    int measure_errors;
+    int measure_heat_flux_shear_stress;
 } dsmc_case_spec;
 
 /* Cloud totals, as printed by dsmcCloud::info (dsmcCloud.C:935-985). */

@@ -66,6 +66,7 @@ namespace {
 
 // OpenFOAM v1706 constants (physicoChemicalConstants, doubleScalar.H).
 const double kB = 1.3806504e-23;
+const double NAvo = 6.0221417930e+23;   // physicoChemical::NA of the same (CODATA 2006) set
 const double PI = 3.14159265358979323846;
 const double SMALL = 1.0e-15;
 const double VSMALL = 1.0e-300;
@@ -1293,6 +1294,32 @@ struct Oracle {
             else if (name == "nColls") v = A[ACC_NCOLLS];
             else if (name == "measuredCollisionRate")
                 v = (N > SMALL && nT > 0) ? A[ACC_NCOLLS] * FN / (N * FN * spec.delta_t) : 0.0;
+            else if (name == "Ma" || name == "rhoMError" || name == "UError" || name == "TError" ||
+                     name == "pError") {
+                // dsmcVolFields.C:1625-1661 and 1859-1873
+                double Ma = 0, gamma = 0, particleCv = 0;
+                if (N > SMALL && Ttra > SMALL) {
+                    double molarCv = 0, molarCp = 0, mMol = 0;
+                    for (int s = 0; s < spec.n_species; ++s) {
+                        const double Xs = A[ACC_COMMON + SACC_PER_SPECIES * s + SACC_N] / N;
+                        mMol += Xs * sp[s].m;
+                        molarCv += Xs * (3.0 + sp[s].rotDof);
+                        molarCp += Xs * (5.0 + sp[s].rotDof);
+                    }
+                    particleCv = molarCv / NAvo;
+                    gamma = molarCp / molarCv;
+                    Ma = std::sqrt(Ux * Ux + Uy * Uy + Uz * Uz) / std::sqrt(gamma * kB / mMol * Ttra);
+                }
+                const double nMean = (N > 1e-3 && nT > 0) ? N / nT : 0.001;
+                const double deno = std::sqrt(nMean * nT);
+                const bool ok = nMean > SMALL && Ma > SMALL && gamma > SMALL && particleCv > SMALL;
+                if (name == "Ma") v = Ma;
+                else if (!ok) v = 0.0;
+                else if (name == "rhoMError") v = 1.0 / deno;
+                else if (name == "UError") v = 1.0 / (deno * Ma * std::sqrt(gamma));
+                else if (name == "TError") v = std::sqrt(kB / particleCv) / deno;
+                else v = std::sqrt(gamma) / deno;
+            }
             else if (name == "meanCollisionRate" || name == "mfp") {
                 double mfp = 0, mcr = 0;
                 if (Ttra > 1.0 && nT > 0) {

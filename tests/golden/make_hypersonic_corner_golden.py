@@ -54,7 +54,8 @@ def main():
         sys.exit(f"usage: python {sys.argv[0]} <reference tree root> (or set HYSTRATH_REFERENCE)")
     d = os.path.join(ref, "run/hyStrath/dsmcFoam+/hypersonicCorner/backup-0.003")
     fields = {}
-    for name in ("rhoN_Ar", "rhoM_Ar", "Ttra_Ar", "p_Ar", "U_Ar", "dsmcSigmaTcRMax", "dsmcNMean_Ar", "mfp_Ar"):
+    for name in ("rhoN_Ar", "rhoM_Ar", "Ttra_Ar", "p_Ar", "U_Ar", "dsmcSigmaTcRMax", "dsmcNMean_Ar", "mfp_Ar",
+                 "Ma_Ar"):
         v = to_cartesian(read_internal(os.path.join(d, name)))
         fields[name] = v.astype(np.float32)
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "hypersonic_corner_0.003.npz")

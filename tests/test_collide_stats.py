@@ -62,8 +62,11 @@ def _lb_energies(cloud_factory, seeds, checkpoints):
 
 def test_gpu_lb_relaxation_matches_oracle(gpu_lib, oracle_mod):
     """N2 heat bath (config 1 at 8^3 cells): translational, rotational and
-    vibrational energy histories of GPU and CPU agree within 2 standard
-    errors at every checkpoint (6 seeds each)."""
+    vibrational energy histories of GPU and CPU, 12 seeds each: the
+    differences of the seed means in units of their standard error, at 4
+    checkpoints x 3 energies, have no more values above 2 than the t
+    distribution leaves room for (at most 2 of 12: 5% expected, P(3 or
+    more) = 2%) and none above 3.5."""
     from hystrath_gb300.dsmc import DsmcCloud
 
     def gpu(sd):
@@ -77,16 +80,19 @@ def test_gpu_lb_relaxation_matches_oracle(gpu_lib, oracle_mod):
         return o
 
     checkpoints = [20, 60, 150, 300]
-    seeds = range(6)
+    seeds = range(12)
     eg = _lb_energies(gpu, seeds, checkpoints)
     ec = _lb_energies(cpu, seeds, checkpoints)
     # normalise by the total energy of each run
     tg = eg / eg.sum(axis=2, keepdims=True)
     tc = ec / ec.sum(axis=2, keepdims=True)
+    zs = []
     for k in range(3):
         mg, mc = tg[:, :, k].mean(0), tc[:, :, k].mean(0)
         se = np.sqrt(tg[:, :, k].var(0, ddof=1) / len(seeds) + tc[:, :, k].var(0, ddof=1) / len(seeds))
-        assert np.all(np.abs(mg - mc) <= 2.5 * se + 1e-4), (k, mg, mc, se)
+        zs.append((mg - mc) / se)
+    z = np.abs(np.concatenate(zs))
+    assert np.sum(z > 2.0) <= 2 and z.max() < 3.5, np.round(z, 2)
     # energy is conserved by LB collisions in a specular box
     tot = eg.sum(axis=2)
     assert np.all(np.abs(tot / tot[:, :1] - 1.0) < 1e-10)
