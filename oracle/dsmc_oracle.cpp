@@ -213,6 +213,9 @@ struct Oracle {
     std::vector<int> cellStart, cellCount;      // occupancy after the last sort
     std::vector<double> sigmaTcRMax, remainder;
     std::vector<double> acc;                    // [C][nAcc]
+    // measureHeatFluxShearStress (dsmcVolFields.C:1186-1206): per cell
+    // sum m u_i u_j (xx xy xz yy yz zz), m |U|^2 u_i, E_int u_i; empty when off
+    std::vector<double> mom;                    // [C][12]
     int nAcc;
     std::vector<WallAcc> wall;
     std::vector<double> inflowAcc;              // [nBFaces][nSpecies]
@@ -430,6 +433,7 @@ struct Oracle {
         inflowAcc.assign(nBFaces * s->n_species, 0.0);
         nAcc = ACC_COMMON + SACC_PER_SPECIES * s->n_species;
         acc.assign(C * nAcc, 0.0);
+        if (s->measure_heat_flux_shear_stress) mom.assign(C * 12, 0.0);
         sigmaTcRMax.assign(C, 0.0);
         remainder.assign(C, 0.0);
         for (long long c = 0; c < C; ++c) {
@@ -1161,6 +1165,23 @@ struct Oracle {
                 S[SACC_N] += 1.0;
                 S[SACC_MCC] += linearKE;
                 if (s.nVib) S[SACC_EVIB] += p.vib * kB * s.thetaV;
+                if (!mom.empty()) {
+                    double* Mo = &mom[c * 12];
+                    const double u = p.U[0], v = p.U[1], w = p.U[2];
+                    const double E = p.erot + (s.nVib ? p.vib * kB * s.thetaV : 0.0);
+                    Mo[0] += mp * u * u;
+                    Mo[1] += mp * u * v;
+                    Mo[2] += mp * u * w;
+                    Mo[3] += mp * v * v;
+                    Mo[4] += mp * v * w;
+                    Mo[5] += mp * w * w;
+                    Mo[6] += linearKE * u;
+                    Mo[7] += linearKE * v;
+                    Mo[8] += linearKE * w;
+                    Mo[9] += E * u;
+                    Mo[10] += E * v;
+                    Mo[11] += E * w;
+                }
             }
         }
         (void)ns;
@@ -1294,6 +1315,34 @@ struct Oracle {
             else if (name == "nColls") v = A[ACC_NCOLLS];
             else if (name == "measuredCollisionRate")
                 v = (N > SMALL && nT > 0) ? A[ACC_NCOLLS] * FN / (N * FN * spec.delta_t) : 0.0;
+            else if (name.rfind("pressureTensor_", 0) == 0 || name.rfind("shearStressTensor_", 0) == 0 ||
+                     name.rfind("heatFluxVector_", 0) == 0) {
+                // dsmcVolFields.C:1511-1607
+                if (mom.empty()) return false;
+                const double* Mo = &mom[c * 12];
+                double E = A[ACC_EROT];
+                for (int q = 0; q < spec.n_species; ++q) E += A[ACC_COMMON + SACC_PER_SPECIES * q + SACC_EVIB];
+                const double U[3] = {Ux, Uy, Uz};
+                const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+                double P[6] = {0, 0, 0, 0, 0, 0};
+                if (N > SMALL && nT > 0)
+                    for (int k = 0; k < 6; ++k) P[k] = rhoN / N * (Mo[k] - A[ACC_M] * U[ia[k]] * U[ib[k]]);
+                static const char* comp[6] = {"xx", "xy", "xz", "yy", "yz", "zz"};
+                v = 0.0;
+                for (int k = 0; k < 6; ++k) {
+                    if (name == std::string("pressureTensor_") + comp[k]) v = P[k];
+                    if (name == std::string("shearStressTensor_") + comp[k])
+                        v = -P[k] + (ia[k] == ib[k] ? (P[0] + P[3] + P[5]) / 3.0 : 0.0);
+                }
+                const int row[3][3] = {{0, 1, 2}, {1, 3, 4}, {2, 4, 5}};
+                for (int i = 0; i < 3; ++i) {
+                    if (name != std::string("heatFluxVector_") + "xyz"[i]) continue;
+                    v = (N > SMALL && nT > 0)
+                            ? rhoN / N * (0.5 * Mo[6 + i] - 0.5 * A[ACC_MCC] * U[i] + Mo[9 + i] - E * U[i]) -
+                                  P[row[i][0]] * U[0] - P[row[i][1]] * U[1] - P[row[i][2]] * U[2]
+                            : 0.0;
+                }
+            }
             else if (name == "Ma" || name == "rhoMError" || name == "UError" || name == "TError" ||
                      name == "pError") {
                 // dsmcVolFields.C:1625-1661 and 1859-1873

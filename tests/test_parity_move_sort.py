@@ -260,3 +260,36 @@ def test_move_sort_channel_full_size_developed(gpu_lib, oracle_mod):
             np.testing.assert_array_equal(fa, fb)
         else:
             np.testing.assert_allclose(fa, fb, rtol=1e-12, atol=1e-40)
+
+
+def test_derived_fields_match_oracle(gpu_lib, oracle_mod):
+    """Mach number, the statistical error fields and the measureHeatFluxShearStress
+    tensors (dsmcVolFields.C:1511-1661, 1859-1873) of the Mach-10 channel's
+    initial state after one sample and one move: GPU fixed-point moments
+    against the oracle's FP64 sums, within 1e-9 of each field's scale."""
+    s = S.config2(seed=41, scale=8)
+    s.measure_heat_flux_shear_stress = 1
+    s.measure_errors = 1
+    g, o, _ = _pair(s, gpu_lib, oracle_mod)
+    for _ in range(2):
+        g.run_phases(S.PHASE_SAMPLE)
+        o.run_phases(S.PHASE_SAMPLE)
+    names = ["Ma", "rhoMError", "UError", "TError", "pError"]
+    names += [f"pressureTensor_{c}" for c in ("xx", "xy", "xz", "yy", "yz", "zz")]
+    names += [f"shearStressTensor_{c}" for c in ("xx", "xy", "xz", "yy", "yz", "zz")]
+    names += [f"heatFluxVector_{c}" for c in "xyz"]
+    ma = g.field("Ma")
+    assert 9.0 < np.median(ma[ma > 0]) < 11.0
+    for f in names:
+        a, b = g.field(f), o.field(f)
+        scale = max(np.abs(b).max(), 1e-300)
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * scale, err_msg=f)
+
+
+def test_heat_flux_fields_need_the_case_switch(gpu_lib):
+    from hystrath_gb300.dsmc import DsmcCloud, DsmcError
+    g = DsmcCloud(S.config0(seed=3))
+    g.initialise()
+    g.evolve(1)
+    with pytest.raises(DsmcError):
+        g.field("heatFluxVector_x")
