@@ -726,6 +726,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.feat, cs.C))) return rc;
     if ((rc = dalloc(h, &B.pred, cs.C))) return rc;
     if ((rc = dalloc(h, &B.useR, cs.C))) return rc;
+    if ((rc = dalloc(h, &B.exceed, cs.C))) return rc;
     if ((rc = dalloc(h, &B.smaxSel, cs.C))) return rc;
     if ((rc = dalloc(h, &B.slowList, cap))) return rc;
     if ((rc = dalloc(h, &B.sortSrc, cap))) return rc;
@@ -1451,6 +1452,7 @@ int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float mar
     // every cell starts on the running maximum until the first prediction
     CUDA_TRY(h, cudaMemset(h->B.pred, 0, sizeof(float) * h->cs.C));
     CUDA_TRY(h, cudaMemset(h->B.useR, 1, h->cs.C));
+    CUDA_TRY(h, cudaMemset(h->B.exceed, 0, sizeof(float) * h->cs.C));
     return DSMC_OK;
 }
 

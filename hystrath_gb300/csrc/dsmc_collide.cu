@@ -491,7 +491,7 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
         tile::k_sbt_select<<<(int)selBlocks, 256, 0, st>>>(cs, B.start, B.ctr, B.ncCell, slotCount);
     else
         tile::k_ntc_select<<<(int)selBlocks, 256, 0, st>>>(cs, B.start, B.smax, B.rem, B.ctr, B.ncCell, slotCount,
-                                                            learned, B.pred, B.useR, B.smaxSel);
+                                                            learned, B.pred, B.useR, B.exceed, B.smaxSel);
     tile::k_ntc_buckets<<<1, 1, 0, st>>>(B.ctr, slotCount, slotCursor);
     tile::k_ntc_list<<<(int)selBlocks, 256, 0, st>>>(cs.C, B.start, B.ncCell, slotCursor, B.work, B.bigList, B.ctr,
                                                       sbt ? 1 : 0);
@@ -506,11 +506,11 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
     }
     tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
                                                                 B.perm, B.subs, learned, B.smaxSel, B.useR,
-                                                                B.obsMax, B.audit);
+                                                                B.exceed, B.obsMax, B.audit);
     if (marks) cudaEventRecord(marks[1], st);
     const int L = B.cfg.lightCells;
     tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * sizeof(tile::LightPicks), st>>>(
-        cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.obsMax, B.audit);
+        cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.exceed, B.obsMax, B.audit);
 }
 
 void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,

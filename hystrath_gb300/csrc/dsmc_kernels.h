@@ -63,6 +63,7 @@ struct StepBuffers {
     float4* feat;             // [C] log n, log T_tr, speed ratio, valid
     float* pred;              // [C] predicted (sigma_T c_R)max
     unsigned char* useR;      // [C] 1: the cell has fallen back to the running maximum
+    float* exceed;            // [C] largest product seen above a prediction (0: none)
     double* smaxSel;          // [C] the maximum this step's selection used
     // selection audit (null when off): per cell, summed over candidates,
     // x = sigma_T c_R / max (the expected acceptances) and

@@ -78,12 +78,14 @@ __device__ __forceinline__ int get16(const uint4& w, int s) {
 // selectedPairs and the remainder, one thread per cell; the candidate count
 // of each cell is kept for k_ntc_list and counted per slot
 // learned: the maximum is the prediction unless the cell has fallen back to
-// the running maximum (or has no prediction); it is kept in smaxSel for the
+// the running maximum, has no prediction, or saw a product above an earlier
+// prediction that this one does not cover (the fallback is kept until a
+// prediction covers the largest such product); it is kept in smaxSel for the
 // acceptance tests of this step
 __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const double* __restrict__ smax, double* rem,
                              Counters* ctr, int* ncCell, unsigned* slotCount, int learned,
                              const float* __restrict__ pred, const unsigned char* __restrict__ useR,
-                             double* smaxSel) {
+                             const float* __restrict__ exceed, double* smaxSel) {
     __shared__ unsigned hist[2 * NBUCKET];
     if (threadIdx.x < 2 * NBUCKET) hist[threadIdx.x] = 0;
     __syncthreads();
@@ -97,7 +99,7 @@ __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const do
             double sm = smax[c];
             if (learned) {
                 const float pv = pred[c];
-                if (!useR[c] && pv > 0.f && pv < 3.0e38f) sm = (double)pv;
+                if (!useR[c] && pv > 0.f && pv < 3.0e38f && pv >= exceed[c]) sm = (double)pv;
                 smaxSel[c] = sm;
             }
             const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cell_volume(cs, c);
@@ -464,11 +466,14 @@ __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& 
 // training, and a learned cell whose prediction was exceeded falls back to
 // the running maximum until the next prediction.
 __device__ __forceinline__ void cell_epilogue(double* smax, long long c, double R, double smax0, double stepMax,
-                                              int learned, unsigned char* useR, float* obsMax, double2* audit,
-                                              float2 au) {
+                                              int learned, unsigned char* useR, float* exceed, float* obsMax,
+                                              double2* audit, float2 au) {
     if (stepMax > R) smax[c] = stepMax;
     obsMax[c] = (float)stepMax;
-    if (learned && stepMax > smax0) useR[c] = 1;
+    if (learned && stepMax > smax0) {
+        useR[c] = 1;
+        if ((float)stepMax > exceed[c]) exceed[c] = (float)stepMax;
+    }
     if (audit) {
         double2 v = audit[c];
         v.x += (double)au.x;
@@ -483,7 +488,7 @@ __device__ __forceinline__ uint32_t cand_tag(int k) { return (uint32_t)TAG_COLLI
 __global__ void __launch_bounds__(WARPS * 32)
 k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, const uint16_t* __restrict__ perm, const uint4* __restrict__ subs,
-                int learned, const double* __restrict__ smaxSel, unsigned char* useR, float* obsMax,
+                int learned, const double* __restrict__ smaxSel, unsigned char* useR, float* exceed, float* obsMax,
                 double2* audit) {
     const unsigned lane = lane_id();
     const uint32_t step = (uint32_t)ctr->step;
@@ -543,7 +548,7 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
             }
         }
         if (lane == 0) {
-            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax, audit, au);
+            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, exceed, obsMax, audit, au);
             if (coll) {
                 acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
                 acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
@@ -606,7 +611,7 @@ __device__ __forceinline__ int warp_argmin(uint32_t hA, bool vA, uint32_t hB, bo
 __global__ void __launch_bounds__(128, 4)
 k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, int learned, const double* __restrict__ smaxSel, unsigned char* useR,
-                float* obsMax, double2* audit) {
+                float* exceed, float* obsMax, double2* audit) {
     extern __shared__ __align__(16) unsigned char lightSmem[];
     LightPicks& pk = reinterpret_cast<LightPicks*>(lightSmem)[threadIdx.x >> 5];
     const int lane = (int)(threadIdx.x & 31u);
@@ -733,7 +738,7 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
                     ++coll;
                 }
             }
-            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, obsMax, audit, au);
+            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, exceed, obsMax, audit, au);
             if (coll) {
                 acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
                 acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;

@@ -61,12 +61,14 @@ def _lb_energies(cloud_factory, seeds, checkpoints):
 
 
 def test_gpu_lb_relaxation_matches_oracle(gpu_lib, oracle_mod):
-    """N2 heat bath (config 1 at 8^3 cells): translational, rotational and
-    vibrational energy histories of GPU and CPU, 12 seeds each: the
-    differences of the seed means in units of their standard error, at 4
-    checkpoints x 3 energies, have no more values above 2 than the t
-    distribution leaves room for (at most 2 of 12: 5% expected, P(3 or
-    more) = 2%) and none above 3.5."""
+    """N2 heat bath (config 1 at 8^3 cells, 16 seeds per side): the
+    rotational and vibrational energy fractions of GPU and CPU at 4
+    checkpoints of the relaxation from 10^4 K (the translational fraction is
+    their complement, so it adds nothing).  In units of the standard error of
+    the difference of the seed means, with no absolute slack: at most 2 of
+    the 8 values above 2 and none above 3.5, and Hotelling's T^2 over the 8
+    (the values are correlated in time) with p above 1e-3."""
+    from scipy.stats import f as f_dist
     from hystrath_gb300.dsmc import DsmcCloud
 
     def gpu(sd):
@@ -75,24 +77,28 @@ def test_gpu_lb_relaxation_matches_oracle(gpu_lib, oracle_mod):
         return g
 
     def cpu(sd):
-        o = oracle_mod.OracleCloud(S.config1(seed=200 + sd, n=8), threads=4)
+        o = oracle_mod.OracleCloud(S.config1(seed=200 + sd, n=8), threads=8)
         o.initialise()
         return o
 
     checkpoints = [20, 60, 150, 300]
-    seeds = range(12)
+    seeds = range(16)
     eg = _lb_energies(gpu, seeds, checkpoints)
     ec = _lb_energies(cpu, seeds, checkpoints)
-    # normalise by the total energy of each run
-    tg = eg / eg.sum(axis=2, keepdims=True)
-    tc = ec / ec.sum(axis=2, keepdims=True)
-    zs = []
-    for k in range(3):
-        mg, mc = tg[:, :, k].mean(0), tc[:, :, k].mean(0)
-        se = np.sqrt(tg[:, :, k].var(0, ddof=1) / len(seeds) + tc[:, :, k].var(0, ddof=1) / len(seeds))
-        zs.append((mg - mc) / se)
-    z = np.abs(np.concatenate(zs))
+    # fractions of each run's total energy: rotational and vibrational
+    xg = (eg / eg.sum(axis=2, keepdims=True))[:, :, 1:].reshape(len(seeds), -1)
+    xc = (ec / ec.sum(axis=2, keepdims=True))[:, :, 1:].reshape(len(seeds), -1)
+    n1, n2, p = len(xg), len(xc), xg.shape[1]
+    d = xg.mean(0) - xc.mean(0)
+    se = np.sqrt(xg.var(0, ddof=1) / n1 + xc.var(0, ddof=1) / n2)
+    z = np.abs(d / se)
     assert np.sum(z > 2.0) <= 2 and z.max() < 3.5, np.round(z, 2)
+    # Hotelling's two-sample T^2 with the pooled covariance
+    Sp = ((n1 - 1) * np.cov(xg, rowvar=False) + (n2 - 1) * np.cov(xc, rowvar=False)) / (n1 + n2 - 2)
+    t2 = (n1 * n2) / (n1 + n2) * d @ np.linalg.solve(Sp, d)
+    F = (n1 + n2 - p - 1) / (p * (n1 + n2 - 2)) * t2
+    pval = float(f_dist.sf(F, p, n1 + n2 - p - 1))
+    assert pval > 1e-3, (pval, np.round(z, 2))
     # energy is conserved by LB collisions in a specular box
     tot = eg.sum(axis=2)
     assert np.all(np.abs(tot / tot[:, :1] - 1.0) < 1e-10)
