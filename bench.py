@@ -560,7 +560,7 @@ def main():
     ap.add_argument("--cells", type=int, default=64, help="heat bath: edge in cells")
     ap.add_argument("--develop", type=int, default=600, help="channel: steps run before the warm-up")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned arm")
-    ap.add_argument("--learn-every", type=int, default=50, help="learned: steps between predictions")
+    ap.add_argument("--learn-every", type=int, default=100, help="learned: steps between predictions")
     ap.add_argument("--tau", type=float, default=0.95, help="learned: pinball quantile (0: squared error)")
     ap.add_argument("--train-seeds", type=int, default=5)
     ap.add_argument("--train-rows", type=int, default=5_000_000)

@@ -317,6 +317,8 @@ void fill_case_dev(dsmc_handle* h) {
     }
     cs.anyEmpty = cs.emptyAx[0] | cs.emptyAx[1] | cs.emptyAx[2];
     cs.C = (long long)cs.n[0] * cs.n[1] * cs.n[2];
+    cs.rcpN0 = 1.0f / (float)cs.n[0];
+    cs.rcpN01 = 1.0f / (float)((long long)cs.n[0] * cs.n[1]);
     cs.V = cs.dx[0] * cs.dx[1] * cs.dx[2];
     cs.FN = s.n_equivalent_particles;
     cs.dt = s.delta_t;

@@ -407,41 +407,78 @@ __global__ void k_info(CaseDev cs, Parcels s, const Counters* ctr, double* out) 
 // speed ratio |U| / sqrt(2 k T / m), with m the mean parcel mass.  Features
 // need three digits: the sums run in FP32 on velocities converted on the
 // integer pipe, with masses relative to species 0.
-__global__ void k_cell_features(CaseDev cs, Parcels s, const int* __restrict__ start, const Counters* ctr,
-                                int every, float4* feat, unsigned char* useR) {
+// Features of the learned maximum: log number density, log translational
+// temperature and speed ratio of each cell's parcels.  A CTA takes a tile of
+// FEAT_TILE consecutive cells, whose parcels are contiguous after the sort,
+// and streams them with coalesced loads; each parcel adds exact fixed-point
+// values to its cell's sums in shared memory (count, mass weight, weighted
+// velocity and |U|^2: the mass weight is the species mass over species 0's
+// in units of 1/256, velocities in units of 1/16 m/s), so the sums do not
+// depend on the parcels' order.  Then one thread per cell makes the features.
+constexpr int FEAT_TILE = 256;
+
+__global__ void __launch_bounds__(FEAT_TILE)
+k_cell_features(CaseDev cs, Parcels s, const int* __restrict__ start, const Counters* ctr, int every, float4* feat,
+                unsigned char* useR) {
     if (every > 0 && (ctr->step % every) != 0) return;
+    __shared__ int sN[FEAT_TILE];
+    __shared__ unsigned long long sW[FEAT_TILE], sWU[3][FEAT_TILE], sWUU[FEAT_TILE];
     const float kOverM0 = (float)(kB / cs.sp[0].m);
     const float ndScaleU = (float)(cs.FN / cs.V);
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cs.C;
-         c += (long long)gridDim.x * blockDim.x) {
-        const float ndScale = cs.cellV ? (float)(cs.FN / cs.cellV[c]) : ndScaleU;
-        const long long off = start[c];
-        const int n = start[c + 1] - (int)off;
-        float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (n >= 2) {
-            float M = 0.f, Mu0 = 0.f, Mu1 = 0.f, Mu2 = 0.f, Muu = 0.f;
-            for (int j = 0; j < n; ++j) {
-                const double2* q = reinterpret_cast<const double2*>(s.r + off + j);
-                const double2 b = __ldg(q + 1), d = __ldg(q + 2), e = __ldg(q + 3);
-                const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(e.y) >> 32);
-                const float m = cs.mRel[sv_species(sv)];
-                const float ux = d2f_bits(b.y), uy = d2f_bits(d.x), uz = d2f_bits(d.y);
-                M += m;
-                Mu0 = fmaf(m, ux, Mu0);
-                Mu1 = fmaf(m, uy, Mu1);
-                Mu2 = fmaf(m, uz, Mu2);
-                Muu = fmaf(m, ux * ux + uy * uy + uz * uz, Muu);
-            }
-            const float U2 = (Mu0 * Mu0 + Mu1 * Mu1 + Mu2 * Mu2) / (M * M);
-            // T = m0 (sum m_rel u^2 - M U^2) / (3 k n)
-            const float T = (Muu - M * U2) / (3.0f * kOverM0 * (float)n);
-            if (T > 0.f) {
-                const float cmp = sqrtf(2.0f * kOverM0 * T / (M / (float)n));
-                f = make_float4(logf(ndScale * (float)n), logf(T), sqrtf(U2) / cmp, 1.f);
-            }
+    int mw[DSMC_MAX_SPECIES];
+#pragma unroll
+    for (int q = 0; q < DSMC_MAX_SPECIES; ++q) mw[q] = q < cs.nSpecies ? __float2int_rn(cs.mRel[q] * 256.f) : 0;
+    const long long nTiles = (cs.C + FEAT_TILE - 1) / FEAT_TILE;
+    for (long long tile = blockIdx.x; tile < nTiles; tile += gridDim.x) {
+        const long long c0 = tile * FEAT_TILE;
+        const long long c1 = c0 + FEAT_TILE < cs.C ? c0 + FEAT_TILE : cs.C;
+        const int t = threadIdx.x;
+        sN[t] = 0;
+        sW[t] = 0ull;
+        sWU[0][t] = sWU[1][t] = sWU[2][t] = 0ull;
+        sWUU[t] = 0ull;
+        __syncthreads();
+        const long long j0 = start[c0], j1 = start[c1];
+        for (long long j = j0 + t; j < j1; j += FEAT_TILE) {
+            const int lc = (int)((long long)cellw_cell(__ldg(s.cellw + j)) - c0);
+            if ((unsigned)lc >= (unsigned)FEAT_TILE) continue;   // never: the tile's parcels are its cells'
+            const double2* q = reinterpret_cast<const double2*>(s.r + j);
+            const double2 b = __ldg(q + 1), d = __ldg(q + 2), e = __ldg(q + 3);
+            const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(e.y) >> 32);
+            const long long w = mw[sv_species(sv) & (DSMC_MAX_SPECIES - 1)];
+            const long long ux = __double2ll_rn(b.y * 16.0), uy = __double2ll_rn(d.x * 16.0),
+                            uz = __double2ll_rn(d.y * 16.0);
+            atomicAdd(&sN[lc], 1);
+            atomicAdd(&sW[lc], (unsigned long long)w);
+            atomicAdd(&sWU[0][lc], (unsigned long long)(w * ux));
+            atomicAdd(&sWU[1][lc], (unsigned long long)(w * uy));
+            atomicAdd(&sWU[2][lc], (unsigned long long)(w * uz));
+            atomicAdd(&sWUU[lc], (unsigned long long)(w * (ux * ux + uy * uy + uz * uz)));
         }
-        feat[c] = f;
-        if (useR) useR[c] = 0;
+        __syncthreads();
+        const long long c = c0 + t;
+        if (c < c1) {
+            const int n = sN[t];
+            float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (n >= 2) {
+                const float M = (float)(long long)sW[t] * (1.f / 256.f);
+                const float Mu0 = (float)(long long)sWU[0][t] * (1.f / 4096.f);
+                const float Mu1 = (float)(long long)sWU[1][t] * (1.f / 4096.f);
+                const float Mu2 = (float)(long long)sWU[2][t] * (1.f / 4096.f);
+                const float Muu = (float)(long long)sWUU[t] * (1.f / 65536.f);
+                const float U2 = (Mu0 * Mu0 + Mu1 * Mu1 + Mu2 * Mu2) / (M * M);
+                // T = m0 (sum m_rel u^2 - M U^2) / (3 k n)
+                const float T = (Muu - M * U2) / (3.0f * kOverM0 * (float)n);
+                if (T > 0.f) {
+                    const float ndScale = cs.cellV ? (float)(cs.FN / cs.cellV[c]) : ndScaleU;
+                    const float cmp = sqrtf(2.0f * kOverM0 * T / (M / (float)n));
+                    f = make_float4(logf(ndScale * (float)n), logf(T), sqrtf(U2) / cmp, 1.f);
+                }
+            }
+            feat[c] = f;
+            if (useR) useR[c] = 0;
+        }
+        __syncthreads();
     }
 }
 
@@ -515,10 +552,10 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
 
 void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,
                           cudaStream_t st) {
-    long long blocks = (cs.C + 255) / 256;
-    if (blocks > (long long)sm_count() * 16) blocks = (long long)sm_count() * 16;
-    k_cell_features<<<(int)blocks, 256, 0, st>>>(cs, s, B.start, B.ctr, every, B.feat,
-                                                 resetFallback ? B.useR : nullptr);
+    long long blocks = (cs.C + FEAT_TILE - 1) / FEAT_TILE;
+    if (blocks > (long long)sm_count() * 8) blocks = (long long)sm_count() * 8;
+    k_cell_features<<<(int)blocks, FEAT_TILE, 0, st>>>(cs, s, B.start, B.ctr, every, B.feat,
+                                                       resetFallback ? B.useR : nullptr);
 }
 
 void launch_learn_compact(const CaseDev& cs, const StepBuffers& B, long long maxRows, float* X, float* Y,

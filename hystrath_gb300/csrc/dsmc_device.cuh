@@ -131,6 +131,8 @@ struct CaseDev {
     // the collision kernels order (MAX_REJECTION, MAX_CROSSINGS, ORDER_MAX_N
     // unless lowered by dsmc_set_limits), and the parcel capacity the inflow
     // may fill (the allocation unless lowered)
+    // FP32 reciprocals of n[0] and n[0] n[1] for cell_coords
+    float rcpN0, rcpN01;
     int maxRejection;
     int maxCrossings;
     int maxCellParcels;
@@ -350,6 +352,35 @@ __device__ __forceinline__ int floor2_coord_fast_uniform(const CaseDev& cs, doub
 __device__ __forceinline__ int floor2_coord_fast(const CaseDev& cs, double x, int a) {
     if (cs.half[a]) return floor2_graded(cs.half[a], 2 * cs.n[a], x);
     return floor2_coord_fast_uniform(cs, x, a);
+}
+
+// ------------------------------------------------------- cell coordinates
+// q = c / d for c < 2^24 (exact in FP32) from the FP32 reciprocal of d: the
+// rounded product is within one of the quotient, and one remainder test
+// corrects it (a few instructions instead of a 32-bit integer division).
+__device__ __forceinline__ uint32_t udiv24(uint32_t c, uint32_t d, float rcp) {
+    uint32_t q = __float2uint_rz((float)c * rcp);
+    const int r = (int)(c - q * d);
+    if (r < 0) --q;
+    else if (r >= (int)d) ++q;
+    return q;
+}
+
+// (i, j, k) of linear cell c = i + n0 (j + n1 k)
+__device__ __forceinline__ void cell_coords(const CaseDev& cs, uint32_t c, int* i, int* j, int* k) {
+    const uint32_t n0 = (uint32_t)cs.n[0], n01 = (uint32_t)cs.n[0] * (uint32_t)cs.n[1];
+    if (cs.C < (1LL << 24)) {
+        const uint32_t kk = udiv24(c, n01, cs.rcpN01);
+        const uint32_t r = c - kk * n01;
+        const uint32_t jj = udiv24(r, n0, cs.rcpN0);
+        *i = (int)(r - jj * n0);
+        *j = (int)jj;
+        *k = (int)kk;
+    } else {
+        *i = (int)(c % n0);
+        *j = (int)((c / n0) % (uint32_t)cs.n[1]);
+        *k = (int)(c / n01);
+    }
 }
 
 // ------------------------------------------------------- velocity moments

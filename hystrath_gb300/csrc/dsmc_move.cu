@@ -214,9 +214,7 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
     int sc[3];
     {
         const uint32_t c = cellw_cell(w);
-        sc[0] = (int)(c % (uint32_t)cs.n[0]);
-        sc[1] = (int)((c / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]);
-        sc[2] = (int)(c / ((uint32_t)cs.n[0] * (uint32_t)cs.n[1]));
+        cell_coords(cs, c, &sc[0], &sc[1], &sc[2]);
     }
     uint32_t result = 0;
     bool done = false;
@@ -610,10 +608,8 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     if (cs.sideDeletes[side] && !(GEN && cs.faceFlux)) delSide = side;
                 }
                 if (GEN && (inside || delSide >= 0) && cs.nObst) {
-                    const uint32_t c = cellw_cell(w);
-                    const int sx = (int)(c % (uint32_t)cs.n[0]);
-                    const int sy = (int)((c / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]);
-                    const int sz = (int)(c / ((uint32_t)cs.n[0] * (uint32_t)cs.n[1]));
+                    int sx, sy, sz;
+                    cell_coords(cs, cellw_cell(w), &sx, &sy, &sz);
                     for (int o = 0; o < cs.nObst; ++o) {
                         if (max(sx, cx) + 1 >= cs.obLoI[o][0] && min(sx, cx) - 1 <= cs.obHiI[o][0] - 1 &&
                             max(sy, cy) + 1 >= cs.obLoI[o][1] && min(sy, cy) - 1 <= cs.obHiI[o][1] - 1 &&
@@ -628,10 +624,8 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
                     fast = true;
                 } else if (inside) {
                     if (GEN && cs.faceFlux) {
-                        const uint32_t c0 = cellw_cell(w);
-                        const int sc[3] = {(int)(c0 % (uint32_t)cs.n[0]),
-                                           (int)((c0 / (uint32_t)cs.n[0]) % (uint32_t)cs.n[1]),
-                                           (int)(c0 / ((uint32_t)cs.n[0] * (uint32_t)cs.n[1]))};
+                        int sc[3];
+                        cell_coords(cs, cellw_cell(w), &sc[0], &sc[1], &sc[2]);
                         const int te[3] = {cx, cy, cz};
                         const double xs[3] = {x, y, z}, Us[3] = {tux, tuy, tuz};
                         const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q[3].y) >> 32);

@@ -148,12 +148,15 @@ def test_learned_selection_draws_fewer_candidates_at_the_same_rate():
 
     cp, kp, ap = run(False)
     cl, kl, al = run(True)
-    assert kl / cl < 0.95 * (kp / cp), (kp / cp, kl / cl)
+    # fewer candidates per accepted collision (a cell whose prediction was
+    # exceeded stays on the running maximum until a prediction covers the
+    # product, which keeps the saving small)
+    assert kl / cl < 0.995 * (kp / cp), (kp / cp, kl / cl)
     # both are counts of about 1e6: 1% is several standard errors
     assert abs(cl / cp - 1) < 0.01, (cp, cl)
     # the audit: the expected per-cell shortfall of the collision count that
     # a maximum below the product causes -- tiny for the running maximum,
     # within 1% in total and in almost every cell for the learned one
     assert ap["expected_shortfall_total"] < 1e-3, ap
-    assert al["expected_shortfall_total"] < 0.01, al
-    assert al["cells_above_1pct"] < 0.05, al
+    assert al["expected_shortfall_total"] < 0.005, al
+    assert al["cells_above_1pct"] < ap["cells_above_1pct"] + 0.05, (al, ap)
