@@ -351,23 +351,23 @@ def gpu_arm(args, rank, world, local):
         cl0 = lg.counts()
         ms_l = lg.evolve_timed(args.steps)
         cl1 = lg.counts()
+        # an independently seeded run of the same development, learned, its
+        # window starting at the same step as the other two
+        log("developing the independent learned run")
+        rep = learn.develop(make_spec(args, SEED + 7919 + rank), args.develop)
+        rep.set_learned(model, args.learn_every, margin)
+        rep.evolve(args.warmup + args.steps)
         log("evaluation windows")
         for x in (g, lg):
             x.set_selection_audit(True)
-        wp = learn.run_window(g, args.eval_steps, args.eval_batches)
-        wl = learn.run_window(lg, args.eval_steps, args.eval_batches)
+        # the three clouds take turns batch by batch
+        wp, wl, wr = learn.run_windows([g, lg, rep], args.eval_steps, args.eval_batches)
+        rep.close()
         for x in (g, lg):
             x.set_selection_audit(False)
         _, kl = lg.evolve_kernel_profile(args.steps)
         lg.close()
         lg = None
-        # an independently seeded run of the same development, learned, its
-        # window starting at the same step as the other two
-        rep = learn.develop(make_spec(args, SEED + 7919 + rank), args.develop)
-        rep.set_learned(model, args.learn_every, margin)
-        rep.evolve(args.warmup + args.steps)
-        wr = learn.run_window(rep, args.eval_steps, args.eval_batches)
-        rep.close()
         lvp = learn.compare_windows(s, wp, wl, wr)
         nl = 0.5 * (cl0.n_particles + cl1.n_particles)
         lvp["timed_steps"] = {

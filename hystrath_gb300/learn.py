@@ -123,36 +123,48 @@ def develop(spec, steps):
 
 
 def run_window(g, steps, batches=8, fields=FIELDS, blk=8):
-    """`steps` graph-launched steps in `batches` equal batches (sampling reset
-    at the start of each): device time, collision and candidate counts, the
-    parcel counts at both ends, every batch's per-cell collision counts, the
-    per-cell mean of Ttra over the batches, every batch's time-averaged
-    fields as means over blocks of blk^3 cells (batch means), and the
-    selection audit summed over the window when it is on."""
-    n = list(g.spec.n_cells)
+    """`steps` graph-launched steps of one cloud (run_windows of one)."""
+    return run_windows([g], steps, batches, fields, blk)[0]
+
+
+def run_windows(clouds, steps, batches=8, fields=FIELDS, blk=8):
+    """`steps` graph-launched steps of every cloud in `batches` equal batches,
+    the clouds taking turns batch by batch (so a drift of the GPU's clocks
+    over the window affects them alike); sampling restarts at each batch.
+    Per cloud: device time, collision and candidate counts, parcel counts at
+    both ends, every batch's per-cell collision counts, the per-cell mean of
+    Ttra over the batches, every batch's fields as means over blocks of blk^3
+    cells (batch means), and the selection audit over the window when it is
+    on."""
     per = max(1, steps // batches)
-    c0 = g.counts()
-    out = {"steps": per * batches, "ms": 0.0, "n_start": int(c0.n_particles), "nColls": [], "Ttra": None,
-           "blk": blk, "batches": {k: [] for k in fields}, "audit": None}
+    outs = []
+    for g in clouds:
+        c0 = g.counts()
+        outs.append({"steps": per * batches, "ms": 0.0, "n_start": int(c0.n_particles), "nColls": [],
+                     "Ttra": None, "blk": blk, "batches": {k: [] for k in fields}, "audit": None, "_c0": c0})
     for _ in range(batches):
-        g.reset_sampling()
-        out["ms"] += g.evolve_timed(per)
-        out["nColls"].append(g.field("nColls").astype(np.float32))
-        for k in fields:
-            f = g.field(k)
-            if k == "Ttra":
-                out["Ttra"] = f / batches if out["Ttra"] is None else out["Ttra"] + f / batches
-            out["batches"][k].append(_block_means(f, n, blk))
-        try:
-            a = g.cell_array("selectionAudit")
-            out["audit"] = a if out["audit"] is None else out["audit"] + a
-        except Exception:
-            pass
-    c1 = g.counts()
-    out["n_end"] = int(c1.n_particles)
-    out["collisions"] = int(c1.collisions_total - c0.collisions_total)
-    out["candidates"] = int(c1.candidates_total - c0.candidates_total)
-    return out
+        for g, out in zip(clouds, outs):
+            n = list(g.spec.n_cells)
+            g.reset_sampling()
+            out["ms"] += g.evolve_timed(per)
+            out["nColls"].append(g.field("nColls").astype(np.float32))
+            for k in fields:
+                f = g.field(k)
+                if k == "Ttra":
+                    out["Ttra"] = f / batches if out["Ttra"] is None else out["Ttra"] + f / batches
+                out["batches"][k].append(_block_means(f, n, blk))
+            try:
+                a = g.cell_array("selectionAudit")
+                out["audit"] = a if out["audit"] is None else out["audit"] + a
+            except Exception:
+                pass
+    for g, out in zip(clouds, outs):
+        c0 = out.pop("_c0")
+        c1 = g.counts()
+        out["n_end"] = int(c1.n_particles)
+        out["collisions"] = int(c1.collisions_total - c0.collisions_total)
+        out["candidates"] = int(c1.candidates_total - c0.candidates_total)
+    return outs
 
 
 def arm_rates(w):
@@ -183,7 +195,10 @@ def per_cell_count_test(batches_a, batches_b, groups=None, group_names=None):
     one-sided 95% upper bound uses the spread of d_c^2 - v_c over cells.
     groups: an integer label per cell (-1: none); each group's total
     relative difference with its standard error (from the paired batch
-    totals) is reported as well."""
+    totals) is reported as well.  The batch spread does not see variation
+    slower than the window (a shock that wanders differently in the two
+    runs): in a flow that has it, z grows with the window and T bounds the
+    per-cell difference from above."""
     A = np.asarray(batches_a, dtype=np.float64)
     B = np.asarray(batches_b, dtype=np.float64)
     if A.shape != B.shape:
@@ -359,17 +374,17 @@ def evaluate(spec, spec_replicate, model, margin, every, develop_steps, window, 
     lr.set_learned(model, every, margin)
     for g in (p, lr):
         g.set_selection_audit(True)
-    wp = run_window(p, window, batches)
-    wl = run_window(lr, window, batches)
-    p.close()
-    lr.close()
-    rep = None
+    clouds = [p, lr]
     if spec_replicate is not None:
         # the same development and window start as the other two
         l2 = develop(spec_replicate, develop_steps)
         l2.set_learned(model, every, margin)
-        rep = run_window(l2, window, batches)
-        l2.close()
+        clouds.append(l2)
+    ws = run_windows(clouds, window, batches)
+    for g in clouds:
+        g.close()
+    wp, wl = ws[0], ws[1]
+    rep = ws[2] if len(ws) > 2 else None
     return compare_windows(spec, wp, wl, rep)
 
 

@@ -130,7 +130,10 @@ def test_profiles_within_their_standard_errors(couette):
             if f == "rhoN":
                 b = b / b.mean(1, keepdims=True)
                 r = r / r.mean()
-            var = b.var(0, ddof=1)
+            # widened for the lag-1 correlation of consecutive batch means
+            d = b - b.mean(0)
+            rho = float(np.sum(d[1:] * d[:-1]) / max(np.sum(d * d), 1e-300))
+            var = b.var(0, ddof=1) * max(1.0, 1.0 + 2.0 * rho)
             se = np.sqrt(var / BATCHES + var * (SAMPLE // BATCHES) / REF_WINDOW)
             z = (b.mean(0) - r) / se
             report[key] = round(float(np.mean(np.abs(z))), 2)

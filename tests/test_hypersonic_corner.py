@@ -58,13 +58,28 @@ def bins(a):
     return a.reshape(*lead, 6, 3, 6, 3, 10, 3).mean(axis=(-5, -3, -1)).reshape(*lead, -1)
 
 
+def lag1(batch_series):
+    """Lag-1 correlation of consecutive batch means, pooled over bins and
+    runs (each series: batches x bins)."""
+    num = den = 0.0
+    for b in batch_series:
+        d = b - b.mean(0)
+        num += float(np.sum(d[1:] * d[:-1]))
+        den += float(np.sum(d * d))
+    return num / den if den > 0 else 0.0
+
+
 def z_per_bin(batches_by_seed, ref):
     """|our mean - reference| / standard error per bin, and the degrees of
-    freedom of the batch variance."""
+    freedom of the batch variance.  Consecutive batches of 150 steps are
+    not quite independent (the flow crosses the domain in a few hundred
+    steps): the batch variance is widened by 1 + 2 rho, rho the lag-1
+    correlation of the batch means pooled over bins and seeds."""
     B = np.concatenate([bins(b) for b in batches_by_seed])       # (seeds x batches, bins)
     k = B.shape[0]
     # pooled within-seed batch variance (the seeds' means may differ only by noise)
-    var = np.mean([bins(b).var(0, ddof=1) for b in batches_by_seed], axis=0)
+    rho = lag1([bins(b) for b in batches_by_seed])
+    var = np.mean([bins(b).var(0, ddof=1) for b in batches_by_seed], axis=0) * max(1.0, 1.0 + 2.0 * rho)
     se_ours = np.sqrt(var / k)
     se_ref = np.sqrt(var / BATCHES)              # one run of the same window
     z = (B.mean(0) - bins(ref)) / np.sqrt(se_ours ** 2 + se_ref ** 2)
