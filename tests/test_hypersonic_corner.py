@@ -8,9 +8,10 @@ The stored fields are one statistical realisation, averaged over 1500 steps
 same window in 10 batches of 150 steps.  Two checks:
 - statistical: per bin of 3 x 3 x 3 cells, the difference between our mean
   and the reference in units of its standard error, from batch means (the
-  reference's realisation has the standard error of one of our runs); at
-  most the fraction of |z| > 2 that Student's t with the batches' degrees of
-  freedom gives, plus three of its standard deviations;
+  reference's realisation has the standard error of one of our runs; the
+  batch variance is widened for the lag-1 correlation of consecutive
+  batches); at most the fraction of |z| > 2 that Student's t with the
+  batches' degrees of freedom gives, plus three of its standard deviations;
 - the earlier percent bands: our seeds' RMS deviation from the reference no
   larger than their spread, the mean bias below 0.3%, spanwise-averaged
   x-profiles within 1%."""
