@@ -239,10 +239,12 @@ def roofline_entries(g, s, args, steps, peak, peak_kind):
                 "traffic": round(tb * N) if tb else None,
                 "ms_per_launch": round(ms, 4), "algorithmic_bytes_per_launch": round(by[key])}
 
-    move_ms = per["move"]
+    move_ms = per["move"] + per["move_slow"]
     gather_ms = per["gather"]
     cand_k = {"k_move+k_move_slow": entry("k_move+k_move_slow", "move", move_ms),
               "k_gather": entry("k_gather", "gather", gather_ms)}
+    cand_k["k_move+k_move_slow"]["ms_k_move"] = round(per["move"], 4)
+    cand_k["k_move+k_move_slow"]["ms_k_move_slow"] = round(per["move_slow"], 4)
     dominant = max(cand_k.values(), key=lambda e: e["ms_per_launch"])
     sort_ms = per["scan"] + per["scatter_index"] + per["gather"] + per["finish"]
     ms_ms = move_ms + per["sample"] + sort_ms

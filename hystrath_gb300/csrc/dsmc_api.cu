@@ -481,7 +481,8 @@ enum {
     MK_START = 0,
     MK_ZERO,          // k_zero_step (and the sample flush of a step without a move)
     MK_INFLOW,        // k_inflow_count/scan/fill/commit
-    MK_MOVE,          // k_move, k_move_slow
+    MK_MOVE,          // k_move
+    MK_MOVE_SLOW,     // k_move_slow
     MK_SAMPLE,        // k_sample_done/finalize/flushed
     MK_SCAN,          // k_scan_reduce/top/down (k_count_dev before them without a move)
     MK_SCATTER,       // k_scatter_index
@@ -515,8 +516,9 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
     mark(MK_ZERO);
     if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
     mark(MK_INFLOW);
-    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st);
-    mark(MK_MOVE);
+    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st, ev ? ev[MK_MOVE] : nullptr);
+    else mark(MK_MOVE);
+    mark(MK_MOVE_SLOW);
     if (phases & DSMC_PHASE_MOVE) launch_sample_commit(cs, B, 0, st);
     mark(MK_SAMPLE);
     if (phases & DSMC_PHASE_SORT) {

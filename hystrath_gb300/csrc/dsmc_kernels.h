@@ -101,7 +101,9 @@ struct InflowDev {
 int scan_scratch_ints(long long C);
 
 void launch_count(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
-void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
+// mid (optional): an event recorded between the fast path and the boundary path
+void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st,
+                 cudaEvent_t mid = nullptr);
 void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
 // mid (optional): an event recorded between the index scatter and the gather
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,

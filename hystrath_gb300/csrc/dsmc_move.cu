@@ -240,8 +240,8 @@ __device__ uint32_t move_slow(const CaseDev& cs, const Parcels& s, long long i, 
         for (int o = 0; o < cs.nObst && !obst; ++o) {
             bool ov = true;
             for (int a = 0; a < 3; ++a) {
-                const int mn = min(sc[a], ci[a]) - 1;
-                const int mx = max(sc[a], ci[a]) + 1;
+                const int mn = min(sc[a], ci[a]);
+                const int mx = max(sc[a], ci[a]);
                 if (mx < cs.obLoI[o][a] || mn > cs.obHiI[o][a] - 1) ov = false;
             }
             obst = ov;
@@ -540,6 +540,122 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
 // velocities anyway, in cell order.
 // GEN = false is the instantiation for uniform meshes without reduced-D axes,
 // solid boxes or face tracking: their branches are compiled out.
+// One iteration of k_move for parcel i (lanes with i >= n take part in the
+// warp-collective counts, appends and sample sums without a parcel).  The
+// batched persistent kernel runs the same iterations.
+template <bool GEN>
+__device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, Counters* ctr, int* slowList,
+                                          int* count, long long* sfix, long long i, long long n, uint32_t step,
+                                          int doSample, unsigned& err) {
+    int key = -1;
+    bool slow = false;
+    int skey = -1;
+    double sux = 0, suy = 0, suz = 0, ser = 0;
+    int svb = 0;
+    if (i < n) {
+        const uint32_t w = s.cellw[i];
+        bool fast = false;
+        {
+            const bool fresh = (w & CELLW_FRESH) != 0;
+            double2* q = reinterpret_cast<double2*>(s.r + i);
+            const double2 q0 = q[0], q1 = q[1], q2 = q[2];
+            double x = q0.x, y = q0.y, z = q1.x;
+            const double ux = q1.y, uy = q2.x, uz = q2.y;
+            // tracking velocity (zero along an empty axis, whose coordinate
+            // is held at the mesh centre: dsmcParcel.C:73-84)
+            double tux = ux, tuy = uy, tuz = uz;
+            if (GEN && cs.anyEmpty) {
+                if (cs.emptyAx[0]) { x = cs.mid[0]; tux = 0.0; }
+                if (cs.emptyAx[1]) { y = cs.mid[1]; tuy = 0.0; }
+                if (cs.emptyAx[2]) { z = cs.mid[2]; tuz = 0.0; }
+            }
+            double tr = cs.dt;
+            if (fresh) {
+                // a parcel inserted this step moves for (1 - U) dt
+                // (dsmcParcel.C:52-59), with the draw of the boundary path
+                const uint32_t pid = (uint32_t)__double_as_longlong(q[3].y);
+                Rng r(cs, pid, step, TAG_MOVE);
+                tr = (1.0 - r.u01()) * cs.dt;
+            } else if (doSample) {
+                const double2 q3 = q[3];
+                const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q3.y) >> 32);
+                skey = (int)(cellw_cell(w) * 8u + (uint32_t)sv_species(sv));
+                sux = ux; suy = uy; suz = uz;
+                ser = q3.x;
+                svb = sv_vib(sv);
+            }
+            const double ex = fma(tux, tr, x);
+            const double ey = fma(tuy, tr, y);
+            const double ez = fma(tuz, tr, z);
+            const int c2x = GEN ? floor2_coord_fast(cs, ex, 0) : floor2_coord_fast_uniform(cs, ex, 0);
+            const int c2y = GEN ? floor2_coord_fast(cs, ey, 1) : floor2_coord_fast_uniform(cs, ey, 1);
+            const int c2z = GEN ? floor2_coord_fast(cs, ez, 2) : floor2_coord_fast_uniform(cs, ez, 2);
+            const int cx = c2x >> 1, cy = c2y >> 1, cz = c2z >> 1;
+            const bool inX = (unsigned)cx < (unsigned)cs.n[0], inY = (unsigned)cy < (unsigned)cs.n[1],
+                       inZ = (unsigned)cz < (unsigned)cs.n[2];
+            bool inside = inX && inY && inZ;
+            // leaving through exactly one side whose every face deletes
+            // (dsmcDeletionPatch, no wall measurement): the straight path
+            // stays inside the other two slabs, so that side is the one hit
+            int delSide = -1;
+            if (!inside && (int)inX + (int)inY + (int)inZ == 2) {
+                const int a = !inX ? 0 : !inY ? 1 : 2;
+                const int c2a = a == 0 ? c2x : a == 1 ? c2y : c2z;
+                const int side = 2 * a + (c2a < 0 ? 0 : 1);
+                if (cs.sideDeletes[side] && !(GEN && cs.faceFlux)) delSide = side;
+            }
+            if (GEN && (inside || delSide >= 0) && cs.nObst) {
+                // the straight path stays in the box of cells spanned by its
+                // end cells: one that misses an obstacle's cells on some axis
+                // cannot touch it (a point on a face plane lies in the
+                // obstacle's cell there)
+                int sx, sy, sz;
+                cell_coords(cs, cellw_cell(w), &sx, &sy, &sz);
+                for (int o = 0; o < cs.nObst; ++o) {
+                    if (max(sx, cx) >= cs.obLoI[o][0] && min(sx, cx) <= cs.obHiI[o][0] - 1 &&
+                        max(sy, cy) >= cs.obLoI[o][1] && min(sy, cy) <= cs.obHiI[o][1] - 1 &&
+                        max(sz, cz) >= cs.obLoI[o][2] && min(sz, cz) <= cs.obHiI[o][2] - 1) {
+                        inside = false;
+                        delSide = -1;
+                    }
+                }
+            }
+            if (delSide >= 0) {
+                s.cellw[i] = CELLW_DELETED;
+                fast = true;
+            } else if (inside) {
+                if (GEN && cs.faceFlux) {
+                    int sc[3];
+                    cell_coords(cs, cellw_cell(w), &sc[0], &sc[1], &sc[2]);
+                    const int te[3] = {cx, cy, cz};
+                    const double xs[3] = {x, y, z}, Us[3] = {tux, tuy, tuz};
+                    const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q[3].y) >> 32);
+                    track_internal(cs, xs, Us, sc, te, sv_species(sv));
+                }
+                q[0] = make_double2(ex, ey);
+                s.r[i].z = ez;
+                const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
+                                    (uint32_t)((c2x & 1) | ((c2y & 1) << 1) | ((c2z & 1) << 2));
+                s.cellw[i] = nw;
+                key = (int)(nw >> 3);
+                fast = true;
+            }
+        }
+        slow = !fast;
+    }
+    agg_count(count, key);
+    // warp-aggregated append of the deferred parcels
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, slow);
+    if (m) {
+        const unsigned lane = lane_id();
+        unsigned long long base0 = 0;
+        if (lane == (unsigned)(__ffs(m) - 1)) base0 = atomicAdd(&ctr->nSlow, (unsigned long long)__popc(m));
+        base0 = __shfl_sync(0xFFFFFFFFu, base0, __ffs(m) - 1);
+        if (slow) slowList[base0 + __popc(m & ((1u << lane) - 1u))] = (int)i;
+    }
+    if (doSample) sample_contrib(sfix, cs.C, skey, sux, suy, suz, ser, svb, &err);
+}
+
 template <bool GEN>
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix) {
@@ -548,112 +664,8 @@ k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long lon
     const int doSample = ctr->pendingSample;
     unsigned err = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const long long i = base + threadIdx.x;
-        int key = -1;
-        bool slow = false;
-        int skey = -1;
-        double sux = 0, suy = 0, suz = 0, ser = 0;
-        int svb = 0;
-        if (i < n) {
-            const uint32_t w = s.cellw[i];
-            bool fast = false;
-            {
-                const bool fresh = (w & CELLW_FRESH) != 0;
-                double2* q = reinterpret_cast<double2*>(s.r + i);
-                const double2 q0 = q[0], q1 = q[1], q2 = q[2];
-                double x = q0.x, y = q0.y, z = q1.x;
-                const double ux = q1.y, uy = q2.x, uz = q2.y;
-                // tracking velocity (zero along an empty axis, whose coordinate
-                // is held at the mesh centre: dsmcParcel.C:73-84)
-                double tux = ux, tuy = uy, tuz = uz;
-                if (GEN && cs.anyEmpty) {
-                    if (cs.emptyAx[0]) { x = cs.mid[0]; tux = 0.0; }
-                    if (cs.emptyAx[1]) { y = cs.mid[1]; tuy = 0.0; }
-                    if (cs.emptyAx[2]) { z = cs.mid[2]; tuz = 0.0; }
-                }
-                double tr = cs.dt;
-                if (fresh) {
-                    // a parcel inserted this step moves for (1 - U) dt
-                    // (dsmcParcel.C:52-59), with the draw of the boundary path
-                    const uint32_t pid = (uint32_t)__double_as_longlong(q[3].y);
-                    Rng r(cs, pid, step, TAG_MOVE);
-                    tr = (1.0 - r.u01()) * cs.dt;
-                } else if (doSample) {
-                    const double2 q3 = q[3];
-                    const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q3.y) >> 32);
-                    skey = (int)(cellw_cell(w) * 8u + (uint32_t)sv_species(sv));
-                    sux = ux; suy = uy; suz = uz;
-                    ser = q3.x;
-                    svb = sv_vib(sv);
-                }
-                const double ex = fma(tux, tr, x);
-                const double ey = fma(tuy, tr, y);
-                const double ez = fma(tuz, tr, z);
-                const int c2x = GEN ? floor2_coord_fast(cs, ex, 0) : floor2_coord_fast_uniform(cs, ex, 0);
-                const int c2y = GEN ? floor2_coord_fast(cs, ey, 1) : floor2_coord_fast_uniform(cs, ey, 1);
-                const int c2z = GEN ? floor2_coord_fast(cs, ez, 2) : floor2_coord_fast_uniform(cs, ez, 2);
-                const int cx = c2x >> 1, cy = c2y >> 1, cz = c2z >> 1;
-                const bool inX = (unsigned)cx < (unsigned)cs.n[0], inY = (unsigned)cy < (unsigned)cs.n[1],
-                           inZ = (unsigned)cz < (unsigned)cs.n[2];
-                bool inside = inX && inY && inZ;
-                // leaving through exactly one side whose every face deletes
-                // (dsmcDeletionPatch, no wall measurement): the straight path
-                // stays inside the other two slabs, so that side is the one hit
-                int delSide = -1;
-                if (!inside && (int)inX + (int)inY + (int)inZ == 2) {
-                    const int a = !inX ? 0 : !inY ? 1 : 2;
-                    const int c2a = a == 0 ? c2x : a == 1 ? c2y : c2z;
-                    const int side = 2 * a + (c2a < 0 ? 0 : 1);
-                    if (cs.sideDeletes[side] && !(GEN && cs.faceFlux)) delSide = side;
-                }
-                if (GEN && (inside || delSide >= 0) && cs.nObst) {
-                    int sx, sy, sz;
-                    cell_coords(cs, cellw_cell(w), &sx, &sy, &sz);
-                    for (int o = 0; o < cs.nObst; ++o) {
-                        if (max(sx, cx) + 1 >= cs.obLoI[o][0] && min(sx, cx) - 1 <= cs.obHiI[o][0] - 1 &&
-                            max(sy, cy) + 1 >= cs.obLoI[o][1] && min(sy, cy) - 1 <= cs.obHiI[o][1] - 1 &&
-                            max(sz, cz) + 1 >= cs.obLoI[o][2] && min(sz, cz) - 1 <= cs.obHiI[o][2] - 1) {
-                            inside = false;
-                            delSide = -1;
-                        }
-                    }
-                }
-                if (delSide >= 0) {
-                    s.cellw[i] = CELLW_DELETED;
-                    fast = true;
-                } else if (inside) {
-                    if (GEN && cs.faceFlux) {
-                        int sc[3];
-                        cell_coords(cs, cellw_cell(w), &sc[0], &sc[1], &sc[2]);
-                        const int te[3] = {cx, cy, cz};
-                        const double xs[3] = {x, y, z}, Us[3] = {tux, tuy, tuz};
-                        const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q[3].y) >> 32);
-                        track_internal(cs, xs, Us, sc, te, sv_species(sv));
-                    }
-                    q[0] = make_double2(ex, ey);
-                    s.r[i].z = ez;
-                    const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
-                                        (uint32_t)((c2x & 1) | ((c2y & 1) << 1) | ((c2z & 1) << 2));
-                    s.cellw[i] = nw;
-                    key = (int)(nw >> 3);
-                    fast = true;
-                }
-            }
-            slow = !fast;
-        }
-        agg_count(count, key);
-        // warp-aggregated append of the deferred parcels
-        const unsigned m = __ballot_sync(0xFFFFFFFFu, slow);
-        if (m) {
-            const unsigned lane = lane_id();
-            unsigned long long base0 = 0;
-            if (lane == (unsigned)(__ffs(m) - 1)) base0 = atomicAdd(&ctr->nSlow, (unsigned long long)__popc(m));
-            base0 = __shfl_sync(0xFFFFFFFFu, base0, __ffs(m) - 1);
-            if (slow) slowList[base0 + __popc(m & ((1u << lane) - 1u))] = (int)i;
-        }
-        if (doSample) sample_contrib(sfix, cs.C, skey, sux, suy, suz, ser, svb, &err);
-    }
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride)
+        move_iter<GEN>(cs, s, ctr, slowList, count, sfix, base + threadIdx.x, n, step, doSample, err);
     if (err) atomicOr(&ctr->err, err);
 }
 
@@ -855,41 +867,62 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_down(const int* __restric
 // grouping them first per block of 2048 parcels (a shared hash of the cells
 // present, one slot reservation per block and cell, stores in runs) measured
 // 5% slower on the 64^3 heat bath and 40% on a cooler, collision-heavy one.
+// One iteration of k_scatter_index for parcel i (lanes with i >= n take part
+// in the warp-collective slot reservation without a parcel).
+__device__ __forceinline__ void scatter_iter(const uint32_t* __restrict__ cellw, Counters* ctr,
+                                             const int* __restrict__ start, int* count, int2* __restrict__ sortSrc,
+                                             long long i, long long n) {
+    const unsigned lane = lane_id();
+    int key = -1;
+    uint32_t w = CELLW_DELETED;
+    if (i < n) {
+        w = __ldg(cellw + i);
+        key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
+    }
+    int lo = 0, hi = 0;
+    if (key >= 0) {
+        lo = __ldg(start + key);
+        hi = __ldg(start + key + 1);
+    }
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
+    const int leader = __ffs(peers) - 1;
+    int old = 0;
+    if (key >= 0 && (int)lane == leader) old = atomicSub(&count[key], __popc(peers));
+    old = __shfl_sync(0xFFFFFFFFu, old, leader);
+    if (key >= 0) {
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        const long long slot = (long long)lo + old - 1 - rank;
+        if (slot < lo || slot >= hi) {
+            // histogram and scatter disagree: record, never write out of range
+            atomicOr(&ctr->err, ERRB_BOUNDS);
+            return;
+        }
+        sortSrc[slot] = make_int2((int)i, (int)w);
+    }
+}
+
 __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_scatter_index(const uint32_t* __restrict__ cellw, Counters* ctr,
                                                        const int* __restrict__ start, int* count,
                                                        int2* __restrict__ sortSrc) {
     const long long n = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    const unsigned lane = lane_id();
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride) {
-        const long long i = base + threadIdx.x;
-        int key = -1;
-        uint32_t w = CELLW_DELETED;
-        if (i < n) {
-            w = __ldg(cellw + i);
-            key = (w == CELLW_DELETED) ? -1 : (int)cellw_cell(w);
-        }
-        int lo = 0, hi = 0;
-        if (key >= 0) {
-            lo = __ldg(start + key);
-            hi = __ldg(start + key + 1);
-        }
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, key);
-        const int leader = __ffs(peers) - 1;
-        int old = 0;
-        if (key >= 0 && (int)lane == leader) old = atomicSub(&count[key], __popc(peers));
-        old = __shfl_sync(0xFFFFFFFFu, old, leader);
-        if (key >= 0) {
-            const int rank = __popc(peers & ((1u << lane) - 1u));
-            const long long slot = (long long)lo + old - 1 - rank;
-            if (slot < lo || slot >= hi) {
-                // histogram and scatter disagree: record, never write out of range
-                atomicOr(&ctr->err, ERRB_BOUNDS);
-                continue;
-            }
-            sortSrc[slot] = make_int2((int)i, (int)w);
-        }
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride)
+        scatter_iter(cellw, ctr, start, count, sortSrc, base + threadIdx.x, n);
+}
+
+// One destination slot j of k_gather.
+__device__ __forceinline__ void gather_slot(const Parcels& src, const Parcels& dst, Counters* ctr,
+                                            const int2* __restrict__ sortSrc, long long j, long long nSrc) {
+    const int2 sk = __ldg(sortSrc + j);
+    const long long i = sk.x;
+    if (i < 0 || i >= nSrc) {
+        atomicOr(&ctr->err, ERRB_BOUNDS);
+        return;
     }
+    const Rec p = ldg_rec(src.r + i);
+    st_rec(dst.r + j, p);
+    __stcs(dst.cellw + j, (uint32_t)sk.y);
+    dst.id[j] = p.id;
 }
 
 __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_gather(Parcels src, Parcels dst, Counters* ctr,
@@ -897,18 +930,8 @@ __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_gather(Parcels src, Parc
     const long long n = ctr->nKept;
     const long long nSrc = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
-        const int2 sk = __ldg(sortSrc + j);
-        const long long i = sk.x;
-        if (i < 0 || i >= nSrc) {
-            atomicOr(&ctr->err, ERRB_BOUNDS);
-            continue;
-        }
-        const Rec p = ldg_rec(src.r + i);
-        st_rec(dst.r + j, p);
-        __stcs(dst.cellw + j, (uint32_t)sk.y);
-        dst.id[j] = p.id;
-    }
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
+        gather_slot(src, dst, ctr, sortSrc, j, nSrc);
 }
 
 // Parcels handed over as arrays (positions and velocities n x 3, ERot,
@@ -1245,12 +1268,13 @@ int grid_for(long long n, int threads, int perSmBlocks) {
 
 int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TILE) + 1; }
 
-void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
+void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st, cudaEvent_t mid) {
     const int T = B.cfg.streamThreads;
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
     const bool general = cs.anyEmpty || cs.nObst || cs.faceFlux || cs.half[0] || cs.half[1] || cs.half[2];
     if (general) k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
     else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
+    if (mid) cudaEventRecord(mid, st);
     k_move_slow<<<grid_for(B.capacity, T, 2), T, 0, st>>>(cs, s, B.ctr, B.slowList,
                                                                                B.bfPatch, B.wall, B.count);
 }

@@ -82,6 +82,32 @@ __device__ __forceinline__ int get16(const uint4& w, int s) {
 // prediction that this one does not cover (the fallback is kept until a
 // prediction covers the largest such product); it is kept in smaxSel for the
 // acceptance tests of this step
+// The candidate count of cell c (0 for a cell with fewer than two parcels
+// or one skipped as too dense, with the error bit set).
+__device__ __forceinline__ int select_cell(const CaseDev& cs, const int* __restrict__ start,
+                                           const double* __restrict__ smax, double* rem, int learned,
+                                           const float* __restrict__ pred, const unsigned char* __restrict__ useR,
+                                           const float* __restrict__ exceed, double* smaxSel, long long c, int* n_out,
+                                           unsigned& err) {
+    int nc = 0;
+    const int n = start[c + 1] - start[c];
+    *n_out = n;
+    if (n > 1) {
+        double sm = smax[c];
+        if (learned) {
+            const float pv = pred[c];
+            if (!useR[c] && pv > 0.f && pv < 3.0e38f && pv >= exceed[c]) sm = (double)pv;
+            smaxSel[c] = sm;
+        }
+        const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cell_volume(cs, c);
+        const double whole = floor(sel);
+        rem[c] = sel - whole;
+        if (n > cs.maxCellParcels || whole >= (double)MAX_CAND) err |= ERRB_DENSE;
+        else nc = (int)whole;
+    }
+    return nc;
+}
+
 __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const double* __restrict__ smax, double* rem,
                              Counters* ctr, int* ncCell, unsigned* slotCount, int learned,
                              const float* __restrict__ pred, const unsigned char* __restrict__ useR,
@@ -93,21 +119,8 @@ __global__ void k_ntc_select(CaseDev cs, const int* __restrict__ start, const do
     unsigned err = 0;
     for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < C;
          c += (long long)gridDim.x * blockDim.x) {
-        int nc = 0;
-        const int n = start[c + 1] - start[c];
-        if (n > 1) {
-            double sm = smax[c];
-            if (learned) {
-                const float pv = pred[c];
-                if (!useR[c] && pv > 0.f && pv < 3.0e38f && pv >= exceed[c]) sm = (double)pv;
-                smaxSel[c] = sm;
-            }
-            const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cell_volume(cs, c);
-            const double whole = floor(sel);
-            rem[c] = sel - whole;
-            if (n > cs.maxCellParcels || whole >= (double)MAX_CAND) err |= ERRB_DENSE;
-            else nc = (int)whole;
-        }
+        int n;
+        const int nc = select_cell(cs, start, smax, rem, learned, pred, useR, exceed, smaxSel, c, &n, err);
         ncCell[c] = nc;
         if (nc > 0) atomicAdd(&hist[slot_of(n, nc)], 1u);
     }
@@ -132,30 +145,40 @@ __global__ void k_ntc_buckets(Counters* ctr, unsigned* slotCount, unsigned* slot
 // order are also listed (by work index) for k_cell_order_big
 // allHeavy: every listed cell is ordered and takes a heavy slot (the
 // Bernoulli-trial selection walks the canonical list of every cell)
+// One warp-wide iteration of k_ntc_list over cells c (lanes past C take part
+// without a cell).
+__device__ __forceinline__ void list_iter(long long C, const int* __restrict__ start, const int* __restrict__ ncCell,
+                                          unsigned* slotCursor, int2* work, int* bigList, Counters* ctr, int allHeavy,
+                                          long long c) {
+    const unsigned lane = threadIdx.x & 31u;
+    int nc = 0, n = 0;
+    if (c < C) {
+        nc = ncCell[c];
+        if (nc > 0) n = start[c + 1] - start[c];
+    }
+    if (!__ballot_sync(0xFFFFFFFFu, nc > 0)) return;
+    const int slot = nc > 0 ? (allHeavy ? NBUCKET + bucket_of(nc) : slot_of(n, nc)) : -1;
+    // one atomic per slot present in the warp
+    const unsigned peers = __match_any_sync(0xFFFFFFFFu, slot);
+    const int leader = __ffs(peers) - 1;
+    unsigned q0 = 0;
+    if (nc > 0 && (int)lane == leader) q0 = atomicAdd(&slotCursor[slot], (unsigned)__popc(peers));
+    q0 = __shfl_sync(0xFFFFFFFFu, q0, leader);
+    if (nc > 0) {
+        const unsigned q = q0 + __popc(peers & ((1u << lane) - 1u));
+        work[q] = make_int2((int)c, nc);
+        if (n > ORDER_WARP_N) bigList[atomicAdd(&ctr->bigCells, 1)] = (int)q;
+    }
+}
+
+// work list of the cells with candidates; cells too large for one warp to
+// order are also listed (by work index) for k_cell_order_big
+// allHeavy: every listed cell is ordered and takes a heavy slot (the
+// Bernoulli-trial selection walks the canonical list of every cell)
 __global__ void k_ntc_list(long long C, const int* __restrict__ start, const int* __restrict__ ncCell,
                            unsigned* slotCursor, int2* work, int* bigList, Counters* ctr, int allHeavy) {
-    const unsigned lane = threadIdx.x & 31u;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < C; base += (long long)gridDim.x * blockDim.x) {
-        const long long c = base + threadIdx.x;
-        int nc = 0, n = 0;
-        if (c < C) {
-            nc = ncCell[c];
-            if (nc > 0) n = start[c + 1] - start[c];
-        }
-        if (!__ballot_sync(0xFFFFFFFFu, nc > 0)) continue;
-        const int slot = nc > 0 ? (allHeavy ? NBUCKET + bucket_of(nc) : slot_of(n, nc)) : -1;
-        // one atomic per slot present in the warp
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, slot);
-        const int leader = __ffs(peers) - 1;
-        unsigned q0 = 0;
-        if (nc > 0 && (int)lane == leader) q0 = atomicAdd(&slotCursor[slot], (unsigned)__popc(peers));
-        q0 = __shfl_sync(0xFFFFFFFFu, q0, leader);
-        if (nc > 0) {
-            const unsigned q = q0 + __popc(peers & ((1u << lane) - 1u));
-            work[q] = make_int2((int)c, nc);
-            if (n > ORDER_WARP_N) bigList[atomicAdd(&ctr->bigCells, 1)] = (int)q;
-        }
-    }
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < C; base += (long long)gridDim.x * blockDim.x)
+        list_iter(C, start, ncCell, slotCursor, work, bigList, ctr, allHeavy, base + threadIdx.x);
 }
 
 // ------------------------------------------------------------ ordering
@@ -202,41 +225,48 @@ struct BlockBar {
 // one warp per heavy cell of at most ORDER_WARP_N parcels: perm[off + r] is
 // the local index of the r-th member in canonical order, subs[q] the start
 // of each sub-cell in it
+// One warp orders heavy work item q (keys: ORDER_WARP_N words of the warp's
+// shared memory).
+__device__ __forceinline__ void order_item(const Parcels& s, const int* __restrict__ start,
+                                           const int2* __restrict__ work, uint16_t* perm, uint4* subs, long long q,
+                                           unsigned long long* keys) {
+    const int lane = (int)(threadIdx.x & 31u);
+    const int c = work[q].x;
+    const long long off = start[c];
+    const int n = start[c + 1] - (int)off;
+    if (n > ORDER_WARP_N) return;
+    int N = 32;
+    while (N < n) N <<= 1;
+    int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int j0 = 0; j0 < N; j0 += 32) {
+        const int j = j0 + lane;
+        unsigned long long key = ~0ull;
+        int sb = 8;
+        if (j < n) {
+            const uint32_t w = s.cellw[off + j];
+            sb = (int)(w & 7u);
+            key = order_key(w, __ldg(s.id + off + j), j);
+        }
+        keys[j] = key;
+#pragma unroll
+        for (int b = 0; b < 8; ++b) cnt[b] += __popc(__ballot_sync(0xFFFFFFFFu, sb == b));
+    }
+    __syncwarp();
+    bitonic(keys, N, lane, 32, WarpBar());
+    for (int r = lane; r < n; r += 32) perm[off + r] = (uint16_t)(keys[r] & 0xFFFFu);
+    if (lane == 0) subs[q] = pack_starts(cnt);
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(WARPS * 32)
 k_cell_order(Parcels s, const int* __restrict__ start, const Counters* ctr, const int2* __restrict__ work,
              uint16_t* perm, uint4* subs) {
     __shared__ unsigned long long keysAll[WARPS][ORDER_WARP_N];
     unsigned long long* keys = keysAll[threadIdx.x >> 5];
-    const int lane = (int)(threadIdx.x & 31u);
     const long long nHeavy = (long long)ctr->nHeavy;
     const long long nWarps = (long long)gridDim.x * WARPS;
-    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nHeavy; q += nWarps) {
-        const int c = work[q].x;
-        const long long off = start[c];
-        const int n = start[c + 1] - (int)off;
-        if (n > ORDER_WARP_N) continue;
-        int N = 32;
-        while (N < n) N <<= 1;
-        int cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int j0 = 0; j0 < N; j0 += 32) {
-            const int j = j0 + lane;
-            unsigned long long key = ~0ull;
-            int sb = 8;
-            if (j < n) {
-                const uint32_t w = s.cellw[off + j];
-                sb = (int)(w & 7u);
-                key = order_key(w, __ldg(s.id + off + j), j);
-            }
-            keys[j] = key;
-#pragma unroll
-            for (int b = 0; b < 8; ++b) cnt[b] += __popc(__ballot_sync(0xFFFFFFFFu, sb == b));
-        }
-        __syncwarp();
-        bitonic(keys, N, lane, 32, WarpBar());
-        for (int r = lane; r < n; r += 32) perm[off + r] = (uint16_t)(keys[r] & 0xFFFFu);
-        if (lane == 0) subs[q] = pack_starts(cnt);
-        __syncwarp();
-    }
+    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nHeavy; q += nWarps)
+        order_item(s, start, work, perm, subs, q, keys);
 }
 
 // one block per listed cell above ORDER_WARP_N parcels (dynamic shared

@@ -201,7 +201,7 @@ class DsmcCloud:
         self._chk(lib().dsmc_evolve_profiled(self.h, n, ph, C.byref(tot)))
         return tot.value, dict(zip(("inflow", "move", "sort", "collide_sample", "end"), list(ph)))
 
-    KERNEL_GROUPS = ("zero", "inflow", "move", "sample", "scan", "scatter_index", "gather", "finish",
+    KERNEL_GROUPS = ("zero", "inflow", "move", "move_slow", "sample", "scan", "scatter_index", "gather", "finish",
                      "learned", "select", "collide_heavy", "collide_light", "pending", "end")
 
     def evolve_kernel_profile(self, n: int):

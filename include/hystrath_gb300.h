@@ -269,7 +269,8 @@ int dsmc_evolve_profiled(dsmc_handle* h, long long n_steps, double* phase_ms, do
 enum {
     DSMC_KGROUP_ZERO = 0,      /* step counters reset */
     DSMC_KGROUP_INFLOW,        /* freestream inflow (count, scan, fill, commit) */
-    DSMC_KGROUP_MOVE,          /* k_move (fast path) + k_move_slow (boundary path) */
+    DSMC_KGROUP_MOVE,          /* k_move (fast path) */
+    DSMC_KGROUP_MOVE_SLOW,     /* k_move_slow (boundary path) */
     DSMC_KGROUP_SAMPLE,        /* sample commit of the fixed-point sums */
     DSMC_KGROUP_SCAN,          /* occupancy scan */
     DSMC_KGROUP_SCATTER,       /* k_scatter_index: a slot per parcel */

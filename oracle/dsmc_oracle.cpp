@@ -661,9 +661,10 @@ struct Oracle {
             for (int o = 0; o < spec.n_obstacles && !obst; ++o) {
                 const dsmc_obstacle& ob = spec.obstacles[o];
                 bool ov = true;
+                // the path stays in the box of cells spanned by its end cells
                 for (int a = 0; a < 3; ++a) {
-                    const int mn = std::min(startCell[a], ci[a]) - 1;
-                    const int mx = std::max(startCell[a], ci[a]) + 1;
+                    const int mn = std::min(startCell[a], ci[a]);
+                    const int mx = std::max(startCell[a], ci[a]);
                     if (mx < ob.lo[a] || mn > ob.hi[a] - 1) ov = false;
                 }
                 obst = ov;
