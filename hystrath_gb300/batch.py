@@ -2,7 +2,9 @@
 their launch shapes.
 
 ``BatchCloud`` wraps ``dsmc_batch_*``: every batched step is one launch of a
-CUDA graph whose children are the cases' captured steps.  ``autotune`` picks,
+CUDA graph whose children are the cases' captured steps, or, in the
+persistent mode, two cooperative persistent launches over all cases (move
+and sort, then collisions) with per-phase (case, tile) work queues.  ``autotune`` picks,
 per size class of the cases, the threads per CTA of the parcel-streaming
 kernels and the cells per CTA of the lane-per-cell collision kernel by timing
 batched steps (coordinate descent over the classes).
@@ -11,7 +13,8 @@ batched steps (coordinate descent over the classes).
 periodic cases drawn from the seed: 8^3..48^3 cells, 5..60 parcels per cell,
 Ar or N2, T_tr log-uniform in 500..20000 K, T_int 300 K, n = 1e20 m^-3,
 dt = 0.2 mean collision times) batched and one case at a time, and prints
-one JSON line with the aggregate collision and parcel-step rates.
+one JSON line with the aggregate collision and parcel-step rates of the
+persistent mode, the graph of case graphs and the cases one at a time.
 """
 from __future__ import annotations
 
@@ -81,6 +84,8 @@ def _bind():
     L.dsmc_batch_set_launch.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     L.dsmc_batch_evolve.argtypes = [vp, C.c_longlong]
     L.dsmc_batch_evolve_timed.argtypes = [vp, C.c_longlong, C.POINTER(C.c_double)]
+    L.dsmc_batch_set_persistent.argtypes = [vp, C.c_int, C.c_int]
+    L.dsmc_batch_get_persistent.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.dsmc_set_launch.argtypes = [vp, C.c_int, C.c_int]
     L.dsmc_get_launch.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L._batch_bound = True
@@ -131,6 +136,12 @@ class BatchCloud:
 
     def set_launch(self, i: int, cta_threads: int, cells_per_cta: int):
         self._chk(lib().dsmc_batch_set_launch(self.h, int(i), int(cta_threads), int(cells_per_cta)))
+
+    def set_persistent(self, move_threads: int, collide_threads: int):
+        """Two persistent cooperative launches per batched step over all
+        cases (move and sort, then collisions); 0, 0: the graph of case
+        graphs."""
+        self._chk(_bind().dsmc_batch_set_persistent(self.h, int(move_threads), int(collide_threads)))
 
     def info(self, i: int) -> S.Info:
         inf = S.Info()
@@ -189,6 +200,27 @@ def autotune(batch: BatchCloud, classes, steps=4, rounds=1, log=None):
     return choice, best_ms
 
 
+MOVE_THREADS = (128, 256, 512)
+COLLIDE_THREADS = (64, 128)
+
+
+def autotune_persistent(batch: BatchCloud, steps=4, log=None):
+    """The (move CTA threads, collision CTA threads = light cells per CTA)
+    pair of the persistent mode with the shortest batched step."""
+    trial = []
+    for t in MOVE_THREADS:
+        for c in COLLIDE_THREADS:
+            batch.set_persistent(t, c)
+            batch.evolve(1)                      # capture and warm
+            ms = batch.evolve_timed(steps) / steps
+            trial.append((ms, (t, c)))
+            if log:
+                log(f"persistent {t}/{c}: {ms:.3f} ms/step")
+    ms, cfg = min(trial)
+    batch.set_persistent(*cfg)
+    return cfg, ms
+
+
 def one_at_a_time(specs, steps, warmup, launch=None):
     """Each case on its own (its own graph launches), back to back."""
     tot_ms = 0.0
@@ -223,19 +255,38 @@ def main():
 
     specs, meta = heat_bath_cases(args.seed, args.cases)
     t0 = time.time()
-    b = BatchCloud(specs)
-    b.initialise()
-    N = sum(b.info(i).n_particles for i in range(b.n))
-    log(f"{b.n} cases, {N} parcels, set up in {time.time() - t0:.1f} s")
     classes = size_classes(specs)
     choice = [(256, 128)] * len(classes)
+    pcfg = (256, 128)
     if not args.no_tune:
+        # tuning steps change the state: the timed runs below start afresh
+        b = BatchCloud(specs)
+        b.initialise()
         choice, _ = autotune(b, classes, log=log)
-    b.evolve(args.warmup)
-    c0, _ = b.totals()
-    ms = b.evolve_timed(args.steps)
-    c1, _ = b.totals()
-    b.close()
+        pcfg, _ = autotune_persistent(b, log=log)
+        b.close()
+
+    def timed(persistent):
+        b = BatchCloud(specs)
+        b.initialise()
+        for k, idx in enumerate(classes):
+            for i in idx:
+                b.set_launch(i, *choice[k])
+        if persistent:
+            b.set_persistent(*pcfg)
+        N = sum(b.info(i).n_particles for i in range(b.n))
+        b.evolve(args.warmup)
+        c0, _ = b.totals()
+        ms = b.evolve_timed(args.steps)
+        c1, _ = b.totals()
+        b.close()
+        return ms, c1 - c0, N
+
+    ms, coll, N = timed(False)
+    log(f"{len(specs)} cases, {N} parcels; graph of case graphs {ms / args.steps:.3f} ms/step "
+        f"({time.time() - t0:.1f} s so far)")
+    msp, collp, _ = timed(True)
+    log(f"persistent {msp / args.steps:.3f} ms/step")
     launch = [None] * len(specs)
     for k, idx in enumerate(classes):
         for i in idx:
@@ -245,11 +296,16 @@ def main():
         "workload": f"{args.cases} periodic heat baths (8^3..48^3 cells, 5..60 parcels/cell, Ar|N2, "
                     "T_tr 500..20000 K, dt = 0.2 mean collision times)",
         "parcels": int(N), "steps": args.steps,
-        "batched": {"ms_per_step": ms / args.steps, "collisions_per_s": (c1 - c0) / (ms * 1e-3),
+        "persistent": {"ms_per_step": msp / args.steps, "collisions_per_s": collp / (msp * 1e-3),
+                       "particle_steps_per_s": N * args.steps / (msp * 1e-3),
+                       "move_threads": pcfg[0], "collide_threads": pcfg[1],
+                       "same_collisions_as_graph_mode": collp == coll},
+        "batched": {"ms_per_step": ms / args.steps, "collisions_per_s": coll / (ms * 1e-3),
                     "particle_steps_per_s": N * args.steps / (ms * 1e-3)},
         "one_at_a_time": {"ms_per_step": ms1 / args.steps, "collisions_per_s": coll1 / (ms1 * 1e-3),
                           "particle_steps_per_s": pst1 / (ms1 * 1e-3)},
         "speedup": ms1 / ms,
+        "speedup_persistent": ms1 / msp,
         "launch_per_class": [{"cases": len(idx), "edge_range": [min(specs[i].n_cells[0] for i in idx),
                                                                max(specs[i].n_cells[0] for i in idx)],
                               "cta_threads": choice[k][0], "cells_per_cta": choice[k][1]}

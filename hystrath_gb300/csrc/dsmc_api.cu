@@ -9,6 +9,7 @@
 // graph and replayed; nothing in a step waits on the host.
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -1542,6 +1543,13 @@ struct dsmc_batch {
     std::vector<dsmc_handle*> cases;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // persistent mode: two cooperative launches per batched step (move and
+    // sort, then collisions) over all cases; 0 threads: graph of case graphs
+    int persistMove = 0, persistCollide = 0;
+    BatchSlot* dSlots = nullptr;     // [2][n]: the cases as seen from each buffer parity
+    BatchCtl* dCtl = nullptr;
+    int pgraphState = 0;             // 0 not tried, 1 captured, -1 capture refused: direct launches
+    cudaGraphExec_t pgraph[2] = {nullptr, nullptr};
     // each case's graph generation when the batch graphs were built: a case
     // whose step graphs were dropped since (learned model, face tracking,
     // launch shape, ...) makes the batch graphs stale
@@ -1639,10 +1647,21 @@ int dsmc_batch_create_from_dirs(int n, const char* const* case_dirs, dsmc_batch*
     return DSMC_OK;
 }
 
+static void drop_persistent_graphs(dsmc_batch* b) {
+    for (int p = 0; p < 2; ++p) {
+        if (b->pgraph[p]) cudaGraphExecDestroy(b->pgraph[p]);
+        b->pgraph[p] = nullptr;
+    }
+    b->pgraphState = 0;
+}
+
 void dsmc_batch_destroy(dsmc_batch* b) {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_batch_graphs(b);
+    drop_persistent_graphs(b);
+    if (b->dSlots) cudaFree(b->dSlots);
+    if (b->dCtl) cudaFree(b->dCtl);
     for (dsmc_handle* h : b->cases) dsmc_destroy(h);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -1674,11 +1693,173 @@ int dsmc_batch_set_launch(dsmc_batch* b, int i, int cta_threads, int cells_per_c
     return DSMC_OK;
 }
 
+int dsmc_batch_set_persistent(dsmc_batch* b, int move_threads, int collide_threads) {
+    if (!move_threads && !collide_threads) {
+        b->persistMove = b->persistCollide = 0;
+        return DSMC_OK;
+    }
+    if (move_threads != 128 && move_threads != 256 && move_threads != 512)
+        return bfail(b, DSMC_ERR_INVALID, "move_threads must be 128, 256 or 512");
+    if (collide_threads != 64 && collide_threads != 128)
+        return bfail(b, DSMC_ERR_INVALID, "collide_threads must be 64 or 128");
+    const int n = (int)b->cases.size();
+    if (n > BATCH_MAX_CASES)
+        return bfail(b, DSMC_ERR_INVALID, "the persistent batch takes at most " + std::to_string(BATCH_MAX_CASES) +
+                                              " cases");
+    for (int i = 0; i < n; ++i) {
+        const dsmc_handle* h = b->cases[i];
+        const CaseDev& cs = h->cs;
+        const char* why = nullptr;
+        if (h->hasInflow) why = "a freestream inflow";
+        else if (cs.nObst) why = "an obstacle";
+        else if (cs.anyEmpty) why = "a reduced-D (empty) axis";
+        else if (cs.half[0] || cs.half[1] || cs.half[2]) why = "a graded axis";
+        else if (cs.faceFlux) why = "face tracking";
+        else if (h->model) why = "a learned maximum";
+        else if (h->B.audit) why = "the selection audit";
+        else if (h->B.macc) why = "measureHeatFluxShearStress";
+        else if (cs.selModel != DSMC_SEL_NTC) why = "simplifiedBernoulliTrials";
+        if (why)
+            return bfail(b, DSMC_ERR_INVALID, "case " + std::to_string(i) + " has " + why +
+                                                  ": the persistent batch kernels take uniform boxes with "
+                                                  "noTimeCounter selection only");
+    }
+    if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, "batch stream");
+    if (!b->dSlots && cudaMalloc(&b->dSlots, sizeof(BatchSlot) * 2 * (size_t)n) != cudaSuccess)
+        return bfail(b, DSMC_ERR_CAPACITY, "cannot allocate the batch slots");
+    if (!b->dCtl) {
+        if (cudaMalloc(&b->dCtl, sizeof(BatchCtl)) != cudaSuccess)
+            return bfail(b, DSMC_ERR_CAPACITY, "cannot allocate the batch control block");
+        cudaMemset(b->dCtl, 0, sizeof(BatchCtl));
+    }
+    if (batch_move_grid(move_threads) <= 0 || batch_collide_grid(collide_threads) <= 0)
+        return bfail(b, DSMC_ERR_CUDA, "no occupancy for the persistent batch kernels");
+    b->persistMove = move_threads;
+    b->persistCollide = collide_threads;
+    drop_persistent_graphs(b);
+    return DSMC_OK;
+}
+
+int dsmc_batch_get_persistent(const dsmc_batch* b, int* move_threads, int* collide_threads) {
+    if (move_threads) *move_threads = b->persistMove;
+    if (collide_threads) *collide_threads = b->persistCollide;
+    return DSMC_OK;
+}
+
+// One batched step of the persistent mode on the batch stream: the tickets
+// cleared, then the move/sort launch and the collision launch.
+static cudaError_t enqueue_persistent_step(dsmc_batch* b, int p) {
+    const int n = (int)b->cases.size();
+    void* tickets = reinterpret_cast<char*>(b->dCtl) + offsetof(BatchCtl, ticket);
+    cudaError_t e = cudaMemsetAsync(tickets, 0, sizeof(unsigned long long) * BATCH_PHASES, b->stream);
+    if (e == cudaSuccess) e = launch_batch_move(b->dSlots + (size_t)p * n, n, b->dCtl, b->persistMove, b->stream);
+    if (e == cudaSuccess)
+        e = launch_batch_collide(b->dSlots + (size_t)p * n, n, b->dCtl, b->persistCollide, b->stream);
+    return e;
+}
+
+// The cases as the persistent kernels see them from each buffer parity.
+static int upload_slots(dsmc_batch* b) {
+    const int n = (int)b->cases.size();
+    std::vector<BatchSlot> sl((size_t)2 * n);
+    for (int p = 0; p < 2; ++p)
+        for (int i = 0; i < n; ++i) {
+            const dsmc_handle* h = b->cases[i];
+            BatchSlot& s = sl[(size_t)p * n + i];
+            s.cs = h->cs;
+            // the collision launch orders cells by warps only: larger cells
+            // are skipped with the dense-cell error
+            if (s.cs.maxCellParcels > WARP_ORDERED_CELL) s.cs.maxCellParcels = WARP_ORDERED_CELL;
+            s.B = h->B;
+            s.src = h->buf[p];
+            s.dst = h->buf[p ^ 1];
+        }
+    if (cudaMemcpy(b->dSlots, sl.data(), sizeof(BatchSlot) * sl.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bfail(b, DSMC_ERR_CUDA, "cannot upload the batch slots");
+    return DSMC_OK;
+}
+
+// The persistent step of each parity captured as a graph (tickets memset and
+// the two cooperative launches); where the capture is refused, the steps are
+// launched directly.
+static void capture_persistent(dsmc_batch* b) {
+    if (b->pgraphState != 0) return;
+    for (int p = 0; p < 2; ++p) {
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t e1 = enqueue_persistent_step(b, p);
+            e = cudaStreamEndCapture(b->stream, &g);
+            if (e1 != cudaSuccess) e = e1;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&b->pgraph[p], g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            drop_persistent_graphs(b);
+            b->pgraphState = -1;
+            return;
+        }
+    }
+    b->pgraphState = 1;
+}
+
+static int batch_evolve_persistent(dsmc_batch* b, long long n, double* total_ms) {
+    int rc = upload_slots(b);
+    if (rc) return rc;
+    for (dsmc_handle* h : b->cases)
+        if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, "case stream");
+    capture_persistent(b);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (total_ms) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, b->stream);
+    }
+    int p = b->cases[0]->cur;
+    for (long long s = 0; s < n; ++s) {
+        for (dsmc_handle* h : b->cases) schedule_pre(h, b->stream);
+        const cudaError_t e = b->pgraphState == 1 ? cudaGraphLaunch(b->pgraph[p], b->stream)
+                                                  : enqueue_persistent_step(b, p);
+        if (e != cudaSuccess)
+            return bfail(b, DSMC_ERR_CUDA, std::string("persistent batch launch: ") + cudaGetErrorString(e));
+        p ^= 1;
+        for (dsmc_handle* h : b->cases) schedule_post(h);
+    }
+    if (total_ms) cudaEventRecord(e1, b->stream);
+    const cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (total_ms) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        *total_ms = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    if (e != cudaSuccess) return bfail(b, DSMC_ERR_CUDA, std::string("persistent batch step: ") + cudaGetErrorString(e));
+    BatchCtl ctl;
+    if (cudaMemcpy(&ctl, b->dCtl, sizeof(ctl), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return bfail(b, DSMC_ERR_CUDA, "cannot read the batch control block");
+    for (size_t i = 0; i < b->cases.size(); ++i) {
+        dsmc_handle* h = b->cases[i];
+        if (n & 1) h->cur ^= 1;
+    }
+    if (ctl.err) {
+        cudaMemset(b->dCtl, 0, sizeof(BatchCtl));
+        return bfail(b, DSMC_ERR_DEVICE, "persistent batch: a grid barrier wait ran out (the step is incomplete)");
+    }
+    for (size_t i = 0; i < b->cases.size(); ++i) {
+        rc = check_device_error(b->cases[i]);
+        if (rc) return bfail(b, rc, "case " + std::to_string(i) + ": " + b->cases[i]->err);
+    }
+    return DSMC_OK;
+}
+
 int dsmc_batch_evolve_timed(dsmc_batch* b, long long n, double* total_ms) {
     // the cases are stepped together, so they share the buffer parity
     const int cur = b->cases[0]->cur;
     for (dsmc_handle* h : b->cases)
         if (h->cur != cur) return bfail(b, DSMC_ERR_INVALID, "cases of a batch must be at the same buffer parity");
+    if (b->persistMove) return batch_evolve_persistent(b, n, total_ms);
     int rc = build_batch_graphs(b);
     if (rc) return rc;
     // the cases' own streams may still hold work (initialisation, reads)

@@ -501,6 +501,148 @@ __global__ void k_learn_compact(CaseDev cs, const int* __restrict__ ncCell, cons
     }
 }
 
+// ---------------------------------------------------------------- batch
+// The collision half of a batched step for every case of a batch, in one
+// persistent launch (phases separated by grid barriers, work items taken from
+// per-phase tickets; see dsmc_persist.cuh).  The per-cell work is the
+// single-case kernels' own (select_cell, list_iter, order_item, heavy_item,
+// light_group), so a batched case collides exactly as it does alone.  Plain
+// noTimeCounter selection only (no learned maximum, no selection audit); a
+// cell above ORDER_WARP_N parcels is skipped with the dense-cell error (the
+// slot's maxCellParcels is lowered to it).
+#include "dsmc_persist.cuh"   // (no includes of its own: it sits in this namespace)
+
+enum { BC_SELECT = 0, BC_BUCKETS, BC_LIST, BC_ORDER, BC_HEAVY, BC_LIGHT, BC_END, BC_NPHASE };
+static_assert(BATCH_TICKETS_COLLIDE + BC_NPHASE <= BATCH_PHASES, "ticket counters of the collision launch");
+
+constexpr int BC_MAX_THREADS = 128;
+
+// dynamic shared memory: per warp its ordering keys and its light picks
+__host__ __device__ constexpr size_t batch_collide_smem(int threads) {
+    return (size_t)(threads / 32) * (tile::ORDER_WARP_N * sizeof(unsigned long long) + sizeof(tile::LightPicks));
+}
+
+__global__ void __launch_bounds__(BC_MAX_THREADS, 4)
+k_batch_collide(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
+    extern __shared__ __align__(16) unsigned char bcSmem[];
+    __shared__ long long pre[BATCH_MAX_CASES + 1];
+    __shared__ unsigned hist[2 * tile::NBUCKET];
+    const int T = blockDim.x;
+    const int W = T >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    unsigned long long* keys =
+        reinterpret_cast<unsigned long long*>(bcSmem) + (size_t)warp * tile::ORDER_WARP_N;
+    tile::LightPicks& pk =
+        reinterpret_cast<tile::LightPicks*>(bcSmem + (size_t)W * tile::ORDER_WARP_N * sizeof(unsigned long long))[warp];
+    for (int ph = 0; ph < BC_NPHASE; ++ph) {
+        long long total;
+        switch (ph) {
+        case BC_SELECT:
+        case BC_LIST:
+            total = persist::phase_items(n, pre, [&](int i) { return (slots[i].cs.C + T - 1) / T; });
+            break;
+        case BC_ORDER:
+        case BC_HEAVY:
+            total = persist::phase_items(n, pre, [&](int i) {
+                return ((long long)slots[i].B.ctr->nHeavy + W - 1) / W;
+            });
+            break;
+        case BC_LIGHT:
+            total = persist::phase_items(n, pre, [&](int i) {
+                const Counters* c = slots[i].B.ctr;
+                return ((long long)(c->nWork - c->nHeavy) + T - 1) / T;
+            });
+            break;
+        default:   // one item per case
+            total = persist::phase_items(n, pre, [&](int) { return 1LL; });
+        }
+        const int tk = BATCH_TICKETS_COLLIDE + ph;
+        for (long long q = persist::next_item(ctl, tk, total); q >= 0; q = persist::next_item(ctl, tk, total)) {
+            const int ci = persist::item_case(pre, n, q);
+            const long long l = q - pre[ci];
+            const BatchSlot& sl = slots[ci];
+            const CaseDev& cs = sl.cs;
+            const StepBuffers& B = sl.B;
+            const Parcels& s = sl.dst;      // the sorted buffer
+            Counters* ctr = B.ctr;
+            unsigned* slotCount = B.buckets;
+            unsigned* slotCursor = B.buckets + 2 * tile::NBUCKET;
+            unsigned err = 0;
+            switch (ph) {
+            case BC_SELECT: {
+                if (tid < 2 * tile::NBUCKET) hist[tid] = 0;
+                __syncthreads();
+                const long long c = l * T + tid;
+                if (c < cs.C) {
+                    int nn;
+                    const int nc = tile::select_cell(cs, B.start, B.smax, B.rem, 0, nullptr, nullptr, nullptr,
+                                                     nullptr, c, &nn, err);
+                    B.ncCell[c] = nc;
+                    if (nc > 0) atomicAdd(&hist[tile::slot_of(nn, nc)], 1u);
+                }
+                __syncthreads();
+                if (tid < 2 * tile::NBUCKET && hist[tid]) atomicAdd(&slotCount[tid], hist[tid]);
+                break;
+            }
+            case BC_BUCKETS:
+                if (tid == 0) {
+                    unsigned off = 0;
+                    for (int b = 2 * tile::NBUCKET - 1; b >= 0; --b) {
+                        slotCursor[b] = off;
+                        off += slotCount[b];
+                        slotCount[b] = 0;
+                        if (b == tile::NBUCKET) ctr->nHeavy = off;
+                    }
+                    ctr->nWork = off;
+                }
+                break;
+            case BC_LIST:
+                tile::list_iter(cs.C, B.start, B.ncCell, slotCursor, B.work, B.bigList, ctr, 0, l * T + tid);
+                break;
+            case BC_ORDER: {
+                const long long qh = l * W + warp;
+                if (qh < (long long)ctr->nHeavy) tile::order_item(s, B.start, B.work, B.perm, B.subs, qh, keys);
+                break;
+            }
+            case BC_HEAVY: {
+                const long long qh = l * W + warp;
+                unsigned long long nColl = 0, nCand = 0;
+                if (qh < (long long)ctr->nHeavy)
+                    tile::heavy_item(cs, s, B.start, B.smax, B.acc, B.work, B.perm, B.subs, 0, nullptr, nullptr,
+                                     nullptr, B.obsMax, nullptr, qh, (uint32_t)ctr->step, err, nColl, nCand);
+                if (lane == 0) {
+                    if (nColl) atomicAdd(&ctr->coll, nColl);
+                    if (nCand) atomicAdd(&ctr->cand, nCand);
+                }
+                break;
+            }
+            case BC_LIGHT: {
+                const long long nWork = (long long)ctr->nWork;
+                const long long qb = (long long)ctr->nHeavy + l * T + warp * 32;
+                unsigned long long nColl = 0, nCand = 0;
+                if (qb < nWork)
+                    tile::light_group(cs, s, B.start, B.smax, B.acc, B.work, 0, nullptr, nullptr, nullptr, B.obsMax,
+                                      nullptr, qb, nWork, (uint32_t)ctr->step, pk, err, nColl, nCand);
+                if (nColl) atomicAdd(&ctr->coll, nColl);
+                if (nCand) atomicAdd(&ctr->cand, nCand);
+                break;
+            }
+            case BC_END:
+                if (tid == 0) {
+                    ctr->pendingSample = 1;
+                    ctr->collTot += ctr->coll;
+                    ctr->candTot += ctr->cand;
+                    ctr->bigCells = 0;
+                    ctr->step += 1;
+                }
+                break;
+            }
+            if (err) atomicOr(&ctr->err, err);
+        }
+        if (!persist::grid_sync(ctl)) return;
+    }
+}
+
 int sm_count() {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -514,6 +656,25 @@ int collide_init() {
     const cudaError_t e = cudaFuncSetAttribute(tile::k_cell_order_big, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                (int)(tile::ORDER_MAX_N * sizeof(unsigned long long)));
     return e == cudaSuccess ? 0 : (int)e;
+}
+
+int batch_collide_grid(int threads) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_collide, threads, batch_collide_smem(threads)) !=
+        cudaSuccess)
+        return 0;
+    return per * sms;
+}
+
+cudaError_t launch_batch_collide(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st) {
+    if (threads > BC_MAX_THREADS || threads < 32 || threads % 32) return cudaErrorInvalidConfiguration;
+    const int grid = batch_collide_grid(threads);
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    void* args[] = {(void*)&slots, (void*)&n, (void*)&ctl};
+    return cudaLaunchCooperativeKernel((const void*)k_batch_collide, dim3(grid), dim3(threads), args,
+                                       batch_collide_smem(threads), st);
 }
 
 void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st,

@@ -28,6 +28,7 @@ constexpr double GREAT = 1.0e15;
 constexpr int MAX_CROSSINGS = 64;
 constexpr int MAX_REJECTION = 100000;
 constexpr int MAX_ORDERED_CELL = 16384;   // parcels of the largest cell the collision kernels order
+constexpr int WARP_ORDERED_CELL = 1024;   // cells up to this size are ordered by one warp
 constexpr int ZV_TAB = 512;     // iMax values tabulated for 1/Zv
 
 // Error bits of the device error word.

@@ -172,6 +172,40 @@ void launch_field(const CaseDev& cs, const StepBuffers& B, int which, double* ou
 void launch_info(const CaseDev& cs, const Parcels& s, const Counters* ctr, double* out7,
                  cudaStream_t st);
 
+// ------------------------------------------------------------ batch
+// One case of a batch as the persistent batch kernels see it: its constants,
+// its buffers, and the parcel buffer the step starts in (src) and the one the
+// sort fills (dst).
+struct BatchSlot {
+    CaseDev cs;
+    StepBuffers B;
+    Parcels src, dst;
+};
+
+// Control block of the persistent batch kernels: the grid barrier (arrival
+// count and generation), an error word (a barrier wait that ran out), and one
+// work-queue ticket per phase (zeroed before every launch).
+constexpr int BATCH_PHASES = 16;
+constexpr int BATCH_TICKETS_MOVE = 0;      // tickets 0..8: the phases of the move/sort launch
+constexpr int BATCH_TICKETS_COLLIDE = 9;   // tickets 9..15: the phases of the collision launch
+constexpr int BATCH_MAX_CASES = 1024;
+struct BatchCtl {
+    unsigned barCount;
+    unsigned barGen;
+    unsigned err;
+    unsigned pad;
+    unsigned long long ticket[BATCH_PHASES];
+};
+constexpr unsigned BATCH_ERR_BARRIER = 1u;
+
+// The two persistent launches of one batched step over n cases (slots in
+// device memory): the move and sort phases, then the collision phases.  Both
+// are cooperative launches sized to the occupancy of their thread count.
+int batch_move_grid(int threads);
+int batch_collide_grid(int threads);
+cudaError_t launch_batch_move(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st);
+cudaError_t launch_batch_collide(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st);
+
 // field selectors of launch_field
 enum {
     F_RHON = 0, F_RHOM, F_UX, F_UY, F_UZ, F_TTRA, F_P, F_TROT, F_TVIB, F_TOV, F_NMEAN, F_NCOLLS,

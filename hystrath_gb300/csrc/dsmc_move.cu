@@ -1254,6 +1254,180 @@ __global__ void k_remainder_init(CaseDev cs, double* rem) {
     rem[c] = r.u01();
 }
 
+// ---------------------------------------------------------------- batch
+// The move and sort half of a batched step for every case of a batch, in one
+// persistent launch (phases separated by grid barriers, work items taken from
+// per-phase tickets; see dsmc_persist.cuh).  The per-parcel work is the
+// single-case kernels' own (move_iter, move_slow, scatter_iter, gather_slot),
+// so a batched case steps exactly as it steps alone.  Cases on a uniform mesh
+// without inflow, obstacles, reduced-D axes or face tracking only.
+#include "dsmc_persist.cuh"   // (no includes of its own: it sits in this namespace)
+
+constexpr int BM_IT = 8;    // iterations of the CTA per move, scatter and gather item
+
+enum { BM_ZERO = 0, BM_MOVE, BM_SLOW, BM_DONE, BM_FINAL, BM_SCAN, BM_SCATTER, BM_GATHER, BM_FINISH, BM_NPHASE };
+static_assert(BATCH_TICKETS_MOVE + BM_NPHASE <= BATCH_TICKETS_COLLIDE, "ticket counters of the move launch");
+
+__global__ void __launch_bounds__(MAX_STREAM_THREADS)
+k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
+    __shared__ long long pre[BATCH_MAX_CASES + 1];
+    const int T = blockDim.x;
+    const int tid = threadIdx.x;
+    for (int ph = 0; ph < BM_NPHASE; ++ph) {
+        long long total;
+        switch (ph) {
+        case BM_MOVE:
+        case BM_SCATTER:
+            total = persist::phase_items(n, pre, [&](int i) {
+                return (slots[i].B.ctr->nMoved + (long long)T * BM_IT - 1) / ((long long)T * BM_IT);
+            });
+            break;
+        case BM_GATHER:
+            total = persist::phase_items(n, pre, [&](int i) {
+                return (slots[i].B.ctr->nKept + (long long)T * BM_IT - 1) / ((long long)T * BM_IT);
+            });
+            break;
+        case BM_SLOW:
+            total = persist::phase_items(n, pre, [&](int i) {
+                return ((long long)slots[i].B.ctr->nSlow + T - 1) / T;
+            });
+            break;
+        case BM_FINAL:
+            total = persist::phase_items(n, pre, [&](int i) {
+                const Counters* c = slots[i].B.ctr;
+                if (c->unflushed < SAMPLES_PER_FLUSH) return 0LL;
+                const long long m = (long long)slots[i].cs.nSpecies * SACC * slots[i].cs.C;
+                return (m + (long long)T * BM_IT - 1) / ((long long)T * BM_IT);
+            });
+            break;
+        default:   // one item per case
+            total = persist::phase_items(n, pre, [&](int) { return 1LL; });
+        }
+        const int tk = BATCH_TICKETS_MOVE + ph;
+        for (long long q = persist::next_item(ctl, tk, total); q >= 0; q = persist::next_item(ctl, tk, total)) {
+            const int ci = persist::item_case(pre, n, q);
+            const long long l = q - pre[ci];
+            const BatchSlot& sl = slots[ci];
+            const CaseDev& cs = sl.cs;
+            const StepBuffers& B = sl.B;
+            Counters* ctr = B.ctr;
+            unsigned err = 0;
+            switch (ph) {
+            case BM_ZERO:
+                if (tid == 0) {
+                    ctr->nMoved = ctr->n;
+                    ctr->coll = ctr->cand = 0;
+                    ctr->wallHits = ctr->inserted = ctr->deleted = 0;
+                    ctr->bigCells = 0;
+                    ctr->nSlow = 0;
+                    ctr->nWork = ctr->nHeavy = 0;
+                }
+                break;
+            case BM_MOVE: {
+                const long long nm = ctr->nMoved;
+                const uint32_t step = (uint32_t)ctr->step;
+                const int doSample = ctr->pendingSample;
+                for (int k = 0; k < BM_IT; ++k) {
+                    const long long base = (l * BM_IT + k) * T;
+                    if (base >= nm) break;
+                    move_iter<false>(cs, sl.src, ctr, B.slowList, B.count, B.sfix, base + tid, nm, step, doSample,
+                                     err);
+                }
+                break;
+            }
+            case BM_SLOW: {
+                const long long k = l * T + tid;
+                if (k < (long long)ctr->nSlow) {
+                    const long long i = B.slowList[k];
+                    const uint32_t w = sl.src.cellw[i];
+                    const uint32_t nw = move_slow(cs, sl.src, i, (uint32_t)ctr->step, w, B.bfPatch, B.wall, &err,
+                                                  &ctr->wallHits);
+                    sl.src.cellw[i] = nw;
+                    if (nw != CELLW_DELETED) atomicAdd(&B.count[nw >> 3], 1);
+                }
+                break;
+            }
+            case BM_DONE:
+                if (tid == 0 && ctr->pendingSample) {
+                    ctr->sampleSteps += 1;
+                    ctr->unflushed += 1;
+                    ctr->pendingSample = 0;
+                }
+                break;
+            case BM_FINAL: {
+                const long long m = (long long)cs.nSpecies * SACC * cs.C;
+                for (int k = 0; k < BM_IT; ++k) {
+                    const long long idx = (l * BM_IT + k) * T + tid;
+                    if (idx >= m) break;
+                    const long long v = B.sfix[idx];
+                    if (!v) continue;
+                    const int kk = (int)((idx / cs.C) % SACC);
+                    const int F = (kk == SACC_UU) ? F_UU : (kk == SACC_EROT) ? F_E : F_U;
+                    B.acc[idx] += (kk == SACC_N || kk == SACC_VIB) ? (double)v : unfix(v, F);
+                    B.sfix[idx] = 0;
+                }
+                break;
+            }
+            case BM_SCAN: {
+                // the whole occupancy scan of the case by this CTA
+                if (tid == 0 && ctr->unflushed >= SAMPLES_PER_FLUSH) ctr->unflushed = 0;
+                const long long C = cs.C;
+                int carry = 0;
+                for (long long c0 = 0; c0 < C; c0 += (long long)T * SCAN_ITEMS) {
+                    const long long b0 = c0 + (long long)tid * SCAN_ITEMS;
+                    int v[SCAN_ITEMS];
+                    int sum = 0;
+#pragma unroll
+                    for (int k = 0; k < SCAN_ITEMS; ++k) {
+                        v[k] = (b0 + k < C) ? B.count[b0 + k] : 0;
+                        sum += v[k];
+                    }
+                    int tot;
+                    int ex = block_exclusive_scan(sum, &tot) + carry;
+#pragma unroll
+                    for (int k = 0; k < SCAN_ITEMS; ++k) {
+                        if (b0 + k < C) B.start[b0 + k] = ex;
+                        ex += v[k];
+                    }
+                    carry += tot;
+                }
+                if (tid == 0) {
+                    B.start[C] = carry;
+                    ctr->nKept = carry;
+                }
+                break;
+            }
+            case BM_SCATTER: {
+                const long long nm = ctr->nMoved;
+                for (int k = 0; k < BM_IT; ++k) {
+                    const long long base = (l * BM_IT + k) * T;
+                    if (base >= nm) break;
+                    scatter_iter(sl.src.cellw, ctr, B.start, B.count, B.sortSrc, base + tid, nm);
+                }
+                break;
+            }
+            case BM_GATHER: {
+                const long long nk = ctr->nKept, nm = ctr->nMoved;
+                for (int k = 0; k < BM_IT; ++k) {
+                    const long long j = (l * BM_IT + k) * T + tid;
+                    if (j < nk) gather_slot(sl.src, sl.dst, ctr, B.sortSrc, j, nm);
+                }
+                break;
+            }
+            case BM_FINISH:
+                if (tid == 0) {
+                    ctr->deleted += (unsigned long long)(ctr->nMoved - ctr->nKept);
+                    ctr->n = ctr->nKept;
+                    ctr->nMoved = ctr->nKept;
+                }
+                break;
+            }
+            if (err) atomicOr(&ctr->err, err);
+        }
+        if (!persist::grid_sync(ctl)) return;
+    }
+}
+
 int grid_for(long long n, int threads, int perSmBlocks) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -1267,6 +1441,21 @@ int grid_for(long long n, int threads, int perSmBlocks) {
 }  // namespace
 
 int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TILE) + 1; }
+
+int batch_move_grid(int threads) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_move, threads, 0) != cudaSuccess) return 0;
+    return per * sms;
+}
+
+cudaError_t launch_batch_move(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st) {
+    const int grid = batch_move_grid(threads);
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    void* args[] = {(void*)&slots, (void*)&n, (void*)&ctl};
+    return cudaLaunchCooperativeKernel((const void*)k_batch_move, dim3(grid), dim3(threads), args, 0, st);
+}
 
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st, cudaEvent_t mid) {
     const int T = B.cfg.streamThreads;

@@ -51,7 +51,7 @@ namespace tile {
 constexpr int WARPS = 4;             // warps per block
 constexpr int LIGHT_N = 64;          // light cells: at most this many parcels
 constexpr int LIGHT_CAND = 16;       //   and fewer candidates than this
-constexpr int ORDER_WARP_N = 1024;   // cells up to this size are ordered by one warp
+constexpr int ORDER_WARP_N = WARP_ORDERED_CELL;   // cells up to this size are ordered by one warp
 constexpr int ORDER_MAX_N = MAX_ORDERED_CELL;   // cells up to this size are ordered by one block
 constexpr int ORDER_BLOCK = 512;     // threads of the block that orders a large cell
 constexpr int NBUCKET = 8;           // candidate-count buckets per class
@@ -514,6 +514,77 @@ __device__ __forceinline__ void cell_epilogue(double* smax, long long c, double 
 
 __device__ __forceinline__ uint32_t cand_tag(int k) { return (uint32_t)TAG_COLLIDE | ((uint32_t)k << 8); }
 
+// One warp runs the candidates of heavy work item q, up to 32 at a time; the
+// cell's collision and candidate counts go to nColl and nCandTot of lane 0.
+__device__ __forceinline__ void heavy_item(const CaseDev& cs, const Parcels& s, const int* __restrict__ start,
+                                           double* smax, double* acc, const int2* __restrict__ work,
+                                           const uint16_t* __restrict__ perm, const uint4* __restrict__ subs,
+                                           int learned, const double* __restrict__ smaxSel, unsigned char* useR,
+                                           float* exceed, float* obsMax, double2* audit, long long q, uint32_t step,
+                                           unsigned& err, unsigned long long& nColl,
+                                           unsigned long long& nCandTot) {
+    const unsigned lane = lane_id();
+    const long long C = cs.C;
+    const int2 it = work[q];
+    const long long c = it.x;
+    const int nCand = it.y;
+    const long long off = start[c];
+    const int n = start[c + 1] - (int)off;
+    const uint4 so = subs[q];
+    const double R = smax[c];
+    const double smax0 = learned ? smaxSel[c] : R;
+    double stepMax = 0.0, collSep = 0.0;
+    unsigned coll = 0;
+    float2 au = make_float2(0.f, 0.f);
+    for (int base = 0; base < nCand; base += 32) {
+        const int k = base + (int)lane;
+        Rng r(cs, (uint32_t)c, step, cand_tag(k));
+        long long gP = 0, gQ = 0;
+        int pP = -1, pQ = -1;
+        if (k < nCand) {
+            draw_pair(r, n, so, &pP, &pQ, &err);
+            gP = off + perm[off + pP];
+            gQ = off + perm[off + pQ];
+        }
+        unsigned pend = __ballot_sync(0xFFFFFFFFu, k < nCand);
+        while (pend) {
+            // ready: no earlier waiting candidate shares a parcel
+            bool ready = (pend >> lane) & 1u;
+            unsigned m = pend;
+            while (m) {
+                const int j = __ffs(m) - 1;
+                m &= m - 1u;
+                const int a = __shfl_sync(0xFFFFFFFFu, pP, j);
+                const int b = __shfl_sync(0xFFFFFFFFu, pQ, j);
+                if (j < (int)lane && (a == pP || a == pQ || b == pP || b == pQ)) ready = false;
+            }
+            if (ready && run_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &collSep, &err,
+                                       audit ? &au : nullptr)) ++coll;
+            __syncwarp();
+            pend &= ~__ballot_sync(0xFFFFFFFFu, ready);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        collSep += __shfl_xor_sync(0xFFFFFFFFu, collSep, o);
+        stepMax = fmax(stepMax, __shfl_xor_sync(0xFFFFFFFFu, stepMax, o));
+        coll += __shfl_xor_sync(0xFFFFFFFFu, coll, o);
+        if (audit) {
+            au.x += __shfl_xor_sync(0xFFFFFFFFu, au.x, o);
+            au.y += __shfl_xor_sync(0xFFFFFFFFu, au.y, o);
+        }
+    }
+    if (lane == 0) {
+        cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, exceed, obsMax, audit, au);
+        if (coll) {
+            acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
+            acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
+        }
+        nColl += coll;
+        nCandTot += (unsigned long long)nCand;
+    }
+}
+
 // one warp per heavy cell, up to 32 candidates at a time
 __global__ void __launch_bounds__(WARPS * 32)
 k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
@@ -523,70 +594,12 @@ k_collide_heavy(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
     const unsigned lane = lane_id();
     const uint32_t step = (uint32_t)ctr->step;
     const long long nHeavy = (long long)ctr->nHeavy;
-    const long long C = cs.C;
     unsigned err = 0;
     unsigned long long nColl = 0, nCandTot = 0;
     const long long nWarps = (long long)gridDim.x * WARPS;
-    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nHeavy; q += nWarps) {
-        const int2 it = work[q];
-        const long long c = it.x;
-        const int nCand = it.y;
-        const long long off = start[c];
-        const int n = start[c + 1] - (int)off;
-        const uint4 so = subs[q];
-        const double R = smax[c];
-        const double smax0 = learned ? smaxSel[c] : R;
-        double stepMax = 0.0, collSep = 0.0;
-        unsigned coll = 0;
-        float2 au = make_float2(0.f, 0.f);
-        for (int base = 0; base < nCand; base += 32) {
-            const int k = base + (int)lane;
-            Rng r(cs, (uint32_t)c, step, cand_tag(k));
-            long long gP = 0, gQ = 0;
-            int pP = -1, pQ = -1;
-            if (k < nCand) {
-                draw_pair(r, n, so, &pP, &pQ, &err);
-                gP = off + perm[off + pP];
-                gQ = off + perm[off + pQ];
-            }
-            unsigned pend = __ballot_sync(0xFFFFFFFFu, k < nCand);
-            while (pend) {
-                // ready: no earlier waiting candidate shares a parcel
-                bool ready = (pend >> lane) & 1u;
-                unsigned m = pend;
-                while (m) {
-                    const int j = __ffs(m) - 1;
-                    m &= m - 1u;
-                    const int a = __shfl_sync(0xFFFFFFFFu, pP, j);
-                    const int b = __shfl_sync(0xFFFFFFFFu, pQ, j);
-                    if (j < (int)lane && (a == pP || a == pQ || b == pP || b == pQ)) ready = false;
-                }
-                if (ready && run_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &collSep, &err,
-                                           audit ? &au : nullptr)) ++coll;
-                __syncwarp();
-                pend &= ~__ballot_sync(0xFFFFFFFFu, ready);
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            collSep += __shfl_xor_sync(0xFFFFFFFFu, collSep, o);
-            stepMax = fmax(stepMax, __shfl_xor_sync(0xFFFFFFFFu, stepMax, o));
-            coll += __shfl_xor_sync(0xFFFFFFFFu, coll, o);
-            if (audit) {
-                au.x += __shfl_xor_sync(0xFFFFFFFFu, au.x, o);
-                au.y += __shfl_xor_sync(0xFFFFFFFFu, au.y, o);
-            }
-        }
-        if (lane == 0) {
-            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, exceed, obsMax, audit, au);
-            if (coll) {
-                acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
-                acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
-            }
-            nColl += coll;
-            nCandTot += (unsigned long long)nCand;
-        }
-    }
+    for (long long q = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); q < nHeavy; q += nWarps)
+        heavy_item(cs, s, start, smax, acc, work, perm, subs, learned, smaxSel, useR, exceed, obsMax, audit, q, step,
+                   err, nColl, nCandTot);
     if (lane == 0) {
         if (nColl) atomicAdd(&ctr->coll, nColl);
         if (nCandTot) atomicAdd(&ctr->cand, nCandTot);
@@ -635,6 +648,142 @@ __device__ __forceinline__ int warp_argmin(uint32_t hA, bool vA, uint32_t hB, bo
     return a ? __ffs(a) - 1 : (b ? 31 + __ffs(b) : -1);
 }
 
+// One warp's group of 32 light work items from qb (lanes past nWork take part
+// in the warp-made picks without a cell); pk: the warp's picks in shared
+// memory.  Collision and candidate counts accumulate in nColl and nCandTot.
+__device__ __forceinline__ void light_group(const CaseDev& cs, const Parcels& s, const int* __restrict__ start,
+                                            double* smax, double* acc, const int2* __restrict__ work, int learned,
+                                            const double* __restrict__ smaxSel, unsigned char* useR, float* exceed,
+                                            float* obsMax, double2* audit, long long qb, long long nWork,
+                                            uint32_t step, LightPicks& pk, unsigned& err, unsigned long long& nColl,
+                                            unsigned long long& nCandTot) {
+    const int lane = (int)(threadIdx.x & 31u);
+    const long long C = cs.C;
+    const long long q = qb + lane;
+    int2 it = make_int2(0, 0);
+    long long off = 0;
+    int n = 0;
+    if (q < nWork) {
+        it = work[q];
+        off = start[it.x];
+        n = start[it.x + 1] - (int)off;
+    }
+    const long long c = it.x;
+    int nCand = it.y;   // 0 past the end of the list
+    if (nCand >= LIGHT_CAND || n > LIGHT_N) {
+        // the list put a heavy cell here: record, never index past the picks
+        err |= ERRB_BOUNDS;
+        nCand = 0;
+    }
+    // every lane's picks, one cell at a time: coalesced loads of the
+    // cell's ids and cell words (the next cell's issued before this
+    // cell's picks), a warp minimum per pick
+    const uint32_t myBase = pick_base(cs, (uint32_t)c, step);
+    int ncN = __shfl_sync(0xFFFFFFFFu, nCand, 0);
+    int nN = __shfl_sync(0xFFFFFFFFu, n, 0);
+    long long offN = __shfl_sync(0xFFFFFFFFu, off, 0);
+    uint32_t idAN = 0, idBN = 0, sAN = 0, sBN = 0;
+    if (ncN) {
+        if (lane < nN) {
+            idAN = __ldg(s.id + offN + lane);
+            sAN = __ldg(s.cellw + offN + lane);
+        }
+        if (lane + 32 < nN) {
+            idBN = __ldg(s.id + offN + lane + 32);
+            sBN = __ldg(s.cellw + offN + lane + 32);
+        }
+    }
+    for (int L = 0; L < 32; ++L) {
+        const int nc = min(ncN, LIGHT_CAND - 1), nL = nN;
+        const uint32_t idA = idAN, idB = idBN, sA = sAN & 7u, sB = sBN & 7u;
+        const uint32_t baseL = __shfl_sync(0xFFFFFFFFu, myBase, L);
+        if (L + 1 < 32) {
+            ncN = __shfl_sync(0xFFFFFFFFu, nCand, L + 1);
+            nN = __shfl_sync(0xFFFFFFFFu, n, L + 1);
+            offN = __shfl_sync(0xFFFFFFFFu, off, L + 1);
+            idAN = idBN = sAN = sBN = 0;
+            if (ncN) {
+                if (lane < nN) {
+                    idAN = __ldg(s.id + offN + lane);
+                    sAN = __ldg(s.cellw + offN + lane);
+                }
+                if (lane + 32 < nN) {
+                    idBN = __ldg(s.id + offN + lane + 32);
+                    sBN = __ldg(s.cellw + offN + lane + 32);
+                }
+            }
+        }
+        if (nc == 0) continue;
+        const bool vA = lane < nL, vB = lane + 32 < nL;
+        // sub-cell occupancy, 8 bits per sub-cell (nL <= LIGHT_N < 256)
+        uint32_t cnt0 = 0, cnt1 = 0;
+        if (vA) (sA < 4 ? cnt0 : cnt1) += 1u << (8u * (sA & 3u));
+        if (vB) (sB < 4 ? cnt0 : cnt1) += 1u << (8u * (sB & 3u));
+        cnt0 = __reduce_add_sync(0xFFFFFFFFu, cnt0);
+        cnt1 = __reduce_add_sync(0xFFFFFFFFu, cnt1);
+        for (int k = 0; k < nc; ++k) {
+            const uint32_t kP = pick_draw(cs, baseL, 2u * k);
+            const int jP = warp_argmin(fmix32(kP ^ idA), vA, fmix32(kP ^ idB), vB);
+            const uint32_t sub = __shfl_sync(0xFFFFFFFFu, jP < 32 ? sA : sB, jP & 31);
+            const bool inSub = (((sub < 4 ? cnt0 : cnt1) >> (8u * (sub & 3u))) & 0xFFu) > 1;
+            const uint32_t kQ = pick_draw(cs, baseL, 2u * k + 1u);
+            const bool qA = vA && lane != jP && (!inSub || sA == sub);
+            const bool qB = vB && lane + 32 != jP && (!inSub || sB == sub);
+            const int jQ = warp_argmin(fmix32(kQ ^ idA), qA, fmix32(kQ ^ idB), qB);
+            if (lane == L) {
+                pk.pq[k][0][L] = (uint8_t)(jP < 0 ? 255 : jP);
+                pk.pq[k][1][L] = (uint8_t)(jQ < 0 ? 255 : jQ);
+            }
+        }
+    }
+    __syncwarp();
+    if (q < nWork) {
+        const double R = smax[c];
+        const double smax0 = learned ? smaxSel[c] : R;
+        double stepMax = 0.0, collSep = 0.0;
+        unsigned coll = 0;
+        float2 au = make_float2(0.f, 0.f);
+        // The lane tests candidates until one is accepted, then collides
+        // it: lanes that reach an accepted candidate in the same pass run
+        // the FP64 exchange together, whatever the rejections before it.
+        int k = 0;
+        while (k < nCand) {
+            bool accepted = false;
+            long long gP = 0, gQ = 0;
+            Rng r(cs, (uint32_t)c, step, cand_tag(k));
+            double cr2 = 0.0;
+            Rec P, Q;
+            while (k < nCand) {
+                const int jP = pk.pq[k][0][lane], jQ = pk.pq[k][1][lane];
+                r = Rng(cs, (uint32_t)c, step, cand_tag(k));
+                ++k;
+                if (jP >= n || jQ >= n) {
+                    err |= ERRB_BOUNDS;
+                    continue;
+                }
+                gP = off + jP;
+                gQ = off + jQ;
+                if (test_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &P, &Q, &cr2, audit ? &au : nullptr)) {
+                    accepted = true;
+                    break;
+                }
+            }
+            if (accepted) {
+                collide_candidate(cs, s, r, gP, gQ, P, Q, cr2, &collSep, &err);
+                ++coll;
+            }
+        }
+        cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, exceed, obsMax, audit, au);
+        if (coll) {
+            acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
+            acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
+        }
+        nColl += coll;
+        nCandTot += (unsigned long long)nCand;
+    }
+    __syncwarp();   // the picks are read before the next cells overwrite them
+}
+
 // one lane per light cell, its candidates one after the other; blockDim.x
 // (the cells per CTA) is 32, 64 or 128, with one LightPicks per warp in
 // dynamic shared memory
@@ -644,140 +793,16 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
                 float* exceed, float* obsMax, double2* audit) {
     extern __shared__ __align__(16) unsigned char lightSmem[];
     LightPicks& pk = reinterpret_cast<LightPicks*>(lightSmem)[threadIdx.x >> 5];
-    const int lane = (int)(threadIdx.x & 31u);
     const uint32_t step = (uint32_t)ctr->step;
     const long long nWork = (long long)ctr->nWork;
     const long long nHeavy = (long long)ctr->nHeavy;
-    const long long C = cs.C;
     unsigned err = 0;
     unsigned long long nColl = 0, nCandTot = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long qb = nHeavy + (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); qb < nWork;
-         qb += stride) {
-        const long long q = qb + lane;
-        int2 it = make_int2(0, 0);
-        long long off = 0;
-        int n = 0;
-        if (q < nWork) {
-            it = work[q];
-            off = start[it.x];
-            n = start[it.x + 1] - (int)off;
-        }
-        const long long c = it.x;
-        int nCand = it.y;   // 0 past the end of the list
-        if (nCand >= LIGHT_CAND || n > LIGHT_N) {
-            // the list put a heavy cell here: record, never index past the picks
-            err |= ERRB_BOUNDS;
-            nCand = 0;
-        }
-        // every lane's picks, one cell at a time: coalesced loads of the
-        // cell's ids and cell words (the next cell's issued before this
-        // cell's picks), a warp minimum per pick
-        const uint32_t myBase = pick_base(cs, (uint32_t)c, step);
-        int ncN = __shfl_sync(0xFFFFFFFFu, nCand, 0);
-        int nN = __shfl_sync(0xFFFFFFFFu, n, 0);
-        long long offN = __shfl_sync(0xFFFFFFFFu, off, 0);
-        uint32_t idAN = 0, idBN = 0, sAN = 0, sBN = 0;
-        if (ncN) {
-            if (lane < nN) {
-                idAN = __ldg(s.id + offN + lane);
-                sAN = __ldg(s.cellw + offN + lane);
-            }
-            if (lane + 32 < nN) {
-                idBN = __ldg(s.id + offN + lane + 32);
-                sBN = __ldg(s.cellw + offN + lane + 32);
-            }
-        }
-        for (int L = 0; L < 32; ++L) {
-            const int nc = min(ncN, LIGHT_CAND - 1), nL = nN;
-            const uint32_t idA = idAN, idB = idBN, sA = sAN & 7u, sB = sBN & 7u;
-            const uint32_t baseL = __shfl_sync(0xFFFFFFFFu, myBase, L);
-            if (L + 1 < 32) {
-                ncN = __shfl_sync(0xFFFFFFFFu, nCand, L + 1);
-                nN = __shfl_sync(0xFFFFFFFFu, n, L + 1);
-                offN = __shfl_sync(0xFFFFFFFFu, off, L + 1);
-                idAN = idBN = sAN = sBN = 0;
-                if (ncN) {
-                    if (lane < nN) {
-                        idAN = __ldg(s.id + offN + lane);
-                        sAN = __ldg(s.cellw + offN + lane);
-                    }
-                    if (lane + 32 < nN) {
-                        idBN = __ldg(s.id + offN + lane + 32);
-                        sBN = __ldg(s.cellw + offN + lane + 32);
-                    }
-                }
-            }
-            if (nc == 0) continue;
-            const bool vA = lane < nL, vB = lane + 32 < nL;
-            // sub-cell occupancy, 8 bits per sub-cell (nL <= LIGHT_N < 256)
-            uint32_t cnt0 = 0, cnt1 = 0;
-            if (vA) (sA < 4 ? cnt0 : cnt1) += 1u << (8u * (sA & 3u));
-            if (vB) (sB < 4 ? cnt0 : cnt1) += 1u << (8u * (sB & 3u));
-            cnt0 = __reduce_add_sync(0xFFFFFFFFu, cnt0);
-            cnt1 = __reduce_add_sync(0xFFFFFFFFu, cnt1);
-            for (int k = 0; k < nc; ++k) {
-                const uint32_t kP = pick_draw(cs, baseL, 2u * k);
-                const int jP = warp_argmin(fmix32(kP ^ idA), vA, fmix32(kP ^ idB), vB);
-                const uint32_t sub = __shfl_sync(0xFFFFFFFFu, jP < 32 ? sA : sB, jP & 31);
-                const bool inSub = (((sub < 4 ? cnt0 : cnt1) >> (8u * (sub & 3u))) & 0xFFu) > 1;
-                const uint32_t kQ = pick_draw(cs, baseL, 2u * k + 1u);
-                const bool qA = vA && lane != jP && (!inSub || sA == sub);
-                const bool qB = vB && lane + 32 != jP && (!inSub || sB == sub);
-                const int jQ = warp_argmin(fmix32(kQ ^ idA), qA, fmix32(kQ ^ idB), qB);
-                if (lane == L) {
-                    pk.pq[k][0][L] = (uint8_t)(jP < 0 ? 255 : jP);
-                    pk.pq[k][1][L] = (uint8_t)(jQ < 0 ? 255 : jQ);
-                }
-            }
-        }
-        __syncwarp();
-        if (q < nWork) {
-            const double R = smax[c];
-            const double smax0 = learned ? smaxSel[c] : R;
-            double stepMax = 0.0, collSep = 0.0;
-            unsigned coll = 0;
-            float2 au = make_float2(0.f, 0.f);
-            // The lane tests candidates until one is accepted, then collides
-            // it: lanes that reach an accepted candidate in the same pass run
-            // the FP64 exchange together, whatever the rejections before it.
-            int k = 0;
-            while (k < nCand) {
-                bool accepted = false;
-                long long gP = 0, gQ = 0;
-                Rng r(cs, (uint32_t)c, step, cand_tag(k));
-                double cr2 = 0.0;
-                Rec P, Q;
-                while (k < nCand) {
-                    const int jP = pk.pq[k][0][lane], jQ = pk.pq[k][1][lane];
-                    r = Rng(cs, (uint32_t)c, step, cand_tag(k));
-                    ++k;
-                    if (jP >= n || jQ >= n) {
-                        err |= ERRB_BOUNDS;
-                        continue;
-                    }
-                    gP = off + jP;
-                    gQ = off + jQ;
-                    if (test_candidate(cs, s, r, gP, gQ, smax0, &stepMax, &P, &Q, &cr2, audit ? &au : nullptr)) {
-                        accepted = true;
-                        break;
-                    }
-                }
-                if (accepted) {
-                    collide_candidate(cs, s, r, gP, gQ, P, Q, cr2, &collSep, &err);
-                    ++coll;
-                }
-            }
-            cell_epilogue(smax, c, R, smax0, stepMax, learned, useR, exceed, obsMax, audit, au);
-            if (coll) {
-                acc[(cs.nSpecies * SACC + CACC_NCOLLS) * C + c] += (double)coll;
-                acc[(cs.nSpecies * SACC + CACC_COLLSEP) * C + c] += collSep;
-            }
-            nColl += coll;
-            nCandTot += (unsigned long long)nCand;
-        }
-        __syncwarp();   // the picks are read before the next cells overwrite them
-    }
+         qb += stride)
+        light_group(cs, s, start, smax, acc, work, learned, smaxSel, useR, exceed, obsMax, audit, qb, nWork, step,
+                    pk, err, nColl, nCandTot);
     if (nColl) atomicAdd(&ctr->coll, nColl);
     if (nCandTot) atomicAdd(&ctr->cand, nCandTot);
     if (err) atomicOr(&ctr->err, err);

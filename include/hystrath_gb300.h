@@ -554,6 +554,22 @@ dsmc_handle* dsmc_batch_case(dsmc_batch* b, int i);
 int dsmc_batch_initialise(dsmc_batch* b);
 int dsmc_batch_set_launch(dsmc_batch* b, int i, int cta_threads, int cells_per_cta);
 int dsmc_batch_evolve(dsmc_batch* b, long long n_steps);
+/* Persistent mode of the batch (no counterpart in the reference): every
+ * batched step is two cooperative persistent launches over all cases -- the
+ * move and sort phases, then the collision phases -- whose CTAs take
+ * (case, tile) work items from a queue per phase and wait at a grid barrier
+ * between phases, so that small and large cases share the SMs; the step of
+ * each buffer parity is captured as a CUDA graph where the driver allows
+ * cooperative launches in a capture, else launched directly.  Results equal
+ * the cases stepped alone.  move_threads: 128, 256 or 512; collide_threads:
+ * 64 or 128 (the light cells per CTA); 0, 0 returns to the graph of case
+ * graphs.  Every case must be a uniform box without inflow, obstacles,
+ * reduced-D axes, face tracking, learned maximum, selection audit or moment
+ * sums, with noTimeCounter selection; cells above 1024 parcels skip their
+ * collisions with the dense-cell error.  A grid barrier wait that runs out
+ * (it cannot while the launch is cooperative) returns DSMC_ERR_DEVICE. */
+int dsmc_batch_set_persistent(dsmc_batch* b, int move_threads, int collide_threads);
+int dsmc_batch_get_persistent(const dsmc_batch* b, int* move_threads, int* collide_threads);
 /* the same, with the device time of the n steps in *total_ms */
 int dsmc_batch_evolve_timed(dsmc_batch* b, long long n_steps, double* total_ms);
 

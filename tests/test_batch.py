@@ -179,3 +179,47 @@ def test_batch_follows_settings_changed_on_a_case():
         for g in alone:
             g.close()
         b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("threads", [(256, 128), (128, 64), (512, 128)])
+def test_persistent_batch_equals_steps_alone(threads):
+    """The persistent mode (two cooperative launches per step over all cases,
+    per-phase work queues) gives every case exactly the state it reaches
+    alone, Ar and N2 alike."""
+    from hystrath_gb300.batch import BatchCloud, heat_bath_cases
+    from hystrath_gb300.dsmc import DsmcCloud
+    specs, _ = heat_bath_cases(5, 256)
+    small = [s for s in specs if s.n_cells[0] <= 14][:6]
+    assert len(small) >= 3
+    b = BatchCloud(small)
+    b.initialise()
+    b.evolve(2)                         # the graph mode first, then switch
+    b.set_persistent(*threads)
+    b.evolve(5)
+    for i, s in enumerate(small):
+        g = DsmcCloud(s)
+        g.initialise()
+        g.evolve(7)
+        ib, ig = b.info(i), g.info()
+        assert ib.collisions_total == ig.collisions_total and ib.candidates_total == ig.candidates_total
+        assert ib.n_particles == ig.n_particles and ib.step == ig.step
+        sb, sg = _state_of_case(b, i), _state(g)
+        for k in sb:
+            assert np.array_equal(sb[k], sg[k]), k
+        np.testing.assert_array_equal(_case_view(b, i).field("Ttra"), g.field("Ttra"))
+        g.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_persistent_batch_rejects_cases_it_cannot_run():
+    from hystrath_gb300.batch import BatchCloud
+    from hystrath_gb300.dsmc import DsmcError
+    b = BatchCloud([S.config1(seed=1, n=8), S.config2(seed=2, scale=8)])
+    b.initialise()
+    with pytest.raises(DsmcError) as e:
+        b.set_persistent(256, 128)
+    assert "case 1" in str(e.value) and "inflow" in str(e.value)
+    b.evolve(2)                          # still steps in the graph mode
+    b.close()
