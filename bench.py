@@ -175,8 +175,10 @@ def kernel_bytes(N, C, n_moved, coll, cand, n_acc):
 
     move:    read pos, U, ERot and species word (64: the step's sample of the
              post-collision state is folded into the move) + cell word (4);
-             write pos (24) + cell word (4), for the parcels moved (the
-             parcels of the last step plus the inserted ones)
+             write the cell word (4), for the parcels moved (the parcels of
+             the last step plus the inserted ones); the end point of a plain
+             move is stored by the gather, which writes the record anyway,
+             so only the inserted parcels' positions (24) are written here
     gather:  read and write the 68-byte state of every kept parcel, plus its
              (source index, cell word) slot entry (8) and the id copy (4)
     sort:    the gather, the index scatter (cell word in, slot entry out:
@@ -188,7 +190,7 @@ def kernel_bytes(N, C, n_moved, coll, cand, n_acc):
              draw (8 B); per candidate the two velocities and species words
              (2 x 32 B); per collision the energies written back (2 x 64 B)
     """
-    move = 96.0 * n_moved
+    move = 72.0 * n_moved + 24.0 * max(n_moved - N, 0.0)
     gather = (2.0 * STATE_BYTES + 12.0) * N
     sort = gather + 12.0 * n_moved + 8.0 * C
     collide = (36.0 + 0.5 * n_acc) * C + 8.0 * N + 64.0 * cand + 128.0 * coll
@@ -359,18 +361,22 @@ def gpu_arm(args, rank, world, local):
         rep = learn.develop(make_spec(args, SEED + 7919 + rank), args.develop)
         rep.set_learned(model, args.learn_every, margin)
         rep.evolve(args.warmup + args.steps)
+        # the control: the same independent run with the plain selection
+        ctl = learn.develop(make_spec(args, SEED + 7919 + rank), args.develop)
+        ctl.evolve(args.warmup + args.steps)
         log("evaluation windows")
         for x in (g, lg):
             x.set_selection_audit(True)
-        # the three clouds take turns batch by batch
-        wp, wl, wr = learn.run_windows([g, lg, rep], args.eval_steps, args.eval_batches)
+        # the four clouds take turns batch by batch
+        wp, wl, wr, wc = learn.run_windows([g, lg, rep, ctl], args.eval_steps, args.eval_batches)
         rep.close()
+        ctl.close()
         for x in (g, lg):
             x.set_selection_audit(False)
         _, kl = lg.evolve_kernel_profile(args.steps)
         lg.close()
         lg = None
-        lvp = learn.compare_windows(s, wp, wl, wr)
+        lvp = learn.compare_windows(s, wp, wl, wr, wc)
         nl = 0.5 * (cl0.n_particles + cl1.n_particles)
         lvp["timed_steps"] = {
             "steps": args.steps,
@@ -387,7 +393,9 @@ def gpu_arm(args, rank, world, local):
         lvp["note"] = ("speed: both arms from the same developed state over the same steps (the learned arm's "
                        "predictions, every {} steps, inside its timed steps); per-cell counts and fields: the "
                        "plain arm against the learned arm of an independently seeded run of the same "
-                       "development (the comparison needs independent runs)".format(args.learn_every))
+                       "development (the comparison needs independent runs); the *_control entries compare "
+                       "the plain arm with the plain selection of that independent run, the same statistics "
+                       "when only the seeds differ".format(args.learn_every))
 
     # kernel groups and the roofline (not the value): K more steps with events
     log("kernel profile")

@@ -64,6 +64,7 @@ struct dsmc_handle {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraph_t graphT[2] = {nullptr, nullptr};   // the captured steps (child graphs of a batch)
     unsigned long long graphGen = 0;   // bumped whenever the step graphs are dropped
+    bool batchOwned = false;           // a case of a dsmc_batch: freed only by dsmc_batch_destroy
     unsigned char* solid = nullptr;
     double* info6 = nullptr;
     double* fieldTmp = nullptr;
@@ -517,7 +518,9 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
     mark(MK_ZERO);
     if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
     mark(MK_INFLOW);
-    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st, ev ? ev[MK_MOVE] : nullptr);
+    // a step that moves and sorts leaves the plain moves' end points to the gather
+    const bool movePending = (phases & DSMC_PHASE_MOVE) && (phases & DSMC_PHASE_SORT);
+    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st, ev ? ev[MK_MOVE] : nullptr, movePending);
     else mark(MK_MOVE);
     mark(MK_MOVE_SLOW);
     if (phases & DSMC_PHASE_MOVE) launch_sample_commit(cs, B, 0, st);
@@ -526,7 +529,7 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
         if (!(phases & DSMC_PHASE_MOVE)) launch_count(cs, B, a, st);
         launch_scan(cs, B, st);
         mark(MK_SCAN);
-        launch_scatter(cs, B, a, b, st, ev ? ev[MK_SCATTER] : nullptr);
+        launch_scatter(cs, B, a, b, st, ev ? ev[MK_SCATTER] : nullptr, movePending);
         mark(MK_GATHER);
         launch_finish_sort(B, st);
     } else {
@@ -849,6 +852,11 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
 
 void dsmc_destroy(dsmc_handle* h) {
     if (!h) return;
+    if (h->batchOwned) {
+        // the batch still steps this case: leave it to dsmc_batch_destroy
+        h->err = "dsmc_destroy: the case belongs to a batch (dsmc_batch_destroy frees it)";
+        return;
+    }
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graphs(h);
     for (void* q : h->allocs) cudaFree(q);
@@ -1619,6 +1627,7 @@ int dsmc_batch_create(int n, const dsmc_case_spec* specs, dsmc_batch** out) {
         for (dsmc_handle* q : b->cases) dsmc_destroy(q);
         return bfail(nullptr, DSMC_ERR_CUDA, "cannot create the batch stream");
     }
+    for (dsmc_handle* q : b->cases) q->batchOwned = true;
     *out = b.release();
     return DSMC_OK;
 }
@@ -1643,6 +1652,7 @@ int dsmc_batch_create_from_dirs(int n, const char* const* case_dirs, dsmc_batch*
         for (dsmc_handle* q : b->cases) dsmc_destroy(q);
         return bfail(nullptr, DSMC_ERR_CUDA, "cannot create the batch stream");
     }
+    for (dsmc_handle* q : b->cases) q->batchOwned = true;
     *out = b.release();
     return DSMC_OK;
 }
@@ -1662,7 +1672,10 @@ void dsmc_batch_destroy(dsmc_batch* b) {
     drop_persistent_graphs(b);
     if (b->dSlots) cudaFree(b->dSlots);
     if (b->dCtl) cudaFree(b->dCtl);
-    for (dsmc_handle* h : b->cases) dsmc_destroy(h);
+    for (dsmc_handle* h : b->cases) {
+        h->batchOwned = false;
+        dsmc_destroy(h);
+    }
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
 }

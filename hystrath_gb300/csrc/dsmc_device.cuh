@@ -44,9 +44,12 @@ enum : uint32_t {
 };
 
 // Cell word layout: bits 0-2 sub-cell (x | y<<1 | z<<2), bits 3-30 cell,
-// bit 31 "fresh" (inserted this step: random step fraction on first move).
+// bit 31 "fresh" before the move (inserted this step: random step fraction
+// on first move) and "move pending" between the move and the gather (the end
+// point x + U dt is not stored yet).
 constexpr uint32_t CELLW_DELETED = 0xFFFFFFFFu;
 constexpr uint32_t CELLW_FRESH = 0x80000000u;
+constexpr uint32_t CELLW_MOVE_PENDING = 0x80000000u;
 __host__ __device__ inline uint32_t cellw_cell(uint32_t w) { return (w & 0x7FFFFFFFu) >> 3; }
 __host__ __device__ inline uint32_t cellw_sub(uint32_t w) { return w & 7u; }
 

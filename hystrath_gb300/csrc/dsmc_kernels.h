@@ -102,12 +102,14 @@ int scan_scratch_ints(long long C);
 
 void launch_count(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
 // mid (optional): an event recorded between the fast path and the boundary path
+// deferPos: the sort follows in the same step, and the end points of plain
+// moves are left to its gather (launch_scatter with movePending)
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st,
-                 cudaEvent_t mid = nullptr);
+                 cudaEvent_t mid = nullptr, bool deferPos = false);
 void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
 // mid (optional): an event recorded between the index scatter and the gather
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
-                    cudaStream_t st, cudaEvent_t mid = nullptr);
+                    cudaStream_t st, cudaEvent_t mid = nullptr, bool movePending = false);
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
 // sample count, pending sample and unflushed samples back to zero (a reset
 // of the time averages)

@@ -546,7 +546,7 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
 template <bool GEN>
 __device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, Counters* ctr, int* slowList,
                                           int* count, long long* sfix, long long i, long long n, uint32_t step,
-                                          int doSample, unsigned& err) {
+                                          int doSample, int deferPos, unsigned& err) {
     int key = -1;
     bool slow = false;
     int skey = -1;
@@ -632,11 +632,18 @@ __device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, C
                     const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(q[3].y) >> 32);
                     track_internal(cs, xs, Us, sc, te, sv_species(sv));
                 }
-                q[0] = make_double2(ex, ey);
-                s.r[i].z = ez;
+                // with the sort following, the end point of a plain move
+                // (x + U dt, no reduced-D axis) is left to the gather, which
+                // reads the record anyway and repeats the same fma; bit 31
+                // of the cell word says so
+                const bool defer = deferPos && !fresh && !(GEN && cs.anyEmpty);
+                if (!defer) {
+                    q[0] = make_double2(ex, ey);
+                    s.r[i].z = ez;
+                }
                 const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
                                     (uint32_t)((c2x & 1) | ((c2y & 1) << 1) | ((c2z & 1) << 2));
-                s.cellw[i] = nw;
+                s.cellw[i] = defer ? (nw | CELLW_MOVE_PENDING) : nw;
                 key = (int)(nw >> 3);
                 fast = true;
             }
@@ -658,14 +665,14 @@ __device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, C
 
 template <bool GEN>
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
-k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix) {
+k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix, int deferPos) {
     const long long n = ctr->nMoved;
     const uint32_t step = (uint32_t)ctr->step;
     const int doSample = ctr->pendingSample;
     unsigned err = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride)
-        move_iter<GEN>(cs, s, ctr, slowList, count, sfix, base + threadIdx.x, n, step, doSample, err);
+        move_iter<GEN>(cs, s, ctr, slowList, count, sfix, base + threadIdx.x, n, step, doSample, deferPos, err);
     if (err) atomicOr(&ctr->err, err);
 }
 
@@ -910,28 +917,39 @@ __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_scatter_index(const uint
         scatter_iter(cellw, ctr, start, count, sortSrc, base + threadIdx.x, n);
 }
 
-// One destination slot j of k_gather.
+// One destination slot j of k_gather.  dt != 0: a cell word with
+// CELLW_MOVE_PENDING marks a parcel whose move ended at x + U dt without being
+// stored (k_move with deferPos); the end point is made here with the same
+// fma, so it is bit for bit the move's.
 __device__ __forceinline__ void gather_slot(const Parcels& src, const Parcels& dst, Counters* ctr,
-                                            const int2* __restrict__ sortSrc, long long j, long long nSrc) {
+                                            const int2* __restrict__ sortSrc, long long j, long long nSrc,
+                                            double dt) {
     const int2 sk = __ldg(sortSrc + j);
     const long long i = sk.x;
     if (i < 0 || i >= nSrc) {
         atomicOr(&ctr->err, ERRB_BOUNDS);
         return;
     }
-    const Rec p = ldg_rec(src.r + i);
+    Rec p = ldg_rec(src.r + i);
+    uint32_t w = (uint32_t)sk.y;
+    if (dt != 0.0 && (w & CELLW_MOVE_PENDING)) {
+        p.x = fma(p.ux, dt, p.x);
+        p.y = fma(p.uy, dt, p.y);
+        p.z = fma(p.uz, dt, p.z);
+        w &= ~CELLW_MOVE_PENDING;
+    }
     st_rec(dst.r + j, p);
-    __stcs(dst.cellw + j, (uint32_t)sk.y);
+    __stcs(dst.cellw + j, w);
     dst.id[j] = p.id;
 }
 
 __global__ void __launch_bounds__(MAX_STREAM_THREADS) k_gather(Parcels src, Parcels dst, Counters* ctr,
-                                                const int2* __restrict__ sortSrc) {
+                                                const int2* __restrict__ sortSrc, double dt) {
     const long long n = ctr->nKept;
     const long long nSrc = ctr->nMoved;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride)
-        gather_slot(src, dst, ctr, sortSrc, j, nSrc);
+        gather_slot(src, dst, ctr, sortSrc, j, nSrc, dt);
 }
 
 // Parcels handed over as arrays (positions and velocities n x 3, ERot,
@@ -1331,7 +1349,7 @@ k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
                     const long long base = (l * BM_IT + k) * T;
                     if (base >= nm) break;
                     move_iter<false>(cs, sl.src, ctr, B.slowList, B.count, B.sfix, base + tid, nm, step, doSample,
-                                     err);
+                                     1, err);
                 }
                 break;
             }
@@ -1410,7 +1428,7 @@ k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
                 const long long nk = ctr->nKept, nm = ctr->nMoved;
                 for (int k = 0; k < BM_IT; ++k) {
                     const long long j = (l * BM_IT + k) * T + tid;
-                    if (j < nk) gather_slot(sl.src, sl.dst, ctr, B.sortSrc, j, nm);
+                    if (j < nk) gather_slot(sl.src, sl.dst, ctr, B.sortSrc, j, nm, cs.dt);
                 }
                 break;
             }
@@ -1457,12 +1475,14 @@ cudaError_t launch_batch_move(const BatchSlot* slots, int n, BatchCtl* ctl, int 
     return cudaLaunchCooperativeKernel((const void*)k_batch_move, dim3(grid), dim3(threads), args, 0, st);
 }
 
-void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st, cudaEvent_t mid) {
+void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st, cudaEvent_t mid,
+                 bool deferPos) {
     const int T = B.cfg.streamThreads;
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
     const bool general = cs.anyEmpty || cs.nObst || cs.faceFlux || cs.half[0] || cs.half[1] || cs.half[2];
-    if (general) k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
-    else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix);
+    const int d = deferPos ? 1 : 0;
+    if (general) k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d);
+    else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d);
     if (mid) cudaEventRecord(mid, st);
     k_move_slow<<<grid_for(B.capacity, T, 2), T, 0, st>>>(cs, s, B.ctr, B.slowList,
                                                                                B.bfPatch, B.wall, B.count);
@@ -1482,13 +1502,12 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st) {
 }
 
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
-                    cudaStream_t st, cudaEvent_t mid) {
-    (void)cs;
+                    cudaStream_t st, cudaEvent_t mid, bool movePending) {
     const int T = B.cfg.streamThreads;
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
     k_scatter_index<<<grid, T, 0, st>>>(src.cellw, B.ctr, B.start, B.count, B.sortSrc);
     if (mid) cudaEventRecord(mid, st);
-    k_gather<<<grid, T, 0, st>>>(src, dst, B.ctr, B.sortSrc);
+    k_gather<<<grid, T, 0, st>>>(src, dst, B.ctr, B.sortSrc, movePending ? cs.dt : 0.0);
 }
 
 void launch_pack(const Parcels& dst, long long n, const double* pos, const double* U, const double* erot,

@@ -314,12 +314,14 @@ def temperature_groups(ttra, k=5):
     return g, names
 
 
-def compare_windows(spec, plain, learned, replicate=None):
+def compare_windows(spec, plain, learned, replicate=None, control=None):
     """The learned_vs_plain report.  plain and learned: run_window results
     from the same developed state (the speed comparison); replicate: a
     run_window of the learned selection from an independently seeded run of
     the same development, the per-cell count and field comparisons (which
-    need independent runs) use it when given."""
+    need independent runs) use it when given; control: the plain selection
+    of that independent run, compared with plain the same way (two plain
+    runs: what the statistics read when only the seeds differ)."""
     del spec
     rp, rl = arm_rates(plain), arm_rates(learned)
     res = {"window_steps": plain["steps"], "plain": rp, "learned": rl,
@@ -338,6 +340,11 @@ def compare_windows(spec, plain, learned, replicate=None):
     res["fields_in_se"] = {k: batch_mean_z(plain["batches"][k], other["batches"][k])
                            for k in plain["batches"] if k in other["batches"]}
     res["fields_in_se"]["block_cells"] = plain["blk"] ** 3
+    if control is not None:
+        res["per_cell_counts_control"] = per_cell_count_test(plain["nColls"], control["nColls"], groups, names)
+        res["per_cell_counts_control"]["runs"] = "independent seeds, both plain"
+        res["fields_in_se_control"] = {k: batch_mean_z(plain["batches"][k], control["batches"][k])
+                                       for k in plain["batches"] if k in control["batches"]}
     return res
 
 
@@ -376,16 +383,19 @@ def evaluate(spec, spec_replicate, model, margin, every, develop_steps, window, 
         g.set_selection_audit(True)
     clouds = [p, lr]
     if spec_replicate is not None:
-        # the same development and window start as the other two
+        # the same development and window start as the other two, learned
+        # and (the control) plain
         l2 = develop(spec_replicate, develop_steps)
         l2.set_learned(model, every, margin)
         clouds.append(l2)
+        clouds.append(develop(spec_replicate, develop_steps))
     ws = run_windows(clouds, window, batches)
     for g in clouds:
         g.close()
     wp, wl = ws[0], ws[1]
     rep = ws[2] if len(ws) > 2 else None
-    return compare_windows(spec, wp, wl, rep)
+    ctl = ws[3] if len(ws) > 3 else None
+    return compare_windows(spec, wp, wl, rep, ctl)
 
 
 def main():

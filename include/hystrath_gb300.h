@@ -430,6 +430,8 @@ int dsmc_phase_times(dsmc_handle* h, double* ms_inflow, double* ms_move, double*
 
 const char* dsmc_last_error(const dsmc_handle* h);
 const char* dsmc_last_global_error(void);
+/* Frees the cloud.  A handle from dsmc_batch_case is left alone (its
+ * dsmc_last_error says so): dsmc_batch_destroy frees the batch's cases. */
 void dsmc_destroy(dsmc_handle* h);
 
 /*

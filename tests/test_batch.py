@@ -207,7 +207,11 @@ def test_persistent_batch_equals_steps_alone(threads):
         sb, sg = _state_of_case(b, i), _state(g)
         for k in sb:
             assert np.array_equal(sb[k], sg[k]), k
-        np.testing.assert_array_equal(_case_view(b, i).field("Ttra"), g.field("Ttra"))
+        view = _case_view(b, i)
+        try:
+            np.testing.assert_array_equal(view.field("Ttra"), g.field("Ttra"))
+        finally:
+            view.h = None   # owned by the batch
         g.close()
     b.close()
 
@@ -222,4 +226,20 @@ def test_persistent_batch_rejects_cases_it_cannot_run():
         b.set_persistent(256, 128)
     assert "case 1" in str(e.value) and "inflow" in str(e.value)
     b.evolve(2)                          # still steps in the graph mode
+    b.close()
+
+
+@pytest.mark.gpu
+def test_destroying_a_batched_case_is_refused():
+    """dsmc_destroy on a handle from dsmc_batch_case leaves the case to the
+    batch (no double free when the batch is destroyed)."""
+    from hystrath_gb300.batch import BatchCloud
+    from hystrath_gb300.dsmc import lib
+    b = BatchCloud([S.config1(seed=1, n=8), S.config1(seed=2, n=8)])
+    b.initialise()
+    h = lib().dsmc_batch_case(b.h, 1)
+    lib().dsmc_destroy(h)
+    assert b"belongs to a batch" in lib().dsmc_last_error(h)
+    b.evolve(2)
+    assert b.info(1).step == 2
     b.close()

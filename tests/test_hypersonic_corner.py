@@ -10,7 +10,8 @@ same window in 10 batches of 150 steps.  Two checks:
   and the reference in units of its standard error, from batch means (the
   reference's realisation has the standard error of one of our runs; the
   batch variance is widened for the lag-1 correlation of consecutive
-  batches); at most the fraction of |z| > 2 that Student's t with the
+  batches, or by how far the two seeds' window means differ where that is
+  more); at most the fraction of |z| > 2 that Student's t with the
   batches' degrees of freedom gives, plus three of its standard deviations;
 - the earlier percent bands: our seeds' RMS deviation from the reference no
   larger than their spread, the mean bias below 0.3%, spanwise-averaged
@@ -71,21 +72,29 @@ def lag1(batch_series):
 
 
 def z_per_bin(batches_by_seed, ref):
-    """|our mean - reference| / standard error per bin, and the degrees of
-    freedom of the batch variance.  Consecutive batches of 150 steps are
-    not quite independent (the flow crosses the domain in a few hundred
-    steps): the batch variance is widened by 1 + 2 rho, rho the lag-1
-    correlation of the batch means pooled over bins and seeds."""
-    B = np.concatenate([bins(b) for b in batches_by_seed])       # (seeds x batches, bins)
-    k = B.shape[0]
-    # pooled within-seed batch variance (the seeds' means may differ only by noise)
-    rho = lag1([bins(b) for b in batches_by_seed])
-    var = np.mean([bins(b).var(0, ddof=1) for b in batches_by_seed], axis=0) * max(1.0, 1.0 + 2.0 * rho)
-    se_ours = np.sqrt(var / k)
-    se_ref = np.sqrt(var / BATCHES)              # one run of the same window
-    z = (B.mean(0) - bins(ref)) / np.sqrt(se_ours ** 2 + se_ref ** 2)
-    dof = len(batches_by_seed) * (BATCHES - 1)
-    return z, dof
+    """(our mean - reference) / standard error per bin, the degrees of
+    freedom of the batch variance, and the factor the variance was widened
+    by.  The variance of one run's window mean is the batch variance / the
+    batches, widened where consecutive batches are not independent: by
+    1 + 2 rho (rho the lag-1 correlation of the batch means, pooled over
+    bins and seeds), and by the seeds' own disagreement where that is
+    larger: the squared differences of the seeds' window means, pooled over
+    bins, against what the batch variance predicts for them (slow motions of
+    the shock, longer than a batch, show up there and in the reference's one
+    realisation alike)."""
+    Bs = [bins(b) for b in batches_by_seed]                    # seeds x (batches, bins)
+    S = len(Bs)
+    means = np.array([b.mean(0) for b in Bs])                  # (seeds, bins)
+    var_b = np.mean([b.var(0, ddof=1) for b in Bs], axis=0)    # pooled within-seed batch variance
+    var_run = var_b / BATCHES                                  # one run's window mean, independent batches
+    widen = max(1.0, 1.0 + 2.0 * lag1(Bs))
+    ok = var_run > 0
+    spread = np.sum((means - means.mean(0)) ** 2, axis=0) / (S - 1)
+    widen = max(widen, float(np.mean(spread[ok] / var_run[ok])))
+    var_run = var_run * widen
+    z = (means.mean(0) - bins(ref)) / np.sqrt(var_run / S + var_run)   # ours (S runs) and the reference's one
+    dof = S * (BATCHES - 1)
+    return z, dof, widen
 
 
 def t_tail(t, dof):
@@ -98,13 +107,13 @@ def test_corner_flow_matches_reference_fields(gpu_lib):
     a, b = run(1), run(2)
     report = {}
     for f in FIELDS:
-        z, dof = z_per_bin([a[f], b[f]], ref[f])
+        z, dof, widen = z_per_bin([a[f], b[f]], ref[f])
         z = z[np.isfinite(z)]
         p2 = float(t_tail(2.0, dof))
         frac = float(np.mean(np.abs(z) > 2.0))
-        report[f] = (round(frac, 4), round(p2, 4), round(float(np.mean(z)), 3))
+        report[f] = (round(frac, 4), round(p2, 4), round(float(np.mean(z)), 3), round(widen, 2))
         assert frac <= p2 + 3.0 * np.sqrt(p2 * (1 - p2) / z.size), (f, report[f])
-    print("fraction of bins with |z| > 2 (ours, expected, mean z):", report)
+    print("fraction of bins with |z| > 2 (ours, expected, mean z, variance widened by):", report)
     for f in ("rhoN", "Ttra", "Ux", "p"):
         r = ref[f].astype(np.float64)
         ma, mb = a[f].mean(0), b[f].mean(0)

@@ -114,3 +114,23 @@ def test_a_common_trend_stays_out_of_the_standard_error():
     assert abs(r["z"]) < 4.0
     assert r["paired_variance_over_mean"] < 0.6
     assert r["rms_rel_diff_upper95"] < 0.012
+
+
+def _window(rng, mu, ms=100.0):
+    nc = _batches(rng, mu)
+    return {"steps": 400, "ms": ms, "n_start": 1000, "n_end": 1000, "collisions": int(nc.sum()),
+            "candidates": int(1.7 * nc.sum()), "nColls": list(nc), "Ttra": 300.0 + mu,
+            "batches": {"rhoN": [rng.normal(1.0, 0.01, 500) for _ in range(8)]}, "blk": 8, "audit": None}
+
+
+def test_compare_windows_reports_the_plain_control():
+    """Learned and control windows from the same distribution: the learned
+    comparison and the plain-vs-plain control read alike."""
+    rng, mu = _mu(8, n=50_000)
+    p, l, r, c = (_window(rng, mu) for _ in range(4))
+    res = learn.compare_windows(None, p, l, r, c)
+    for key in ("per_cell_counts", "per_cell_counts_control"):
+        assert abs(res[key]["z"]) < 4.0, key
+    assert res["per_cell_counts_control"]["runs"] == "independent seeds, both plain"
+    assert set(res["fields_in_se_control"]) == {"rhoN"}
+    assert "per_cell_counts_control" not in learn.compare_windows(None, p, l, r)
