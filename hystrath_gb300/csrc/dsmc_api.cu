@@ -65,6 +65,14 @@ struct dsmc_handle {
     cudaGraph_t graphT[2] = {nullptr, nullptr};   // the captured steps (child graphs of a batch)
     unsigned long long graphGen = 0;   // bumped whenever the step graphs are dropped
     bool batchOwned = false;           // a case of a dsmc_batch: freed only by dsmc_batch_destroy
+    // spatial decomposition: the two halves of a step (inflow and move to the
+    // packed migrants; the sort onwards) as graphs per parity, whether a step
+    // is between its halves, and its moved-parcel count as of then
+    cudaGraphExec_t half1[2] = {nullptr, nullptr};
+    cudaGraphExec_t half2[2] = {nullptr, nullptr};
+    bool midStep = false;
+    long long nMovedHost = 0;
+    long long nMigHost = 0;
     unsigned char* solid = nullptr;
     double* info6 = nullptr;
     double* fieldTmp = nullptr;
@@ -401,6 +409,8 @@ void fill_case_dev(dsmc_handle* h) {
     cs.maxCrossings = MAX_CROSSINGS;
     cs.maxCellParcels = MAX_ORDERED_CELL;
     cs.capacityLimit = 1LL << 62;
+    cs.domAxis = -1;
+    cs.domLo = cs.domHi = 0;
 }
 
 Parcels& cur_soa(dsmc_handle* h) { return h->buf[h->cur]; }
@@ -437,7 +447,9 @@ int check_device_error(dsmc_handle* h) {
             m += " a cell above " + std::to_string(h->cs.maxCellParcels) +
                  " parcels or 2^24 candidates (its collisions were skipped);";
         if (e & ERRB_IDS) m += " parcel id space exhausted (more than 2^32 parcels inserted since the start);";
-        return fail(h, e & ERRB_CAPACITY ? DSMC_ERR_CAPACITY : DSMC_ERR_DEVICE, m);
+        if (e & ERRB_MIGRANT) m += " a migrant for a cell outside this domain (dropped);";
+        if (e & ERRB_MIGRANT_CAP) m += " more migrants than the migrant buffer holds (the rest dropped);";
+        return fail(h, (e & (ERRB_CAPACITY | ERRB_MIGRANT_CAP)) ? DSMC_ERR_CAPACITY : DSMC_ERR_DEVICE, m);
     }
     return DSMC_OK;
 }
@@ -501,7 +513,9 @@ enum {
 
 // Enqueue one step on the handle's stream (graph capture or direct launch).
 // ev: NULL, or MK_COUNT events recorded at the marks above.
-void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) {
+// part: 0 the whole step; for a divided cloud 1 the inflow, the move and the
+// packed migrants, 2 the rest (received migrants are added in between).
+void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev, int part) {
     const CaseDev& cs = h->cs;
     StepBuffers& B = h->B;
     cudaStream_t st = h->stream;
@@ -510,21 +524,27 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev) 
     auto mark = [&](int k) {
         if (ev) cudaEventRecord(ev[k], st);
     };
-    mark(MK_START);
-    launch_zero_step(B, st);
-    // a sample pending from the previous step is taken by the move kernel,
-    // or here when this step does not move
-    if (!(phases & DSMC_PHASE_MOVE)) launch_sample_flush(cs, B, a, 0, st);
-    mark(MK_ZERO);
-    if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
-    mark(MK_INFLOW);
     // a step that moves and sorts leaves the plain moves' end points to the gather
     const bool movePending = (phases & DSMC_PHASE_MOVE) && (phases & DSMC_PHASE_SORT);
-    if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st, ev ? ev[MK_MOVE] : nullptr, movePending);
-    else mark(MK_MOVE);
-    mark(MK_MOVE_SLOW);
-    if (phases & DSMC_PHASE_MOVE) launch_sample_commit(cs, B, 0, st);
-    mark(MK_SAMPLE);
+    if (part != 2) {
+        mark(MK_START);
+        launch_zero_step(B, st);
+        // a sample pending from the previous step is taken by the move
+        // kernel, or here when this step does not move
+        if (!(phases & DSMC_PHASE_MOVE)) launch_sample_flush(cs, B, a, 0, st);
+        mark(MK_ZERO);
+        if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
+        mark(MK_INFLOW);
+        if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st, ev ? ev[MK_MOVE] : nullptr, movePending);
+        else mark(MK_MOVE);
+        mark(MK_MOVE_SLOW);
+        if (phases & DSMC_PHASE_MOVE) launch_sample_commit(cs, B, 0, st);
+        if (part == 1) {
+            launch_pack_migrants(cs, B, a, st);
+            return;
+        }
+        mark(MK_SAMPLE);
+    }
     if (phases & DSMC_PHASE_SORT) {
         if (!(phases & DSMC_PHASE_MOVE)) launch_count(cs, B, a, st);
         launch_scan(cs, B, st);
@@ -578,7 +598,7 @@ int build_graphs(dsmc_handle* h) {
         if (h->graph[p]) continue;
         cudaGraph_t g;
         CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        enqueue_step(h, p, DSMC_PHASE_ALL, nullptr);
+        enqueue_step(h, p, DSMC_PHASE_ALL, nullptr, 0);
         CUDA_TRY(h, cudaStreamEndCapture(h->stream, &g));
         CUDA_TRY(h, cudaGraphInstantiate(&h->graph[p], g, 0));
         h->graphT[p] = g;
@@ -593,9 +613,39 @@ void drop_graphs(dsmc_handle* h) {
     for (int p = 0; p < 2; ++p) {
         if (h->graph[p]) cudaGraphExecDestroy(h->graph[p]);
         if (h->graphT[p]) cudaGraphDestroy(h->graphT[p]);
+        if (h->half1[p]) cudaGraphExecDestroy(h->half1[p]);
+        if (h->half2[p]) cudaGraphExecDestroy(h->half2[p]);
         h->graph[p] = nullptr;
         h->graphT[p] = nullptr;
+        h->half1[p] = h->half2[p] = nullptr;
     }
+}
+
+// The two halves of a divided cloud's step, captured per parity.
+int build_half_graphs(dsmc_handle* h) {
+    for (int p = 0; p < 2; ++p) {
+        for (int part = 1; part <= 2; ++part) {
+            cudaGraphExec_t& ex = part == 1 ? h->half1[p] : h->half2[p];
+            if (ex) continue;
+            cudaGraph_t g;
+            CUDA_TRY(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_step(h, p, DSMC_PHASE_ALL, nullptr, part);
+            CUDA_TRY(h, cudaStreamEndCapture(h->stream, &g));
+            const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            CUDA_TRY(h, e);
+        }
+    }
+    return DSMC_OK;
+}
+
+// The whole-step entry points do not run a divided cloud (its migrants
+// must be handed over between the two halves).
+int refuse_divided(dsmc_handle* h, const char* fn) {
+    if (h->cs.domAxis < 0) return DSMC_OK;
+    return fail(h, DSMC_ERR_INVALID,
+                std::string(fn) + ": the cloud is divided (dsmc_set_domain); it steps with dsmc_step_begin, "
+                                  "dsmc_get_migrants / dsmc_add_migrants and dsmc_step_end");
 }
 
 int sort_current(dsmc_handle* h, long long n) {
@@ -608,6 +658,8 @@ int sort_current(dsmc_handle* h, long long n) {
     c = *h->ctrHost;
     c.n = n;
     c.nMoved = n;
+    c.nMig = 0;
+    c.migIn = 0;
     *h->ctrHost = c;
     CUDA_TRY(h, cudaMemcpy(B.ctr, h->ctrHost, sizeof(Counters), cudaMemcpyHostToDevice));
     launch_cellw(cs, cur_soa(h), n, st);
@@ -751,6 +803,7 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     if ((rc = dalloc(h, &B.inflowAcc, ni))) return rc;
     if ((rc = dalloc(h, &B.inflowCount, ni))) return rc;
     if ((rc = dalloc(h, &B.inflowOff, ni + 1))) return rc;
+    if ((rc = dalloc(h, &B.inflowOffLocal, ni + 1))) return rc;
     if ((rc = dalloc(h, &B.inflowTerm, ni))) return rc;
     // graded mesh: half-node tables, cell volumes and boundary-face areas
     if (spec->node_coords[0] || spec->node_coords[1] || spec->node_coords[2]) {
@@ -859,6 +912,7 @@ void dsmc_destroy(dsmc_handle* h) {
     }
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graphs(h);
+    if (h->B.migIn) cudaFree(h->B.migIn);
     for (void* q : h->allocs) cudaFree(q);
     if (h->ctrHost) cudaFreeHost(h->ctrHost);
     if (h->ctrRing) cudaFreeHost(h->ctrRing);
@@ -920,7 +974,9 @@ int dsmc_initialise(dsmc_handle* h) {
 }
 
 int dsmc_evolve(dsmc_handle* h, long long n) {
-    int rc = build_graphs(h);
+    int rc = refuse_divided(h, "dsmc_evolve");
+    if (rc) return rc;
+    rc = build_graphs(h);
     if (rc) return rc;
     for (long long i = 0; i < n; ++i) {
         schedule_pre(h, h->stream);
@@ -936,11 +992,12 @@ int dsmc_evolve(dsmc_handle* h, long long n) {
 // event time.
 int profile_steps(dsmc_handle* h, long long n, double* per_mark, double* total_ms) {
     if (n <= 0) return fail(h, DSMC_ERR_INVALID, "n must be positive");
+    if (int rc = refuse_divided(h, "the profiled steps")) return rc;
     std::vector<cudaEvent_t> ev((size_t)n * MK_COUNT);
     for (auto& e : ev) CUDA_TRY(h, cudaEventCreate(&e));
     for (long long i = 0; i < n; ++i) {
         schedule_pre(h, h->stream);
-        enqueue_step(h, h->cur, DSMC_PHASE_ALL, &ev[(size_t)i * MK_COUNT]);
+        enqueue_step(h, h->cur, DSMC_PHASE_ALL, &ev[(size_t)i * MK_COUNT], 0);
         h->cur ^= 1;
         schedule_post(h);
     }
@@ -983,7 +1040,9 @@ int dsmc_evolve_kernel_profile(dsmc_handle* h, long long n, double* group_ms, in
 }
 
 int dsmc_evolve_timed(dsmc_handle* h, long long n, double* total_ms) {
-    int rc = build_graphs(h);
+    int rc = refuse_divided(h, "dsmc_evolve_timed");
+    if (rc) return rc;
+    rc = build_graphs(h);
     if (rc) return rc;
     cudaEvent_t e0, e1;
     CUDA_TRY(h, cudaEventCreate(&e0));
@@ -1006,10 +1065,11 @@ int dsmc_evolve_timed(dsmc_handle* h, long long n, double* total_ms) {
 }
 
 int dsmc_run_phases(dsmc_handle* h, unsigned phases) {
+    if (int rc = refuse_divided(h, "dsmc_run_phases")) return rc;
     cudaEvent_t ev[MK_COUNT];
     for (int k = 0; k < MK_COUNT; ++k) cudaEventCreate(&ev[k]);
     if (phases == DSMC_PHASE_ALL) schedule_pre(h, h->stream);
-    enqueue_step(h, h->cur, phases, ev);
+    enqueue_step(h, h->cur, phases, ev, 0);
     if (phases == DSMC_PHASE_ALL) schedule_post(h);
     CUDA_TRY(h, cudaGetLastError());
     if (phases & DSMC_PHASE_SORT) h->cur ^= 1;
@@ -1307,7 +1367,9 @@ int dsmc_counts(dsmc_handle* h, dsmc_counts_t* o) {
 int dsmc_evolve_counts(dsmc_handle* h, long long n, dsmc_counts_t* out) {
     if (n < 0) return fail(h, DSMC_ERR_INVALID, "n must not be negative");
     if (n > 0 && !out) return fail(h, DSMC_ERR_INVALID, "dsmc_evolve_counts: out is NULL");
-    int rc = build_graphs(h);
+    int rc = refuse_divided(h, "dsmc_evolve_counts");
+    if (rc) return rc;
+    rc = build_graphs(h);
     if (rc) return rc;
     if (n > h->ctrRingN) {
         if (h->ctrRing) cudaFreeHost(h->ctrRing);
@@ -1506,6 +1568,109 @@ int dsmc_set_selection_audit(dsmc_handle* h, int on) {
     h->B.audit = on ? h->auditBuf : nullptr;
     drop_graphs(h);   // the collision kernels take the buffer as a parameter
     return DSMC_OK;
+}
+
+// ------------------------------------------------------- spatial decomposition
+int dsmc_set_domain(dsmc_handle* h, int axis, int lo, int hi) {
+    if (h->batchOwned) return fail(h, DSMC_ERR_INVALID, "dsmc_set_domain: the case belongs to a batch");
+    if (h->midStep) return fail(h, DSMC_ERR_INVALID, "dsmc_set_domain: a step is between its halves");
+    if (axis < -1 || axis > 2) return fail(h, DSMC_ERR_INVALID, "dsmc_set_domain: axis must be -1, 0, 1 or 2");
+    if (axis >= 0 && !(0 <= lo && lo < hi && hi <= h->cs.n[axis]))
+        return fail(h, DSMC_ERR_INVALID, "dsmc_set_domain: need 0 <= lo < hi <= " + std::to_string(h->cs.n[axis]) +
+                                             " cells along the axis");
+    if (axis >= 0 && h->cs.C >= (1LL << 24))
+        return fail(h, DSMC_ERR_INVALID, "dsmc_set_domain: meshes of 2^24 cells and more are not divided");
+    StepBuffers& B = h->B;
+    if (axis >= 0 && !B.migList) {
+        // the migrants of one step: an eighth of the capacity (a domain
+        // thinner than a step's travel needs more; the overflow is reported)
+        B.migCap = B.capacity / 8 + 65536;
+        int rc;
+        if ((rc = dalloc(h, &B.migList, B.migCap))) return rc;
+        if ((rc = dalloc(h, &B.migOut, B.migCap * MIGRANT_WORDS))) return rc;
+    }
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->cs.domAxis = axis;
+    h->cs.domLo = axis >= 0 ? lo : 0;
+    h->cs.domHi = axis >= 0 ? hi : 0;
+    drop_graphs(h);
+    // the parcels of other domains' cells leave now
+    CUDA_TRY(h, cudaMemcpy(h->ctrHost, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost));
+    const long long n = h->ctrHost->n;
+    if (axis >= 0 && n > 0) {
+        flush_sample(h);
+        return sort_current(h, n);
+    }
+    return DSMC_OK;
+}
+
+int dsmc_step_begin(dsmc_handle* h, long long* n_migrants) {
+    if (h->cs.domAxis < 0) return fail(h, DSMC_ERR_INVALID, "dsmc_step_begin: the cloud is not divided");
+    if (h->midStep) return fail(h, DSMC_ERR_INVALID, "dsmc_step_begin: the previous step has not ended");
+    int rc = build_half_graphs(h);
+    if (rc) return rc;
+    schedule_pre(h, h->stream);
+    CUDA_TRY(h, cudaGraphLaunch(h->half1[h->cur], h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ctrHost, h->B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->midStep = true;
+    h->nMovedHost = h->ctrHost->nMoved;
+    h->nMigHost = std::min((long long)h->ctrHost->nMig, h->B.migCap);
+    if (n_migrants) *n_migrants = h->nMigHost;
+    return DSMC_OK;
+}
+
+int dsmc_get_migrants(dsmc_handle* h, void* dst, long long n) {
+    if (!h->midStep) return fail(h, DSMC_ERR_INVALID, "dsmc_get_migrants: no step between its halves");
+    if (n < 0 || n > h->nMigHost)
+        return fail(h, DSMC_ERR_INVALID, "dsmc_get_migrants: n must lie in [0, " + std::to_string(h->nMigHost) + "]");
+    if (n == 0) return DSMC_OK;
+    if (!dst) return fail(h, DSMC_ERR_INVALID, "dsmc_get_migrants: dst is NULL");
+    CUDA_TRY(h, cudaMemcpyAsync(dst, h->B.migOut, (size_t)n * MIGRANT_WORDS * 4, cudaMemcpyDefault, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    return DSMC_OK;
+}
+
+int dsmc_add_migrants(dsmc_handle* h, const void* src, long long n) {
+    if (!h->midStep) return fail(h, DSMC_ERR_INVALID, "dsmc_add_migrants: no step between its halves");
+    if (n < 0) return fail(h, DSMC_ERR_INVALID, "dsmc_add_migrants: n must not be negative");
+    if (n == 0) return DSMC_OK;
+    if (!src) return fail(h, DSMC_ERR_INVALID, "dsmc_add_migrants: src is NULL");
+    StepBuffers& B = h->B;
+    const long long limit = std::min(B.capacity, h->cs.capacityLimit);
+    if (h->nMovedHost + n > limit)
+        return fail(h, DSMC_ERR_CAPACITY, "dsmc_add_migrants: " + std::to_string(n) + " migrants exceed the capacity");
+    cudaPointerAttributes at{};
+    const bool onDevice = cudaPointerGetAttributes(&at, src) == cudaSuccess &&
+                          (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
+    cudaGetLastError();   // a host pointer may leave an error behind on older runtimes
+    const uint32_t* d = static_cast<const uint32_t*>(src);
+    if (!onDevice) {
+        if (n > B.migInCap) {
+            if (B.migIn) cudaFree(B.migIn);
+            B.migIn = nullptr;
+            B.migInCap = 0;
+            void* q = nullptr;
+            CUDA_TRY(h, cudaMalloc(&q, (size_t)n * MIGRANT_WORDS * 4));
+            B.migIn = static_cast<uint32_t*>(q);
+            B.migInCap = n;
+        }
+        CUDA_TRY(h, cudaMemcpyAsync(B.migIn, src, (size_t)n * MIGRANT_WORDS * 4, cudaMemcpyHostToDevice, h->stream));
+        d = B.migIn;
+    }
+    launch_unpack_migrants(h->cs, B, cur_soa(h), d, n, h->nMovedHost, h->stream);
+    CUDA_TRY(h, cudaGetLastError());
+    h->nMovedHost += n;
+    return DSMC_OK;
+}
+
+int dsmc_step_end(dsmc_handle* h) {
+    if (!h->midStep) return fail(h, DSMC_ERR_INVALID, "dsmc_step_end: no step between its halves");
+    CUDA_TRY(h, cudaGraphLaunch(h->half2[h->cur], h->stream));
+    h->cur ^= 1;
+    h->midStep = false;
+    schedule_post(h);
+    return check_device_error(h);
 }
 
 // ------------------------------------------------------- loop caps

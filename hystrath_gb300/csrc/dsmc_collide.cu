@@ -130,6 +130,9 @@ __global__ void k_zero_step(Counters* ctr) {
     ctr->nSlow = 0;
     ctr->nWork = 0;
     ctr->nHeavy = 0;
+    ctr->nMig = 0;
+    ctr->migIn = 0;
+    ctr->inflowLocal = 0;
 }
 
 // ---------------------------------------------------------------- moments

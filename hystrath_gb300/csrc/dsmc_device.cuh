@@ -34,7 +34,7 @@ constexpr int ZV_TAB = 512;     // iMax values tabulated for 1/Zv
 // Error bits of the device error word.
 enum : unsigned {
     ERRB_CROSSINGS = 1u, ERRB_REJECTION = 2u, ERRB_CAPACITY = 4u, ERRB_BOUNDS = 8u,
-    ERRB_PATCH = 16u, ERRB_DENSE = 32u, ERRB_IDS = 64u
+    ERRB_PATCH = 16u, ERRB_DENSE = 32u, ERRB_IDS = 64u, ERRB_MIGRANT = 128u, ERRB_MIGRANT_CAP = 256u
 };
 
 // Random-stream tags (counter word 3) shared with the CPU replay.
@@ -131,12 +131,12 @@ struct CaseDev {
     long long nBFaces;
     int nAcc;           // doubles per cell of sampling accumulators
     int hasWallMeasure;
+    // FP32 reciprocals of n[0] and n[0] n[1] for cell_coords
+    float rcpN0, rcpN01;
     // caps of the loops the reference runs without bound and of the cell size
     // the collision kernels order (MAX_REJECTION, MAX_CROSSINGS, ORDER_MAX_N
     // unless lowered by dsmc_set_limits), and the parcel capacity the inflow
     // may fill (the allocation unless lowered)
-    // FP32 reciprocals of n[0] and n[0] n[1] for cell_coords
-    float rcpN0, rcpN01;
     int maxRejection;
     int maxCrossings;
     int maxCellParcels;
@@ -145,6 +145,11 @@ struct CaseDev {
     // (dsmcCloud.C:1420-1490 depends on iMax, species and pair omega only):
     // invZvTab[((p * DSMC_MAX_SPECIES + q) * ZV_TAB) + iMax]
     const double* invZvTab;
+    // spatial decomposition (dsmc_set_domain): the cloud owns the parcels of
+    // the cells with domLo <= index < domHi along axis domAxis; -1: all cells
+    int domAxis;
+    int domLo, domHi;
+    int pad2;
 };
 
 // Sampling accumulators: per cell, per species s at s*SACC + k.
@@ -385,6 +390,15 @@ __device__ __forceinline__ void cell_coords(const CaseDev& cs, uint32_t c, int* 
         *j = (int)((c / n0) % (uint32_t)cs.n[1]);
         *k = (int)(c / n01);
     }
+}
+
+// Whether linear cell c belongs to this cloud's domain (dsmc_set_domain).
+__device__ __forceinline__ bool cell_owned(const CaseDev& cs, uint32_t c) {
+    if (cs.domAxis < 0) return true;
+    int i, j, k;
+    cell_coords(cs, c, &i, &j, &k);
+    const int v = cs.domAxis == 0 ? i : cs.domAxis == 1 ? j : k;
+    return v >= cs.domLo && v < cs.domHi;
 }
 
 // ------------------------------------------------------- velocity moments

@@ -26,6 +26,13 @@ struct Counters {
     int unflushed;              // samples held in the fixed-point sums
     unsigned long long nWork;   // cells with candidates this step
     unsigned long long nHeavy;  // of which one warp each (the first nHeavy of the work list)
+    // spatial decomposition: parcels that left for another domain this step
+    // (their indices in migList) and parcels received from other domains;
+    // the inflow's insertions into owned cells (inflowTotal counts every
+    // inflow face: the parcel ids of the undivided case)
+    unsigned long long nMig;
+    long long migIn;
+    long long inflowLocal;
 };
 
 // Launch shape of one cloud's step, chosen by the autotuner: threads per CTA
@@ -71,6 +78,15 @@ struct StepBuffers {
     // because the maximum used was below the product)
     double2* audit;
     int* slowList;            // [capacity] parcels that take the boundary path this step
+    // spatial decomposition (allocated by dsmc_set_domain): indices of the
+    // step's migrants, their packed records (MIGRANT_WORDS words each) and a
+    // staging buffer for migrants handed over in host memory
+    int* migList;             // [migCap]
+    uint32_t* migOut;         // [migCap * MIGRANT_WORDS]
+    uint32_t* migIn;          // [migInCap * MIGRANT_WORDS]
+    long long migCap;
+    long long migInCap;
+    int* inflowOffLocal;      // [nInflowFaces * nSpecies + 1] inflow offsets of the owned faces
     int2* sortSrc;            // [capacity] (source index, cell word) of each destination slot of the sort
     // inflow
     int nInflowFaces;
@@ -102,6 +118,9 @@ int scan_scratch_ints(long long C);
 
 void launch_count(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
 // mid (optional): an event recorded between the fast path and the boundary path
+// A migrant between domains: the 64-byte parcel record and its cell word.
+constexpr int MIGRANT_WORDS = 17;
+
 // deferPos: the sort follows in the same step, and the end points of plain
 // moves are left to its gather (launch_scatter with movePending)
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st,
@@ -111,6 +130,12 @@ void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,
                     cudaStream_t st, cudaEvent_t mid = nullptr, bool movePending = false);
 void launch_finish_sort(const StepBuffers& B, cudaStream_t st);
+// spatial decomposition: the step's migrants packed into B.migOut (their end
+// points made) and dropped from the cloud; n migrants at src (device
+// memory, MIGRANT_WORDS words each) appended at slot base and counted
+void launch_pack_migrants(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st);
+void launch_unpack_migrants(const CaseDev& cs, const StepBuffers& B, const Parcels& s, const uint32_t* src,
+                            long long n, long long base, cudaStream_t st);
 // sample count, pending sample and unflushed samples back to zero (a reset
 // of the time averages)
 void launch_reset_sample_counters(const StepBuffers& B, cudaStream_t st);

@@ -546,9 +546,11 @@ __device__ __forceinline__ void sample_contrib(long long* sfix, long long C, int
 template <bool GEN>
 __device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, Counters* ctr, int* slowList,
                                           int* count, long long* sfix, long long i, long long n, uint32_t step,
-                                          int doSample, int deferPos, unsigned& err) {
+                                          int doSample, int deferPos, int* migList, long long migCap,
+                                          unsigned& err) {
     int key = -1;
     bool slow = false;
+    bool migrant = false;
     int skey = -1;
     double sux = 0, suy = 0, suz = 0, ser = 0;
     int svb = 0;
@@ -644,7 +646,13 @@ __device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, C
                 const uint32_t nw = ((uint32_t)(cx + cs.n[0] * (cy + cs.n[1] * cz)) << 3) |
                                     (uint32_t)((c2x & 1) | ((c2y & 1) << 1) | ((c2z & 1) << 2));
                 s.cellw[i] = defer ? (nw | CELLW_MOVE_PENDING) : nw;
-                key = (int)(nw >> 3);
+                if (GEN && cs.domAxis >= 0) {
+                    // a move that ends in another domain's cell: the parcel
+                    // leaves as a migrant (a processor patch, Cloud.C:255-466)
+                    const int ca = cs.domAxis == 0 ? cx : cs.domAxis == 1 ? cy : cz;
+                    migrant = ca < cs.domLo || ca >= cs.domHi;
+                }
+                key = migrant ? -1 : (int)(nw >> 3);
                 fast = true;
             }
         }
@@ -660,19 +668,36 @@ __device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, C
         base0 = __shfl_sync(0xFFFFFFFFu, base0, __ffs(m) - 1);
         if (slow) slowList[base0 + __popc(m & ((1u << lane) - 1u))] = (int)i;
     }
+    if (GEN && cs.domAxis >= 0) {
+        // warp-aggregated append of the migrants
+        const unsigned mm = __ballot_sync(0xFFFFFFFFu, migrant);
+        if (mm) {
+            const unsigned lane = lane_id();
+            unsigned long long b0 = 0;
+            if (lane == (unsigned)(__ffs(mm) - 1)) b0 = atomicAdd(&ctr->nMig, (unsigned long long)__popc(mm));
+            b0 = __shfl_sync(0xFFFFFFFFu, b0, __ffs(mm) - 1);
+            const long long q = (long long)b0 + __popc(mm & ((1u << lane) - 1u));
+            if (migrant) {
+                if (q < migCap) migList[q] = (int)i;
+                else err |= ERRB_MIGRANT_CAP;
+            }
+        }
+    }
     if (doSample) sample_contrib(sfix, cs.C, skey, sux, suy, suz, ser, svb, &err);
 }
 
 template <bool GEN>
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
-k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix, int deferPos) {
+k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix, int deferPos,
+       int* migList, long long migCap) {
     const long long n = ctr->nMoved;
     const uint32_t step = (uint32_t)ctr->step;
     const int doSample = ctr->pendingSample;
     unsigned err = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride)
-        move_iter<GEN>(cs, s, ctr, slowList, count, sfix, base + threadIdx.x, n, step, doSample, deferPos, err);
+        move_iter<GEN>(cs, s, ctr, slowList, count, sfix, base + threadIdx.x, n, step, doSample, deferPos, migList,
+                       migCap, err);
     if (err) atomicOr(&ctr->err, err);
 }
 
@@ -741,7 +766,7 @@ __global__ void k_set_pending(Counters* ctr) { ctr->pendingSample = 1; }
 // The boundary path for the parcels k_move deferred, densely packed.
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_move_slow(CaseDev cs, Parcels s, Counters* ctr, const int* __restrict__ slowList, const int* __restrict__ bfPatch,
-            double* wall, int* count) {
+            double* wall, int* count, int* migList, long long migCap) {
     const long long nSlow = (long long)ctr->nSlow;
     const uint32_t step = (uint32_t)ctr->step;
     unsigned err = 0;
@@ -751,9 +776,80 @@ k_move_slow(CaseDev cs, Parcels s, Counters* ctr, const int* __restrict__ slowLi
         const uint32_t w = s.cellw[i];
         const uint32_t nw = move_slow(cs, s, i, step, w, bfPatch, wall, &err, &ctr->wallHits);
         s.cellw[i] = nw;
-        if (nw != CELLW_DELETED) atomicAdd(&count[nw >> 3], 1);
+        if (nw == CELLW_DELETED) continue;
+        if (cs.domAxis >= 0 && !cell_owned(cs, nw >> 3)) {
+            // the boundary path ended in another domain's cell: a migrant
+            const unsigned long long q = atomicAdd(&ctr->nMig, 1ull);
+            if ((long long)q < migCap) migList[q] = (int)i;
+            else err |= ERRB_MIGRANT_CAP;
+            continue;
+        }
+        atomicAdd(&count[nw >> 3], 1);
     }
     if (err) atomicOr(&ctr->err, err);
+}
+
+// The step's migrants, packed for the exchange: the record with its end
+// point made (a plain move's is left to the gather otherwise) and the cell
+// word; each leaves this cloud (deleted from the sort's point of view).
+__global__ void k_pack_migrants(Parcels s, Counters* ctr, const int* __restrict__ migList, uint32_t* out,
+                                long long migCap, double dt) {
+    const long long nm = min((long long)ctr->nMig, migCap);
+    for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < nm;
+         j += (long long)gridDim.x * blockDim.x) {
+        const long long i = migList[j];
+        Rec p = ldg_rec(s.r + i);
+        uint32_t w = s.cellw[i];
+        if (w & CELLW_MOVE_PENDING) {
+            p.x = fma(p.ux, dt, p.x);
+            p.y = fma(p.uy, dt, p.y);
+            p.z = fma(p.uz, dt, p.z);
+            w &= ~CELLW_MOVE_PENDING;
+        }
+        const uint32_t* pw = reinterpret_cast<const uint32_t*>(&p);
+        uint32_t* o = out + j * MIGRANT_WORDS;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) o[k] = pw[k];
+        o[16] = w;
+        s.cellw[i] = CELLW_DELETED;
+    }
+}
+
+// n migrants from other domains appended at slots base.. and counted in
+// their cells; one for a cell this cloud does not own is dropped (error
+// bit).
+__global__ void k_unpack_migrants(CaseDev cs, Parcels s, Counters* ctr, const uint32_t* __restrict__ src,
+                                  long long n, long long base, int* count) {
+    unsigned err = 0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long b0 = (long long)blockIdx.x * blockDim.x; b0 < n; b0 += stride) {
+        const long long k = b0 + threadIdx.x;
+        int key = -1;
+        if (k < n) {
+            const uint32_t* q = src + k * MIGRANT_WORDS;
+            Rec p;
+            uint32_t* pw = reinterpret_cast<uint32_t*>(&p);
+#pragma unroll
+            for (int t = 0; t < 16; ++t) pw[t] = q[t];
+            const uint32_t w = q[16] & ~CELLW_MOVE_PENDING;
+            const uint32_t c = cellw_cell(w);
+            st_rec(s.r + base + k, p);
+            if ((long long)c < cs.C && cell_owned(cs, c)) {
+                s.cellw[base + k] = w;
+                key = (int)c;
+            } else {
+                s.cellw[base + k] = CELLW_DELETED;
+                err |= ERRB_MIGRANT;
+            }
+        }
+        agg_count(count, key);
+    }
+    if (err) atomicOr(&ctr->err, err);
+}
+
+__global__ void k_migrants_commit(Counters* ctr, long long n) {
+    ctr->nMoved += n;
+    ctr->migIn += n;
 }
 
 __global__ void k_count(Parcels s, long long n, int* count) {
@@ -997,7 +1093,8 @@ __global__ void k_ids_from_records(Parcels s, long long n) {
 }
 
 __global__ void k_finish_sort(Counters* ctr) {
-    ctr->deleted += (unsigned long long)(ctr->nMoved - ctr->nKept);
+    // parcels dropped by the sort: deleted, or sent to another domain
+    ctr->deleted += (unsigned long long)(ctr->nMoved - ctr->nKept) - ctr->nMig;
     ctr->n = ctr->nKept;
     ctr->nMoved = ctr->nKept;
 }
@@ -1018,8 +1115,8 @@ __global__ void k_end_step(Counters* ctr) {
 // ---------------------------------------------------------------- inflow
 // One thread per (inflow face, species): Bird eq. 4.22 flux accumulation and
 // the integer-plus-remainder count (dsmcFreeStreamInflowPatch.C:96-141,226-236).
-// One thread per (inflow face, species): the flux accumulation and the
-// integer-plus-remainder count (dsmcFreeStreamInflowPatch.C:96-141,226-236).
+// A divided cloud counts every inflow face (the face remainders and the
+// parcel ids stay those of the undivided case) and fills only its own.
 __global__ void k_inflow_count(CaseDev cs, int nFaces, const long long* __restrict__ face,
                                const double* __restrict__ term, double* accum, int* cnt, const Counters* ctr) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1040,51 +1137,66 @@ __global__ void k_inflow_count(CaseDev cs, int nFaces, const long long* __restri
     cnt[t] = nI;
 }
 
-__global__ void k_inflow_scan(const int* cnt, int n, int* off, Counters* ctr, long long capacity) {
-    // single block
-    int carry = 0;
+// Offsets of the (face, species) counts over every inflow face (off: the
+// parcel ids) and over the faces of owned cells (offLocal: the slots; equal
+// to off for an undivided cloud).  Single block.
+__global__ void k_inflow_scan(CaseDev cs, const int* cnt, int n, const int* __restrict__ cellOf, int* off,
+                              int* offLocal, Counters* ctr, long long capacity) {
+    const int ns = cs.nSpecies;
+    int carry = 0, carryL = 0;
     for (int b0 = 0; b0 < n; b0 += blockDim.x) {
         const int b = b0 + threadIdx.x;
         const int v = (b < n) ? cnt[b] : 0;
-        int total;
+        const int vL = (b < n && cell_owned(cs, (uint32_t)cellOf[b / ns])) ? v : 0;
+        int total, totalL;
         const int ex = block_exclusive_scan(v, &total);
-        if (b < n) off[b] = carry + ex;
+        const int exL = block_exclusive_scan(vL, &totalL);
+        if (b < n) {
+            off[b] = carry + ex;
+            offLocal[b] = carryL + exL;
+        }
         carry += total;
+        carryL += totalL;
     }
     if (threadIdx.x == 0) {
         off[n] = carry;
-        if (ctr->n + carry > capacity) {
+        offLocal[n] = carryL;
+        if (ctr->n + carryL > capacity) {
             atomicOr(&ctr->err, ERRB_CAPACITY);
-            off[n] = -1;
+            offLocal[n] = -1;
             ctr->inflowTotal = 0;
+            ctr->inflowLocal = 0;
         } else {
             ctr->inflowTotal = carry;
+            ctr->inflowLocal = carryL;
         }
     }
 }
 
 // One thread per inserted parcel (dsmcFreeStreamInflowPatch.C:237-364): the
-// parcel's (face, species) is found by bisection of the count offsets, and
-// every parcel draws from its own stream (face, step, species, parcel).
+// parcel's (face, species) is found by bisection of the owned faces' count
+// offsets, its id from the offsets over every face, and every parcel draws
+// from its own stream (face, step, species, parcel).
 __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long long* __restrict__ face,
                               const int* __restrict__ side, const int* __restrict__ cellOf,
-                              const int* __restrict__ bfPatch, const int* __restrict__ off, Parcels s,
-                              Counters* ctr) {
+                              const int* __restrict__ bfPatch, const int* __restrict__ off,
+                              const int* __restrict__ offLocal, Parcels s, Counters* ctr) {
     const int ns = cs.nSpecies;
     const int nt = nFaces * ns;
-    const long long total = off[nt];
+    const long long total = offLocal[nt];
     if (total <= 0) return;     // nothing inserted (or capacity exceeded: -1)
     unsigned err = 0;
-    for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total;
-         g += (long long)gridDim.x * blockDim.x) {
-        // the (face, species) slot t with off[t] <= g < off[t + 1]
+    for (long long gl = (long long)blockIdx.x * blockDim.x + threadIdx.x; gl < total;
+         gl += (long long)gridDim.x * blockDim.x) {
+        // the (face, species) slot t with offLocal[t] <= gl < offLocal[t + 1]
         int lo = 0, hi = nt;
         while (hi - lo > 1) {
             const int mid = (lo + hi) >> 1;
-            if (off[mid] <= g) lo = mid; else hi = mid;
+            if (offLocal[mid] <= gl) lo = mid; else hi = mid;
         }
         const int t = lo;
-        const int q = (int)(g - off[t]);
+        const int q = (int)(gl - offLocal[t]);
+        const long long g = (long long)off[t] + q;     // over every face: the id
         const int f = t / ns, m = t % ns;
         const long long bf = face[f];
         const int sd = side[f];
@@ -1132,7 +1244,7 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
         U[c] = scT * g2 + pt.U[c];
         const double erot = eq_rot(r, pt.Trot, sp.rotDof, &err);
         const int vib = eq_vib(r, pt.Tvib, sp);
-        const long long slot = ctr->n + g;
+        const long long slot = ctr->n + gl;
         Rec p;
         p.x = x[0]; p.y = x[1]; p.z = x[2];
         p.ux = U[0]; p.uy = U[1]; p.uz = U[2];
@@ -1155,13 +1267,13 @@ __global__ void k_inflow_fill(CaseDev cs, InflowDev in, int nFaces, const long l
 
 __global__ void k_inflow_commit(Counters* ctr) {
     const long long add = ctr->inflowTotal;
-    ctr->inserted = (unsigned long long)add;
+    ctr->inserted = (unsigned long long)ctr->inflowLocal;
     // parcel ids are 32-bit and must stay unique (the light-cell picks and
     // the canonical (sub-cell, id) order rely on it): flag the step whose
     // insertions run past 2^32 ids
     if ((unsigned long long)ctr->nextId + (unsigned long long)add > 0x100000000ull) ctr->err |= ERRB_IDS;
     ctr->nextId += add;
-    ctr->nMoved = ctr->n + add;
+    ctr->nMoved = ctr->n + ctr->inflowLocal;
 }
 
 // ---------------------------------------------------------------- mesh fill
@@ -1265,7 +1377,9 @@ __global__ void k_cellw(CaseDev cs, Parcels s, long long n) {
         sb |= (c2 & 1) << a;
     }
     const uint32_t fresh = s.cellw[i] & CELLW_FRESH;
-    s.cellw[i] = (((uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2])) << 3) | (uint32_t)sb) | fresh;
+    const uint32_t c = (uint32_t)(ci[0] + cs.n[0] * (ci[1] + cs.n[1] * ci[2]));
+    // a divided cloud keeps only the parcels of its own cells
+    s.cellw[i] = cell_owned(cs, c) ? ((c << 3) | (uint32_t)sb) | fresh : CELLW_DELETED;
 }
 
 __global__ void k_remainder_init(CaseDev cs, double* rem) {
@@ -1352,7 +1466,7 @@ k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
                     const long long base = (l * BM_IT + k) * T;
                     if (base >= nm) break;
                     move_iter<false>(cs, sl.src, ctr, B.slowList, B.count, B.sfix, base + tid, nm, step, doSample,
-                                     1, err);
+                                     1, nullptr, 0, err);
                 }
                 break;
             }
@@ -1482,13 +1596,25 @@ void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cuda
                  bool deferPos) {
     const int T = B.cfg.streamThreads;
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
-    const bool general = cs.anyEmpty || cs.nObst || cs.faceFlux || cs.half[0] || cs.half[1] || cs.half[2];
+    const bool general = cs.anyEmpty || cs.nObst || cs.faceFlux || cs.half[0] || cs.half[1] || cs.half[2] ||
+                         cs.domAxis >= 0;
     const int d = deferPos ? 1 : 0;
-    if (general) k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d);
-    else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d);
+    if (general) k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d, B.migList, B.migCap);
+    else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d, nullptr, 0);
     if (mid) cudaEventRecord(mid, st);
-    k_move_slow<<<grid_for(B.capacity, T, 2), T, 0, st>>>(cs, s, B.ctr, B.slowList,
-                                                                               B.bfPatch, B.wall, B.count);
+    k_move_slow<<<grid_for(B.capacity, T, 2), T, 0, st>>>(cs, s, B.ctr, B.slowList, B.bfPatch, B.wall, B.count,
+                                                          B.migList, B.migCap);
+}
+
+void launch_pack_migrants(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
+    k_pack_migrants<<<grid_for(B.migCap, 256, 2), 256, 0, st>>>(s, B.ctr, B.migList, B.migOut, B.migCap, cs.dt);
+}
+
+void launch_unpack_migrants(const CaseDev& cs, const StepBuffers& B, const Parcels& s, const uint32_t* src,
+                            long long n, long long base, cudaStream_t st) {
+    if (n <= 0) return;
+    k_unpack_migrants<<<grid_for(n, 256, 8), 256, 0, st>>>(cs, s, B.ctr, src, n, base, B.count);
+    k_migrants_commit<<<1, 1, 0, st>>>(B.ctr, n);
 }
 
 void launch_count(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st) {
@@ -1600,11 +1726,11 @@ void launch_inflow(const CaseDev& cs, const InflowDev& in, const StepBuffers& B,
     const int grid = (nt + 255) / 256;
     k_inflow_count<<<grid, 256, 0, st>>>(cs, B.nInflowFaces, B.inflowFace, B.inflowTerm, B.inflowAcc,
                                          B.inflowCount, B.ctr);
-    k_inflow_scan<<<1, 1024, 0, st>>>(B.inflowCount, nt, B.inflowOff, B.ctr,
+    k_inflow_scan<<<1, 1024, 0, st>>>(cs, B.inflowCount, nt, B.inflowCell, B.inflowOff, B.inflowOffLocal, B.ctr,
                                       cs.capacityLimit < B.capacity ? cs.capacityLimit : B.capacity);
     k_inflow_fill<<<grid_for(B.capacity, 256, 8), 256, 0, st>>>(cs, in, B.nInflowFaces, B.inflowFace,
                                                                 B.inflowSide, B.inflowCell, B.bfPatch,
-                                                                B.inflowOff, s, B.ctr);
+                                                                B.inflowOff, B.inflowOffLocal, s, B.ctr);
     k_inflow_commit<<<1, 1, 0, st>>>(B.ctr);
 }
 

@@ -15,6 +15,10 @@ import numpy as np
 
 from . import spec as S
 
+# a migrant between domains: the 64-byte parcel record and the 4-byte cell
+# word (DSMC_MIGRANT_BYTES of the C header)
+MIGRANT_BYTES = 68
+
 _lib = None
 
 
@@ -91,6 +95,11 @@ def _load() -> C.CDLL:
     L.dsmc_mlp_predict.argtypes = [vp, vp, C.c_longlong, vp]
     L.dsmc_set_learned.argtypes = [vp, vp, C.c_int, C.c_float]
     L.dsmc_learn_record.argtypes = [vp, C.c_longlong, vp, vp, C.POINTER(C.c_longlong)]
+    L.dsmc_set_domain.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.dsmc_step_begin.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.dsmc_get_migrants.argtypes = [vp, vp, C.c_longlong]
+    L.dsmc_add_migrants.argtypes = [vp, vp, C.c_longlong]
+    L.dsmc_step_end.argtypes = [vp]
     _lib = L
     return L
 
@@ -228,6 +237,41 @@ class DsmcCloud:
 
     def run_phases(self, phases: int):
         self._chk(lib().dsmc_run_phases(self.h, phases))
+
+    # ------------------------------------------------ spatial decomposition
+    def set_domain(self, axis: int, lo: int = 0, hi: int = 0):
+        """Own only the cells lo <= index < hi along axis (-1: all cells)."""
+        self._chk(lib().dsmc_set_domain(self.h, int(axis), int(lo), int(hi)))
+
+    def step_begin(self) -> int:
+        """Inflow and move of a divided cloud; returns the migrant count."""
+        n = C.c_longlong(0)
+        self._chk(lib().dsmc_step_begin(self.h, C.byref(n)))
+        return n.value
+
+    def get_migrants(self, n: int, dst=None):
+        """The step's first n migrants: into dst (a device pointer, int) or,
+        without dst, as a host array of n x MIGRANT_BYTES bytes."""
+        if dst is not None:
+            self._chk(lib().dsmc_get_migrants(self.h, C.c_void_p(int(dst)), int(n)))
+            return None
+        out = np.empty((int(n), MIGRANT_BYTES), dtype=np.uint8)
+        if n:
+            self._chk(lib().dsmc_get_migrants(self.h, out.ctypes.data_as(C.c_void_p), int(n)))
+        return out
+
+    def add_migrants(self, src, n: int = None):
+        """Migrants from other domains: a host array of n x MIGRANT_BYTES
+        bytes, or a device pointer (int) with n."""
+        if isinstance(src, np.ndarray):
+            src = np.ascontiguousarray(src, dtype=np.uint8).reshape(-1, MIGRANT_BYTES)
+            self._chk(lib().dsmc_add_migrants(self.h, src.ctypes.data_as(C.c_void_p), len(src)))
+        else:
+            self._chk(lib().dsmc_add_migrants(self.h, C.c_void_p(int(src)), int(n)))
+
+    def step_end(self):
+        """Sort, collisions and sampling of a divided cloud's step."""
+        self._chk(lib().dsmc_step_end(self.h))
 
     def phase_times(self):
         v = [C.c_double() for _ in range(5)]

@@ -435,6 +435,40 @@ const char* dsmc_last_global_error(void);
 void dsmc_destroy(dsmc_handle* h);
 
 /*
+ * Spatial decomposition, the reference's processor patches: Cloud::move
+ * (Cloud.C:255-466) hands a parcel that reaches a processor patch to the
+ * neighbouring domain, and the step's totals are summed over the processors
+ * (noTimeCounter.C:312-314, dsmcCloud.C:938-958).  Here a cloud keeps the
+ * whole case but owns only the parcels of the cells with lo <= index < hi
+ * along axis (0 x, 1 y, 2 z; meshes below 2^24 cells): dsmc_set_domain drops
+ * the others (also from later dsmc_initialise / dsmc_set_particles /
+ * dsmc_restore), and a parcel whose move ends in another domain's cell
+ * leaves the cloud as a migrant, its move complete.  The inflow counts every
+ * inflow face, so the parcel ids are those of the undivided case, and
+ * inserts into owned cells only.  Collisions and sampling are per cell and
+ * keyed by the global cell: the domains of a divided case together step
+ * exactly as the undivided case does.  axis = -1 undoes the division (the
+ * parcels stay).  A divided cloud steps in two halves with the migrants
+ * handed over between them:
+ *   dsmc_step_begin   inflow and move; the migrants packed on the device
+ *   dsmc_get_migrants n migrants, DSMC_MIGRANT_BYTES each (the 64-byte parcel
+ *                     record and the 4-byte cell word), to host or device
+ *                     memory
+ *   dsmc_add_migrants migrants from other domains (host or device memory),
+ *                     before the sort; one for a cell this cloud does not own
+ *                     is dropped and reported by dsmc_step_end
+ *   dsmc_step_end     occupancy sort, collisions, sampling
+ * The whole-step calls (dsmc_evolve, dsmc_evolve_timed, dsmc_evolve_counts,
+ * dsmc_run_phases, the profiles) return DSMC_ERR_INVALID on a divided cloud.
+ */
+#define DSMC_MIGRANT_BYTES 68
+int dsmc_set_domain(dsmc_handle* h, int axis, int lo, int hi);
+int dsmc_step_begin(dsmc_handle* h, long long* n_migrants);
+int dsmc_get_migrants(dsmc_handle* h, void* dst, long long n);
+int dsmc_add_migrants(dsmc_handle* h, const void* src, long long n);
+int dsmc_step_end(dsmc_handle* h);
+
+/*
  * Cell start offsets for callers that must not allocate device memory.  This
  * entry point has no counterpart in the reference (whose occupancy lists live
  * in host memory); it is the exclusive scan of the occupancy sort, offered to

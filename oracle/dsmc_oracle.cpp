@@ -25,6 +25,8 @@
 //   samplers              dsmcCloud.C:1015-1051, 1181-1244, 1327-1531
 //   sampling              .../dsmcVolFields/dsmcVolFields.C:1071-1290 (sums), 1365-1876 (fields)
 //   mesh fill             .../initialiseDsmcParcels/derived/dsmcMeshFill/dsmcMeshFill.C:68-238
+//   processor transfer    src/lagrangian/basic/Cloud/Cloud.C:255-466 (stepBegin / addMigrants /
+//                         stepEnd: a divided case's migrants arrive with their move complete)
 //
 // Random numbers: the reference draws from one sequential OpenFOAM Random
 // stream, which lives outside the reference and cannot be replayed.  Here
@@ -225,6 +227,11 @@ struct Oracle {
     uint32_t nextId;
     long long sampleSteps;
     long long collLast, candLast, collTot, candTot, wallHitsLast, insertedLast, deletedLast;
+    // spatial decomposition (dsmc_set_domain's restatement): the parcels of
+    // cells lo <= index < hi along domAxis are this domain's; -1: all
+    int domAxis = -1, domLo = 0, domHi = 0;
+    std::vector<uint32_t> migOut;               // the step's migrants, 17 words each
+    long long migLast = 0;                      // migrants sent by the last step
     int err;
     int nThreads;
     std::string msg;
@@ -872,6 +879,11 @@ struct Oracle {
             }
         }
         for (Parcel& p : added) p.id = nextId++;
+        // a divided case: every domain counts every face (the face remainders
+        // and the ids are those of the undivided case) and keeps its own
+        if (domAxis >= 0)
+            added.erase(std::remove_if(added.begin(), added.end(), [&](const Parcel& p) { return !owned(p.cell); }),
+                        added.end());
         insertedLast = (long long)added.size();
         P.insert(P.end(), added.begin(), added.end());
         if (e) err = 1;
@@ -1189,6 +1201,72 @@ struct Oracle {
         sampleSteps++;
     }
 
+    // ------------------------------------------------ spatial decomposition
+    bool owned(long long c) const {
+        if (domAxis < 0) return true;
+        const long long ix[3] = {c % n[0], (c / n[0]) % n[1], c / ((long long)n[0] * n[1])};
+        return ix[domAxis] >= domLo && ix[domAxis] < domHi;
+    }
+
+    void setDomain(int axis, int lo, int hi) {
+        domAxis = axis;
+        domLo = lo;
+        domHi = hi;
+        P.erase(std::remove_if(P.begin(), P.end(), [&](const Parcel& p) { return p.cell >= 0 && !owned(p.cell); }),
+                P.end());
+        sort();
+    }
+
+    // inflow and move; a parcel whose move ends in another domain's cell is
+    // packed as a migrant (record words, then the cell word) and leaves
+    long long stepBegin() {
+        inflow();
+        move();
+        migOut.clear();
+        long long m = 0;
+        for (Parcel& p : P) {
+            if (p.cell < 0 || owned(p.cell)) continue;
+            uint32_t w[17];
+            std::memcpy(w, p.x, 24);
+            std::memcpy(w + 6, p.U, 24);
+            std::memcpy(w + 12, &p.erot, 8);
+            w[14] = p.id;
+            w[15] = (uint32_t)p.type | ((uint32_t)p.vib << 8);
+            w[16] = ((uint32_t)p.cell << 3) | (uint32_t)p.sub;
+            migOut.insert(migOut.end(), w, w + 17);
+            p.cell = -1;
+            ++m;
+        }
+        migLast = m;
+        return m;
+    }
+
+    void addMigrants(const uint32_t* w, long long n) {
+        for (long long k = 0; k < n; ++k, w += 17) {
+            Parcel p{};
+            std::memcpy(p.x, w, 24);
+            std::memcpy(p.U, w + 6, 24);
+            std::memcpy(&p.erot, w + 12, 8);
+            p.id = w[14];
+            p.type = (int)(w[15] & 0xFFu);
+            p.vib = (int)(w[15] >> 8);
+            p.cell = (int)((w[16] & 0x7FFFFFFFu) >> 3);
+            p.sub = (int)(w[16] & 7u);
+            p.fresh = 0;
+            if (p.cell >= C || !owned(p.cell)) { err = 1; continue; }
+            P.push_back(p);
+        }
+    }
+
+    // sort, collisions, sampling (the migrants sent are not deletions)
+    void stepEnd() {
+        sort();
+        deletedLast -= migLast;
+        collide();
+        sample();
+        step++;
+    }
+
     void runPhases(unsigned ph) {
         if (ph & DSMC_PHASE_INFLOW) inflow();
         if (ph & DSMC_PHASE_MOVE) move();
@@ -1455,6 +1533,30 @@ int oracle_run_phases(oracle_handle* h, unsigned phases) {
     return h->o.err ? DSMC_ERR_DEVICE : DSMC_OK;
 }
 
+int oracle_set_domain(oracle_handle* h, int axis, int lo, int hi) {
+    if (axis < -1 || axis > 2 || (axis >= 0 && !(0 <= lo && lo < hi && hi <= h->o.n[axis]))) return DSMC_ERR_INVALID;
+    h->o.setDomain(axis, lo, hi);
+    return DSMC_OK;
+}
+
+long long oracle_step_begin(oracle_handle* h) { return h->o.stepBegin(); }
+
+int oracle_get_migrants(oracle_handle* h, void* dst, long long n) {
+    if (n < 0 || n * 17 > (long long)h->o.migOut.size()) return DSMC_ERR_INVALID;
+    std::memcpy(dst, h->o.migOut.data(), (size_t)n * 68);
+    return DSMC_OK;
+}
+
+int oracle_add_migrants(oracle_handle* h, const void* src, long long n) {
+    h->o.addMigrants(static_cast<const uint32_t*>(src), n);
+    return h->o.err ? DSMC_ERR_DEVICE : DSMC_OK;
+}
+
+int oracle_step_end(oracle_handle* h) {
+    h->o.stepEnd();
+    return h->o.err ? DSMC_ERR_DEVICE : DSMC_OK;
+}
+
 int oracle_evolve(oracle_handle* h, long long n) {
     for (long long i = 0; i < n; ++i) h->o.runPhases(DSMC_PHASE_ALL);
     return h->o.err ? DSMC_ERR_DEVICE : DSMC_OK;
@@ -1481,6 +1583,9 @@ int oracle_set_particles(oracle_handle* h, long long n, const double* pos, const
         p.sub = sb;
     }
     o.nextId = mx;
+    if (o.domAxis >= 0)
+        o.P.erase(std::remove_if(o.P.begin(), o.P.end(), [&](const Parcel& p) { return !o.owned(p.cell); }),
+                  o.P.end());
     o.sort();
     return DSMC_OK;
 }

@@ -57,6 +57,12 @@ def lib() -> C.CDLL:
         L.oracle_u01_from.restype = C.c_double
         L.oracle_u01_from.argtypes = [C.c_uint, C.c_uint]
         L.oracle_last_error.restype = C.c_char_p
+        L.oracle_set_domain.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+        L.oracle_step_begin.restype = C.c_longlong
+        L.oracle_step_begin.argtypes = [vp]
+        L.oracle_get_migrants.argtypes = [vp, vp, C.c_longlong]
+        L.oracle_add_migrants.argtypes = [vp, vp, C.c_longlong]
+        L.oracle_step_end.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -107,6 +113,27 @@ class OracleCloud:
 
     def evolve(self, n):
         self._chk(lib().oracle_evolve(self.h, n))
+
+    # the spatial decomposition's two half-steps (the library's dsmc_set_domain,
+    # dsmc_step_begin, dsmc_get_migrants, dsmc_add_migrants, dsmc_step_end)
+    def set_domain(self, axis, lo=0, hi=0):
+        self._chk(lib().oracle_set_domain(self.h, int(axis), int(lo), int(hi)))
+
+    def step_begin(self):
+        return int(lib().oracle_step_begin(self.h))
+
+    def get_migrants(self, n):
+        out = np.empty((int(n), 68), dtype=np.uint8)
+        if n:
+            self._chk(lib().oracle_get_migrants(self.h, out.ctypes.data_as(C.c_void_p), int(n)))
+        return out
+
+    def add_migrants(self, src, n=None):
+        src = np.ascontiguousarray(src, dtype=np.uint8).reshape(-1, 68)
+        self._chk(lib().oracle_add_migrants(self.h, src.ctypes.data_as(C.c_void_p), len(src)))
+
+    def step_end(self):
+        self._chk(lib().oracle_step_end(self.h))
 
     def set_particles(self, pos, U, erot=None, vib=None, species=None, ids=None, fresh=False):
         n = len(pos)
