@@ -332,6 +332,7 @@ def gpu_arm(args, rank, world, local):
         log("developing the learned arm")
         lg = learn.develop(s, args.develop)
         lg.set_learned(model, args.learn_every, margin)
+        lg.set_learned_forget(args.forget)
         lg.evolve(args.warmup)
         # the selection audit (per-cell expected collision shortfall) in the
         # evaluation windows; switched on after the timed steps
@@ -360,6 +361,7 @@ def gpu_arm(args, rank, world, local):
         log("developing the independent learned run")
         rep = learn.develop(make_spec(args, SEED + 7919 + rank), args.develop)
         rep.set_learned(model, args.learn_every, margin)
+        rep.set_learned_forget(args.forget)
         rep.evolve(args.warmup + args.steps)
         # the control: the same independent run with the plain selection
         ctl = learn.develop(make_spec(args, SEED + 7919 + rank), args.develop)
@@ -390,6 +392,7 @@ def gpu_arm(args, rank, world, local):
         lvp["learned_kernels_ms_per_step"] = {k: round(v / args.steps, 4) for k, v in kl.items()}
         lvp["model"] = model_desc
         lvp["every"] = args.learn_every
+        lvp["forget"] = args.forget
         lvp["note"] = ("speed: both arms from the same developed state over the same steps (the learned arm's "
                        "predictions, every {} steps, inside its timed steps); per-cell counts and fields: the "
                        "plain arm against the learned arm of an independently seeded run of the same "
@@ -572,6 +575,8 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned arm")
     ap.add_argument("--learn-every", type=int, default=100, help="learned: steps between predictions")
     ap.add_argument("--tau", type=float, default=0.95, help="learned: pinball quantile (0: squared error)")
+    ap.add_argument("--forget", type=float, default=1.0,
+                    help="learned: kept fraction of a cell's remembered excess at each prediction")
     ap.add_argument("--train-seeds", type=int, default=5)
     ap.add_argument("--train-rows", type=int, default=5_000_000)
     ap.add_argument("--train-steps", type=int, default=20000)

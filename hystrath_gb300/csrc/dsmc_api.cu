@@ -94,6 +94,7 @@ struct dsmc_handle {
     const MlpModel* model = nullptr;
     int learnEvery = 0;
     float learnMargin = 0.f;
+    float learnForget = 1.f;      // kept fraction of a cell's remembered excess at a prediction
 };
 
 namespace {
@@ -562,7 +563,7 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev, 
     if (phases & DSMC_PHASE_COLLIDE) {
         const Parcels& cur = (phases & DSMC_PHASE_SORT) ? b : a;
         if (h->model) {
-            launch_cell_features(cs, B, cur, h->learnEvery, 1, st);
+            launch_cell_features(cs, B, cur, h->learnEvery, 1, st, h->learnForget);
             mlp_launch_infer(h->model, B.feat, cs.C, B.pred, h->learnMargin, &B.ctr->step, h->learnEvery, st);
         }
         mark(MK_LEARNED);
@@ -1200,6 +1201,16 @@ int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n
         CUDA_TRY(h, cudaMemcpy(out, h->B.audit, sizeof(double2) * C, cudaMemcpyDeviceToHost));
         return DSMC_OK;
     }
+    if (nm == "learnedFeatures") {
+        // the learned maximum's inputs of the current state, per cell: log
+        // number density, log translational temperature, speed ratio, valid
+        if (n != 4 * C) return fail(h, DSMC_ERR_INVALID, "n must equal 4 x the number of cells");
+        launch_cell_features(h->cs, h->B, cur_soa(h), 0, 0, h->stream);
+        CUDA_TRY(h, cudaGetLastError());
+        CUDA_TRY(h, cudaMemcpyAsync(out, h->B.feat, sizeof(float4) * C, cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        return DSMC_OK;
+    }
     if (nm == "inflowAccumulator") {
         const int ns = h->spec.n_species;
         if (n != h->cs.nBFaces * ns) return fail(h, DSMC_ERR_INVALID, "n must equal boundary faces x species");
@@ -1218,7 +1229,7 @@ int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n
     }
     return fail(h, DSMC_ERR_INVALID, "unknown cell array " + nm +
                                          "; valid: count start sigmaTcRMax collisionSelectionRemainder accumulators "
-                                         "inflowAccumulator selectionAudit");
+                                         "inflowAccumulator selectionAudit learnedFeatures");
 }
 
 int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long long n) {
@@ -1528,6 +1539,13 @@ int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float mar
     CUDA_TRY(h, cudaMemset(h->B.pred, 0, sizeof(float) * h->cs.C));
     CUDA_TRY(h, cudaMemset(h->B.useR, 1, h->cs.C));
     CUDA_TRY(h, cudaMemset(h->B.exceed, 0, sizeof(float) * h->cs.C));
+    return DSMC_OK;
+}
+
+int dsmc_set_learned_forget(dsmc_handle* h, float forget) {
+    if (!(forget >= 0.f && forget <= 1.f)) return fail(h, DSMC_ERR_INVALID, "forget must lie in [0, 1]");
+    h->learnForget = forget;
+    drop_graphs(h);
     return DSMC_OK;
 }
 

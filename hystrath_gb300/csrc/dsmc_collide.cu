@@ -405,24 +405,23 @@ __global__ void k_info(CaseDev cs, Parcels s, const Counters* ctr, double* out) 
 }
 
 // ------------------------------------------------------- learned maximum
-// Features of the learned (sigma_T c_R)max, one thread per cell: log number
-// density, log translational temperature of the cell's parcels and their
-// speed ratio |U| / sqrt(2 k T / m), with m the mean parcel mass.  Features
-// need three digits: the sums run in FP32 on velocities converted on the
-// integer pipe, with masses relative to species 0.
 // Features of the learned maximum: log number density, log translational
-// temperature and speed ratio of each cell's parcels.  A CTA takes a tile of
-// FEAT_TILE consecutive cells, whose parcels are contiguous after the sort,
-// and streams them with coalesced loads; each parcel adds exact fixed-point
-// values to its cell's sums in shared memory (count, mass weight, weighted
-// velocity and |U|^2: the mass weight is the species mass over species 0's
-// in units of 1/256, velocities in units of 1/16 m/s), so the sums do not
-// depend on the parcels' order.  Then one thread per cell makes the features.
+// temperature and speed ratio |U| / sqrt(2 k T / m) (m the mean parcel mass)
+// of each cell's parcels.  A CTA takes a tile of FEAT_TILE consecutive cells,
+// whose parcels are contiguous after the sort, and streams them warp by warp
+// with coalesced loads; each parcel's exact fixed-point values (mass weight:
+// the species mass over species 0's in units of 1/256; velocities in units
+// of 1/16 m/s) are summed over the warp's runs of equal cells and added to
+// the cell's sums in shared memory by the run's last lane, so the sums do
+// not depend on the parcels' order.  (Every parcel adding to shared memory
+// itself measured 1.44 ms for the 13.1M-parcel heat bath: twenty-odd lanes
+// of a warp contend for one cell's 64-bit sums.)  Then one thread per cell
+// makes the features.
 constexpr int FEAT_TILE = 256;
 
 __global__ void __launch_bounds__(FEAT_TILE)
 k_cell_features(CaseDev cs, Parcels s, const int* __restrict__ start, const Counters* ctr, int every, float4* feat,
-                unsigned char* useR) {
+                unsigned char* useR, float* exceed, float forget) {
     if (every > 0 && (ctr->step % every) != 0) return;
     __shared__ int sN[FEAT_TILE];
     __shared__ unsigned long long sW[FEAT_TILE], sWU[3][FEAT_TILE], sWUU[FEAT_TILE];
@@ -442,21 +441,43 @@ k_cell_features(CaseDev cs, Parcels s, const int* __restrict__ start, const Coun
         sWUU[t] = 0ull;
         __syncthreads();
         const long long j0 = start[c0], j1 = start[c1];
-        for (long long j = j0 + t; j < j1; j += FEAT_TILE) {
-            const int lc = (int)((long long)cellw_cell(__ldg(s.cellw + j)) - c0);
-            if ((unsigned)lc >= (unsigned)FEAT_TILE) continue;   // never: the tile's parcels are its cells'
-            const double2* q = reinterpret_cast<const double2*>(s.r + j);
-            const double2 b = __ldg(q + 1), d = __ldg(q + 2), e = __ldg(q + 3);
-            const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(e.y) >> 32);
-            const long long w = mw[sv_species(sv) & (DSMC_MAX_SPECIES - 1)];
-            const long long ux = __double2ll_rn(b.y * 16.0), uy = __double2ll_rn(d.x * 16.0),
-                            uz = __double2ll_rn(d.y * 16.0);
-            atomicAdd(&sN[lc], 1);
-            atomicAdd(&sW[lc], (unsigned long long)w);
-            atomicAdd(&sWU[0][lc], (unsigned long long)(w * ux));
-            atomicAdd(&sWU[1][lc], (unsigned long long)(w * uy));
-            atomicAdd(&sWU[2][lc], (unsigned long long)(w * uz));
-            atomicAdd(&sWUU[lc], (unsigned long long)(w * (ux * ux + uy * uy + uz * uz)));
+        const int lane = t & 31;
+        for (long long jb = j0 + (t & ~31); jb < j1; jb += FEAT_TILE) {
+            const long long j = jb + lane;
+            int lc = -1;
+            long long v[5] = {0, 0, 0, 0, 0};
+            if (j < j1) {
+                lc = (int)((long long)cellw_cell(__ldg(s.cellw + j)) - c0);
+                if ((unsigned)lc >= (unsigned)FEAT_TILE) lc = -1;   // never: the tile's parcels are its cells'
+            }
+            if (lc >= 0) {
+                const double2* q = reinterpret_cast<const double2*>(s.r + j);
+                const double2 b = __ldg(q + 1), d = __ldg(q + 2), e = __ldg(q + 3);
+                const uint32_t sv = (uint32_t)((unsigned long long)__double_as_longlong(e.y) >> 32);
+                const long long w = mw[sv_species(sv) & (DSMC_MAX_SPECIES - 1)];
+                const long long ux = __double2ll_rn(b.y * 16.0), uy = __double2ll_rn(d.x * 16.0),
+                                uz = __double2ll_rn(d.y * 16.0);
+                v[0] = w;
+                v[1] = w * ux;
+                v[2] = w * uy;
+                v[3] = w * uz;
+                v[4] = w * (ux * ux + uy * uy + uz * uz);
+            }
+            // the warp's runs of equal cells (the parcels are sorted by cell)
+            const int prev = __shfl_up_sync(0xFFFFFFFFu, lc, 1);
+            const unsigned hm = __ballot_sync(0xFFFFFFFFu, lane == 0 || prev != lc);
+            const int segStart = 31 - __clz(hm & (0xFFFFFFFFu >> (31 - lane)));
+#pragma unroll
+            for (int k = 0; k < 5; ++k) v[k] = seg_sum(v[k], segStart);
+            const bool tail = lane == 31 || ((hm >> (lane + 1)) & 1u);
+            if (tail && lc >= 0) {
+                atomicAdd(&sN[lc], lane - segStart + 1);
+                atomicAdd(&sW[lc], (unsigned long long)v[0]);
+                atomicAdd(&sWU[0][lc], (unsigned long long)v[1]);
+                atomicAdd(&sWU[1][lc], (unsigned long long)v[2]);
+                atomicAdd(&sWU[2][lc], (unsigned long long)v[3]);
+                atomicAdd(&sWUU[lc], (unsigned long long)v[4]);
+            }
         }
         __syncthreads();
         const long long c = c0 + t;
@@ -480,6 +501,7 @@ k_cell_features(CaseDev cs, Parcels s, const int* __restrict__ start, const Coun
             }
             feat[c] = f;
             if (useR) useR[c] = 0;
+            if (exceed) exceed[c] *= forget;
         }
         __syncthreads();
     }
@@ -715,11 +737,12 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
 }
 
 void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,
-                          cudaStream_t st) {
+                          cudaStream_t st, float forget) {
     long long blocks = (cs.C + FEAT_TILE - 1) / FEAT_TILE;
     if (blocks > (long long)sm_count() * 8) blocks = (long long)sm_count() * 8;
     k_cell_features<<<(int)blocks, FEAT_TILE, 0, st>>>(cs, s, B.start, B.ctr, every, B.feat,
-                                                       resetFallback ? B.useR : nullptr);
+                                                       resetFallback ? B.useR : nullptr,
+                                                       resetFallback && forget < 1.f ? B.exceed : nullptr, forget);
 }
 
 void launch_learn_compact(const CaseDev& cs, const StepBuffers& B, long long maxRows, float* X, float* Y,

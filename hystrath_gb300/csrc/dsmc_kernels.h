@@ -148,8 +148,10 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
 // per-cell features of the learned maximum; every > 0: only on steps that are
 // multiples of every, every == 0: always; resetFallback: the cells go back to
 // the prediction
+// resetFallback: a prediction follows (the cells' fallback flags are cleared
+// and their remembered excess multiplied by forget)
 void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,
-                          cudaStream_t st);
+                          cudaStream_t st, float forget = 1.f);
 // compacts (features, log observed maximum) of the cells with candidates in
 // the last step; returns the count in *nOut (device)
 void launch_learn_compact(const CaseDev& cs, const StepBuffers& B, long long maxRows, float* X, float* Y,

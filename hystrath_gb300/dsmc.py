@@ -94,6 +94,7 @@ def _load() -> C.CDLL:
     L.dsmc_mlp_grad.argtypes = [vp, vp, vp, C.c_int, vp, vp]
     L.dsmc_mlp_predict.argtypes = [vp, vp, C.c_longlong, vp]
     L.dsmc_set_learned.argtypes = [vp, vp, C.c_int, C.c_float]
+    L.dsmc_set_learned_forget.argtypes = [vp, C.c_float]
     L.dsmc_learn_record.argtypes = [vp, C.c_longlong, vp, vp, C.POINTER(C.c_longlong)]
     L.dsmc_set_domain.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     L.dsmc_step_begin.argtypes = [vp, C.POINTER(C.c_longlong)]
@@ -312,6 +313,8 @@ class DsmcCloud:
             a = np.empty(lib().dsmc_n_boundary_faces(self.h) * self.spec.n_species)
         elif name == "selectionAudit":
             a = np.empty((self.n_cells, 2))
+        elif name == "learnedFeatures":
+            a = np.empty((self.n_cells, 4), np.float32)
         else:
             a = np.empty(self.n_cells)
         self._chk(lib().dsmc_get_cell_array(self.h, name.encode(), _p(a), a.size))
@@ -431,6 +434,11 @@ class DsmcCloud:
         """Attach a trained model (None: the plain running maximum)."""
         self._learned = model   # keep the model alive while attached
         self._chk(lib().dsmc_set_learned(self.h, model.h if model else None, int(every), float(margin)))
+
+    def set_learned_forget(self, forget: float):
+        """Fraction of a cell's remembered excess over its predictions kept
+        at each prediction (1: kept for good; 0: forgotten)."""
+        self._chk(lib().dsmc_set_learned_forget(self.h, float(forget)))
 
     def learn_record(self, max_rows: int):
         """(features[n,3], log observed maximum[n]) of the cells that had

@@ -305,7 +305,10 @@ int dsmc_get_particles(dsmc_handle* h, long long capacity, long long* n, double*
  * freestream inflow carries to the next step (accumulatedParcelsToInsert_,
  * dsmcFreeStreamInflowPatch.C:131-141), zero on faces without inflow; and
  * with the selection audit on, "selectionAudit" (double, n = 2 x cells,
- * cell major): the audit sums of dsmc_set_selection_audit. */
+ * cell major): the audit sums of dsmc_set_selection_audit; "learnedFeatures"
+ * (float, n = 4 x cells, cell major, read only): the learned maximum's
+ * inputs of the current state (log number density, log translational
+ * temperature, speed ratio, 1 where valid). */
 int dsmc_get_cell_array(dsmc_handle* h, const char* name, void* out, long long n);
 int dsmc_set_cell_array(dsmc_handle* h, const char* name, const void* in, long long n);
 
@@ -539,6 +542,13 @@ int dsmc_set_selection_audit(dsmc_handle* h, int on);
 /* attach a model (NULL: plain running maximum); predictions every `every`
    steps, used as exp(prediction + margin) */
 int dsmc_set_learned(dsmc_handle* h, const dsmc_mlp* model, int every, float margin);
+/* A learned cell whose candidates produced a sigma_T c_R above the value it
+   selected with falls back to the running maximum until the next
+   prediction, and a later prediction is used only if it reaches the largest
+   such product remembered for the cell.  At every prediction the memory is
+   multiplied by `forget` in [0, 1]: 1 (the default) keeps it for good, 0
+   forgets it at every prediction. */
+int dsmc_set_learned_forget(dsmc_handle* h, float forget);
 /* after a step: (features, log largest product among the step's candidates)
    of the cells that had candidates, at most max_rows of them */
 int dsmc_learn_record(dsmc_handle* h, long long max_rows, float* X, float* Y, long long* n_out);

@@ -4,6 +4,7 @@ training, and what the trained network gains inside noTimeCounter (GPU)."""
 import numpy as np
 import pytest
 
+from hystrath_gb300 import spec as S
 from oracle import mlp_oracle as MO
 
 
@@ -160,3 +161,72 @@ def test_learned_selection_draws_fewer_candidates_at_the_same_rate():
     assert ap["expected_shortfall_total"] < 1e-3, ap
     assert al["expected_shortfall_total"] < 0.005, al
     assert al["cells_above_1pct"] < ap["cells_above_1pct"] + 0.05, (al, ap)
+
+
+def _features_restated(g):
+    """The learned maximum's inputs restated from the cloud's parcels: the
+    same exact fixed-point sums per cell (mass weight round(256 m/m0),
+    velocity round(16 u)), then the features in FP32."""
+    st = g.particles()
+    sp = g.spec
+    m0 = sp.species[0].mass
+    mrel = np.array([np.float32(sp.species[q].mass / m0) for q in range(sp.n_species)], dtype=np.float32)
+    w = np.rint(mrel * np.float32(256.0)).astype(np.int64)[st["species"]]
+    u = np.rint(st["U"] * 16.0).astype(np.int64)
+    c = st["cell"].astype(np.int64)
+    C = g.n_cells
+    N = np.bincount(c, minlength=C).astype(np.int64)
+    W = np.bincount(c, weights=w, minlength=C).astype(np.int64)      # exact below 2^53
+    WU = [np.zeros(C, np.int64) for _ in range(3)]
+    for a in range(3):
+        np.add.at(WU[a], c, w * u[:, a])
+    WUU = np.zeros(C, np.int64)
+    np.add.at(WUU, c, w * (u * u).sum(1))
+    f32 = np.float32
+    M = W.astype(f32) * f32(1 / 256)
+    Mu = [x.astype(f32) * f32(1 / 4096) for x in WU]
+    Muu = WUU.astype(f32) * f32(1 / 65536)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        U2 = (Mu[0] * Mu[0] + Mu[1] * Mu[1] + Mu[2] * Mu[2]) / (M * M)
+        kOverM0 = f32(1.380649e-23 / m0)
+        T = (Muu - M * U2) / (f32(3.0) * kOverM0 * N.astype(f32))
+        nd = f32(sp.n_equivalent_particles / np.prod([sp.cell_size[a] for a in range(3)]))
+        cmp = np.sqrt(f32(2.0) * kOverM0 * T / (M / N.astype(f32)))
+        valid = (N >= 2) & (T > 0)
+        out = np.zeros((C, 4), np.float32)
+        out[valid, 0] = np.log(nd * N[valid].astype(f32))
+        out[valid, 1] = np.log(T[valid])
+        out[valid, 2] = np.sqrt(U2[valid]) / cmp[valid]
+        out[valid, 3] = 1.0
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["channel", "mixture"])
+def test_cell_features_match_a_restatement(gpu_lib, case):
+    """The feature pass (warp runs of equal cells summed before the shared
+    sums) against a numpy restatement of the same exact sums: the developed
+    channel at 1/8 scale (one species, two or three cells per warp) and an
+    N2-Ar box (mass weights 256 and 365)."""
+    from hystrath_gb300.dsmc import DsmcCloud
+    if case == "channel":
+        s = S.config2(seed=31, scale=8)
+    else:
+        s = S.make_box_case((12, 12, 12), 1e-3, S.N2, fn=2e9, dt=2e-7, seed=32, n_density=5e19,
+                            t_tra=3000.0, t_rot=300.0, t_vib=300.0, side_model=S.BC_SPECULAR,
+                            collision=S.COLL_LB_VHS)
+        s.n_species = 2
+        S.set_species(s, 1, S.AR)
+        s.init_number_density[1] = 5e19
+    g = DsmcCloud(s)
+    g.initialise()
+    g.evolve(60)
+    got = g.cell_array("learnedFeatures")
+    want = _features_restated(g)
+    g.close()
+    assert np.array_equal(got[:, 3], want[:, 3])
+    v = want[:, 3] == 1
+    assert v.sum() > 0.5 * len(v)
+    np.testing.assert_allclose(got[v, 0], want[v, 0], rtol=3e-7, atol=0)     # log n: exact counts, logf ulps
+    np.testing.assert_allclose(got[v, 1], want[v, 1], rtol=0, atol=1e-4)      # log T: FP32 cancellation
+    np.testing.assert_allclose(got[v, 2], want[v, 2], rtol=1e-4, atol=1e-6)
