@@ -333,6 +333,7 @@ void fill_case_dev(dsmc_handle* h) {
     cs.V = cs.dx[0] * cs.dx[1] * cs.dx[2];
     cs.FN = s.n_equivalent_particles;
     cs.dt = s.delta_t;
+    cs.selK = cs.FN * cs.dt / cs.V;
     for (int a = 0; a < 3; ++a)
         cs.invDtFa[a] = 1.0 / (cs.dt * cs.dx[a == 0 ? 1 : 0] * cs.dx[a == 2 ? 1 : 2]);
     cs.seedLo = (uint32_t)s.seed;

@@ -111,6 +111,7 @@ struct CaseDev {
     long long nFacesAll;
     double V;
     double FN, dt;
+    double selK;         // FN dt / V: the selection factor of a uniform mesh's cells
     double invDtFa[3];   // 1 / (dt * area of a face normal to each axis)
     uint32_t seedLo, seedHi;
     int nSpecies;

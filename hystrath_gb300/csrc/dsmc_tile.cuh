@@ -99,7 +99,12 @@ __device__ __forceinline__ int select_cell(const CaseDev& cs, const int* __restr
             if (!useR[c] && pv > 0.f && pv < 3.0e38f && pv >= exceed[c]) sm = (double)pv;
             smaxSel[c] = sm;
         }
-        const double sel = rem[c] + 0.5 * n * (n - 1) * cs.FN * sm * cs.dt / cell_volume(cs, c);
+        // rem + 0.5 n (n - 1) FN sm dt / V: on a uniform mesh FN dt / V is
+        // one factor of the case, which leaves no FP64 division per cell (on
+        // GB300 the division's dozen FP64 instructions dominated this pass)
+        const double pairs = (double)((n * (n - 1)) >> 1);
+        const double k = cs.cellV ? cs.FN * cs.dt / cs.cellV[c] : cs.selK;
+        const double sel = fma(pairs, sm * k, rem[c]);
         const double whole = floor(sel);
         rem[c] = sel - whole;
         if (n > cs.maxCellParcels || whole >= (double)MAX_CAND) err |= ERRB_DENSE;

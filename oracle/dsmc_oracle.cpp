@@ -1523,6 +1523,14 @@ void oracle_set_threads(oracle_handle* h, int n_threads) { h->o.nThreads = n_thr
 // another implementation advanced to that step).
 void oracle_set_step(oracle_handle* h, long long step) { h->o.step = step; }
 
+// Restarts the time averages (every sampling sum and the sample count), as
+// the library's dsmc_reset_sampling does.
+void oracle_reset_sampling(oracle_handle* h) {
+    std::fill(h->o.acc.begin(), h->o.acc.end(), 0.0);
+    std::fill(h->o.mom.begin(), h->o.mom.end(), 0.0);
+    h->o.sampleSteps = 0;
+}
+
 int oracle_initialise(oracle_handle* h) {
     h->o.initialise();
     return h->o.err ? DSMC_ERR_DEVICE : DSMC_OK;

@@ -35,6 +35,7 @@ def lib() -> C.CDLL:
         L.oracle_destroy.argtypes = [vp]
         L.oracle_set_threads.argtypes = [vp, C.c_int]
         L.oracle_set_step.argtypes = [vp, C.c_longlong]
+        L.oracle_reset_sampling.argtypes = [vp]
         for f in ("oracle_initialise",):
             getattr(L, f).argtypes = [vp]
         L.oracle_run_phases.argtypes = [vp, C.c_uint]
@@ -107,6 +108,10 @@ class OracleCloud:
 
     def initialise(self):
         self._chk(lib().oracle_initialise(self.h))
+
+    def reset_sampling(self):
+        """Restarts the time averages (the library's dsmc_reset_sampling)."""
+        lib().oracle_reset_sampling(self.h)
 
     def run_phases(self, phases):
         self._chk(lib().oracle_run_phases(self.h, phases))

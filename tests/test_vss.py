@@ -121,6 +121,74 @@ def test_gpu_vss_momentum_exchange_matches_oracle(gpu_lib, oracle_mod):
     assert np.all(np.abs(hg.mean(0) - hc.mean(0)) <= 2.5 * se + 5e-3), (hg.mean(0), hc.mean(0), se)
 
 
+def _anisotropic_lb_vss(cloud, fn, mass, checkpoints):
+    """The cloud's x velocities doubled (T_x four times T_y, T_z), then the
+    fractions of the total energy held by the x motion, by rotation and by
+    vibration at each checkpoint (fn: real molecules per parcel, which the
+    reported internal energies include).  The x fraction relaxes through the
+    deflection law (VSS alpha), the internal ones through Larsen-Borgnakke."""
+    st = cloud.particles()
+    U = st["U"].copy()
+    U[:, 0] *= 2.0
+    cloud.set_particles(st["pos"], U, st["erot"], st["vib"], st["species"], st["id"])
+    row, last = [], 0
+    for t in checkpoints:
+        cloud.evolve(t - last)
+        last = t
+        i = cloud.info()
+        U = cloud.particles()["U"]
+        ex = 0.5 * mass * np.sum(U[:, 0] ** 2)
+        erot, evib = i.rotational_e / fn, i.vibrational_e / fn
+        tot = 0.5 * mass * np.sum(U ** 2) + erot + evib
+        row.append((ex / tot, erot / tot, evib / tot))
+    return row
+
+
+@pytest.mark.gpu
+def test_gpu_lb_vss_relaxation_matches_oracle(gpu_lib, oracle_mod):
+    """LarsenBorgnakkeVariableSoftSphere (N2, alpha 1.36) from an anisotropic
+    start (T_x = 4 T_y = 4 T_z at 10^4 K mean): the x, rotational and
+    vibrational energy fractions of GPU and CPU at 4 checkpoints, 16 seeds
+    per side.  In units of the standard error of the difference of the seed
+    means, with no absolute slack: at most 2 of the 12 values above 2 and none
+    above 3.5, and Hotelling's T^2 over the 12 with p above 1e-3."""
+    from scipy.stats import f as f_dist
+    from hystrath_gb300.dsmc import DsmcCloud
+
+    def spec(seed):
+        s = S.config1(seed=seed, n=8)
+        s.binary_collision_model = S.COLL_LB_VSS
+        return s
+
+    checkpoints = [5, 15, 40, 120]
+    seeds = range(16)
+    mass = S.N2["mass"]
+    xg, xc = [], []
+    for sd in seeds:
+        g = DsmcCloud(spec(300 + sd))
+        g.initialise()
+        xg.append(_anisotropic_lb_vss(g, g.spec.n_equivalent_particles, mass, checkpoints))
+        g.close()
+        o_spec = spec(400 + sd)
+        o = oracle_mod.OracleCloud(o_spec, threads=8)
+        o.initialise()
+        xc.append(_anisotropic_lb_vss(o, o_spec.n_equivalent_particles, mass, checkpoints))
+    xg = np.array(xg).reshape(len(seeds), -1)
+    xc = np.array(xc).reshape(len(seeds), -1)
+    # the x fraction relaxes from 2/3 of the kinetic energy towards 1/3
+    assert xg[:, 0].mean() > xg[:, -3].mean() + 0.05
+    n1, n2, p = len(xg), len(xc), xg.shape[1]
+    d = xg.mean(0) - xc.mean(0)
+    se = np.sqrt(xg.var(0, ddof=1) / n1 + xc.var(0, ddof=1) / n2)
+    z = np.abs(d / se)
+    assert np.sum(z > 2.0) <= 2 and z.max() < 3.5, np.round(z, 2)
+    Sp = ((n1 - 1) * np.cov(xg, rowvar=False) + (n2 - 1) * np.cov(xc, rowvar=False)) / (n1 + n2 - 2)
+    t2 = (n1 * n2) / (n1 + n2) * d @ np.linalg.solve(Sp, d)
+    F = (n1 + n2 - p - 1) / (p * (n1 + n2 - 2)) * t2
+    pval = float(f_dist.sf(F, p, n1 + n2 - p - 1))
+    assert pval > 1e-3, (pval, np.round(z, 2))
+
+
 @pytest.mark.gpu
 def test_gpu_lb_vss_conserves_energy(gpu_lib):
     from hystrath_gb300.dsmc import DsmcCloud
