@@ -421,11 +421,53 @@ __device__ __forceinline__ void audit_add(float2* au, double sigma, double smax0
     au->y += fmaxf(a - 1.0f, 0.0f);
 }
 
+// The part of a record a collision reads and writes: the velocity, the
+// rotational energy and the tail word (id, species and vibrational level).
+// Positions stay in memory (the separation reads them on its own), so they
+// are not held across the exchange, and a collision stores 40 of the 64
+// bytes.
+struct CollRec {
+    double ux, uy, uz, erot;
+    uint32_t id, sv;
+};
+
+__device__ __forceinline__ CollRec ld_coll(const Rec* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 b = q[1], c = q[2], d = q[3];
+    CollRec v;
+    v.ux = b.y; v.uy = c.x; v.uz = c.y;
+    v.erot = d.x;
+    const unsigned long long t = (unsigned long long)__double_as_longlong(d.y);
+    v.id = (uint32_t)t;
+    v.sv = (uint32_t)(t >> 32);
+    return v;
+}
+
+__device__ __forceinline__ void st_coll(Rec* p, const CollRec& v) {
+    double2* q = reinterpret_cast<double2*>(p);
+    reinterpret_cast<double*>(p)[3] = v.ux;
+    q[2] = make_double2(v.uy, v.uz);
+    q[3] = make_double2(v.erot, __longlong_as_double((long long)(((unsigned long long)v.sv << 32) | v.id)));
+}
+
+// the separation only feeds the mean collision separation field: FP32
+// after the FP64 differences
+__device__ __forceinline__ float coll_separation(const Rec* a, const Rec* b) {
+    const double2* qa = reinterpret_cast<const double2*>(a);
+    const double2* qb = reinterpret_cast<const double2*>(b);
+    const double2 a0 = qa[0], b0 = qb[0];
+    const double az = qa[1].x, bz = qb[1].x;
+    const float dx = (float)(a0.x - b0.x);
+    const float dy = (float)(a0.y - b0.y);
+    const float dz = (float)(az - bz);
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
 __device__ __forceinline__ bool test_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
-                                               long long gQ, double smax0, double* stepMax, Rec* P, Rec* Q,
-                                               double* cr2, float2* au) {
-    *P = ld_rec(s.r + gP);
-    *Q = ld_rec(s.r + gQ);
+                                               long long gQ, double smax0, double* stepMax, CollRec* P,
+                                               CollRec* Q, double* cr2, float2* au) {
+    *P = ld_coll(s.r + gP);
+    *Q = ld_coll(s.r + gQ);
     const int tP = sv_species(P->sv), tQ = sv_species(Q->sv);
     const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
     const double d0 = P->ux - Q->ux, d1 = P->uy - Q->uy, d2 = P->uz - Q->uz;
@@ -437,8 +479,9 @@ __device__ __forceinline__ bool test_candidate(const CaseDev& cs, const Parcels&
 }
 
 __device__ __forceinline__ void collide_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
-                                                  long long gQ, Rec P, Rec Q, double cr2, double* collSep,
+                                                  long long gQ, CollRec P, CollRec Q, double cr2, double* collSep,
                                                   unsigned* err) {
+    *collSep += (double)coll_separation(s.r + gP, s.r + gQ);
     const int tP = sv_species(P.sv), tQ = sv_species(Q.sv);
     const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
     Post o;
@@ -452,47 +495,17 @@ __device__ __forceinline__ void collide_candidate(const CaseDev& cs, const Parce
     Q.ux = o.UQ[0]; Q.uy = o.UQ[1]; Q.uz = o.UQ[2];
     P.erot = o.eP; Q.erot = o.eQ;
     P.sv = make_sv(tP, o.vP); Q.sv = make_sv(tQ, o.vQ);
-    st_rec(s.r + gP, P);
-    st_rec(s.r + gQ, Q);
-    // the separation only feeds the mean collision separation field: FP32
-    // after the FP64 differences
-    const float dx = (float)(P.x - Q.x);
-    const float dy = (float)(P.y - Q.y);
-    const float dz = (float)(P.z - Q.z);
-    *collSep += (double)sqrtf(dx * dx + dy * dy + dz * dz);
+    st_coll(s.r + gP, P);
+    st_coll(s.r + gQ, Q);
 }
 
 __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
                                               long long gQ, double smax0, double* stepMax, double* collSep,
                                               unsigned* err, float2* au = nullptr) {
-    Rec P = ld_rec(s.r + gP), Q = ld_rec(s.r + gQ);
-    const int tP = sv_species(P.sv), tQ = sv_species(Q.sv);
-    const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
-    Post o;
-    o.UP[0] = P.ux; o.UP[1] = P.uy; o.UP[2] = P.uz;
-    o.UQ[0] = Q.ux; o.UQ[1] = Q.uy; o.UQ[2] = Q.uz;
-    const double d0 = o.UP[0] - o.UQ[0], d1 = o.UP[1] - o.UQ[1], d2 = o.UP[2] - o.UQ[2];
-    const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
-    const double sigma = sigma_cr(pr, cr2);
-    if (sigma > *stepMax) *stepMax = sigma;
-    if (au) audit_add(au, sigma, smax0);
-    if (!(sigma > r.u01() * smax0)) return false;      // (sigma/smax0) > U with smax0 > 0
-    o.eP = P.erot; o.eQ = Q.erot;
-    o.vP = sv_vib(P.sv); o.vQ = sv_vib(Q.sv);
-    collide_pair(cs, r, pr, tP, tQ, cr2, o, err);
-    if (o.vP > SV_MAX_VIB || o.vQ > SV_MAX_VIB) *err |= ERRB_BOUNDS;
-    P.ux = o.UP[0]; P.uy = o.UP[1]; P.uz = o.UP[2];
-    Q.ux = o.UQ[0]; Q.uy = o.UQ[1]; Q.uz = o.UQ[2];
-    P.erot = o.eP; Q.erot = o.eQ;
-    P.sv = make_sv(tP, o.vP); Q.sv = make_sv(tQ, o.vQ);
-    st_rec(s.r + gP, P);
-    st_rec(s.r + gQ, Q);
-    // the separation only feeds the mean collision separation field: FP32
-    // after the FP64 differences
-    const float dx = (float)(P.x - Q.x);
-    const float dy = (float)(P.y - Q.y);
-    const float dz = (float)(P.z - Q.z);
-    *collSep += (double)sqrtf(dx * dx + dy * dy + dz * dz);
+    CollRec P, Q;
+    double cr2;
+    if (!test_candidate(cs, s, r, gP, gQ, smax0, stepMax, &P, &Q, &cr2, au)) return false;
+    collide_candidate(cs, s, r, gP, gQ, P, Q, cr2, collSep, err);
     return true;
 }
 
@@ -757,7 +770,7 @@ __device__ __forceinline__ void light_group(const CaseDev& cs, const Parcels& s,
             long long gP = 0, gQ = 0;
             Rng r(cs, (uint32_t)c, step, cand_tag(k));
             double cr2 = 0.0;
-            Rec P, Q;
+            CollRec P, Q;
             while (k < nCand) {
                 const int jP = pk.pq[k][0][lane], jQ = pk.pq[k][1][lane];
                 r = Rng(cs, (uint32_t)c, step, cand_tag(k));
