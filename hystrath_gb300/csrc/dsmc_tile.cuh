@@ -180,10 +180,41 @@ __device__ __forceinline__ void list_iter(long long C, const int* __restrict__ s
 // order are also listed (by work index) for k_cell_order_big
 // allHeavy: every listed cell is ordered and takes a heavy slot (the
 // Bernoulli-trial selection walks the canonical list of every cell)
+// The 16 slot cursors are shared by every cell of the mesh, so the block
+// reserves its cells' places in shared memory first and takes them from the
+// cursors with one atomic per slot present (a reservation per warp queued
+// every warp of the grid on the light slots' cursor).  The order inside a
+// slot does not matter: cells are independent.
 __global__ void k_ntc_list(long long C, const int* __restrict__ start, const int* __restrict__ ncCell,
                            unsigned* slotCursor, int2* work, int* bigList, Counters* ctr, int allHeavy) {
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < C; base += (long long)gridDim.x * blockDim.x)
-        list_iter(C, start, ncCell, slotCursor, work, bigList, ctr, allHeavy, base + threadIdx.x);
+    __shared__ unsigned blkCnt[2 * NBUCKET], blkBase[2 * NBUCKET];
+    const unsigned lane = threadIdx.x & 31u;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < C; base += (long long)gridDim.x * blockDim.x) {
+        if (threadIdx.x < 2 * NBUCKET) blkCnt[threadIdx.x] = 0;
+        __syncthreads();
+        const long long c = base + threadIdx.x;
+        int nc = 0, n = 0;
+        if (c < C) {
+            nc = ncCell[c];
+            if (nc > 0) n = start[c + 1] - start[c];
+        }
+        const int slot = nc > 0 ? (allHeavy ? NBUCKET + bucket_of(nc) : slot_of(n, nc)) : -1;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, slot);
+        const int leader = __ffs(peers) - 1;
+        unsigned off = 0;
+        if (nc > 0 && (int)lane == leader) off = atomicAdd(&blkCnt[slot], (unsigned)__popc(peers));
+        off = __shfl_sync(0xFFFFFFFFu, off, leader);
+        __syncthreads();
+        if (threadIdx.x < 2 * NBUCKET && blkCnt[threadIdx.x])
+            blkBase[threadIdx.x] = atomicAdd(&slotCursor[threadIdx.x], blkCnt[threadIdx.x]);
+        __syncthreads();
+        if (nc > 0) {
+            const unsigned q = blkBase[slot] + off + __popc(peers & ((1u << lane) - 1u));
+            work[q] = make_int2((int)c, nc);
+            if (n > ORDER_WARP_N) bigList[atomicAdd(&ctr->bigCells, 1)] = (int)q;
+        }
+        __syncthreads();   // blkCnt and blkBase are reused by the next pass
+    }
 }
 
 // ------------------------------------------------------------ ordering
