@@ -422,9 +422,11 @@ def gpu_arm(args, rank, world, local):
         t0 = time.perf_counter()
         g.set_particles(pin["pos"], pin["U"], pin["erot"], pin["vib"], pin["species"], pin["id"])
         ce0 = g.counts()
+        ta = time.perf_counter()
         for _ in range(args.steps):
             g.evolve(1)
             g.counts()      # the step's collision counters back on the host
+        tb = time.perf_counter()
         ttra = g.field("Ttra")
         t1 = time.perf_counter()
         ce1 = g.counts()
@@ -435,6 +437,8 @@ def gpu_arm(args, rank, world, local):
                "collisions_per_s": (ce1.collisions_total - ce0.collisions_total) * world / (t1 - t0),
                "h2d_bytes_per_step": nbytes_state / args.steps,
                "d2h_bytes_per_step": counts_bytes + ttra.nbytes / args.steps,
+               "upload_ms": round((ta - t0) * 1e3, 2), "steps_ms": round((tb - ta) * 1e3, 2),
+               "field_ms": round((t1 - tb) * 1e3, 2),
                "note": f"the whole parcel state ({nbytes_state / 1e9:.2f} GB) uploaded once from pinned host "
                        f"memory and spread over the {args.steps} steps; every step's counters read back; one "
                        "field read at the end"}
