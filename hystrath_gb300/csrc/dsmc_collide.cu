@@ -547,6 +547,10 @@ __host__ __device__ constexpr size_t batch_collide_smem(int threads) {
     return (size_t)(threads / 32) * (tile::ORDER_WARP_N * sizeof(unsigned long long) + sizeof(tile::LightPicks));
 }
 
+// Phases [P0, P1) in one launch: selection, list and ordering; the heavy
+// cells; the light cells and the end of the step, as three launches with
+// their own phases' registers.
+template <int P0, int P1>
 __global__ void __launch_bounds__(BC_MAX_THREADS, 4)
 k_batch_collide(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
     extern __shared__ __align__(16) unsigned char bcSmem[];
@@ -559,7 +563,8 @@ k_batch_collide(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
         reinterpret_cast<unsigned long long*>(bcSmem) + (size_t)warp * tile::ORDER_WARP_N;
     tile::LightPicks& pk =
         reinterpret_cast<tile::LightPicks*>(bcSmem + (size_t)W * tile::ORDER_WARP_N * sizeof(unsigned long long))[warp];
-    for (int ph = 0; ph < BC_NPHASE; ++ph) {
+#pragma unroll
+    for (int ph = P0; ph < P1; ++ph) {
         long long total;
         switch (ph) {
         case BC_SELECT:
@@ -664,8 +669,28 @@ k_batch_collide(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
             }
             if (err) atomicOr(&ctr->err, err);
         }
-        if (!persist::grid_sync(ctl)) return;
+        if (ph + 1 < P1 && !persist::grid_sync(ctl)) return;
     }
+}
+
+template <int P0, int P1>
+int batch_collide_grid_of(int threads) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_collide<P0, P1>, threads,
+                                                      batch_collide_smem(threads)) != cudaSuccess)
+        return 0;
+    return per * sms;
+}
+
+template <int P0, int P1>
+cudaError_t launch_batch_collide_part(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st) {
+    const int grid = batch_collide_grid_of<P0, P1>(threads);
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    void* args[] = {(void*)&slots, (void*)&n, (void*)&ctl};
+    return cudaLaunchCooperativeKernel((const void*)k_batch_collide<P0, P1>, dim3(grid), dim3(threads), args,
+                                       batch_collide_smem(threads), st);
 }
 
 int sm_count() {
@@ -683,23 +708,20 @@ int collide_init() {
     return e == cudaSuccess ? 0 : (int)e;
 }
 
+// the smallest resident grid of the three launches (0: one cannot run)
 int batch_collide_grid(int threads) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_collide, threads, batch_collide_smem(threads)) !=
-        cudaSuccess)
-        return 0;
-    return per * sms;
+    const int a = batch_collide_grid_of<BC_SELECT, BC_HEAVY>(threads);
+    const int b = batch_collide_grid_of<BC_HEAVY, BC_LIGHT>(threads);
+    const int c = batch_collide_grid_of<BC_LIGHT, BC_NPHASE>(threads);
+    return std::min(a, std::min(b, c));
 }
 
 cudaError_t launch_batch_collide(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st) {
     if (threads > BC_MAX_THREADS || threads < 32 || threads % 32) return cudaErrorInvalidConfiguration;
-    const int grid = batch_collide_grid(threads);
-    if (grid <= 0) return cudaErrorInvalidConfiguration;
-    void* args[] = {(void*)&slots, (void*)&n, (void*)&ctl};
-    return cudaLaunchCooperativeKernel((const void*)k_batch_collide, dim3(grid), dim3(threads), args,
-                                       batch_collide_smem(threads), st);
+    cudaError_t e = launch_batch_collide_part<BC_SELECT, BC_HEAVY>(slots, n, ctl, threads, st);
+    if (e == cudaSuccess) e = launch_batch_collide_part<BC_HEAVY, BC_LIGHT>(slots, n, ctl, threads, st);
+    if (e == cudaSuccess) e = launch_batch_collide_part<BC_LIGHT, BC_NPHASE>(slots, n, ctl, threads, st);
+    return e;
 }
 
 void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st,

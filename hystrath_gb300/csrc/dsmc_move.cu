@@ -1418,12 +1418,19 @@ constexpr int BM_IT = 8;    // iterations of the CTA per move, scatter and gathe
 enum { BM_ZERO = 0, BM_MOVE, BM_SLOW, BM_DONE, BM_FINAL, BM_SCAN, BM_SCATTER, BM_GATHER, BM_FINISH, BM_NPHASE };
 static_assert(BATCH_TICKETS_MOVE + BM_NPHASE <= BATCH_TICKETS_COLLIDE, "ticket counters of the move launch");
 
+// Phases [P0, P1) in one launch: the step runs as three launches (zero and
+// move; boundary path, sample commit and scan; scatter, gather and finish),
+// so that each is compiled and made resident with its own phases' registers
+// (one launch of every phase took the boundary path's and the scan's 124
+// registers everywhere and held the move to 16 warps per SM).
+template <int P0, int P1>
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
     __shared__ long long pre[BATCH_MAX_CASES + 1];
     const int T = blockDim.x;
     const int tid = threadIdx.x;
-    for (int ph = 0; ph < BM_NPHASE; ++ph) {
+#pragma unroll
+    for (int ph = P0; ph < P1; ++ph) {
         long long total;
         switch (ph) {
         case BM_MOVE:
@@ -1574,8 +1581,27 @@ k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
             }
             if (err) atomicOr(&ctr->err, err);
         }
-        if (!persist::grid_sync(ctl)) return;
+        if (ph + 1 < P1 && !persist::grid_sync(ctl)) return;
     }
+}
+
+constexpr int BM_SPLIT1 = BM_SLOW, BM_SPLIT2 = BM_SCATTER;
+
+template <int P0, int P1>
+int batch_move_grid_of(int threads) {
+    int dev = 0, sms = 0, per = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_move<P0, P1>, threads, 0) != cudaSuccess) return 0;
+    return per * sms;
+}
+
+template <int P0, int P1>
+cudaError_t launch_batch_move_part(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st) {
+    const int grid = batch_move_grid_of<P0, P1>(threads);
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    void* args[] = {(void*)&slots, (void*)&n, (void*)&ctl};
+    return cudaLaunchCooperativeKernel((const void*)k_batch_move<P0, P1>, dim3(grid), dim3(threads), args, 0, st);
 }
 
 int grid_for(long long n, int threads, int perSmBlocks) {
@@ -1592,19 +1618,19 @@ int grid_for(long long n, int threads, int perSmBlocks) {
 
 int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TILE) + 1; }
 
+// the smallest resident grid of the three launches (0: one cannot run)
 int batch_move_grid(int threads) {
-    int dev = 0, sms = 0, per = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_move, threads, 0) != cudaSuccess) return 0;
-    return per * sms;
+    const int a = batch_move_grid_of<0, BM_SPLIT1>(threads);
+    const int b = batch_move_grid_of<BM_SPLIT1, BM_SPLIT2>(threads);
+    const int c = batch_move_grid_of<BM_SPLIT2, BM_NPHASE>(threads);
+    return std::min(a, std::min(b, c));
 }
 
 cudaError_t launch_batch_move(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st) {
-    const int grid = batch_move_grid(threads);
-    if (grid <= 0) return cudaErrorInvalidConfiguration;
-    void* args[] = {(void*)&slots, (void*)&n, (void*)&ctl};
-    return cudaLaunchCooperativeKernel((const void*)k_batch_move, dim3(grid), dim3(threads), args, 0, st);
+    cudaError_t e = launch_batch_move_part<0, BM_SPLIT1>(slots, n, ctl, threads, st);
+    if (e == cudaSuccess) e = launch_batch_move_part<BM_SPLIT1, BM_SPLIT2>(slots, n, ctl, threads, st);
+    if (e == cudaSuccess) e = launch_batch_move_part<BM_SPLIT2, BM_NPHASE>(slots, n, ctl, threads, st);
+    return e;
 }
 
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st, cudaEvent_t mid,
