@@ -3,8 +3,9 @@ their launch shapes.
 
 ``BatchCloud`` wraps ``dsmc_batch_*``: every batched step is one launch of a
 CUDA graph whose children are the cases' captured steps, or, in the
-persistent mode, two cooperative persistent launches over all cases (move
-and sort, then collisions) with per-phase (case, tile) work queues.  ``autotune`` picks,
+persistent mode, cooperative persistent launches over all cases (three
+ranges of the move and sort phases, three of the collision phases) with
+per-phase (case, tile) work queues.  ``autotune`` picks,
 per size class of the cases, the threads per CTA of the parcel-streaming
 kernels and the cells per CTA of the lane-per-cell collision kernel by timing
 batched steps (coordinate descent over the classes).

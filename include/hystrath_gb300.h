@@ -601,8 +601,9 @@ int dsmc_batch_initialise(dsmc_batch* b);
 int dsmc_batch_set_launch(dsmc_batch* b, int i, int cta_threads, int cells_per_cta);
 int dsmc_batch_evolve(dsmc_batch* b, long long n_steps);
 /* Persistent mode of the batch (no counterpart in the reference): every
- * batched step is two cooperative persistent launches over all cases -- the
- * move and sort phases, then the collision phases -- whose CTAs take
+ * batched step is six cooperative persistent launches over all cases -- three
+ * ranges of the move and sort phases, then three of the collision phases,
+ * each with its own register footprint -- whose CTAs take
  * (case, tile) work items from a queue per phase and wait at a grid barrier
  * between phases, so that small and large cases share the SMs; the step of
  * each buffer parity is captured as a CUDA graph where the driver allows
