@@ -3,7 +3,7 @@ their launch shapes.
 
 ``BatchCloud`` wraps ``dsmc_batch_*``: every batched step is one launch of a
 CUDA graph whose children are the cases' captured steps, or, in the
-persistent mode, cooperative persistent launches over all cases (three
+persistent mode, cooperative persistent launches over all cases (four
 ranges of the move and sort phases, three of the collision phases) with
 per-phase (case, tile) work queues.  ``autotune`` picks,
 per size class of the cases, the threads per CTA of the parcel-streaming

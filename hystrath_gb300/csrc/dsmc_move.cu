@@ -1418,8 +1418,9 @@ constexpr int BM_IT = 8;    // iterations of the CTA per move, scatter and gathe
 enum { BM_ZERO = 0, BM_MOVE, BM_SLOW, BM_DONE, BM_FINAL, BM_SCAN, BM_SCATTER, BM_GATHER, BM_FINISH, BM_NPHASE };
 static_assert(BATCH_TICKETS_MOVE + BM_NPHASE <= BATCH_TICKETS_COLLIDE, "ticket counters of the move launch");
 
-// Phases [P0, P1) in one launch: the step runs as three launches (zero and
-// move; boundary path, sample commit and scan; scatter, gather and finish),
+// Phases [P0, P1) in one launch: the step runs as four launches (zero and
+// move; boundary path, sample commit and scan; index scatter; gather and
+// finish),
 // so that each is compiled and made resident with its own phases' registers
 // (one launch of every phase took the boundary path's and the scan's 124
 // registers everywhere and held the move to 16 warps per SM).
@@ -1585,7 +1586,7 @@ k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
     }
 }
 
-constexpr int BM_SPLIT1 = BM_SLOW, BM_SPLIT2 = BM_SCATTER;
+constexpr int BM_SPLIT1 = BM_SLOW, BM_SPLIT2 = BM_SCATTER, BM_SPLIT3 = BM_GATHER;
 
 template <int P0, int P1>
 int batch_move_grid_of(int threads) {
@@ -1622,14 +1623,16 @@ int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TIL
 int batch_move_grid(int threads) {
     const int a = batch_move_grid_of<0, BM_SPLIT1>(threads);
     const int b = batch_move_grid_of<BM_SPLIT1, BM_SPLIT2>(threads);
-    const int c = batch_move_grid_of<BM_SPLIT2, BM_NPHASE>(threads);
-    return std::min(a, std::min(b, c));
+    const int c = batch_move_grid_of<BM_SPLIT2, BM_SPLIT3>(threads);
+    const int d = batch_move_grid_of<BM_SPLIT3, BM_NPHASE>(threads);
+    return std::min(std::min(a, b), std::min(c, d));
 }
 
 cudaError_t launch_batch_move(const BatchSlot* slots, int n, BatchCtl* ctl, int threads, cudaStream_t st) {
     cudaError_t e = launch_batch_move_part<0, BM_SPLIT1>(slots, n, ctl, threads, st);
     if (e == cudaSuccess) e = launch_batch_move_part<BM_SPLIT1, BM_SPLIT2>(slots, n, ctl, threads, st);
-    if (e == cudaSuccess) e = launch_batch_move_part<BM_SPLIT2, BM_NPHASE>(slots, n, ctl, threads, st);
+    if (e == cudaSuccess) e = launch_batch_move_part<BM_SPLIT2, BM_SPLIT3>(slots, n, ctl, threads, st);
+    if (e == cudaSuccess) e = launch_batch_move_part<BM_SPLIT3, BM_NPHASE>(slots, n, ctl, threads, st);
     return e;
 }
 

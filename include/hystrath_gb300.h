@@ -601,7 +601,7 @@ int dsmc_batch_initialise(dsmc_batch* b);
 int dsmc_batch_set_launch(dsmc_batch* b, int i, int cta_threads, int cells_per_cta);
 int dsmc_batch_evolve(dsmc_batch* b, long long n_steps);
 /* Persistent mode of the batch (no counterpart in the reference): every
- * batched step is six cooperative persistent launches over all cases -- three
+ * batched step is seven cooperative persistent launches over all cases -- four
  * ranges of the move and sort phases, then three of the collision phases,
  * each with its own register footprint -- whose CTAs take
  * (case, tile) work items from a queue per phase and wait at a grid barrier
