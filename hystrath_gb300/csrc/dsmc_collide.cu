@@ -549,9 +549,10 @@ __host__ __device__ constexpr size_t batch_collide_smem(int threads) {
 
 // Phases [P0, P1) in one launch: selection, list and ordering; the heavy
 // cells; the light cells and the end of the step, as three launches with
-// their own phases' registers.
+// their own phases' registers (the heavy cells' up to 170: at 128 they
+// spill).
 template <int P0, int P1>
-__global__ void __launch_bounds__(BC_MAX_THREADS, 4)
+__global__ void __launch_bounds__(BC_MAX_THREADS, P0 == BC_HEAVY ? 3 : 4)
 k_batch_collide(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
     extern __shared__ __align__(16) unsigned char bcSmem[];
     __shared__ long long pre[BATCH_MAX_CASES + 1];
