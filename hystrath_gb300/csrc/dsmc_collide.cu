@@ -755,7 +755,8 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
                                                                 B.exceed, B.obsMax, B.audit);
     if (marks) cudaEventRecord(marks[1], st);
     const int L = B.cfg.lightCells;
-    tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * sizeof(tile::LightPicks), st>>>(
+    tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * (sizeof(tile::LightPicks) + sizeof(tile::LightDefer)),
+                            st>>>(
         cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.exceed, B.obsMax, B.audit);
 }
 

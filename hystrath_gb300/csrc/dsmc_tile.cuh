@@ -509,10 +509,9 @@ __device__ __forceinline__ bool test_candidate(const CaseDev& cs, const Parcels&
     return sigma > r.u01() * smax0;
 }
 
-__device__ __forceinline__ void collide_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
-                                                  long long gQ, CollRec P, CollRec Q, double cr2, double* collSep,
-                                                  unsigned* err) {
-    *collSep += (double)coll_separation(s.r + gP, s.r + gQ);
+// The exchange of an accepted pair and the stores of its two parcels.
+__device__ __forceinline__ void exchange_pair(const CaseDev& cs, const Parcels& s, Rng& r, long long gP, long long gQ,
+                                              CollRec P, CollRec Q, double cr2, unsigned* err) {
     const int tP = sv_species(P.sv), tQ = sv_species(Q.sv);
     const PairDev& pr = cs.pair[tP * DSMC_MAX_SPECIES + tQ];
     Post o;
@@ -528,6 +527,13 @@ __device__ __forceinline__ void collide_candidate(const CaseDev& cs, const Parce
     P.sv = make_sv(tP, o.vP); Q.sv = make_sv(tQ, o.vQ);
     st_coll(s.r + gP, P);
     st_coll(s.r + gQ, Q);
+}
+
+__device__ __forceinline__ void collide_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
+                                                  long long gQ, const CollRec& P, const CollRec& Q, double cr2,
+                                                  double* collSep, unsigned* err) {
+    *collSep += (double)coll_separation(s.r + gP, s.r + gQ);
+    exchange_pair(cs, s, r, gP, gQ, P, Q, cr2, err);
 }
 
 __device__ __forceinline__ bool run_candidate(const CaseDev& cs, const Parcels& s, Rng& r, long long gP,
@@ -697,6 +703,31 @@ __device__ __forceinline__ int warp_argmin(uint32_t hA, bool vA, uint32_t hB, bo
     return a ? __ffs(a) - 1 : (b ? 31 + __ffs(b) : -1);
 }
 
+// Accepted candidates of single-candidate light cells whose exchange is
+// deferred: a warp collects them (parcel indices and cell) until 32 are
+// waiting and then runs 32 exchanges with every lane busy.  On this part an
+// FP64 instruction occupies the pipe for the whole warp whatever its active
+// lanes, and on the channel 93% of the light cells have one candidate, of
+// which 57% are accepted: run where they were tested, the exchanges kept
+// half the FP64 pipe's lanes idle.  The exchange repeats the test's one
+// draw and reloads the pair, so the result is bit for bit the immediate
+// one (no other candidate touches the pair's parcels in this step).
+struct LightDefer {
+    int4 e[64];      // (gP, gQ, cell, -)
+    int count;
+};
+
+__device__ __forceinline__ void exchange_deferred(const CaseDev& cs, const Parcels& s, const int4& e, uint32_t step,
+                                                  unsigned* err) {
+    const long long gP = e.x, gQ = e.y;
+    const CollRec P = ld_coll(s.r + gP), Q = ld_coll(s.r + gQ);
+    Rng r(cs, (uint32_t)e.z, step, cand_tag(0));
+    (void)r.u01();   // the acceptance test's draw
+    const double d0 = P.ux - Q.ux, d1 = P.uy - Q.uy, d2 = P.uz - Q.uz;
+    const double cr2 = d0 * d0 + d1 * d1 + d2 * d2;
+    exchange_pair(cs, s, r, gP, gQ, P, Q, cr2, err);
+}
+
 // One warp's group of 32 light work items from qb (lanes past nWork take part
 // in the warp-made picks without a cell); pk: the warp's picks in shared
 // memory.  Collision and candidate counts accumulate in nColl and nCandTot.
@@ -705,7 +736,7 @@ __device__ __forceinline__ void light_group(const CaseDev& cs, const Parcels& s,
                                             const double* __restrict__ smaxSel, unsigned char* useR, float* exceed,
                                             float* obsMax, double2* audit, long long qb, long long nWork,
                                             uint32_t step, LightPicks& pk, unsigned& err, unsigned long long& nColl,
-                                            unsigned long long& nCandTot) {
+                                            unsigned long long& nCandTot, LightDefer* dq = nullptr) {
     const int lane = (int)(threadIdx.x & 31u);
     const long long C = cs.C;
     const long long q = qb + lane;
@@ -786,6 +817,8 @@ __device__ __forceinline__ void light_group(const CaseDev& cs, const Parcels& s,
         }
     }
     __syncwarp();
+    bool defer = false;
+    long long dP = 0, dQ = 0;
     if (q < nWork) {
         const double R = smax[c];
         const double smax0 = learned ? smaxSel[c] : R;
@@ -795,7 +828,27 @@ __device__ __forceinline__ void light_group(const CaseDev& cs, const Parcels& s,
         // The lane tests candidates until one is accepted, then collides
         // it: lanes that reach an accepted candidate in the same pass run
         // the FP64 exchange together, whatever the rejections before it.
+        // A single candidate is only tested here when its exchange can be
+        // deferred to the warp's queue.
         int k = 0;
+        if (dq && nCand == 1) {
+            const int jP = pk.pq[0][0][lane], jQ = pk.pq[0][1][lane];
+            k = 1;
+            if (jP >= n || jQ >= n) {
+                err |= ERRB_BOUNDS;
+            } else {
+                dP = off + jP;
+                dQ = off + jQ;
+                Rng r(cs, (uint32_t)c, step, cand_tag(0));
+                CollRec P, Q;
+                double cr2;
+                if (test_candidate(cs, s, r, dP, dQ, smax0, &stepMax, &P, &Q, &cr2, audit ? &au : nullptr)) {
+                    defer = true;
+                    collSep += (double)coll_separation(s.r + dP, s.r + dQ);
+                    ++coll;
+                }
+            }
+        }
         while (k < nCand) {
             bool accepted = false;
             long long gP = 0, gQ = 0;
@@ -830,18 +883,39 @@ __device__ __forceinline__ void light_group(const CaseDev& cs, const Parcels& s,
         nColl += coll;
         nCandTot += (unsigned long long)nCand;
     }
+    if (dq) {
+        // queue the deferred exchanges; run 32 once 32 are waiting
+        const unsigned m = __ballot_sync(0xFFFFFFFFu, defer);
+        int cnt = dq->count;
+        if (defer) dq->e[cnt + __popc(m & ((1u << lane) - 1u))] = make_int4((int)dP, (int)dQ, (int)c, 0);
+        cnt += __popc(m);
+        __syncwarp();
+        if (cnt >= 32) {
+            exchange_deferred(cs, s, dq->e[lane], step, &err);
+            __syncwarp();
+            if (lane < cnt - 32) dq->e[lane] = dq->e[32 + lane];
+            cnt -= 32;
+        }
+        __syncwarp();
+        if (lane == 0) dq->count = cnt;
+    }
     __syncwarp();   // the picks are read before the next cells overwrite them
 }
 
 // one lane per light cell, its candidates one after the other; blockDim.x
-// (the cells per CTA) is 32, 64 or 128, with one LightPicks per warp in
-// dynamic shared memory
+// (the cells per CTA) is 32, 64 or 128, with one LightPicks and one
+// LightDefer per warp in dynamic shared memory
 __global__ void __launch_bounds__(128, 4)
 k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* smax, double* acc, Counters* ctr,
                 const int2* __restrict__ work, int learned, const double* __restrict__ smaxSel, unsigned char* useR,
                 float* exceed, float* obsMax, double2* audit) {
     extern __shared__ __align__(16) unsigned char lightSmem[];
-    LightPicks& pk = reinterpret_cast<LightPicks*>(lightSmem)[threadIdx.x >> 5];
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    LightPicks& pk = reinterpret_cast<LightPicks*>(lightSmem)[w];
+    LightDefer* dq = reinterpret_cast<LightDefer*>(lightSmem + nw * sizeof(LightPicks)) + w;
+    const unsigned lane = lane_id();
+    if (lane == 0) dq->count = 0;
+    __syncwarp();
     const uint32_t step = (uint32_t)ctr->step;
     const long long nWork = (long long)ctr->nWork;
     const long long nHeavy = (long long)ctr->nHeavy;
@@ -851,7 +925,9 @@ k_collide_light(CaseDev cs, Parcels s, const int* __restrict__ start, double* sm
     for (long long qb = nHeavy + (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); qb < nWork;
          qb += stride)
         light_group(cs, s, start, smax, acc, work, learned, smaxSel, useR, exceed, obsMax, audit, qb, nWork, step,
-                    pk, err, nColl, nCandTot);
+                    pk, err, nColl, nCandTot, dq);
+    // the exchanges still waiting
+    if ((int)lane < dq->count) exchange_deferred(cs, s, dq->e[lane], step, &err);
     if (nColl) atomicAdd(&ctr->coll, nColl);
     if (nCandTot) atomicAdd(&ctr->cand, nCandTot);
     if (err) atomicOr(&ctr->err, err);
