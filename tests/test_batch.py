@@ -184,9 +184,9 @@ def test_batch_follows_settings_changed_on_a_case():
 @pytest.mark.gpu
 @pytest.mark.parametrize("threads", [(256, 128), (128, 64), (512, 128)])
 def test_persistent_batch_equals_steps_alone(threads):
-    """The persistent mode (two cooperative launches per step over all cases,
-    per-phase work queues) gives every case exactly the state it reaches
-    alone, Ar and N2 alike."""
+    """The persistent mode (cooperative launches of phase ranges over all
+    cases, per-phase work queues) gives every case exactly the state it
+    reaches alone, Ar and N2 alike."""
     from hystrath_gb300.batch import BatchCloud, heat_bath_cases
     from hystrath_gb300.dsmc import DsmcCloud
     specs, _ = heat_bath_cases(5, 256)
@@ -242,4 +242,36 @@ def test_destroying_a_batched_case_is_refused():
     assert b"belongs to a batch" in lib().dsmc_last_error(h)
     b.evolve(2)
     assert b.info(1).step == 2
+    b.close()
+
+
+@pytest.mark.gpu
+def test_dense_heavy_cells_persistent_equal_alone():
+    """A dense case (about 400 parcels and a few hundred candidates per cell:
+    many conflict rounds of a heavy cell's warp) in the persistent batch
+    reaches the state it reaches alone, bit for bit."""
+    from hystrath_gb300.batch import BatchCloud
+    from hystrath_gb300.dsmc import DsmcCloud
+
+    def dense():
+        s = S.config1(seed=91, n=6)
+        s.n_equivalent_particles /= 8.0
+        s.delta_t *= 50.0
+        return s
+
+    g = DsmcCloud(dense())
+    g.initialise()
+    g.evolve(1)
+    assert g.counts().candidates_last_step / 216 > 128
+    g.evolve(3)
+    b = BatchCloud([dense(), S.config1(seed=92, n=8)])
+    b.initialise()
+    b.set_persistent(256, 128)
+    b.evolve(4)
+    ib, ig = b.info(0), g.info()
+    assert ib.collisions_total == ig.collisions_total and ib.candidates_total == ig.candidates_total
+    sb, sg = _state_of_case(b, 0), _state(g)
+    for k in sb:
+        assert np.array_equal(sb[k], sg[k]), k
+    g.close()
     b.close()
