@@ -61,6 +61,10 @@ struct dsmc_handle {
     int cur = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // the heavy-cell collisions' branch of a captured step, beside the light
+    // cells' (the two take disjoint cells)
+    cudaStream_t side = nullptr;
+    cudaEvent_t forkEv = nullptr, joinEv = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraph_t graphT[2] = {nullptr, nullptr};   // the captured steps (child graphs of a batch)
     unsigned long long graphGen = 0;   // bumped whenever the step graphs are dropped
@@ -568,7 +572,10 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev, 
             mlp_launch_infer(h->model, B.feat, cs.C, B.pred, h->learnMargin, &B.ctr->step, h->learnEvery, st);
         }
         mark(MK_LEARNED);
-        launch_collide(cs, B, cur, h->model ? 1 : 0, st, ev ? ev + MK_SELECT : nullptr);
+        // with event marks (the profiled steps) the heavy and light kernels
+        // run one after the other so that each is timed alone
+        if (ev) launch_collide(cs, B, cur, h->model ? 1 : 0, st, ev + MK_SELECT);
+        else launch_collide(cs, B, cur, h->model ? 1 : 0, st, nullptr, h->side, h->forkEv, h->joinEv);
     } else {
         mark(MK_LEARNED);
         mark(MK_SELECT);
@@ -764,6 +771,9 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     h->B.capacity = cap;
 
     CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CUDA_TRY(h, cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+    CUDA_TRY(h, cudaEventCreateWithFlags(&h->forkEv, cudaEventDisableTiming));
+    CUDA_TRY(h, cudaEventCreateWithFlags(&h->joinEv, cudaEventDisableTiming));
     if (collide_init()) return fail(h, DSMC_ERR_CUDA, "cannot raise the shared-memory limit of the cell-order kernel");
     StepBuffers& B = h->B;
     if ((rc = alloc_soa(h, &h->buf[0], cap))) return rc;
@@ -919,6 +929,9 @@ void dsmc_destroy(dsmc_handle* h) {
     if (h->ctrHost) cudaFreeHost(h->ctrHost);
     if (h->ctrRing) cudaFreeHost(h->ctrRing);
     if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->side) cudaStreamDestroy(h->side);
+    if (h->forkEv) cudaEventDestroy(h->forkEv);
+    if (h->joinEv) cudaEventDestroy(h->joinEv);
     delete h;
 }
 

@@ -726,7 +726,7 @@ cudaError_t launch_batch_collide(const BatchSlot* slots, int n, BatchCtl* ctl, i
 }
 
 void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st,
-                    cudaEvent_t* marks) {
+                    cudaEvent_t* marks, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join) {
     const int sms = sm_count();
     long long selBlocks = (cs.C + 255) / 256;
     if (selBlocks > (long long)sms * 8) selBlocks = (long long)sms * 8;
@@ -750,14 +750,25 @@ void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, i
         if (marks) cudaEventRecord(marks[1], st);
         return;
     }
-    tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, st>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
+    // the heavy cells (their long tail: a few dense cells' warps) beside the
+    // light cells when a side stream is given
+    const bool branch = side && fork && join && !marks;
+    cudaStream_t hs = st;
+    if (branch) {
+        cudaEventRecord(fork, st);
+        cudaStreamWaitEvent(side, fork, 0);
+        hs = side;
+    }
+    tile::k_collide_heavy<<<sms * 4, tile::WARPS * 32, 0, hs>>>(cs, s, B.start, B.smax, B.acc, B.ctr, B.work,
                                                                 B.perm, B.subs, learned, B.smaxSel, B.useR,
                                                                 B.exceed, B.obsMax, B.audit);
+    if (branch) cudaEventRecord(join, side);
     if (marks) cudaEventRecord(marks[1], st);
     const int L = B.cfg.lightCells;
     tile::k_collide_light<<<sms * 4 * (128 / L), L, (L / 32) * (sizeof(tile::LightPicks) + sizeof(tile::LightDefer)),
                             st>>>(
         cs, s, B.start, B.smax, B.acc, B.ctr, B.work, learned, B.smaxSel, B.useR, B.exceed, B.obsMax, B.audit);
+    if (branch) cudaStreamWaitEvent(st, join, 0);
 }
 
 void launch_cell_features(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int every, int resetFallback,

@@ -143,8 +143,12 @@ void launch_reset_sample_counters(const StepBuffers& B, cudaStream_t st);
 // cells that fell back to it) instead of the running maximum alone
 // marks (optional): two events, recorded after the selection, list and
 // ordering kernels and after the heavy-cell kernel
+// side (optional, without marks): the heavy cells' kernel runs on it, forked
+// from st by the event fork and joined back by join, beside the light
+// cells' kernel on st (disjoint cells: the state is the same either way)
 void launch_collide(const CaseDev& cs, const StepBuffers& B, const Parcels& s, int learned, cudaStream_t st,
-                    cudaEvent_t* marks = nullptr);
+                    cudaEvent_t* marks = nullptr, cudaStream_t side = nullptr, cudaEvent_t fork = nullptr,
+                    cudaEvent_t join = nullptr);
 // per-cell features of the learned maximum; every > 0: only on steps that are
 // multiples of every, every == 0: always; resetFallback: the cells go back to
 // the prediction
