@@ -539,10 +539,26 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev, 
         // kernel, or here when this step does not move
         if (!(phases & DSMC_PHASE_MOVE)) launch_sample_flush(cs, B, a, 0, st);
         mark(MK_ZERO);
-        if ((phases & DSMC_PHASE_INFLOW) && h->hasInflow) launch_inflow(cs, h->inflow, B, a, st);
-        mark(MK_INFLOW);
-        if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st, ev ? ev[MK_MOVE] : nullptr, movePending);
-        else mark(MK_MOVE);
+        // in a captured step the inflow runs on the side branch while the
+        // last step's parcels move (the inserted ones, appended after them,
+        // move once it has joined); the profiled steps and divided clouds
+        // keep the sequential order
+        const bool inflow = (phases & DSMC_PHASE_INFLOW) && h->hasInflow;
+        const bool branch = inflow && (phases & DSMC_PHASE_MOVE) && !ev && cs.domAxis < 0;
+        if (branch) {
+            cudaEventRecord(h->forkEv, st);
+            cudaStreamWaitEvent(h->side, h->forkEv, 0);
+            launch_inflow(cs, h->inflow, B, a, h->side);
+            cudaEventRecord(h->joinEv, h->side);
+            launch_move(cs, B, a, st, nullptr, movePending, 1);
+            cudaStreamWaitEvent(st, h->joinEv, 0);
+            launch_move(cs, B, a, st, nullptr, movePending, 2);
+        } else {
+            if (inflow) launch_inflow(cs, h->inflow, B, a, st);
+            mark(MK_INFLOW);
+            if (phases & DSMC_PHASE_MOVE) launch_move(cs, B, a, st, ev ? ev[MK_MOVE] : nullptr, movePending);
+            else mark(MK_MOVE);
+        }
         mark(MK_MOVE_SLOW);
         if (phases & DSMC_PHASE_MOVE) launch_sample_commit(cs, B, 0, st);
         if (part == 1) {

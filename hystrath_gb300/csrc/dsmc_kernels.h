@@ -123,8 +123,11 @@ constexpr int MIGRANT_WORDS = 17;
 
 // deferPos: the sort follows in the same step, and the end points of plain
 // moves are left to its gather (launch_scatter with movePending)
+// range: 0 every parcel [0, nMoved), then the boundary path; 1 the last
+// step's parcels [0, n) only (needs nothing of this step's inflow); 2 the
+// inserted parcels [n, nMoved), then the boundary path
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st,
-                 cudaEvent_t mid = nullptr, bool deferPos = false);
+                 cudaEvent_t mid = nullptr, bool deferPos = false, int range = 0);
 void launch_scan(const CaseDev& cs, const StepBuffers& B, cudaStream_t st);
 // mid (optional): an event recorded between the index scatter and the gather
 void launch_scatter(const CaseDev& cs, const StepBuffers& B, const Parcels& src, const Parcels& dst,

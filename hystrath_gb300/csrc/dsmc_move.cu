@@ -686,17 +686,26 @@ __device__ __forceinline__ void move_iter(const CaseDev& cs, const Parcels& s, C
     if (doSample) sample_contrib(sfix, cs.C, skey, sux, suy, suz, ser, svb, &err);
 }
 
+// range: MOVE_ALL the parcels [0, nMoved); MOVE_KEPT the parcels of the last
+// step [0, n), which needs nothing of this step's inflow; MOVE_INSERTED the
+// inserted ones [n, nMoved), none of which is sampled.
+enum { MOVE_ALL = 0, MOVE_KEPT, MOVE_INSERTED };
+
 template <bool GEN>
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_move(CaseDev cs, Parcels s, Counters* ctr, int* slowList, int* count, long long* sfix, int deferPos,
-       int* migList, long long migCap) {
-    const long long n = ctr->nMoved;
+       int* migList, long long migCap, int range) {
+    long long lo = 0, hi = range == MOVE_KEPT ? ctr->n : ctr->nMoved;
     const uint32_t step = (uint32_t)ctr->step;
-    const int doSample = ctr->pendingSample;
+    int doSample = ctr->pendingSample;
+    if (range == MOVE_INSERTED) {
+        lo = ctr->n;
+        doSample = 0;
+    }
     unsigned err = 0;
     const long long stride = (long long)gridDim.x * blockDim.x;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < n; base += stride)
-        move_iter<GEN>(cs, s, ctr, slowList, count, sfix, base + threadIdx.x, n, step, doSample, deferPos, migList,
+    for (long long base = lo + (long long)blockIdx.x * blockDim.x; base < hi; base += stride)
+        move_iter<GEN>(cs, s, ctr, slowList, count, sfix, base + threadIdx.x, hi, step, doSample, deferPos, migList,
                        migCap, err);
     if (err) atomicOr(&ctr->err, err);
 }
@@ -1637,14 +1646,16 @@ cudaError_t launch_batch_move(const BatchSlot* slots, int n, BatchCtl* ctl, int 
 }
 
 void launch_move(const CaseDev& cs, const StepBuffers& B, const Parcels& s, cudaStream_t st, cudaEvent_t mid,
-                 bool deferPos) {
+                 bool deferPos, int range) {
     const int T = B.cfg.streamThreads;
     const int grid = grid_for(B.capacity, T, B.cfg.streamCtasPerSm);
     const bool general = cs.anyEmpty || cs.nObst || cs.faceFlux || cs.half[0] || cs.half[1] || cs.half[2] ||
                          cs.domAxis >= 0;
     const int d = deferPos ? 1 : 0;
-    if (general) k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d, B.migList, B.migCap);
-    else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d, nullptr, 0);
+    if (general)
+        k_move<true><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d, B.migList, B.migCap, range);
+    else k_move<false><<<grid, T, 0, st>>>(cs, s, B.ctr, B.slowList, B.count, B.sfix, d, nullptr, 0, range);
+    if (range == MOVE_KEPT) return;   // the inserted parcels' move and the boundary path follow
     if (mid) cudaEventRecord(mid, st);
     k_move_slow<<<grid_for(B.capacity, T, 2), T, 0, st>>>(cs, s, B.ctr, B.slowList, B.bfPatch, B.wall, B.count,
                                                           B.migList, B.migCap);
