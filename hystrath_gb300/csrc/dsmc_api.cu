@@ -521,6 +521,8 @@ enum {
 // ev: NULL, or MK_COUNT events recorded at the marks above.
 // part: 0 the whole step; for a divided cloud 1 the inflow, the move and the
 // packed migrants, 2 the rest (received migrants are added in between).
+constexpr long long HEAVY_BRANCH_MIN_CELLS = 1LL << 18;
+
 void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev, int part) {
     const CaseDev& cs = h->cs;
     StepBuffers& B = h->B;
@@ -590,8 +592,12 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev, 
         mark(MK_LEARNED);
         // with event marks (the profiled steps) the heavy and light kernels
         // run one after the other so that each is timed alone
-        if (ev) launch_collide(cs, B, cur, h->model ? 1 : 0, st, ev + MK_SELECT);
-        else launch_collide(cs, B, cur, h->model ? 1 : 0, st, nullptr, h->side, h->forkEv, h->joinEv);
+        // the heavy cells' branch only pays on large meshes: for a case of a
+        // few thousand cells its fork and join cost more than the overlap
+        // gives (256 small heat baths one at a time: 111 -> 118 ms per step)
+        const bool heavyBranch = !ev && cs.C >= HEAVY_BRANCH_MIN_CELLS;
+        if (heavyBranch) launch_collide(cs, B, cur, h->model ? 1 : 0, st, nullptr, h->side, h->forkEv, h->joinEv);
+        else launch_collide(cs, B, cur, h->model ? 1 : 0, st, ev ? ev + MK_SELECT : nullptr);
     } else {
         mark(MK_LEARNED);
         mark(MK_SELECT);
