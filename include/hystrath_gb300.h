@@ -3,8 +3,11 @@
  *
  * One handle owns one DSMC cloud on one GPU: its parcel state in HBM (one
  * 64-byte record per parcel plus a cell word), per-cell collision and sampling
- * state, the stream it runs on and its captured step graph.  The entry points replace the calls that the
- * dsmcFoam+ driver makes on a dsmcCloud:
+ * state, the stream it runs on (and a second stream that carries the step's
+ * concurrent branches -- the inflow beside the move, the heavy cells'
+ * collisions beside the light cells' -- joined back into the first before
+ * the step ends) and its captured step graphs.  The entry points replace the
+ * calls that the dsmcFoam+ driver makes on a dsmcCloud:
  *
  *   reference (path in hystrath/hyStrath)                         this ABI
  *   dsmcCloud ctor  src/lagrangian/dsmc/clouds/dsmcCloud.C:586-691  dsmc_create / dsmc_create_from_spec
