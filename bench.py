@@ -161,13 +161,15 @@ STATE_BYTES = 68
 # sample_finalize, sample_flushed; scan_reduce, scan_top, scan_down;
 # scatter_index, gather, finish_sort; ntc_select, ntc_buckets, ntc_list,
 # cell_order, cell_order_big, collide_heavy, collide_light; set_pending;
-# end_step -- plus inflow_count/scan/fill/commit with an inflow patch and
-# cell_features, mlp_infer with the learned maximum
+# end_step -- plus, with an inflow patch, inflow_count/scan/fill/commit and
+# a second move launch (the inserted parcels move after the inflow, which
+# runs beside the first), and cell_features, mlp_infer with the learned
+# maximum
 KERNELS_PER_STEP = 21
 
 
 def kernels_per_step(has_inflow, learned):
-    return KERNELS_PER_STEP + (4 if has_inflow else 0) + (2 if learned else 0)
+    return KERNELS_PER_STEP + (5 if has_inflow else 0) + (2 if learned else 0)
 
 
 def kernel_bytes(N, C, n_moved, coll, cand, n_acc):
