@@ -61,8 +61,9 @@ struct dsmc_handle {
     int cur = 0;
     int device = 0;
     cudaStream_t stream = nullptr;
-    // the heavy-cell collisions' branch of a captured step, beside the light
-    // cells' (the two take disjoint cells)
+    // the side branch of a captured step: the inflow beside the move of the
+    // last step's parcels, and the heavy cells' collisions beside the light
+    // cells' (forked from and joined back into stream within the step)
     cudaStream_t side = nullptr;
     cudaEvent_t forkEv = nullptr, joinEv = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -591,10 +592,10 @@ void enqueue_step(dsmc_handle* h, int parity, unsigned phases, cudaEvent_t* ev, 
         }
         mark(MK_LEARNED);
         // with event marks (the profiled steps) the heavy and light kernels
-        // run one after the other so that each is timed alone
-        // the heavy cells' branch only pays on large meshes: for a case of a
-        // few thousand cells its fork and join cost more than the overlap
-        // gives (256 small heat baths one at a time: 111 -> 118 ms per step)
+        // run one after the other so that each is timed alone; the heavy
+        // cells' branch only pays on large meshes: for a case of a few
+        // thousand cells its fork and join cost more than the overlap gives
+        // (256 small heat baths one at a time: 111 -> 118 ms per step)
         const bool heavyBranch = !ev && cs.C >= HEAVY_BRANCH_MIN_CELLS;
         if (heavyBranch) launch_collide(cs, B, cur, h->model ? 1 : 0, st, nullptr, h->side, h->forkEv, h->joinEv);
         else launch_collide(cs, B, cur, h->model ? 1 : 0, st, ev ? ev + MK_SELECT : nullptr);
