@@ -1429,10 +1429,9 @@ static_assert(BATCH_TICKETS_MOVE + BM_NPHASE <= BATCH_TICKETS_COLLIDE, "ticket c
 
 // Phases [P0, P1) in one launch: the step runs as four launches (zero and
 // move; boundary path, sample commit and scan; index scatter; gather and
-// finish),
-// so that each is compiled and made resident with its own phases' registers
-// (one launch of every phase took the boundary path's and the scan's 124
-// registers everywhere and held the move to 16 warps per SM).
+// finish), so that each is compiled and made resident with its own phases'
+// registers (one launch of every phase took the boundary path's and the
+// scan's 124 registers everywhere and held the move to 16 warps per SM).
 template <int P0, int P1>
 __global__ void __launch_bounds__(MAX_STREAM_THREADS)
 k_batch_move(const BatchSlot* __restrict__ slots, int n, BatchCtl* ctl) {
@@ -1628,7 +1627,7 @@ int grid_for(long long n, int threads, int perSmBlocks) {
 
 int scan_scratch_ints(long long C) { return (int)((C + SCAN_TILE - 1) / SCAN_TILE) + 1; }
 
-// the smallest resident grid of the three launches (0: one cannot run)
+// the smallest resident grid of the four launches (0: one cannot run)
 int batch_move_grid(int threads) {
     const int a = batch_move_grid_of<0, BM_SPLIT1>(threads);
     const int b = batch_move_grid_of<BM_SPLIT1, BM_SPLIT2>(threads);
