@@ -275,3 +275,61 @@ def test_dense_heavy_cells_persistent_equal_alone():
         assert np.array_equal(sb[k], sg[k]), k
     g.close()
     b.close()
+
+
+class _FakeBatch:
+    """Stands in for BatchCloud in the tuner tests (no GPU): the time of a
+    batched step is a sum of per-class costs of the launch shapes set."""
+
+    def __init__(self, classes, cost):
+        self.classes, self.cost = classes, cost
+        self.shape = {}
+        self.persistent = None
+        self.timed = 0
+
+    def set_launch(self, i, t, c):
+        self.shape[i] = (t, c)
+
+    def set_persistent(self, t, c):
+        self.persistent = (t, c)
+
+    def evolve(self, n=1):
+        pass
+
+    def evolve_timed(self, n):
+        self.timed += 1
+        if self.persistent is not None:
+            t, c = self.persistent
+            return n * (10.0 + abs(t - 256) / 128.0 + (0.5 if c == 128 else 0.0))
+        ms = 0.0
+        for k, idx in enumerate(self.classes):
+            ms += self.cost(k, self.shape[idx[0]])
+        return n * ms
+
+
+def test_autotune_picks_each_class_minimum():
+    """Coordinate descent over size classes: every class ends on the launch
+    shape of least cost (the costs are separable), and that shape is what
+    the batch's cases carry."""
+    from hystrath_gb300.batch import CELLS_PER_CTA, CTA_THREADS, autotune
+    classes = [[0, 1], [2], [3, 4, 5]]
+    best = {0: (128, 32), 1: (512, 128), 2: (256, 64)}
+
+    def cost(k, cfg):
+        return 1.0 + (0.0 if cfg == best[k] else 0.3 + 0.001 * (cfg[0] + cfg[1]))
+
+    b = _FakeBatch(classes, cost)
+    choice, ms = autotune(b, classes, steps=2)
+    assert choice == [best[0], best[1], best[2]]
+    assert abs(ms - 3.0) < 1e-12
+    for k, idx in enumerate(classes):
+        assert all(b.shape[i] == best[k] for i in idx)
+    assert b.timed == len(classes) * len(CTA_THREADS) * len(CELLS_PER_CTA)
+
+
+def test_autotune_persistent_picks_and_applies_the_minimum():
+    from hystrath_gb300.batch import autotune_persistent
+    b = _FakeBatch([[0]], lambda k, cfg: 0.0)
+    cfg, ms = autotune_persistent(b, steps=3)
+    assert cfg == (256, 64) and abs(ms - 10.0) < 1e-12
+    assert b.persistent == (256, 64)
