@@ -400,7 +400,9 @@ def gpu_arm(args, rank, world, local):
                        "plain arm against the learned arm of an independently seeded run of the same "
                        "development (the comparison needs independent runs); the *_control entries compare "
                        "the plain arm with the plain selection of that independent run, the same statistics "
-                       "when only the seeds differ".format(args.learn_every))
+                       "when only the seeds differ; Tvib is held by a few hundred excited parcels that outlive "
+                       "the window, so its z values read the run-to-run spread of that population (the control "
+                       "shows the same shift), not the selection".format(args.learn_every))
 
     # kernel groups and the roofline (not the value): K more steps with events
     log("kernel profile")
