@@ -121,3 +121,26 @@ def test_oracle_lb_equipartition(oracle_mod):
     E0 = None
     assert abs(Trot / Ttr - 1.0) < 0.05, (Ttr, Trot)
     del E0
+
+
+def test_oracle_reset_sampling_restarts_the_averages(oracle_mod):
+    """After a restart of the averages the oracle's fields average only the
+    steps sampled since: the number density averaged over steps 5..8 (a
+    restart after step 4) equals twice the average over steps 1..8 minus the
+    average over steps 1..4 of an identical cloud (rhoN is linear in the
+    sampled counts)."""
+    from hystrath_gb300 import spec as S
+    a = oracle_mod.OracleCloud(S.config1(seed=4, n=6), threads=2)
+    b = oracle_mod.OracleCloud(S.config1(seed=4, n=6), threads=2)
+    for o in (a, b):
+        o.initialise()
+        o.evolve(4)
+    first4 = b.field("rhoN")
+    a.reset_sampling()
+    assert a.info().sample_steps == 0
+    a.evolve(4)
+    b.evolve(4)
+    assert a.info().sample_steps == 4 and b.info().sample_steps == 8
+    last4 = a.field("rhoN")
+    assert np.abs(last4).sum() > 0
+    np.testing.assert_allclose(last4, 2.0 * b.field("rhoN") - first4, rtol=1e-12, atol=1e-3 * np.abs(last4).max() * 1e-9)
