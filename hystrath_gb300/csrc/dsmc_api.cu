@@ -791,6 +791,11 @@ int dsmc_create_from_spec(const dsmc_case_spec* spec, dsmc_handle** out) {
     h->expectedN = (long long)(ndSum * fluidV / cs.FN);
     long long cap = spec->max_particles;
     if (cap <= 0) cap = (long long)((h->hasInflow ? 2.0 : 1.3) * h->expectedN) + 65536;
+    // parcel indices are 32-bit in the sort's slots, the boundary-path and
+    // migrant lists and the collision queues
+    if (cap > 0x7FFFFFFFLL)
+        return fail(h, DSMC_ERR_CAPACITY, "a cloud holds at most 2^31 - 1 parcels (capacity " + std::to_string(cap) +
+                                              "): divide the case into domains (dsmc_set_domain)");
     h->B.capacity = cap;
 
     CUDA_TRY(h, cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));

@@ -177,7 +177,8 @@ typedef struct {
     double init_velocity[3];
     double init_t_tra_xyz[3];        /* >0: per-axis translational temperatures
                                         (anisotropic start; not a reference key) */
-    long long max_particles;         /* capacity; 0 = 2x the initial fill + inflow margin */
+    long long max_particles;         /* capacity; 0 = 2x the initial fill + inflow margin; at most
+                                        2^31 - 1 (32-bit parcel indices), else DSMC_ERR_CAPACITY */
 
     /* Rectilinear grading (blockMesh simpleGrading): for a graded axis the
      * n_cells[a] + 1 node coordinates, strictly increasing (origin[a] and
